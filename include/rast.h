@@ -1,0 +1,160 @@
+/* librast: C ABI of the GB300 (sm_103a) rasteriser hot path.
+ *
+ * It replaces canmom/rasteriser's per-frame path, draw_frame (drawing.cpp:205-258, declared at
+ * headers/drawing.h:16-18), and the geometry.h / shading.h calls it makes. Plain pointers and
+ * sizes only; the C++ drop-in (rasteriser_gb300/cpp) and the Python binding
+ * (rasteriser_gb300/abi.py) sit on top.
+ *
+ * Results match the reference exactly: coverage, depth and the index of the triangle that wins
+ * each pixel are bit for bit those of the reference's sequential loop (nearest first, then lowest
+ * triangle index), and the RGB8 frame is computed with the reference's shading arithmetic.
+ *
+ * Threading: a context is used by one host thread at a time. Device work of a context runs in
+ * order on its stream.
+ */
+#ifndef RAST_H
+#define RAST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAST_ABI_VERSION 1
+
+typedef enum rast_status {
+    RAST_OK = 0,
+    RAST_ERR_INVALID_ARG = 1,   /* null pointer, zero or oversized frame, negative count */
+    RAST_ERR_BAD_INDEX = 2,     /* a triangle refers to a vertex, normal, uv or material that does not exist */
+    RAST_ERR_NO_MESH = 3,       /* draw before rast_upload_mesh */
+    RAST_ERR_CUDA = 4,          /* a CUDA runtime call failed; rast_last_error has the text */
+    RAST_ERR_OUT_OF_MEMORY = 5,
+    RAST_ERR_BIN_OVERFLOW = 6,  /* a device draw overflowed the tile-bin pool; the pool has been
+                                   grown, draw the frame again */
+    RAST_ERR_TIMEOUT = 7,       /* a bounded device-side wait gave up */
+    RAST_ERR_NO_DEVICE = 8
+} rast_status;
+
+typedef struct rast_ctx rast_ctx;
+
+/* Frame flags. */
+#define RAST_WIND_CLOCKWISE 1u /* Args::wind_clockwise (arguments.h:13): front faces have
+                                  signed_area_2d <= 0 and shading normals are negated */
+#define RAST_CLEAR 2u          /* treat the frame as cleared to 0 and the depth buffer to 1.0
+                                  before drawing, as the reference's spin loop does
+                                  (renderer.cpp:107-108); the incoming buffers are not read */
+#define RAST_FLAT 4u           /* Args::flat (arguments.h:12). Accepted and ignored, as in the
+                                  reference, which parses the flag but never reads it */
+
+/* ------------------------------------------------------------------------------------------ */
+/* host-side geometry (no device work)                                                         */
+/* ------------------------------------------------------------------------------------------ */
+
+/* The per-frame matrices of draw_frame (drawing.cpp:221-229; geometry.cpp:22-33):
+ *   model     = transformation_matrix(scale, disp, angles)  = T * Ry * Rx * Rz * S
+ *   view      = transformation_matrix(1, (0,0,-3), 0)
+ *   modelview = view * model
+ *   camera    = perspective(radians(fovy_deg), width/height, z_near, z_far) * modelview
+ *   normal    = transpose(inverse(modelview))                (geometry.cpp:101)
+ * Each output (nullable) receives 16 floats, column major. disp and angles are xyz; angles are
+ * the YXZ Tait-Bryan angles (rx, ry, rz) in radians. The reference fixes fovy / near / far to
+ * 45 / 0.1 / 6 (geometry.cpp:30); pass those for an identical camera. */
+rast_status rast_frame_matrices(uint32_t width, uint32_t height, float scale, const float disp[3],
+                                const float angles[3], float fovy_deg, float z_near, float z_far,
+                                float model[16], float view[16], float modelview[16], float camera[16],
+                                float normal[16]);
+
+/* Light::transform (geometry.cpp:124-133): trans_dir = normalize(xyz(view * (direction, 0))).
+ * lights_in: n records of 7 floats (direction xyz, intensity, colour rgb; light.h:7-14).
+ * lights_out: n records of 7 floats with trans_dir in place of direction (may alias lights_in). */
+rast_status rast_transform_lights(const float view[16], const float* lights_in, int32_t n, float* lights_out);
+
+/* ------------------------------------------------------------------------------------------ */
+/* context                                                                                     */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Creates a context on CUDA device `device` with its own non-blocking stream. */
+rast_status rast_create(rast_ctx** out, int device);
+void rast_destroy(rast_ctx* ctx);
+
+/* Text of the last error on this context (or of the last failed rast_create when ctx is NULL). */
+const char* rast_last_error(const rast_ctx* ctx);
+const char* rast_status_string(rast_status s);
+int rast_abi_version(void);
+
+/* Makes the context launch on `stream` (a cudaStream_t; NULL restores its own stream). */
+rast_status rast_set_stream(rast_ctx* ctx, void* stream);
+void* rast_get_stream(const rast_ctx* ctx);
+
+/* ------------------------------------------------------------------------------------------ */
+/* scene data (device resident until replaced)                                                 */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Uploads a mesh in the reference's host layouts (the vectors draw_frame receives):
+ *   pos: nv * 3 floats (vector<vec3> model_vertices)
+ *   nrm: nn * 3 floats (vector<vec3> model_vertnormals)
+ *   uv:  nuv * 2 floats (vector<vec2> vertuvs; may be NULL when nuv == 0)
+ *   tris: ntri * 10 int32, the Triangle layout of face.h:6-13 (vertices[3], normals[3], uvs[3],
+ *         material); vector<Triangle>::data() can be passed as is
+ *   kd:  nmat * 3 floats, each material's constant albedo (Material::diffuse_colour,
+ *        material.h:13; the value Material::sample returns without a texture, material.cpp:24)
+ * Every index is checked on the host first. The reference reads out of bounds on a bad index
+ * (drawing.cpp:165-173); here such a mesh is refused with RAST_ERR_BAD_INDEX. A uv index < 0
+ * means "no uv", as in the reference (drawing.cpp:168). Synchronous. */
+rast_status rast_upload_mesh(rast_ctx* ctx, const float* pos, int64_t nv, const float* nrm, int64_t nn,
+                             const float* uv, int64_t nuv, const int32_t* tris, int64_t ntri,
+                             const float* kd, int32_t nmat);
+
+/* Sets the frame's lights: n records of 7 floats (trans_dir xyz, intensity, colour rgb), i.e.
+ * already transformed (rast_transform_lights). Shading sums them in this order
+ * (shading.cpp:24-34). 0 <= n <= 4096. */
+rast_status rast_set_lights(rast_ctx* ctx, const float* lights7, int32_t n);
+
+/* ------------------------------------------------------------------------------------------ */
+/* drawing                                                                                     */
+/* ------------------------------------------------------------------------------------------ */
+
+/* One frame of draw_frame with HOST buffers (the reference's calling convention): copies the
+ * frame and depth buffers in (unless RAST_CLEAR), renders, copies them back; returns when done.
+ *   camera, normal: the frame's camera and normal matrices (rast_frame_matrices)
+ *   rgb_planar: width*height*3 bytes, planar (x + y*width + c*width*height) as CImg stores
+ *               CImg<unsigned char>(W,H,1,3) (renderer.cpp:85); read and written
+ *   depth: width*height floats (CImg<float>(W,H,1,1), renderer.cpp:86); read and written; the
+ *          incoming value is the depth every fragment must beat (drawing.cpp:119)
+ *   tri_id (nullable): width*height uint32, the index of the triangle that wrote each pixel in
+ *          this call, or 0xFFFFFFFF
+ * Pixels no fragment wins keep their colour and depth. 1 <= width, height <= 32768. */
+rast_status rast_draw(rast_ctx* ctx, const float camera[16], const float normal[16], uint32_t width,
+                      uint32_t height, uint32_t flags, uint8_t* rgb_planar, float* depth, uint32_t* tri_id);
+
+/* The same with DEVICE buffers, enqueued on the context's stream and not waited for. */
+rast_status rast_draw_device(rast_ctx* ctx, const float camera[16], const float normal[16], uint32_t width,
+                             uint32_t height, uint32_t flags, uint8_t* d_rgb_planar, float* d_depth,
+                             uint32_t* d_tri_id);
+
+/* Waits for the context's stream; reports device-side conditions of earlier draws
+ * (RAST_ERR_BIN_OVERFLOW). */
+rast_status rast_sync(rast_ctx* ctx);
+
+/* Counters of the last completed draw (call after rast_sync):
+ *   [0] front-facing triangles      [1] bounding-box pixels tested
+ *   [2] inside fragments            [3] pixels written
+ *   [4] triangles on the binned path [5] tile-bin entries
+ *   [6] kernel launches of the draw  [7] reserved */
+rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
+
+/* Tuning knobs (see rast_set_option keys). Values outside the supported set are refused. */
+#define RAST_OPT_SMALL_MAX_PIXELS 1   /* bounding boxes up to this many pixels are rasterised by
+                                         the per-triangle path; larger ones are binned (1..65536) */
+#define RAST_OPT_TILE_SIZE 2          /* tile edge for binning: 8, 16 or 32 */
+#define RAST_OPT_BIN_CAPACITY 3       /* initial tile-bin pool, entries */
+rast_status rast_set_option(rast_ctx* ctx, int option, int64_t value);
+rast_status rast_get_option(rast_ctx* ctx, int option, int64_t* value);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAST_H */

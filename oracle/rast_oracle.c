@@ -1,0 +1,190 @@
+/* Oracle test infrastructure: plain-C restatement of canmom/rasteriser's draw_frame. Only tests,
+ * the smoke check and bench.py's CPU-baseline leg use it, and only as the checker.
+ *
+ * Every floating-point expression keeps the reference's operation order; the file is compiled
+ * with -ffp-contract=off so that no multiply-add is fused. glm arithmetic follows the order fixed
+ * by the project's glm subset (rasteriser_gb300/compat/glm/detail/subset_core.hpp). */
+#include "rast_oracle.h"
+
+#include <math.h>
+#include <stddef.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct { float x, y, z, w; } v4;
+typedef struct { float x, y, z; } v3;
+
+/* glm::min / glm::max for scalars (x < y ? x : y, x > y ? x : y). */
+static inline float gmin(float x, float y) { return x < y ? x : y; }
+static inline float gmax(float x, float y) { return x > y ? x : y; }
+
+/* mat4 * vec4 as (c0*x + c1*y) + (c2*z + c3*w), column-major m. Row r of the result. */
+static inline float mrow(const float* m, int r, float x, float y, float z, float w) {
+    float lo = m[0 + r] * x + m[4 + r] * y;
+    float hi = m[8 + r] * z + m[12 + r] * w;
+    return lo + hi;
+}
+
+/* geometry.cpp:44-50 (transform_point), 52-60 (z_divide), 62-74 (remap_ndc, ndc_to_raster). */
+static inline v4 raster_vertex(const float* cam, const float* p, float wf, float hf) {
+    float cx = mrow(cam, 0, p[0], p[1], p[2], 1.f);
+    float cy = mrow(cam, 1, p[0], p[1], p[2], 1.f);
+    float cz = mrow(cam, 2, p[0], p[1], p[2], 1.f);
+    float cw = mrow(cam, 3, p[0], p[1], p[2], 1.f);
+    float nx = cx / cw, ny = cy / cw, nz = cz / cw, iw = 1.f / cw;
+    v4 r;
+    r.x = 0.5f * (nx + 1.0f) * wf;
+    r.y = 0.5f * (-ny + 1.0f) * hf;
+    r.z = nz;
+    r.w = iw;
+    return r;
+}
+
+/* geometry.cpp:35-42 (transform_direction) with the normal matrix. */
+static inline v3 camera_normal(const float* nm, const float* n) {
+    v3 r;
+    r.x = mrow(nm, 0, n[0], n[1], n[2], 0.f);
+    r.y = mrow(nm, 1, n[0], n[1], n[2], 0.f);
+    r.z = mrow(nm, 2, n[0], n[1], n[2], 0.f);
+    return r;
+}
+
+void oracle_raster_vertices(const float* camera, const float* pos, int64_t nv, uint32_t width,
+                            uint32_t height, float* out4) {
+    const float wf = (float)(int)width, hf = (float)(int)height;
+    for (int64_t i = 0; i < nv; ++i) {
+        v4 r = raster_vertex(camera, pos + 3 * i, wf, hf);
+        out4[4 * i + 0] = r.x;
+        out4[4 * i + 1] = r.y;
+        out4[4 * i + 2] = r.z;
+        out4[4 * i + 3] = r.w;
+    }
+}
+
+/* shading.cpp:20-34. lights7: trans_dir xyz, intensity, colour rgb. */
+static inline void shade(v3 n, v3 albedo, const float* lights7, int32_t nl, uint32_t* out3) {
+    const float one_over_pi = 0.318309886183790671537767526745028724f;
+    float ax = 0.f, ay = 0.f, az = 0.f; /* std::accumulate from vec3(0) */
+    for (int32_t l = 0; l < nl; ++l) {
+        const float* L = lights7 + 7 * l;
+        float I = L[3];
+        float cx = I * L[4], cy = I * L[5], cz = I * L[6];
+        cx = cx * albedo.x;
+        cy = cy * albedo.y;
+        cz = cz * albedo.z;
+        float d = (n.x * -L[0] + n.y * -L[1]) + n.z * -L[2];
+        float m = gmax(0.f, d);
+        cx = cx * m;
+        cy = cy * m;
+        cz = cz * m;
+        cx = cx * one_over_pi;
+        cy = cy * one_over_pi;
+        cz = cz * one_over_pi;
+        ax = ax + cx;
+        ay = ay + cy;
+        az = az + cz;
+    }
+    out3[0] = (uint32_t)gmin(ax, 255.f);
+    out3[1] = (uint32_t)gmin(ay, 255.f);
+    out3[2] = (uint32_t)gmin(az, 255.f);
+}
+
+void oracle_shade(const float* normal3, const float* albedo3, const float* lights7, int32_t nl,
+                  uint32_t* out3) {
+    v3 n = {normal3[0], normal3[1], normal3[2]};
+    v3 a = {albedo3[0], albedo3[1], albedo3[2]};
+    shade(n, a, lights7, nl, out3);
+}
+
+int oracle_draw_frame(const oracle_frame* f, uint8_t* frame, float* depth, uint32_t* tri_id,
+                      uint64_t* stats) {
+    if (!f || !frame || !depth || f->width == 0 || f->height == 0) return -1;
+    const uint32_t W = f->width, H = f->height;
+    const size_t plane = (size_t)W * H;
+    const float wf = (float)(int)W, hf = (float)(int)H;
+    /* drawing.cpp:84: vec2 image_bottom_right(image_width - 1, image_height - 1) */
+    const float brx_lim = (float)(W - 1u), bry_lim = (float)(H - 1u);
+    const int cw = f->wind_clockwise != 0;
+    uint64_t n_front = 0, n_tested = 0, n_inside = 0, n_pass = 0;
+
+    /* drawing.cpp:236 and 241-247: normals to camera space, vertices to raster space. */
+    v4* rv = (v4*)malloc((size_t)(f->nv > 0 ? f->nv : 1) * sizeof(v4));
+    v3* cn = (v3*)malloc((size_t)(f->nn > 0 ? f->nn : 1) * sizeof(v3));
+    if (!rv || !cn) { free(rv); free(cn); return -1; }
+    for (int64_t i = 0; i < f->nv; ++i) rv[i] = raster_vertex(f->camera, f->pos + 3 * i, wf, hf);
+    for (int64_t i = 0; i < f->nn; ++i) cn[i] = camera_normal(f->normal_matrix, f->nrm + 3 * i);
+
+    /* drawing.cpp:250-257: faces in order. */
+    for (int64_t t = 0; t < f->ntri; ++t) {
+        const int32_t* tri = f->tris + 10 * t;
+        /* drawing.cpp:165-173: de-index */
+        v4 v0 = rv[tri[0]], v1 = rv[tri[1]], v2 = rv[tri[2]];
+        v3 n0 = cn[tri[3]], n1 = cn[tri[4]], n2 = cn[tri[5]];
+        const float* kd = f->kd + 3 * tri[9];
+        v3 albedo = {kd[0], kd[1], kd[2]};
+
+        /* geometry.cpp:76-83 signed_area_2d, drawing.cpp:176-178 culling */
+        float sa = -0.5f * (v0.x * v1.y - v1.x * v0.y + v1.x * v2.y - v2.x * v1.y + v2.x * v0.y - v0.x * v2.y);
+        int front = (sa > 0) != cw;
+        if (!front) continue;
+        ++n_front;
+
+        /* drawing.cpp:77-93 bounding_box */
+        float mnx = gmin(gmin(v0.x, v1.x), v2.x), mny = gmin(gmin(v0.y, v1.y), v2.y);
+        float mxx = gmax(gmax(v0.x, v1.x), v2.x), mxy = gmax(gmax(v0.y, v1.y), v2.y);
+        uint32_t tlx = (uint32_t)gmin(gmax(mnx, 0.f), brx_lim);
+        uint32_t tly = (uint32_t)gmin(gmax(mny, 0.f), bry_lim);
+        uint32_t brx = (uint32_t)gmin(gmax(ceilf(mxx), 0.f), brx_lim);
+        uint32_t bry = (uint32_t)gmin(gmax(ceilf(mxy), 0.f), bry_lim);
+
+        /* drawing.cpp:191-201 and update_pixel 96-149 */
+        for (uint32_t y = tly; y <= bry; ++y) {
+            for (uint32_t x = tlx; x <= brx; ++x) {
+                ++n_tested;
+                const float px = (float)x, py = (float)y;
+                /* drawing.cpp:36-49 edge / barycentric */
+                float area = (v1.x - v0.x) * (v2.y - v0.y) - (v1.y - v0.y) * (v2.x - v0.x);
+                float b0 = ((v2.x - v1.x) * (py - v1.y) - (v2.y - v1.y) * (px - v1.x)) / area;
+                float b1 = ((v0.x - v2.x) * (py - v2.y) - (v0.y - v2.y) * (px - v2.x)) / area;
+                float b2 = ((v1.x - v0.x) * (py - v0.y) - (v1.y - v0.y) * (px - v0.x)) / area;
+                if (!(b0 >= 0.f && b1 >= 0.f && b2 >= 0.f)) continue;
+                ++n_inside;
+                /* drawing.cpp:115-121 depth test */
+                float z = v0.z * b0 + v1.z * b1 + v2.z * b2;
+                const size_t p = (size_t)x + (size_t)y * W;
+                if (!(z < depth[p])) continue;
+                ++n_pass;
+                depth[p] = z;
+                /* drawing.cpp:125-132 perspective-correct normal */
+                float i0 = v0.w * b0, i1 = v1.w * b1, i2 = v2.w * b2;
+                float dd = 1.f / (i0 + i1 + i2);
+                v3 s;
+                s.x = i0 * n0.x + i1 * n1.x + i2 * n2.x;
+                s.y = i0 * n0.y + i1 * n1.y + i2 * n2.y;
+                s.z = i0 * n0.z + i1 * n1.z + i2 * n2.z;
+                s.x = dd * s.x;
+                s.y = dd * s.y;
+                s.z = dd * s.z;
+                float inv = 1.0f / sqrtf((s.x * s.x + s.y * s.y) + s.z * s.z);
+                v3 nrm = {s.x * inv, s.y * inv, s.z * inv};
+                if (cw) { nrm.x = -nrm.x; nrm.y = -nrm.y; nrm.z = -nrm.z; }
+                /* drawing.cpp:138-146 shade and write planar RGB */
+                uint32_t rgb[3];
+                shade(nrm, albedo, f->lights, f->nl, rgb);
+                frame[p] = (uint8_t)rgb[0];
+                frame[p + plane] = (uint8_t)rgb[1];
+                frame[p + 2 * plane] = (uint8_t)rgb[2];
+                if (tri_id) tri_id[p] = (uint32_t)t;
+            }
+        }
+    }
+    free(rv);
+    free(cn);
+    if (stats) {
+        stats[0] = n_front;
+        stats[1] = n_tested;
+        stats[2] = n_inside;
+        stats[3] = n_pass;
+    }
+    return 0;
+}

@@ -1,0 +1,54 @@
+/* Oracle test infrastructure: a plain-C restatement of canmom/rasteriser's per-frame path
+ * (draw_frame, drawing.cpp:205-258), used only by tests, the smoke check and the CPU-baseline leg
+ * of bench.py as the checker. Parity status: pinned bit for bit (depth and RGB) against the
+ * reference's own drawing.cpp / geometry.cpp / shading.cpp compiled from source (oracle/_ref) on
+ * the scenes in tests/golden. It adds what the reference computes but does not expose: the
+ * index of the triangle that wrote each pixel, and fragment counts. */
+#ifndef RAST_ORACLE_H
+#define RAST_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_frame {
+    /* mesh, in the reference's layouts */
+    const float* pos;      /* nv * 3 */
+    int64_t nv;
+    const int32_t* tris;   /* ntri * 10: vertices[3], normals[3], uvs[3], material (face.h:6-13) */
+    int64_t ntri;
+    const float* nrm;      /* nn * 3 */
+    int64_t nn;
+    const float* uv;       /* nuv * 2 */
+    int64_t nuv;
+    const float* kd;       /* nmat * 3, constant albedo per material */
+    int32_t nmat;
+    /* per frame */
+    const float* camera;        /* 16, column major: projection * view * model */
+    const float* normal_matrix; /* 16, column major: transpose(inverse(view * model)) */
+    const float* lights;        /* nl * 7: trans_dir xyz (already transformed), intensity, colour rgb */
+    int32_t nl;
+    uint32_t width, height;
+    int32_t wind_clockwise;
+} oracle_frame;
+
+/* stats (nullable) receives: [0] front-facing triangles, [1] bounding-box pixels tested,
+ * [2] inside fragments, [3] depth-test passes. Returns 0, or -1 on a bad argument. */
+int oracle_draw_frame(const oracle_frame* f, uint8_t* frame_planar, float* depth, uint32_t* tri_id,
+                      uint64_t* stats);
+
+/* Per-vertex stage only: raster x, y, NDC z and 1/w_clip per vertex (out4: nv * 4). */
+void oracle_raster_vertices(const float* camera, const float* pos, int64_t nv, uint32_t width,
+                            uint32_t height, float* out4);
+
+/* One fragment of shading.cpp:24-34. */
+void oracle_shade(const float* normal3, const float* albedo3, const float* lights7, int32_t nl,
+                  uint32_t* out3);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,90 @@
+"""Builds librast.so (the CUDA kernels and the C ABI) in-tree for sm_103a.
+
+Translation units are compiled in parallel and only when a source or header is newer than the
+object. The kernels are compiled with -fmad=false, IEEE division and square root and no flush to
+zero; the host code with -ffp-contract=off. Both decide bit-exact parity with the reference.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OBJ = os.path.join(PKG, "_build")
+LIB_DIR = os.path.join(PKG, "_lib")
+LIB = os.path.join(LIB_DIR, "librast.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc_path():
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found; the CUDA toolkit is required to build librast")
+    return cand
+
+
+def _units():
+    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-I" + os.path.join(PKG, "compat")]
+    host = ["-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-std=c++17", "-O3"]
+    kern = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
+                   "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]
+    return [
+        ("rast_kernels.cu", kern + inc),
+        ("rast_api.cpp", host + inc),
+        ("rast_host_math.cpp", host + inc),
+    ]
+
+
+def _headers():
+    hs = [os.path.join(ROOT, "include", "rast.h")]
+    for d, _, fs in os.walk(CSRC):
+        hs += [os.path.join(d, f) for f in fs if f.endswith((".h", ".cuh"))]
+    for d, _, fs in os.walk(os.path.join(PKG, "compat")):
+        hs += [os.path.join(d, f) for f in fs]
+    return hs
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose=False, force=False):
+    """Compile librast.so if anything changed; returns its path."""
+    nvcc = nvcc_path()
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(LIB_DIR, exist_ok=True)
+    headers = _headers()
+    jobs, objs = [], []
+    for src, flags in _units():
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ, src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            jobs.append([nvcc, "-c", s, "-o", o] + flags)
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        return r.stderr
+
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        logs = list(ex.map(run, jobs))
+    if verbose:
+        for lg in logs:
+            print(lg)
+    if force or jobs or _stale(LIB, objs):
+        run([nvcc, "-shared", "-o", LIB] + ARCH + objs + ["-Xcompiler", "-fPIC"])
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True)
+    print(LIB)

@@ -1,0 +1,211 @@
+"""ctypes binding of librast's C ABI (include/rast.h).
+
+``Renderer`` mirrors the reference's per-frame entry point: ``draw_frame`` takes the mesh, the
+lights, the ``Args`` fields that matter (size, winding, model transform) and caller-owned frame and
+depth buffers, and renders into them exactly as canmom/rasteriser's draw_frame (drawing.cpp:205-258)
+does, through the CUDA kernels. There is no CPU fallback: without the built library or a GPU the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+RAST_OK = 0
+STATUS_NAMES = {0: "RAST_OK", 1: "RAST_ERR_INVALID_ARG", 2: "RAST_ERR_BAD_INDEX", 3: "RAST_ERR_NO_MESH",
+                4: "RAST_ERR_CUDA", 5: "RAST_ERR_OUT_OF_MEMORY", 6: "RAST_ERR_BIN_OVERFLOW",
+                7: "RAST_ERR_TIMEOUT", 8: "RAST_ERR_NO_DEVICE"}
+WIND_CLOCKWISE, CLEAR, FLAT = 1, 2, 4
+OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY = 1, 2, 3
+NO_TRIANGLE = 0xFFFFFFFF
+
+# Every function include/rast.h declares, with its ctypes signature.
+_F, _I32, _I64, _U32, _P = C.POINTER(C.c_float), C.c_int32, C.c_int64, C.c_uint32, C.c_void_p
+SIGNATURES = {
+    "rast_frame_matrices": (C.c_int, [_U32, _U32, C.c_float, _F, _F, C.c_float, C.c_float, C.c_float,
+                                      _F, _F, _F, _F, _F]),
+    "rast_transform_lights": (C.c_int, [_F, _F, _I32, _F]),
+    "rast_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+    "rast_destroy": (None, [_P]),
+    "rast_last_error": (C.c_char_p, [_P]),
+    "rast_status_string": (C.c_char_p, [C.c_int]),
+    "rast_abi_version": (C.c_int, []),
+    "rast_set_stream": (C.c_int, [_P, _P]),
+    "rast_get_stream": (_P, [_P]),
+    "rast_upload_mesh": (C.c_int, [_P, _F, _I64, _F, _I64, _F, _I64, C.POINTER(C.c_int32), _I64, _F, _I32]),
+    "rast_set_lights": (C.c_int, [_P, _F, _I32]),
+    "rast_draw": (C.c_int, [_P, _F, _F, _U32, _U32, _U32, C.POINTER(C.c_uint8), _F, C.POINTER(C.c_uint32)]),
+    "rast_draw_device": (C.c_int, [_P, _F, _F, _U32, _U32, _U32, _P, _P, _P]),
+    "rast_sync": (C.c_int, [_P]),
+    "rast_get_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "rast_set_option": (C.c_int, [_P, C.c_int, _I64]),
+    "rast_get_option": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
+}
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load librast.so (building it first when it is missing). Raises if it cannot be loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"librast is not built ({path}); run __graft_entry__.build()")
+        _build.build()
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class RastError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fp(a):
+    return a.ctypes.data_as(_F) if a is not None else None
+
+
+def frame_matrices(width, height, scale=1.0, disp=(0, 0, 0), angles=(0, 0, 0), fovy_deg=45.0, z_near=0.1,
+                   z_far=6.0):
+    """The draw_frame matrices (model, view, modelview, camera, normal) as (16,) float32 arrays."""
+    lib = load()
+    outs = [np.zeros(16, np.float32) for _ in range(5)]
+    d, a = _f32(disp), _f32(angles)
+    st = lib.rast_frame_matrices(width, height, scale, _fp(d), _fp(a), fovy_deg, z_near, z_far,
+                                 *[_fp(o) for o in outs])
+    if st != RAST_OK:
+        raise RastError(st, "rast_frame_matrices")
+    return dict(zip(["model", "view", "modelview", "camera", "normal"], outs))
+
+
+def transform_lights(view, lights7):
+    lib = load()
+    li = _f32(lights7).copy()
+    out = np.empty_like(li)
+    st = lib.rast_transform_lights(_fp(_f32(view)), _fp(li), li.shape[0], _fp(out))
+    if st != RAST_OK:
+        raise RastError(st, "rast_transform_lights")
+    return out
+
+
+def scene_frame_inputs(scene):
+    """Camera matrix, normal matrix and transformed lights of a scene's frame."""
+    m = frame_matrices(scene.width, scene.height, scene.scale, scene.disp, scene.angles, scene.fovy_deg,
+                       scene.z_near, scene.z_far)
+    return m["camera"], m["normal"], transform_lights(m["view"], scene.lights), m
+
+
+class Renderer:
+    """One librast context on one device."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = _P()
+        st = self.lib.rast_create(C.byref(h), device)
+        if st != RAST_OK:
+            raise RastError(st, self.lib.rast_last_error(None).decode())
+        self.h = h
+        self._mesh_digest = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rast_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st != RAST_OK:
+            raise RastError(st, f"{what}: {self.lib.rast_last_error(self.h).decode()}")
+
+    # scene data -----------------------------------------------------------------------------
+    def upload_mesh(self, pos, nrm, uv, tris, kd):
+        pos, nrm, uv, kd = _f32(pos), _f32(nrm), _f32(uv), _f32(kd)
+        tris = np.ascontiguousarray(tris, np.int32)
+        st = self.lib.rast_upload_mesh(self.h, _fp(pos), pos.shape[0], _fp(nrm), nrm.shape[0],
+                                       _fp(uv) if uv.size else None, uv.shape[0],
+                                       tris.ctypes.data_as(C.POINTER(C.c_int32)), tris.shape[0], _fp(kd), kd.shape[0])
+        self._check(st, "rast_upload_mesh")
+
+    def upload_scene_mesh(self, scene):
+        dg = scene.mesh_digest()
+        if dg != self._mesh_digest:
+            self.upload_mesh(scene.pos, scene.nrm, scene.uv, scene.tris, scene.kd)
+            self._mesh_digest = dg
+
+    def set_lights(self, lights7):
+        li = _f32(lights7).reshape(-1, 7)
+        self._check(self.lib.rast_set_lights(self.h, _fp(li), li.shape[0]), "rast_set_lights")
+
+    def set_option(self, opt, value):
+        self._check(self.lib.rast_set_option(self.h, opt, int(value)), "rast_set_option")
+
+    def get_option(self, opt):
+        v = C.c_int64()
+        self._check(self.lib.rast_get_option(self.h, opt, C.byref(v)), "rast_get_option")
+        return v.value
+
+    def set_stream(self, stream_handle):
+        self._check(self.lib.rast_set_stream(self.h, _P(stream_handle) if stream_handle else None), "rast_set_stream")
+
+    # drawing --------------------------------------------------------------------------------
+    def draw(self, camera, normal, width, height, flags=0, frame=None, depth=None, want_ids=False):
+        """Host-buffer draw. frame: (3, H, W) uint8, depth: (H, W) float32, both read and written."""
+        frame = np.zeros((3, height, width), np.uint8) if frame is None else frame
+        depth = np.ones((height, width), np.float32) if depth is None else depth
+        assert frame.dtype == np.uint8 and frame.flags.c_contiguous and frame.size == 3 * width * height
+        assert depth.dtype == np.float32 and depth.flags.c_contiguous and depth.size == width * height
+        ids = np.empty((height, width), np.uint32) if want_ids else None
+        st = self.lib.rast_draw(self.h, _fp(_f32(camera)), _fp(_f32(normal)), width, height, flags,
+                                frame.ctypes.data_as(C.POINTER(C.c_uint8)), _fp(depth),
+                                ids.ctypes.data_as(C.POINTER(C.c_uint32)) if ids is not None else None)
+        self._check(st, "rast_draw")
+        return frame, depth, ids
+
+    def draw_device(self, camera, normal, width, height, flags, d_rgb, d_depth, d_ids=0):
+        """Device-buffer draw on the context's stream; pointers are integers (e.g. tensor.data_ptr())."""
+        st = self.lib.rast_draw_device(self.h, _fp(_f32(camera)), _fp(_f32(normal)), width, height, flags,
+                                       _P(d_rgb), _P(d_depth), _P(d_ids) if d_ids else None)
+        self._check(st, "rast_draw_device")
+
+    def sync(self):
+        self._check(self.lib.rast_sync(self.h), "rast_sync")
+
+    def stats(self):
+        out = (C.c_uint64 * 8)()
+        self._check(self.lib.rast_get_stats(self.h, out), "rast_get_stats")
+        keys = ["front", "tested", "inside", "written", "binned_tris", "bin_entries", "launches", "reserved"]
+        return dict(zip(keys, list(out)))
+
+    def draw_scene(self, scene, frame=None, depth=None, want_ids=True, clear=False):
+        """draw_frame for a Scene: uploads its mesh if it changed, sets its lights, renders."""
+        self.upload_scene_mesh(scene)
+        cam, nm, lights, _ = scene_frame_inputs(scene)
+        self.set_lights(lights)
+        flags = (WIND_CLOCKWISE if scene.wind_clockwise else 0) | (CLEAR if clear else 0)
+        return self.draw(cam, nm, scene.width, scene.height, flags, frame, depth, want_ids)

@@ -1,0 +1,441 @@
+// Host side of librast's C ABI (include/rast.h): contexts, validation, device buffers and the
+// orchestration of one draw. The kernels are in rast_kernels.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "rast.h"
+#include "rast_internal.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+// A device allocation that grows and never shrinks.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t want) {
+        if (want <= bytes) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+}  // namespace
+
+struct rast_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // mesh
+    DevBuf pos, tris10, tri_v, tri_nm, nrm, kd;
+    rast::DeviceMesh mesh;
+    bool has_mesh = false;
+
+    // lights
+    DevBuf lights;
+    int32_t nl = 0;
+
+    // per-draw scratch
+    DevBuf rv, keys, large, counters, tile_offset, entries, stats;
+    int64_t cap_large = 0, cap_entries = 0;
+    bool keys_armed_clear = false;
+    int64_t keys_px = 0;
+
+    // host-pointer draws stage through these
+    DevBuf d_rgb, d_depth, d_ids;
+
+    // options
+    uint32_t small_max = 256;
+    uint32_t tile = 16;
+    int64_t bin_capacity = 0;  // 0: sized from the mesh
+
+    uint64_t last_launches = 0;
+};
+
+namespace {
+
+rast_status fail(rast_ctx* c, rast_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    else g_create_error = msg;
+    return s;
+}
+
+rast_status cuda_fail(rast_ctx* c, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(c, e == cudaErrorMemoryAllocation ? RAST_ERR_OUT_OF_MEMORY : RAST_ERR_CUDA, m);
+}
+
+#define RAST_CUDA(ctx, call)                                      \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+constexpr uint32_t kMaxDim = 32768;
+constexpr int32_t kMaxLights = 4096;
+
+rast_status check_index(const int32_t* tris, int64_t ntri, int64_t nv, int64_t nn, int64_t nuv, int32_t nmat,
+                        std::string& msg) {
+    if (ntri >= 0xFFFFFFFFll) {
+        msg = "too many triangles (the triangle index must fit in 32 bits)";
+        return RAST_ERR_INVALID_ARG;
+    }
+    for (int64_t i = 0; i < ntri; ++i) {
+        const int32_t* t = tris + 10 * i;
+        for (int k = 0; k < 3; ++k) {
+            if (t[k] < 0 || t[k] >= nv) {
+                msg = "triangle " + std::to_string(i) + " vertex index " + std::to_string(t[k]) + " out of range";
+                return RAST_ERR_BAD_INDEX;
+            }
+            if (t[3 + k] < 0 || t[3 + k] >= nn) {
+                msg = "triangle " + std::to_string(i) + " normal index " + std::to_string(t[3 + k]) + " out of range";
+                return RAST_ERR_BAD_INDEX;
+            }
+            if (t[6 + k] >= nuv) {
+                msg = "triangle " + std::to_string(i) + " uv index " + std::to_string(t[6 + k]) + " out of range";
+                return RAST_ERR_BAD_INDEX;
+            }
+        }
+        if (t[9] < 0 || t[9] >= nmat) {
+            msg = "triangle " + std::to_string(i) + " material " + std::to_string(t[9]) + " out of range";
+            return RAST_ERR_BAD_INDEX;
+        }
+    }
+    return RAST_OK;
+}
+
+uint32_t tile_shift(uint32_t tile) { return tile == 8 ? 3u : (tile == 16 ? 4u : 5u); }
+
+// Sizes the per-draw scratch for a width x height frame.
+rast_status ensure_scratch(rast_ctx* c, uint32_t w, uint32_t h, uint32_t tiles) {
+    const int64_t npx = (int64_t)w * h;
+    RAST_CUDA(c, c->rv.reserve(sizeof(float4) * (size_t)std::max<int64_t>(c->mesh.nv, 1)));
+    if (c->keys.bytes < sizeof(unsigned long long) * (size_t)npx) c->keys_armed_clear = false;
+    RAST_CUDA(c, c->keys.reserve(sizeof(unsigned long long) * (size_t)npx));
+    c->cap_large = std::max<int64_t>(c->mesh.ntri, 1);
+    RAST_CUDA(c, c->large.reserve(sizeof(rast::BinnedTri) * (size_t)c->cap_large));
+    RAST_CUDA(c, c->counters.reserve(sizeof(uint32_t) * (rast::kCounterHeader + 2 * (size_t)tiles)));
+    RAST_CUDA(c, c->tile_offset.reserve(sizeof(uint32_t) * ((size_t)tiles + 1)));
+    if (c->cap_entries == 0)
+        c->cap_entries = c->bin_capacity > 0 ? c->bin_capacity : std::max<int64_t>(1 << 20, 2 * c->mesh.ntri);
+    RAST_CUDA(c, c->entries.reserve(sizeof(uint32_t) * (size_t)c->cap_entries));
+    RAST_CUDA(c, c->stats.reserve(sizeof(unsigned long long) * 8));
+    return RAST_OK;
+}
+
+rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, uint32_t w, uint32_t h,
+                         uint32_t flags, uint8_t* d_rgb, float* d_depth, uint32_t* d_ids) {
+    if (!c->has_mesh) return fail(c, RAST_ERR_NO_MESH, "no mesh uploaded");
+    const uint32_t tiles_x = (w + c->tile - 1) / c->tile, tiles_y = (h + c->tile - 1) / c->tile;
+    const uint32_t n_tiles = tiles_x * tiles_y;
+    rast_status st = ensure_scratch(c, w, h, n_tiles);
+    if (st != RAST_OK) return st;
+    const bool clear = (flags & RAST_CLEAR) != 0;
+    const int64_t npx = (int64_t)w * h;
+    if (clear && (!c->keys_armed_clear || c->keys_px != npx)) {
+        if (rast::launch_arm_keys_clear(c->keys.as<unsigned long long>(), npx, c->stream) < 0)
+            return cuda_fail(c, cudaGetLastError(), "arm keys");
+    }
+    RAST_CUDA(c, cudaMemsetAsync(c->counters.ptr, 0, sizeof(uint32_t) * (rast::kCounterHeader + 2 * (size_t)n_tiles),
+                                 c->stream));
+    RAST_CUDA(c, cudaMemsetAsync(c->stats.ptr, 0, sizeof(unsigned long long) * 8, c->stream));
+
+    rast::FrameScratch s;
+    s.rv = c->rv.as<float4>();
+    s.keys = c->keys.as<unsigned long long>();
+    s.large = c->large.as<rast::BinnedTri>();
+    s.counters = c->counters.as<uint32_t>();
+    s.tile_offset = c->tile_offset.as<uint32_t>();
+    s.entries = c->entries.as<uint32_t>();
+    s.stats = c->stats.as<unsigned long long>();
+    s.cap_large = c->cap_large;
+    s.cap_entries = c->cap_entries;
+
+    rast::DrawParams p;
+    std::memcpy(p.camera.m, camera, sizeof p.camera.m);
+    std::memcpy(p.normal.m, normal, sizeof p.normal.m);
+    p.width = w;
+    p.height = h;
+    p.flags = flags;
+    p.small_max = c->small_max;
+    p.tile = c->tile;
+    p.tiles_x = tiles_x;
+    p.tiles_y = tiles_y;
+    p.nl = c->nl;
+    p.lights = c->lights.as<float>();
+    p.rgb = d_rgb;
+    p.depth = d_depth;
+    p.tri_id = d_ids;
+    const int n = rast::launch_draw(c->mesh, s, p, c->stream);
+    if (n < 0) return cuda_fail(c, cudaGetLastError(), "launch draw");
+    c->last_launches = (uint64_t)n;
+    c->keys_armed_clear = clear;
+    c->keys_px = npx;
+    return RAST_OK;
+}
+
+// Reads the device status word and clears it; grows the bin pool after an overflow.
+rast_status collect_status(rast_ctx* c) {
+    if (!c->counters.ptr) return RAST_OK;
+    uint32_t status = 0;
+    RAST_CUDA(c, cudaMemcpy(&status, c->counters.as<uint32_t>() + 1, sizeof status, cudaMemcpyDeviceToHost));
+    if (status & rast::STATUS_BIN_OVERFLOW) {
+        unsigned long long need = 0;
+        RAST_CUDA(c, cudaMemcpy(&need, c->stats.as<unsigned long long>() + rast::STAT_BIN_ENTRIES, sizeof need,
+                                cudaMemcpyDeviceToHost));
+        c->cap_entries = std::max<int64_t>((int64_t)need + (int64_t)need / 4, 2 * c->cap_entries);
+        RAST_CUDA(c, c->entries.reserve(sizeof(uint32_t) * (size_t)c->cap_entries));
+        uint32_t zero = 0;
+        RAST_CUDA(c, cudaMemcpy(c->counters.as<uint32_t>() + 1, &zero, sizeof zero, cudaMemcpyHostToDevice));
+        c->keys_armed_clear = false;
+        return fail(c, RAST_ERR_BIN_OVERFLOW, "tile-bin pool overflowed; it was grown to " +
+                                                  std::to_string(c->cap_entries) + " entries, draw again");
+    }
+    if (status) return fail(c, RAST_ERR_CUDA, "device status " + std::to_string(status));
+    return RAST_OK;
+}
+
+bool valid_matrix_args(const float* camera, const float* normal) { return camera && normal; }
+
+}  // namespace
+
+extern "C" {
+
+int rast_abi_version(void) { return RAST_ABI_VERSION; }
+
+const char* rast_status_string(rast_status s) {
+    switch (s) {
+        case RAST_OK: return "ok";
+        case RAST_ERR_INVALID_ARG: return "invalid argument";
+        case RAST_ERR_BAD_INDEX: return "index out of range";
+        case RAST_ERR_NO_MESH: return "no mesh";
+        case RAST_ERR_CUDA: return "CUDA error";
+        case RAST_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case RAST_ERR_BIN_OVERFLOW: return "tile-bin pool overflow";
+        case RAST_ERR_TIMEOUT: return "device wait timed out";
+        case RAST_ERR_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* rast_last_error(const rast_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+rast_status rast_create(rast_ctx** out, int device) {
+    if (!out) return fail(nullptr, RAST_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(nullptr, RAST_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= n) return fail(nullptr, RAST_ERR_INVALID_ARG, "device ordinal out of range");
+    DeviceGuard g(device);
+    rast_ctx* c = new rast_ctx();
+    c->device = device;
+    e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(nullptr, RAST_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    c->stream = c->own_stream;
+    *out = c;
+    return RAST_OK;
+}
+
+void rast_destroy(rast_ctx* c) {
+    if (!c) return;
+    DeviceGuard g(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (DevBuf* b : {&c->pos, &c->tris10, &c->tri_v, &c->tri_nm, &c->nrm, &c->kd, &c->lights, &c->rv, &c->keys,
+                      &c->large, &c->counters, &c->tile_offset, &c->entries, &c->stats, &c->d_rgb, &c->d_depth,
+                      &c->d_ids})
+        b->release();
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+rast_status rast_set_stream(rast_ctx* c, void* stream) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    return RAST_OK;
+}
+
+void* rast_get_stream(const rast_ctx* c) { return c ? static_cast<void*>(c->stream) : nullptr; }
+
+rast_status rast_upload_mesh(rast_ctx* c, const float* pos, int64_t nv, const float* nrm, int64_t nn, const float* uv,
+                             int64_t nuv, const int32_t* tris, int64_t ntri, const float* kd, int32_t nmat) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    if (nv < 0 || nn < 0 || nuv < 0 || ntri < 0 || nmat < 0) return fail(c, RAST_ERR_INVALID_ARG, "negative count");
+    if ((nv && !pos) || (nn && !nrm) || (nuv && !uv) || (ntri && !tris) || (nmat && !kd))
+        return fail(c, RAST_ERR_INVALID_ARG, "null array with a nonzero count");
+    std::string msg;
+    rast_status st = check_index(tris, ntri, nv, nn, nuv, nmat, msg);
+    if (st != RAST_OK) return fail(c, st, msg);
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->has_mesh = false;
+    RAST_CUDA(c, c->pos.reserve(sizeof(float) * 3 * (size_t)std::max<int64_t>(nv, 1)));
+    RAST_CUDA(c, c->nrm.reserve(sizeof(float) * 3 * (size_t)std::max<int64_t>(nn, 1)));
+    RAST_CUDA(c, c->kd.reserve(sizeof(float) * 3 * (size_t)std::max<int32_t>(nmat, 1)));
+    RAST_CUDA(c, c->tris10.reserve(sizeof(int32_t) * 10 * (size_t)std::max<int64_t>(ntri, 1)));
+    RAST_CUDA(c, c->tri_v.reserve(sizeof(int32_t) * 3 * (size_t)std::max<int64_t>(ntri, 1)));
+    RAST_CUDA(c, c->tri_nm.reserve(sizeof(int4) * (size_t)std::max<int64_t>(ntri, 1)));
+    if (nv) RAST_CUDA(c, cudaMemcpyAsync(c->pos.ptr, pos, sizeof(float) * 3 * nv, cudaMemcpyHostToDevice, c->stream));
+    if (nn) RAST_CUDA(c, cudaMemcpyAsync(c->nrm.ptr, nrm, sizeof(float) * 3 * nn, cudaMemcpyHostToDevice, c->stream));
+    if (nmat) RAST_CUDA(c, cudaMemcpyAsync(c->kd.ptr, kd, sizeof(float) * 3 * nmat, cudaMemcpyHostToDevice, c->stream));
+    if (ntri) {
+        RAST_CUDA(c, cudaMemcpyAsync(c->tris10.ptr, tris, sizeof(int32_t) * 10 * ntri, cudaMemcpyHostToDevice, c->stream));
+        if (rast::launch_split_triangles(c->tris10.as<int32_t>(), ntri, c->tri_v.as<int32_t>(), c->tri_nm.as<int4>(),
+                                         c->stream) < 0)
+            return cuda_fail(c, cudaGetLastError(), "split triangles");
+    }
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->mesh.pos = c->pos.as<float>();
+    c->mesh.tri_v = c->tri_v.as<int32_t>();
+    c->mesh.tri_nm = c->tri_nm.as<int4>();
+    c->mesh.nrm = c->nrm.as<float>();
+    c->mesh.kd = c->kd.as<float>();
+    c->mesh.nv = nv;
+    c->mesh.ntri = ntri;
+    c->mesh.nn = nn;
+    c->mesh.nmat = nmat;
+    c->has_mesh = true;
+    c->cap_entries = 0;  // re-sized for the new mesh on the next draw
+    return RAST_OK;
+}
+
+rast_status rast_set_lights(rast_ctx* c, const float* lights7, int32_t n) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    if (n < 0 || n > kMaxLights || (n && !lights7)) return fail(c, RAST_ERR_INVALID_ARG, "bad light count or pointer");
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, c->lights.reserve(sizeof(float) * 7 * (size_t)std::max(n, 1)));
+    if (n)
+        RAST_CUDA(c, cudaMemcpyAsync(c->lights.ptr, lights7, sizeof(float) * 7 * n, cudaMemcpyHostToDevice, c->stream));
+    // The host array may be reused by the caller as soon as this returns.
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->nl = n;
+    return RAST_OK;
+}
+
+rast_status rast_draw_device(rast_ctx* c, const float camera[16], const float normal[16], uint32_t w, uint32_t h,
+                             uint32_t flags, uint8_t* d_rgb, float* d_depth, uint32_t* d_ids) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    if (!valid_matrix_args(camera, normal) || !d_rgb || !d_depth)
+        return fail(c, RAST_ERR_INVALID_ARG, "null matrix or buffer");
+    if (w == 0 || h == 0 || w > kMaxDim || h > kMaxDim) return fail(c, RAST_ERR_INVALID_ARG, "frame size out of range");
+    DeviceGuard g(c->device);
+    return enqueue_draw(c, camera, normal, w, h, flags, d_rgb, d_depth, d_ids);
+}
+
+rast_status rast_draw(rast_ctx* c, const float camera[16], const float normal[16], uint32_t w, uint32_t h,
+                      uint32_t flags, uint8_t* rgb, float* depth, uint32_t* ids) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    if (!valid_matrix_args(camera, normal) || !rgb || !depth)
+        return fail(c, RAST_ERR_INVALID_ARG, "null matrix or buffer");
+    if (w == 0 || h == 0 || w > kMaxDim || h > kMaxDim) return fail(c, RAST_ERR_INVALID_ARG, "frame size out of range");
+    DeviceGuard g(c->device);
+    const size_t npx = (size_t)w * h;
+    RAST_CUDA(c, c->d_rgb.reserve(3 * npx));
+    RAST_CUDA(c, c->d_depth.reserve(sizeof(float) * npx));
+    if (ids) RAST_CUDA(c, c->d_ids.reserve(sizeof(uint32_t) * npx));
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        if (!(flags & RAST_CLEAR)) {
+            RAST_CUDA(c, cudaMemcpyAsync(c->d_rgb.ptr, rgb, 3 * npx, cudaMemcpyHostToDevice, c->stream));
+            RAST_CUDA(c, cudaMemcpyAsync(c->d_depth.ptr, depth, sizeof(float) * npx, cudaMemcpyHostToDevice, c->stream));
+        }
+        rast_status st = enqueue_draw(c, camera, normal, w, h, flags, c->d_rgb.as<uint8_t>(), c->d_depth.as<float>(),
+                                      ids ? c->d_ids.as<uint32_t>() : nullptr);
+        if (st != RAST_OK) return st;
+        RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+        st = collect_status(c);
+        if (st == RAST_ERR_BIN_OVERFLOW) continue;  // pool grown; draw again from the same inputs
+        if (st != RAST_OK) return st;
+        RAST_CUDA(c, cudaMemcpyAsync(rgb, c->d_rgb.ptr, 3 * npx, cudaMemcpyDeviceToHost, c->stream));
+        RAST_CUDA(c, cudaMemcpyAsync(depth, c->d_depth.ptr, sizeof(float) * npx, cudaMemcpyDeviceToHost, c->stream));
+        if (ids) RAST_CUDA(c, cudaMemcpyAsync(ids, c->d_ids.ptr, sizeof(uint32_t) * npx, cudaMemcpyDeviceToHost, c->stream));
+        RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+        return RAST_OK;
+    }
+    return fail(c, RAST_ERR_BIN_OVERFLOW, "tile-bin pool still overflowing after regrowth");
+}
+
+rast_status rast_sync(rast_ctx* c) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    return collect_status(c);
+}
+
+rast_status rast_get_stats(rast_ctx* c, uint64_t out[8]) {
+    if (!c || !out) return RAST_ERR_INVALID_ARG;
+    std::memset(out, 0, sizeof(uint64_t) * 8);
+    if (!c->stats.ptr) return RAST_OK;
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    unsigned long long s[8];
+    RAST_CUDA(c, cudaMemcpy(s, c->stats.ptr, sizeof s, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 8; ++i) out[i] = s[i];
+    out[rast::STAT_LAUNCHES] = c->last_launches;
+    return RAST_OK;
+}
+
+rast_status rast_set_option(rast_ctx* c, int option, int64_t value) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    switch (option) {
+        case RAST_OPT_SMALL_MAX_PIXELS:
+            if (value < 1 || value > 65536) return fail(c, RAST_ERR_INVALID_ARG, "small_max out of range");
+            c->small_max = (uint32_t)value;
+            return RAST_OK;
+        case RAST_OPT_TILE_SIZE:
+            if (value != 8 && value != 16 && value != 32) return fail(c, RAST_ERR_INVALID_ARG, "tile must be 8, 16 or 32");
+            c->tile = (uint32_t)value;
+            return RAST_OK;
+        case RAST_OPT_BIN_CAPACITY:
+            if (value < 0 || value > (int64_t)1 << 31) return fail(c, RAST_ERR_INVALID_ARG, "bin capacity out of range");
+            c->bin_capacity = value;
+            c->cap_entries = 0;
+            return RAST_OK;
+    }
+    return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
+}
+
+rast_status rast_get_option(rast_ctx* c, int option, int64_t* value) {
+    if (!c || !value) return RAST_ERR_INVALID_ARG;
+    switch (option) {
+        case RAST_OPT_SMALL_MAX_PIXELS: *value = c->small_max; return RAST_OK;
+        case RAST_OPT_TILE_SIZE: *value = c->tile; return RAST_OK;
+        case RAST_OPT_BIN_CAPACITY: *value = c->cap_entries ? c->cap_entries : c->bin_capacity; return RAST_OK;
+    }
+    return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
+}
+
+}  // extern "C"

@@ -1,0 +1,80 @@
+// Internal interface between the host side of librast (rast_api.cpp) and its kernels
+// (rast_kernels.cu). Not installed; the public interface is include/rast.h.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rast {
+
+// Raster-space vertex of the reference (geometry.cpp:135-142): x, y in pixels, NDC z, 1/w_clip.
+// Stored as float4 so a gather is one 16-byte load.
+
+// One triangle on the binned path: everything the per-tile raster needs, 64 bytes.
+struct alignas(16) BinnedTri {
+    float x0, y0, x1, y1;   // raster xy of vertices 0, 1
+    float x2, y2, z0, z1;   // raster xy of vertex 2, NDC z of vertices 0, 1
+    float z2, area, thr, sgn;  // NDC z of vertex 2; barycentric denominator; early-reject bound
+    uint32_t tri, tl, br, pad; // triangle index; bounding box corners packed as x | y << 16
+};
+
+struct Mat4 { float m[16]; };  // column major, m[c*4 + r]
+
+enum StatIndex : int {
+    STAT_FRONT = 0, STAT_TESTED = 1, STAT_INSIDE = 2, STAT_WRITTEN = 3,
+    STAT_BINNED_TRIS = 4, STAT_BIN_ENTRIES = 5, STAT_LAUNCHES = 6, STAT_RESERVED = 7
+};
+
+// Device status word bits.
+enum StatusBits : uint32_t { STATUS_BIN_OVERFLOW = 1u, STATUS_LARGE_OVERFLOW = 2u };
+
+struct DeviceMesh {
+    const float* pos = nullptr;      // nv * 3
+    const int32_t* tri_v = nullptr;  // ntri * 3 vertex indices
+    const int4* tri_nm = nullptr;    // ntri: normal indices 0..2, material
+    const float* nrm = nullptr;      // nn * 3
+    const float* kd = nullptr;       // nmat * 3
+    int64_t nv = 0, ntri = 0, nn = 0;
+    int32_t nmat = 0;
+};
+
+// Per-draw scratch owned by the context.
+struct FrameScratch {
+    float4* rv = nullptr;               // nv raster vertices
+    unsigned long long* keys = nullptr; // W*H packed (order-preserving depth << 32 | triangle)
+    BinnedTri* large = nullptr;         // binned triangles, capacity cap_large
+    uint32_t* counters = nullptr;       // [0] n_large, [1] status, [2..] tile counts, then cursors
+    uint32_t* tile_offset = nullptr;    // n_tiles + 1
+    uint32_t* entries = nullptr;        // bin entries, capacity cap_entries
+    unsigned long long* stats = nullptr;  // 8 counters
+    int64_t cap_large = 0, cap_entries = 0;
+};
+
+struct DrawParams {
+    Mat4 camera, normal;
+    uint32_t width, height;
+    uint32_t flags;
+    uint32_t small_max;     // bounding boxes up to this many pixels take the per-triangle path
+    uint32_t tile;          // tile edge: 8, 16, 32
+    uint32_t tiles_x, tiles_y;
+    int32_t nl;
+    const float* lights;    // device, nl * 7
+    uint8_t* rgb;           // device planar RGB8
+    float* depth;           // device
+    uint32_t* tri_id;       // device, nullable
+};
+
+// Number of counter words before the per-tile counts in FrameScratch::counters.
+constexpr int kCounterHeader = 4;
+
+// Launches every kernel of one draw on `stream`. Returns the number of kernel launches made
+// (memsets excluded) or -1 with cudaGetLastError() set.
+int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams& p, cudaStream_t stream);
+
+// Fills keys[0, n) with the value a cleared depth buffer (1.0) arms them with.
+int launch_arm_keys_clear(unsigned long long* keys, int64_t n, cudaStream_t stream);
+
+// Splits the reference's Triangle records (10 int32 each) into tri_v and tri_nm on the device.
+int launch_split_triangles(const int32_t* tris10, int64_t ntri, int32_t* tri_v, int4* tri_nm, cudaStream_t stream);
+
+}  // namespace rast

@@ -1,0 +1,823 @@
+// Kernels of the per-frame rasteriser path for sm_103a (GB300).
+//
+// Parity contract: coverage, depth and the winning triangle of every pixel are bit for bit those
+// of canmom/rasteriser's draw_frame (drawing.cpp:205-258). Every floating-point step that decides
+// them is one IEEE round-to-nearest operation in the reference's order, written with __f*_rn
+// intrinsics (never contracted into FMA), and the file is built with -fmad=false besides.
+//
+// Pipeline of one frame:
+//   k_vertex        transform_vertices + z_divide_all + ndc_to_raster_all (geometry.cpp:85-142)
+//   k_setup_raster  per triangle: de-index, signed_area_2d cull, bounding_box (drawing.cpp:77-93,
+//                   160-188); triangles with small boxes are rasterised here by their warp, the
+//                   rest are appended to the binned list and counted into 16x16 (8/32) tiles
+//   k_bin_scan      exclusive scan of the tile counts
+//   k_bin_scatter   binned triangles into per-tile lists
+//   k_tile_raster   one CTA per tile; each thread owns a pixel and keeps its minimum key in a
+//                   register; warp ballots skip triangles that miss a warp's 8x4 block
+//   k_resolve       per pixel: decode the winner, recompute its barycentrics, perspective-correct
+//                   normal, Lambert shading over the lights (shading.cpp:20-34), planar RGB8 +
+//                   depth writes
+//
+// Depth test: the reference keeps a fragment when `ndcdepth < depth(x,y)` while walking the
+// triangles in order (drawing.cpp:119), so a pixel ends with the smallest depth and, among equal
+// depths, the earliest triangle. Here every fragment proposes the 64-bit key
+// (order(depth) << 32 | triangle) and the pixel keeps the minimum, which is the same winner
+// whatever order the fragments arrive in.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rast_internal.h"
+
+namespace rast {
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr unsigned long long kNoWinner = 0xFFFFFFFFull;  // low word of a key with no fragment
+
+// ---------------------------------------------------------------------------------------------
+// exact arithmetic helpers
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float dvd(float a, float b) { return __fdiv_rn(a, b); }
+// glm::min / glm::max on scalars: x < y ? x : y and x > y ? x : y (NaN and -0 follow from this).
+__device__ __forceinline__ float gmin(float x, float y) { return x < y ? x : y; }
+__device__ __forceinline__ float gmax(float x, float y) { return x > y ? x : y; }
+
+// Row r of mat4 * vec4, summed (c0*x + c1*y) + (c2*z + c3*w).
+__device__ __forceinline__ float mrow(const Mat4& M, int r, float x, float y, float z, float w) {
+    const float lo = add(mul(M.m[r], x), mul(M.m[4 + r], y));
+    const float hi = add(mul(M.m[8 + r], z), mul(M.m[12 + r], w));
+    return add(lo, hi);
+}
+
+// Total order on non-NaN floats that matches `<`, with -0 and +0 equal.
+__device__ __forceinline__ uint32_t depth_order(float z) {
+    uint32_t u = __float_as_uint(z);
+    u = (u == 0x80000000u) ? 0u : u;
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// Initial key of a pixel whose depth buffer holds d: a fragment (z, t) beats it exactly when
+// z < d. For NaN d nothing may pass, and the key sits below every fragment key.
+__device__ __forceinline__ unsigned long long arm_key(float d) {
+    if (d != d) return kNoWinner;
+    return (static_cast<unsigned long long>(depth_order(d)) << 32) - 1ull;
+}
+
+__device__ __forceinline__ unsigned long long frag_key(float z, uint32_t tri) {
+    return (static_cast<unsigned long long>(depth_order(z)) << 32) | tri;
+}
+
+// Edge-function data of one triangle (drawing.cpp:36-49): the vertex deltas are the same
+// subtractions the reference repeats for every pixel, taken once.
+struct EdgeTri {
+    float x0, y0, x1, y1, x2, y2;
+    float d12x, d12y, d20x, d20y, d01x, d01y;
+    float z0, z1, z2, area, nthr, sgn;
+};
+
+__device__ __forceinline__ void make_edge_tri(float4 a, float4 b, float4 c, EdgeTri& T) {
+    T.x0 = a.x; T.y0 = a.y; T.x1 = b.x; T.y1 = b.y; T.x2 = c.x; T.y2 = c.y;
+    T.z0 = a.z; T.z1 = b.z; T.z2 = c.z;
+    T.d12x = sub(c.x, b.x); T.d12y = sub(c.y, b.y);
+    T.d20x = sub(a.x, c.x); T.d20y = sub(a.y, c.y);
+    T.d01x = sub(b.x, a.x); T.d01y = sub(b.y, a.y);
+    // area = edge(v2, v0, v1) = (v1.x-v0.x)*(v2.y-v0.y) - (v1.y-v0.y)*(v2.x-v0.x)
+    T.area = sub(mul(T.d01x, sub(c.y, a.y)), mul(T.d01y, sub(c.x, a.x)));
+    // Early reject: when |area| is a normal number >= 2^-26, an edge value e with
+    // sgn(area)*e < -|area|*2^-100 gives e/area <= -2^-100 after rounding, so that barycentric is
+    // negative and the pixel is outside; such pixels skip the three divisions. Every other pixel
+    // takes the reference's divisions. The bound is exact (a power-of-two scale of a normal).
+    const float aa = fabsf(T.area);
+    if (aa >= 0x1p-26f && aa < __int_as_float(0x7f800000)) {
+        T.nthr = -mul(aa, 0x1p-100f);
+        T.sgn = T.area > 0.f ? 1.f : -1.f;
+    } else {
+        T.nthr = __int_as_float(0xff800000);  // -inf: never rejects early
+        T.sgn = 1.f;
+    }
+}
+
+// update_pixel's barycentric and inside test (drawing.cpp:108-111) at integer pixel (px, py).
+__device__ __forceinline__ bool inside_test(const EdgeTri& T, float px, float py, float& b0, float& b1,
+                                            float& b2) {
+    const float e0 = sub(mul(T.d12x, sub(py, T.y1)), mul(T.d12y, sub(px, T.x1)));
+    const float e1 = sub(mul(T.d20x, sub(py, T.y2)), mul(T.d20y, sub(px, T.x2)));
+    const float e2 = sub(mul(T.d01x, sub(py, T.y0)), mul(T.d01y, sub(px, T.x0)));
+    if (mul(T.sgn, e0) < T.nthr || mul(T.sgn, e1) < T.nthr || mul(T.sgn, e2) < T.nthr) return false;
+    b0 = dvd(e0, T.area);
+    b1 = dvd(e1, T.area);
+    b2 = dvd(e2, T.area);
+    return b0 >= 0.f && b1 >= 0.f && b2 >= 0.f;
+}
+
+// screen_interpolate of the NDC depths (drawing.cpp:51-56, 115-116).
+__device__ __forceinline__ float interp_depth(const EdgeTri& T, float b0, float b1, float b2) {
+    return add(add(mul(T.z0, b0), mul(T.z1, b1)), mul(T.z2, b2));
+}
+
+// bounding_box (drawing.cpp:77-93): truncated clamp of the min corner, clamp of the ceiled max
+// corner, both to [0, W-1] x [0, H-1].
+__device__ __forceinline__ void bounding_box(float4 a, float4 b, float4 c, float lim_x, float lim_y,
+                                             uint32_t& tlx, uint32_t& tly, uint32_t& brx, uint32_t& bry) {
+    const float mnx = gmin(gmin(a.x, b.x), c.x), mny = gmin(gmin(a.y, b.y), c.y);
+    const float mxx = gmax(gmax(a.x, b.x), c.x), mxy = gmax(gmax(a.y, b.y), c.y);
+    tlx = __float2uint_rz(gmin(gmax(mnx, 0.f), lim_x));
+    tly = __float2uint_rz(gmin(gmax(mny, 0.f), lim_y));
+    brx = __float2uint_rz(gmin(gmax(ceilf(mxx), 0.f), lim_x));
+    bry = __float2uint_rz(gmin(gmax(ceilf(mxy), 0.f), lim_y));
+}
+
+// signed_area_2d (geometry.cpp:76-83), summed left to right, and the culling rule
+// (drawing.cpp:176-178).
+__device__ __forceinline__ bool front_facing(float4 a, float4 b, float4 c, bool cw) {
+    float s = mul(a.x, b.y);
+    s = sub(s, mul(b.x, a.y));
+    s = add(s, mul(b.x, c.y));
+    s = sub(s, mul(c.x, b.y));
+    s = add(s, mul(c.x, a.y));
+    s = sub(s, mul(a.x, c.y));
+    const float sa = mul(-0.5f, s);
+    return (sa > 0.f) != cw;
+}
+
+__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t n = __shfl_up_sync(kFull, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+// First lane j whose inclusive prefix exceeds k (the owner of work item k).
+__device__ __forceinline__ int owner_of(const uint32_t* incl, uint32_t k) {
+    int lo = 0, hi = 31;
+#pragma unroll
+    for (int it = 0; it < 5; ++it) {
+        const int mid = (lo + hi) >> 1;
+        if (incl[mid] > k) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+// q = n / d for n <= 2^24, d >= 1: a float-reciprocal estimate (within 2 of the quotient at
+// that range) corrected to the exact quotient.
+__device__ __forceinline__ uint32_t div_small(uint32_t n, uint32_t d, float rd) {
+    uint32_t q = __float2uint_rz(__fmul_rn(__uint2float_rn(n), rd));
+    while (q > 0u && q * d > n) --q;
+    while ((q + 1u) * d <= n) ++q;
+    return q;
+}
+
+// ---------------------------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------------------------
+
+// Vertex stage: clip = camera * (x, y, z, 1); (x/w, y/w, z/w, 1/w); x, y to raster pixels with
+// the y flip (geometry.cpp:44-74).
+__global__ void __launch_bounds__(256) k_vertex(const float* __restrict__ pos, int64_t nv, Mat4 cam, float wf,
+                                                float hf, float4* __restrict__ rv) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
+        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        const float cx = mrow(cam, 0, x, y, z, 1.f);
+        const float cy = mrow(cam, 1, x, y, z, 1.f);
+        const float cz = mrow(cam, 2, x, y, z, 1.f);
+        const float cw = mrow(cam, 3, x, y, z, 1.f);
+        const float nx = dvd(cx, cw), ny = dvd(cy, cw), nz = dvd(cz, cw), iw = dvd(1.f, cw);
+        const float X = mul(mul(0.5f, add(nx, 1.0f)), wf);
+        const float Y = mul(mul(0.5f, add(-ny, 1.0f)), hf);
+        rv[i] = make_float4(X, Y, nz, iw);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_arm_from_depth(const float* __restrict__ depth, int64_t n,
+                                                        unsigned long long* __restrict__ keys) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        keys[i] = arm_key(depth[i]);
+}
+
+__global__ void __launch_bounds__(256) k_arm_clear(unsigned long long* __restrict__ keys, int64_t n) {
+    const unsigned long long v = arm_key(1.0f);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        keys[i] = v;
+}
+
+__global__ void __launch_bounds__(256) k_split_triangles(const int32_t* __restrict__ tris10, int64_t ntri,
+                                                         int32_t* __restrict__ tri_v, int4* __restrict__ tri_nm) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ntri; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t* t = tris10 + 10 * i;
+        tri_v[3 * i] = t[0];
+        tri_v[3 * i + 1] = t[1];
+        tri_v[3 * i + 2] = t[2];
+        tri_nm[i] = make_int4(t[3], t[4], t[5], t[9]);
+    }
+}
+
+constexpr int kSetupThreads = 256;
+constexpr int kSetupWarps = kSetupThreads / 32;
+
+// Per-warp staging of 32 triangles for the cooperative pixel loop (structure of arrays, so lanes
+// reading different triangles hit different banks).
+struct SetupStage {
+    float x0[32], y0[32], x1[32], y1[32], x2[32], y2[32];
+    float d12x[32], d12y[32], d20x[32], d20y[32], d01x[32], d01y[32];
+    float z0[32], z1[32], z2[32], area[32], nthr[32], sgn[32], rbw[32];
+    uint32_t tlx[32], tly[32], bw[32], incl[32];
+};
+
+struct SetupArgs {
+    const int32_t* tri_v;
+    const float4* rv;
+    int64_t ntri;
+    float lim_x, lim_y;
+    uint32_t width, height;
+    uint32_t small_max;
+    uint32_t tile_shift;
+    uint32_t tiles_x, n_tiles;
+    bool cw;
+    unsigned long long* keys;
+    BinnedTri* large;
+    int64_t cap_large;
+    uint32_t* counters;  // [0] n_large, [1] status, then tile counts
+    unsigned long long* stats;
+};
+
+// One thread per triangle. Front-facing triangles whose bounding box holds at most small_max
+// pixels are rasterised by their warp: the 32 boxes are laid end to end and the warp walks the
+// concatenation 32 pixels at a time, so lanes stay busy whatever the box sizes. Larger triangles
+// go to the binned list, and their warp adds them to the tile counts the same way.
+__global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
+    __shared__ SetupStage stage[kSetupWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    SetupStage& S = stage[warp];
+    const int64_t t = blockIdx.x * (int64_t)kSetupThreads + threadIdx.x;
+
+    uint32_t n_small = 0, n_tiles = 0;
+    uint32_t tlx = 0, tly = 0, brx = 0, bry = 0;
+    EdgeTri T;
+    unsigned long long c_front = 0;
+    bool large = false;
+    if (t < a.ntri) {
+        const int32_t i0 = a.tri_v[3 * t], i1 = a.tri_v[3 * t + 1], i2 = a.tri_v[3 * t + 2];
+        const float4 v0 = a.rv[i0], v1 = a.rv[i1], v2 = a.rv[i2];
+        if (front_facing(v0, v1, v2, a.cw)) {
+            c_front = 1;
+            bounding_box(v0, v1, v2, a.lim_x, a.lim_y, tlx, tly, brx, bry);
+            const uint32_t bw = brx - tlx + 1u, bh = bry - tly + 1u;
+            const unsigned long long npx = (unsigned long long)bw * bh;
+            make_edge_tri(v0, v1, v2, T);
+            if (npx <= a.small_max) {
+                n_small = (uint32_t)npx;
+            } else {
+                large = true;
+            }
+        }
+    }
+
+    // Binned path: append, and count the tiles the box overlaps.
+    const unsigned lmask = __ballot_sync(kFull, large);
+    if (lmask) {
+        uint32_t base = 0;
+        if (lane == __ffs(lmask) - 1) base = atomicAdd(&a.counters[0], (uint32_t)__popc(lmask));
+        base = __shfl_sync(kFull, base, __ffs(lmask) - 1);
+        if (large) {
+            const uint32_t slot = base + __popc(lmask & ((1u << lane) - 1u));
+            if (slot < a.cap_large) {
+                BinnedTri r;
+                r.x0 = T.x0; r.y0 = T.y0; r.x1 = T.x1; r.y1 = T.y1;
+                r.x2 = T.x2; r.y2 = T.y2; r.z0 = T.z0; r.z1 = T.z1;
+                r.z2 = T.z2; r.area = T.area; r.thr = T.nthr; r.sgn = T.sgn;
+                r.tri = (uint32_t)t; r.tl = tlx | (tly << 16); r.br = brx | (bry << 16); r.pad = 0;
+                a.large[slot] = r;
+                const uint32_t tx0 = tlx >> a.tile_shift, tx1 = brx >> a.tile_shift;
+                const uint32_t ty0 = tly >> a.tile_shift, ty1 = bry >> a.tile_shift;
+                n_tiles = (tx1 - tx0 + 1u) * (ty1 - ty0 + 1u);
+            } else {
+                atomicOr(&a.counters[1], STATUS_LARGE_OVERFLOW);
+            }
+        }
+    }
+
+    unsigned long long c_tested = 0, c_inside = 0;
+
+    // Cooperative pixel loop over the warp's small triangles.
+    {
+        const uint32_t incl = warp_inclusive_scan(n_small, lane);
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        if (total) {
+            S.x0[lane] = T.x0; S.y0[lane] = T.y0; S.x1[lane] = T.x1; S.y1[lane] = T.y1;
+            S.x2[lane] = T.x2; S.y2[lane] = T.y2;
+            S.d12x[lane] = T.d12x; S.d12y[lane] = T.d12y; S.d20x[lane] = T.d20x; S.d20y[lane] = T.d20y;
+            S.d01x[lane] = T.d01x; S.d01y[lane] = T.d01y;
+            S.z0[lane] = T.z0; S.z1[lane] = T.z1; S.z2[lane] = T.z2;
+            S.area[lane] = T.area; S.nthr[lane] = T.nthr; S.sgn[lane] = T.sgn;
+            const uint32_t bw = brx - tlx + 1u;
+            S.tlx[lane] = tlx; S.tly[lane] = tly; S.bw[lane] = bw;
+            S.rbw[lane] = __frcp_rn((float)bw);
+            S.incl[lane] = incl;
+            __syncwarp();
+            const uint32_t tri_base = (uint32_t)(blockIdx.x * (int64_t)kSetupThreads + warp * 32);
+            for (uint32_t base = 0; base < total; base += 32) {
+                const uint32_t k = base + lane;
+                if (k < total) {
+                    const int j = owner_of(S.incl, k);
+                    const uint32_t start = j ? S.incl[j - 1] : 0u;
+                    const uint32_t local = k - start;
+                    const uint32_t w = S.bw[j];
+                    const uint32_t dy = div_small(local, w, S.rbw[j]);
+                    const uint32_t x = S.tlx[j] + (local - dy * w), y = S.tly[j] + dy;
+                    EdgeTri U;
+                    U.x0 = S.x0[j]; U.y0 = S.y0[j]; U.x1 = S.x1[j]; U.y1 = S.y1[j]; U.x2 = S.x2[j]; U.y2 = S.y2[j];
+                    U.d12x = S.d12x[j]; U.d12y = S.d12y[j]; U.d20x = S.d20x[j]; U.d20y = S.d20y[j];
+                    U.d01x = S.d01x[j]; U.d01y = S.d01y[j];
+                    U.area = S.area[j]; U.nthr = S.nthr[j]; U.sgn = S.sgn[j];
+                    float b0, b1, b2;
+                    ++c_tested;
+                    if (inside_test(U, (float)x, (float)y, b0, b1, b2)) {
+                        ++c_inside;
+                        U.z0 = S.z0[j]; U.z1 = S.z1[j]; U.z2 = S.z2[j];
+                        const float z = interp_depth(U, b0, b1, b2);
+                        if (z == z && x < a.width && y < a.height)
+                            atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + (uint32_t)j));
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+
+    // Cooperative tile counting over the warp's binned triangles.
+    {
+        const uint32_t incl = warp_inclusive_scan(n_tiles, lane);
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        if (total) {
+            const uint32_t tx0 = tlx >> a.tile_shift, tx1 = brx >> a.tile_shift;
+            S.tlx[lane] = tx0; S.tly[lane] = tly >> a.tile_shift;
+            S.bw[lane] = tx1 - tx0 + 1u;
+            S.rbw[lane] = __frcp_rn((float)(tx1 - tx0 + 1u));
+            S.incl[lane] = incl;
+            __syncwarp();
+            for (uint32_t base = 0; base < total; base += 32) {
+                const uint32_t k = base + lane;
+                if (k < total) {
+                    const int j = owner_of(S.incl, k);
+                    const uint32_t local = k - (j ? S.incl[j - 1] : 0u);
+                    const uint32_t w = S.bw[j];
+                    const uint32_t dy = div_small(local, w, S.rbw[j]);
+                    const uint32_t tile = (S.tly[j] + dy) * a.tiles_x + S.tlx[j] + (local - dy * w);
+                    if (tile < a.n_tiles) atomicAdd(&a.counters[kCounterHeader + tile], 1u);
+                }
+            }
+        }
+    }
+
+    c_front = warp_sum64(c_front);
+    c_tested = warp_sum64(c_tested);
+    c_inside = warp_sum64(c_inside);
+    if (lane == 0) {
+        if (c_front) atomicAdd(&a.stats[STAT_FRONT], c_front);
+        if (c_tested) atomicAdd(&a.stats[STAT_TESTED], c_tested);
+        if (c_inside) atomicAdd(&a.stats[STAT_INSIDE], c_inside);
+    }
+}
+
+// Exclusive scan of the per-tile counts into tile_offset[0..n_tiles]; one CTA of 1024 threads
+// walks the counts 4096 at a time. Flags an overflow of the bin pool.
+__global__ void __launch_bounds__(1024) k_bin_scan(const uint32_t* __restrict__ counters, uint32_t n_tiles,
+                                                   uint32_t* __restrict__ offset, int64_t cap_entries,
+                                                   uint32_t* __restrict__ status, unsigned long long* stats) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t carry_s;
+    const uint32_t* cnt = counters + kCounterHeader;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) carry_s = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n_tiles; base += 4096) {
+        uint32_t v[4];
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = base + tid * 4 + k;
+            v[k] = i < n_tiles ? cnt[i] : 0u;
+            s += v[k];
+        }
+        const uint32_t incl = warp_inclusive_scan(s, lane);
+        if (lane == 31) warp_tot[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = warp_tot[lane];
+            warp_tot[lane] = warp_inclusive_scan(w, lane) - w;
+        }
+        __syncthreads();
+        uint32_t run = carry_s + warp_tot[warp] + incl - s;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = base + tid * 4 + k;
+            if (i < n_tiles) offset[i] = run;
+            run += v[k];
+        }
+        __syncthreads();
+        if (tid == 1023) carry_s = run;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        offset[n_tiles] = carry_s;
+        stats[STAT_BIN_ENTRIES] = carry_s;
+        if ((int64_t)carry_s > cap_entries) atomicOr(status, STATUS_BIN_OVERFLOW);
+    }
+}
+
+struct ScatterArgs {
+    const BinnedTri* large;
+    uint32_t n_tiles;
+    const uint32_t* counters;  // [0] n_large
+    uint32_t* cursors;         // n_tiles, zeroed
+    const uint32_t* offset;
+    uint32_t* entries;
+    int64_t cap_large, cap_entries;
+    uint32_t tile_shift, tiles_x;
+    unsigned long long* stats;
+};
+
+// Writes every binned triangle's index into the lists of the tiles its box overlaps. Lanes of a
+// warp share the work of their 32 triangles' tiles, as in k_setup_raster.
+__global__ void __launch_bounds__(256) k_bin_scatter(ScatterArgs a) {
+    __shared__ uint32_t s_tx0[8][32], s_ty0[8][32], s_tw[8][32], s_incl[8][32];
+    __shared__ float s_rtw[8][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t n_large = (uint32_t)min((int64_t)a.counters[0], a.cap_large);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.stats[STAT_BINNED_TRIS] = n_large;
+    for (uint32_t wb = (blockIdx.x * 256u + warp * 32u); wb < n_large; wb += gridDim.x * 256u) {
+        const uint32_t i = wb + lane;
+        uint32_t n = 0, tx0 = 0, ty0 = 0, tw = 1;
+        if (i < n_large) {
+            const uint32_t tl = a.large[i].tl, br = a.large[i].br;
+            tx0 = (tl & 0xFFFFu) >> a.tile_shift;
+            ty0 = (tl >> 16) >> a.tile_shift;
+            const uint32_t tx1 = (br & 0xFFFFu) >> a.tile_shift, ty1 = (br >> 16) >> a.tile_shift;
+            tw = tx1 - tx0 + 1u;
+            n = tw * (ty1 - ty0 + 1u);
+        }
+        const uint32_t incl = warp_inclusive_scan(n, lane);
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        s_tx0[warp][lane] = tx0; s_ty0[warp][lane] = ty0; s_tw[warp][lane] = tw;
+        s_rtw[warp][lane] = __frcp_rn((float)tw); s_incl[warp][lane] = incl;
+        __syncwarp();
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t k = base + lane;
+            if (k < total) {
+                const int j = owner_of(s_incl[warp], k);
+                const uint32_t local = k - (j ? s_incl[warp][j - 1] : 0u);
+                const uint32_t w = s_tw[warp][j];
+                const uint32_t dy = div_small(local, w, s_rtw[warp][j]);
+                const uint32_t tile = (s_ty0[warp][j] + dy) * a.tiles_x + s_tx0[warp][j] + (local - dy * w);
+                if (tile < a.n_tiles) {
+                    const uint32_t pos = a.offset[tile] + atomicAdd(&a.cursors[tile], 1u);
+                    if ((int64_t)pos < a.cap_entries) a.entries[pos] = wb + (uint32_t)j;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+constexpr int kTileChunk = 256;
+
+struct TileStage {
+    float x0[kTileChunk], y0[kTileChunk], x1[kTileChunk], y1[kTileChunk], x2[kTileChunk], y2[kTileChunk];
+    float d12x[kTileChunk], d12y[kTileChunk], d20x[kTileChunk], d20y[kTileChunk], d01x[kTileChunk],
+        d01y[kTileChunk];
+    float z0[kTileChunk], z1[kTileChunk], z2[kTileChunk], area[kTileChunk], nthr[kTileChunk], sgn[kTileChunk];
+    uint32_t tri[kTileChunk], tl[kTileChunk], br[kTileChunk];
+};
+
+struct TileArgs {
+    const BinnedTri* large;
+    const uint32_t* counters;  // tile counts after kCounterHeader
+    const uint32_t* offset;
+    const uint32_t* entries;
+    int64_t cap_entries;
+    unsigned long long* keys;
+    uint32_t width, height, tiles_x;
+    unsigned long long* stats;
+};
+
+// One CTA per TS x TS tile; each thread owns PPT pixels (a warp covers an 8x4 block per pixel
+// slot) and keeps their minimum keys in registers, so the tile needs no atomics. The per-triangle
+// pass of k_setup_raster ran earlier on the stream, so the tile's keys are final apart from this
+// CTA and are read and written back plainly.
+template <int TS>
+__global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
+    constexpr int kThreads = (TS * TS < 256) ? TS * TS : 256;
+    constexpr int kPPT = (TS * TS) / kThreads;  // pixels per thread
+    constexpr int kBlocksX = TS / 8;             // 8x4 blocks across a tile
+    __shared__ TileStage S;
+    const uint32_t tile = blockIdx.x;
+    const uint32_t count = a.counters[kCounterHeader + tile];
+    if (count == 0) return;
+    const uint32_t first = a.offset[tile];
+    const uint32_t tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    uint32_t px[kPPT], py[kPPT];
+    bool valid[kPPT];
+    unsigned long long best[kPPT], orig[kPPT];
+#pragma unroll
+    for (int s = 0; s < kPPT; ++s) {
+        const int blk = warp + s * (kThreads / 32);
+        px[s] = tx * TS + (blk % kBlocksX) * 8 + (lane & 7);
+        py[s] = ty * TS + (blk / kBlocksX) * 4 + (lane >> 3);
+        valid[s] = px[s] < a.width && py[s] < a.height;
+        orig[s] = valid[s] ? a.keys[(size_t)py[s] * a.width + px[s]] : ~0ull;
+        best[s] = orig[s];
+    }
+    unsigned long long c_tested = 0, c_inside = 0;
+
+    for (uint32_t c0 = 0; c0 < count; c0 += kTileChunk) {
+        const uint32_t n = min((uint32_t)kTileChunk, count - c0);
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += kThreads) {
+            const uint32_t e = first + c0 + i;
+            const BinnedTri r = a.large[(int64_t)e < a.cap_entries ? a.entries[e] : 0];
+            S.x0[i] = r.x0; S.y0[i] = r.y0; S.x1[i] = r.x1; S.y1[i] = r.y1; S.x2[i] = r.x2; S.y2[i] = r.y2;
+            S.d12x[i] = sub(r.x2, r.x1); S.d12y[i] = sub(r.y2, r.y1);
+            S.d20x[i] = sub(r.x0, r.x2); S.d20y[i] = sub(r.y0, r.y2);
+            S.d01x[i] = sub(r.x1, r.x0); S.d01y[i] = sub(r.y1, r.y0);
+            S.z0[i] = r.z0; S.z1[i] = r.z1; S.z2[i] = r.z2;
+            S.area[i] = r.area; S.nthr[i] = r.thr; S.sgn[i] = r.sgn;
+            S.tri[i] = r.tri; S.tl[i] = r.tl; S.br[i] = r.br;
+        }
+        __syncthreads();
+        for (uint32_t j = 0; j < n; ++j) {
+            const uint32_t tl = S.tl[j], br = S.br[j];
+            const uint32_t tlx = tl & 0xFFFFu, tly = tl >> 16, brx = br & 0xFFFFu, bry = br >> 16;
+#pragma unroll
+            for (int s = 0; s < kPPT; ++s) {
+                const bool in_box = valid[s] && px[s] >= tlx && px[s] <= brx && py[s] >= tly && py[s] <= bry;
+                if (!__any_sync(kFull, in_box)) continue;
+                bool covered = false;
+                if (in_box) {
+                    EdgeTri U;
+                    U.x0 = S.x0[j]; U.y0 = S.y0[j]; U.x1 = S.x1[j]; U.y1 = S.y1[j]; U.x2 = S.x2[j]; U.y2 = S.y2[j];
+                    U.d12x = S.d12x[j]; U.d12y = S.d12y[j]; U.d20x = S.d20x[j]; U.d20y = S.d20y[j];
+                    U.d01x = S.d01x[j]; U.d01y = S.d01y[j];
+                    U.area = S.area[j]; U.nthr = S.nthr[j]; U.sgn = S.sgn[j];
+                    float b0, b1, b2;
+                    ++c_tested;
+                    if (inside_test(U, (float)px[s], (float)py[s], b0, b1, b2)) {
+                        covered = true;
+                        U.z0 = S.z0[j]; U.z1 = S.z1[j]; U.z2 = S.z2[j];
+                        const float z = interp_depth(U, b0, b1, b2);
+                        if (z == z) {
+                            const unsigned long long k = frag_key(z, S.tri[j]);
+                            best[s] = k < best[s] ? k : best[s];
+                        }
+                    }
+                }
+                // Coverage mask of the warp's 8x4 block for this triangle.
+                const unsigned mask = __ballot_sync(kFull, covered);
+                if (lane == 0) c_inside += __popc(mask);
+            }
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < kPPT; ++s)
+        if (valid[s] && best[s] != orig[s]) a.keys[(size_t)py[s] * a.width + px[s]] = best[s];
+
+    c_tested = warp_sum64(c_tested);
+    if (lane == 0) {
+        atomicAdd(&a.stats[STAT_TESTED], c_tested);
+        atomicAdd(&a.stats[STAT_INSIDE], c_inside);
+    }
+}
+
+struct ResolveArgs {
+    const unsigned long long* keys;
+    unsigned long long* keys_rearm;  // non-null in clear mode: keys are re-armed for the next frame
+    const int32_t* tri_v;
+    const int4* tri_nm;
+    const float4* rv;
+    const float* nrm;
+    const float* kd;
+    const float* lights;
+    int32_t nl;
+    Mat4 normal;
+    uint32_t width;
+    int64_t npx;
+    bool cw, clear;
+    uint8_t* rgb;
+    float* depth;
+    uint32_t* tri_id;
+    unsigned long long* stats;
+};
+
+// transform_direction with the normal matrix (geometry.cpp:35-42, 97-108).
+__device__ __forceinline__ float3 camera_normal(const Mat4& M, const float* n) {
+    const float x = n[0], y = n[1], z = n[2];
+    return make_float3(mrow(M, 0, x, y, z, 0.f), mrow(M, 1, x, y, z, 0.f), mrow(M, 2, x, y, z, 0.f));
+}
+
+// Per pixel: the winning triangle's fragment is recomputed and shaded exactly as update_pixel
+// shades it (drawing.cpp:108-146, shading.cpp:20-34).
+__global__ void __launch_bounds__(256) k_resolve(ResolveArgs a) {
+    const unsigned long long rearm = arm_key(1.0f);
+    unsigned long long written = 0;
+    const int64_t plane = a.npx;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.npx; p += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long key = a.keys[p];
+        if (a.keys_rearm) a.keys_rearm[p] = rearm;
+        const uint32_t t = (uint32_t)(key & 0xFFFFFFFFull);
+        if (t == 0xFFFFFFFFu) {
+            if (a.clear) {
+                a.rgb[p] = 0; a.rgb[p + plane] = 0; a.rgb[p + 2 * plane] = 0;
+                a.depth[p] = 1.0f;
+            }
+            if (a.tri_id) a.tri_id[p] = 0xFFFFFFFFu;
+            continue;
+        }
+        ++written;
+        const uint32_t y = (uint32_t)(p / a.width), x = (uint32_t)(p - (int64_t)y * a.width);
+        const float4 v0 = a.rv[a.tri_v[3 * (int64_t)t]], v1 = a.rv[a.tri_v[3 * (int64_t)t + 1]],
+                     v2 = a.rv[a.tri_v[3 * (int64_t)t + 2]];
+        EdgeTri T;
+        make_edge_tri(v0, v1, v2, T);
+        const float pxf = (float)x, pyf = (float)y;
+        const float e0 = sub(mul(T.d12x, sub(pyf, T.y1)), mul(T.d12y, sub(pxf, T.x1)));
+        const float e1 = sub(mul(T.d20x, sub(pyf, T.y2)), mul(T.d20y, sub(pxf, T.x2)));
+        const float e2 = sub(mul(T.d01x, sub(pyf, T.y0)), mul(T.d01y, sub(pxf, T.x0)));
+        const float b0 = dvd(e0, T.area), b1 = dvd(e1, T.area), b2 = dvd(e2, T.area);
+        a.depth[p] = interp_depth(T, b0, b1, b2);
+        if (a.tri_id) a.tri_id[p] = t;
+
+        // drawing.cpp:125-132: perspective-correct, normalised normal.
+        const int4 nm = a.tri_nm[t];
+        const float3 n0 = camera_normal(a.normal, a.nrm + 3 * (int64_t)nm.x);
+        const float3 n1 = camera_normal(a.normal, a.nrm + 3 * (int64_t)nm.y);
+        const float3 n2 = camera_normal(a.normal, a.nrm + 3 * (int64_t)nm.z);
+        const float i0 = mul(v0.w, b0), i1 = mul(v1.w, b1), i2 = mul(v2.w, b2);
+        const float dd = dvd(1.f, add(add(i0, i1), i2));
+        float sx = add(add(mul(i0, n0.x), mul(i1, n1.x)), mul(i2, n2.x));
+        float sy = add(add(mul(i0, n0.y), mul(i1, n1.y)), mul(i2, n2.y));
+        float sz = add(add(mul(i0, n0.z), mul(i1, n1.z)), mul(i2, n2.z));
+        sx = mul(dd, sx); sy = mul(dd, sy); sz = mul(dd, sz);
+        const float inv = dvd(1.0f, __fsqrt_rn(add(add(mul(sx, sx), mul(sy, sy)), mul(sz, sz))));
+        float nx = mul(sx, inv), ny = mul(sy, inv), nz = mul(sz, inv);
+        if (a.cw) { nx = -nx; ny = -ny; nz = -nz; }
+
+        // shading.cpp:20-34 with the material's constant albedo (material.cpp:24).
+        const float* kd = a.kd + 3 * (int64_t)nm.w;
+        const float ar = kd[0], ag = kd[1], ab = kd[2];
+        const float one_over_pi = 0.318309886183790671537767526745028724f;
+        float accr = 0.f, accg = 0.f, accb = 0.f;
+        for (int l = 0; l < a.nl; ++l) {
+            const float* L = a.lights + 7 * l;
+            const float I = __ldg(L + 3);
+            float cr = mul(I, __ldg(L + 4)), cg = mul(I, __ldg(L + 5)), cb = mul(I, __ldg(L + 6));
+            cr = mul(cr, ar); cg = mul(cg, ag); cb = mul(cb, ab);
+            const float d = add(add(mul(nx, -__ldg(L)), mul(ny, -__ldg(L + 1))), mul(nz, -__ldg(L + 2)));
+            const float m = gmax(0.f, d);
+            cr = mul(mul(cr, m), one_over_pi);
+            cg = mul(mul(cg, m), one_over_pi);
+            cb = mul(mul(cb, m), one_over_pi);
+            accr = add(accr, cr); accg = add(accg, cg); accb = add(accb, cb);
+        }
+        a.rgb[p] = (uint8_t)__float2uint_rz(gmin(accr, 255.f));
+        a.rgb[p + plane] = (uint8_t)__float2uint_rz(gmin(accg, 255.f));
+        a.rgb[p + 2 * plane] = (uint8_t)__float2uint_rz(gmin(accb, 255.f));
+    }
+    written = warp_sum64(written);
+    if ((threadIdx.x & 31) == 0 && written) atomicAdd(&a.stats[STAT_WRITTEN], written);
+}
+
+int grid_for(int64_t n, int threads, int max_blocks) {
+    int64_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    return (int)(b < max_blocks ? b : max_blocks);
+}
+
+template <int TS>
+void launch_tile(const TileArgs& ta, uint32_t n_tiles, cudaStream_t stream) {
+    constexpr int kThreads = (TS * TS < 256) ? TS * TS : 256;
+    k_tile_raster<TS><<<n_tiles, kThreads, 0, stream>>>(ta);
+}
+
+}  // namespace
+
+int launch_split_triangles(const int32_t* tris10, int64_t ntri, int32_t* tri_v, int4* tri_nm, cudaStream_t stream) {
+    k_split_triangles<<<grid_for(ntri, 256, 1 << 16), 256, 0, stream>>>(tris10, ntri, tri_v, tri_nm);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_arm_keys_clear(unsigned long long* keys, int64_t n, cudaStream_t stream) {
+    k_arm_clear<<<grid_for(n, 256, 1 << 16), 256, 0, stream>>>(keys, n);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams& p, cudaStream_t stream) {
+    const bool clear = (p.flags & 2u) != 0;  // RAST_CLEAR
+    const bool cw = (p.flags & 1u) != 0;     // RAST_WIND_CLOCKWISE
+    const int64_t npx = (int64_t)p.width * p.height;
+    const uint32_t n_tiles = p.tiles_x * p.tiles_y;
+    const uint32_t shift = p.tile == 8 ? 3u : (p.tile == 16 ? 4u : 5u);
+    int launches = 0;
+
+    if (!clear) {
+        k_arm_from_depth<<<grid_for(npx, 256, 1 << 16), 256, 0, stream>>>(p.depth, npx, s.keys);
+        ++launches;
+    }
+    k_vertex<<<grid_for(mesh.nv, 256, 1 << 16), 256, 0, stream>>>(mesh.pos, mesh.nv, p.camera, (float)(int)p.width,
+                                                                   (float)(int)p.height, s.rv);
+    ++launches;
+
+    SetupArgs sa;
+    sa.tri_v = mesh.tri_v;
+    sa.rv = s.rv;
+    sa.ntri = mesh.ntri;
+    sa.lim_x = (float)(p.width - 1u);
+    sa.lim_y = (float)(p.height - 1u);
+    sa.width = p.width;
+    sa.height = p.height;
+    sa.small_max = p.small_max;
+    sa.tile_shift = shift;
+    sa.tiles_x = p.tiles_x;
+    sa.n_tiles = n_tiles;
+    sa.cw = cw;
+    sa.keys = s.keys;
+    sa.large = s.large;
+    sa.cap_large = s.cap_large;
+    sa.counters = s.counters;
+    sa.stats = s.stats;
+    if (mesh.ntri > 0) {
+        k_setup_raster<<<(unsigned)((mesh.ntri + kSetupThreads - 1) / kSetupThreads), kSetupThreads, 0, stream>>>(sa);
+        ++launches;
+    }
+
+    k_bin_scan<<<1, 1024, 0, stream>>>(s.counters, n_tiles, s.tile_offset, s.cap_entries, s.counters + 1, s.stats);
+    ++launches;
+
+    ScatterArgs sc;
+    sc.large = s.large;
+    sc.n_tiles = n_tiles;
+    sc.counters = s.counters;
+    sc.cursors = s.counters + kCounterHeader + n_tiles;
+    sc.offset = s.tile_offset;
+    sc.entries = s.entries;
+    sc.cap_large = s.cap_large;
+    sc.cap_entries = s.cap_entries;
+    sc.tile_shift = shift;
+    sc.tiles_x = p.tiles_x;
+    sc.stats = s.stats;
+    k_bin_scatter<<<grid_for(s.cap_large, 256, 4 * 152), 256, 0, stream>>>(sc);
+    ++launches;
+
+    TileArgs ta;
+    ta.large = s.large;
+    ta.counters = s.counters;
+    ta.offset = s.tile_offset;
+    ta.entries = s.entries;
+    ta.cap_entries = s.cap_entries;
+    ta.keys = s.keys;
+    ta.width = p.width;
+    ta.height = p.height;
+    ta.tiles_x = p.tiles_x;
+    ta.stats = s.stats;
+    if (p.tile == 8) launch_tile<8>(ta, n_tiles, stream);
+    else if (p.tile == 16) launch_tile<16>(ta, n_tiles, stream);
+    else launch_tile<32>(ta, n_tiles, stream);
+    ++launches;
+
+    ResolveArgs ra;
+    ra.keys = s.keys;
+    ra.keys_rearm = clear ? s.keys : nullptr;
+    ra.tri_v = mesh.tri_v;
+    ra.tri_nm = mesh.tri_nm;
+    ra.rv = s.rv;
+    ra.nrm = mesh.nrm;
+    ra.kd = mesh.kd;
+    ra.lights = p.lights;
+    ra.nl = p.nl;
+    ra.normal = p.normal;
+    ra.width = p.width;
+    ra.npx = npx;
+    ra.cw = cw;
+    ra.clear = clear;
+    ra.rgb = p.rgb;
+    ra.depth = p.depth;
+    ra.tri_id = p.tri_id;
+    ra.stats = s.stats;
+    k_resolve<<<grid_for(npx, 256, 152 * 16), 256, 0, stream>>>(ra);
+    ++launches;
+
+    return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
+}
+
+}  // namespace rast

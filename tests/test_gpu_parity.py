@@ -1,0 +1,217 @@
+"""Parity of the CUDA path (through the C ABI) with the reference's draw_frame.
+
+Bar: depth buffer and winning-triangle index bit for bit; coverage therefore exact; RGB8 within
+1/255 per channel (RGB_TOL below). The checkers are the golden fixtures made by the reference's own
+code and the C restatement (oracle port) run here on the same inputs.
+"""
+import numpy as np
+import pytest
+
+import edge_scenes as E
+import golden_io
+from rasteriser_gb300 import abi
+from rasteriser_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+RGB_TOL = 1  # per channel, in 1/255 units
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def flags_of(sc, clear=False):
+    return (abi.WIND_CLOCKWISE if sc.wind_clockwise else 0) | (abi.CLEAR if clear else 0)
+
+
+def gpu_draw(r, sc, cam, nm, lights7, frame=None, depth=None, clear=False):
+    r.upload_scene_mesh(sc)
+    r.set_lights(lights7)
+    f = None if frame is None else frame.copy()
+    d = None if depth is None else depth.copy()
+    return r.draw(cam, nm, sc.width, sc.height, flags_of(sc, clear), f, d, want_ids=True)
+
+
+def assert_parity(gpu, want_frame, want_depth, want_ids=None):
+    fg, dg, ig = gpu
+    assert np.array_equal(bits(dg), bits(want_depth)), f"depth differs at {np.argwhere(bits(dg) != bits(want_depth))[:5]}"
+    if want_ids is not None:
+        assert np.array_equal(ig, want_ids), f"winning triangle differs at {np.argwhere(ig != want_ids)[:5]}"
+    diff = np.abs(fg.astype(np.int16) - want_frame.astype(np.int16))
+    assert diff.max() <= RGB_TOL, f"RGB differs by {diff.max()}"
+
+
+@pytest.mark.parametrize("name", golden_io.names())
+def test_golden(renderer, port, name):
+    sc, g = golden_io.load(name)
+    out = gpu_draw(renderer, sc, g["camera"], g["normal"], g["lights7"])
+    _, _, ids, _ = port.draw(sc, g["camera"], g["normal"], g["lights7"])
+    assert_parity(out, g["frame"], g["depth"], ids)
+    assert np.array_equal(out[0], g["frame"]), "RGB not bit-exact (within tolerance, but expected exact)"
+
+
+def random_scenes():
+    out = []
+    for seed in range(6):
+        out.append(S.soup(3000 + 1231 * seed, 200 + 83 * seed, 150 + 41 * seed, seed=200 + seed,
+                          area_range=(0.2, 3000.0 * (seed + 1))).with_view(wind_clockwise=bool(seed % 3 == 1)))
+    out.append(S.config_displaced_sphere(200, 100, 640, 360).with_view(angles=(0.4, 2.1, -0.7)))
+    out.append(S.config_displaced_sphere(64, 32, 97, 61).with_view(scale=3.0))  # fills and overflows the frame
+    out.append(S.icosphere(2).with_view(width=1280, height=720, fovy_deg=60.0, z_near=0.1, z_far=100.0, scale=1.6))
+    out += E.all_edge_scenes()
+    return out
+
+
+@pytest.mark.parametrize("idx", range(len(random_scenes())))
+@pytest.mark.parametrize("tile,small_max", [(16, 256), (8, 1), (32, 65536), (16, 16)])
+def test_against_port(renderer, port, idx, tile, small_max):
+    sc = random_scenes()[idx]
+    renderer.set_option(abi.OPT_TILE_SIZE, tile)
+    renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, small_max)
+    try:
+        cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+        out = gpu_draw(renderer, sc, cam, nm, lights)
+        fp, dp, ip, st = port.draw(sc, cam, nm, lights)
+        assert_parity(out, fp, dp, ip)
+        s = renderer.stats()
+        assert (s["front"], s["tested"], s["inside"]) == (int(st[0]), int(st[1]), int(st[2]))
+        assert s["written"] == int((ip != abi.NO_TRIANGLE).sum())
+    finally:
+        renderer.set_option(abi.OPT_TILE_SIZE, 16)
+        renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, 256)
+
+
+def test_read_modify_write_buffers(renderer, port):
+    """Existing depth is the value to beat (drawing.cpp:119); untouched pixels keep their colour."""
+    sc = S.soup(8000, 300, 200, seed=17, area_range=(0.5, 4000.0))
+    rng = np.random.default_rng(5)
+    depth = rng.uniform(-1.5, 1.5, (sc.height, sc.width)).astype(np.float32)
+    depth[::7, ::5] = -0.0
+    depth[1::7, ::5] = 0.0
+    depth[3::11, ::3] = np.nan
+    depth[5::13, 1::4] = -np.inf
+    depth[6::13, 2::4] = np.inf
+    frame = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    out = gpu_draw(renderer, sc, cam, nm, lights, frame, depth)
+    fp, dp, ip, _ = port.draw(sc, cam, nm, lights, frame, depth)
+    assert_parity(out, fp, dp, ip)
+
+
+def test_clear_flag_equals_fresh_buffers(renderer):
+    sc = S.config_icosphere_small()
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    fresh = gpu_draw(renderer, sc, cam, nm, lights)
+    junk_f = np.full((3, sc.height, sc.width), 77, np.uint8)
+    junk_d = np.full((sc.height, sc.width), -5.0, np.float32)
+    for _ in range(3):  # the clear path re-arms its keys for the next frame
+        cl = gpu_draw(renderer, sc, cam, nm, lights, junk_f, junk_d, clear=True)
+        assert np.array_equal(cl[0], fresh[0]) and np.array_equal(bits(cl[1]), bits(fresh[1]))
+        assert np.array_equal(cl[2], fresh[2])
+
+
+def test_idempotent_redraw(renderer):
+    """Drawing the same frame again into its own output changes nothing: every fragment now meets
+    an equal or nearer depth, and the test is strict."""
+    sc = S.soup(20000, 640, 360, seed=23)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    f1, d1, _ = gpu_draw(renderer, sc, cam, nm, lights)
+    f2, d2, i2 = gpu_draw(renderer, sc, cam, nm, lights, f1, d1)
+    assert np.array_equal(f2, f1) and np.array_equal(bits(d2), bits(d1))
+    assert np.all(i2 == abi.NO_TRIANGLE)
+
+
+def test_deterministic_over_reruns(renderer):
+    sc = S.soup(60000, 800, 600, seed=29, area_range=(1.0, 2000.0))
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    first = gpu_draw(renderer, sc, cam, nm, lights)
+    for _ in range(10):
+        again = gpu_draw(renderer, sc, cam, nm, lights)
+        assert np.array_equal(again[2], first[2]) and np.array_equal(bits(again[1]), bits(first[1]))
+        assert np.array_equal(again[0], first[0])
+
+
+def test_bin_pool_overflow_recovers(renderer, port):
+    """A pool far too small for the frame: the host draw grows it and redraws; the result is exact."""
+    sc = S.soup(5000, 400, 300, seed=31, area_range=(200.0, 5000.0))
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    renderer.set_option(abi.OPT_BIN_CAPACITY, 16)
+    try:
+        out = gpu_draw(renderer, sc, cam, nm, lights)
+        fp, dp, ip, _ = port.draw(sc, cam, nm, lights)
+        assert_parity(out, fp, dp, ip)
+        assert renderer.get_option(abi.OPT_BIN_CAPACITY) > 16
+    finally:
+        renderer.set_option(abi.OPT_BIN_CAPACITY, 0)
+
+
+def test_device_draw_reports_bin_overflow(renderer, port):
+    torch = pytest.importorskip("torch")
+    sc = S.soup(5000, 400, 300, seed=37, area_range=(200.0, 5000.0))
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    renderer.upload_scene_mesh(sc)
+    renderer.set_lights(lights)
+    rgb = torch.zeros((3, sc.height, sc.width), dtype=torch.uint8, device="cuda")
+    dep = torch.ones((sc.height, sc.width), dtype=torch.float32, device="cuda")
+    renderer.set_option(abi.OPT_BIN_CAPACITY, 8)
+    try:
+        renderer.draw_device(cam, nm, sc.width, sc.height, abi.CLEAR, rgb.data_ptr(), dep.data_ptr())
+        with pytest.raises(abi.RastError) as ei:
+            renderer.sync()
+        assert ei.value.status == 6
+        renderer.draw_device(cam, nm, sc.width, sc.height, abi.CLEAR, rgb.data_ptr(), dep.data_ptr())
+        renderer.sync()
+        fp, dp, _, _ = port.draw(sc, cam, nm, lights)
+        assert np.array_equal(bits(dep.cpu().numpy()), bits(dp))
+        assert np.abs(rgb.cpu().numpy().astype(int) - fp).max() <= RGB_TOL
+    finally:
+        renderer.set_option(abi.OPT_BIN_CAPACITY, 0)
+
+
+def test_bad_index_is_refused(renderer):
+    sc = S.square_scene()
+    tris = sc.tris.copy()
+    for col, val in [(0, 4), (1, -1), (3, 1), (5, -2), (6, 4), (9, 1), (9, -1)]:
+        t = tris.copy()
+        t[1, col] = val
+        with pytest.raises(abi.RastError) as ei:
+            renderer.upload_mesh(sc.pos, sc.nrm, sc.uv, t, sc.kd)
+        assert ei.value.status == 2
+    renderer._mesh_digest = None
+
+
+def test_invalid_arguments(renderer):
+    sc = S.square_scene()
+    renderer.upload_scene_mesh(sc)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    for w, h in [(0, 10), (10, 0), (40000, 10)]:
+        with pytest.raises(abi.RastError) as ei:
+            renderer.draw(cam, nm, w, h, 0, np.zeros((3, max(h, 1), max(w, 1)), np.uint8),
+                          np.ones((max(h, 1), max(w, 1)), np.float32))
+        assert ei.value.status == 1
+    with pytest.raises(abi.RastError):
+        renderer.set_option(abi.OPT_TILE_SIZE, 12)
+    with pytest.raises(abi.RastError):
+        renderer.set_lights(np.zeros((5000, 7), np.float32))
+
+
+@pytest.mark.parametrize("key", sorted(golden_io.full_size()))
+def test_full_size_against_reference_digest(renderer, port, key):
+    """Full-size frames (1,046,528 triangles at 1920x1080; 4M at 3840x2160) against the digests of
+    the reference's own output, and against the port run here."""
+    import hashlib
+    e = golden_io.full_size()[key]
+    sc = golden_io.full_size_scene(e)
+    if sc.mesh_digest() != e["mesh"]:
+        pytest.skip("generated mesh differs from the one the digest was made for")
+    cam = np.array(e["camera"], np.float32)
+    nm = np.array(e["normal"], np.float32)
+    lights = np.array(e["lights7"], np.float32)
+    fg, dg, ig = gpu_draw(renderer, sc, cam, nm, lights)
+    assert hashlib.sha256(np.ascontiguousarray(dg).tobytes()).hexdigest() == e["depth"]
+    assert hashlib.sha256(np.ascontiguousarray(fg).tobytes()).hexdigest() == e["frame_rgb"]
+    fp, dp, ip, st = port.draw(sc, cam, nm, lights)
+    assert np.array_equal(ig, ip)
+    s = renderer.stats()
+    assert (s["front"], s["tested"], s["inside"]) == (int(st[0]), int(st[1]), int(st[2]))
