@@ -1,0 +1,413 @@
+#!/usr/bin/env python
+"""Benchmark of the rasteriser hot path (draw_frame) on GB300.
+
+Workload (default): the displaced UV sphere, 1024x512 segments (523,266 vertices, 1,046,528
+triangles, flat per-face normals), 1920x1080, 3 directional lights, spun about y by 1/60 rad per
+frame (the reference's spin loop at 60 frames/s). A step is one frame: the spin loop's clear plus
+draw_frame, on device-resident buffers, with L2 flushed (a 256 MiB write) between steps outside
+the timed region.
+
+One JSON line on rank 0: value = frames/s over all ranks; e2e = the same through the C ABI with
+host buffers (rast_draw: host->device copy of the frame and depth buffers, draw, device->host copy
+of both), mesh resident; roofline of the dominant kernel from per-stage CUDA events; the CPU
+baseline (the oracle port, one core) on a bounded sample of the same frames.
+
+--impl reference times the reference's CPU path on the host cores instead (the oracle port, one
+frame per thread on all cores; the reference's own sources are not present on the GPU host).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s @1080p 1M-tri (1 GB300); shade px/s learned vs plain @≤1/255 err"
+FLUSH_BYTES = 256 << 20
+SPIN_FRAMES = 60
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["displaced_sphere", "soup", "icosphere"], default="displaced_sphere")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
+    ap.add_argument("--device-only", action="store_true", help="only the device-resident timed loop (profiling)")
+    ap.add_argument("--no-soak", action="store_true", help="skip the clock-sampling soak loop (profiling)")
+    ap.add_argument("--small-max", type=int, default=None)
+    ap.add_argument("--tile", type=int, default=None)
+    return ap.parse_args()
+
+
+def make_scene(name):
+    from rasteriser_gb300 import scenes as S
+    if name == "displaced_sphere":
+        return S.config_displaced_sphere(), "displaced_sphere_1024x512_1080p_spin60"
+    if name == "soup":
+        return S.config_soup(), "triangle_soup_4M_2160p"
+    return S.config_icosphere_small(), "icosphere_l4_480p"
+
+
+def frame_inputs(scene, n_frames):
+    from rasteriser_gb300 import abi
+    from rasteriser_gb300 import scenes as S
+    out = []
+    for f in range(n_frames):
+        sc = scene.with_view(angles=S.spin_angles(f))
+        cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+        out.append((sc, cam, nm, lights))
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+        return False
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        rows = [r.split(", ") for r in self.out.strip().splitlines() if r.count(",") >= 8]
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(stage, sc, st):
+    """Compulsory bytes each stage must move for one frame (inputs read once, outputs written once)."""
+    W, H = sc.width, sc.height
+    npx = W * H
+    nv, ntri = sc.pos.shape[0], sc.ntri
+    if stage == "vertex":
+        return 12 * nv + 16 * nv
+    if stage == "setup_raster":
+        # indices + three gathered raster vertices per triangle, an 8-byte atomic per inside fragment
+        # of the per-triangle path, a 64-byte record per binned triangle
+        small_frags = max(0, st["inside"] - st.get("tile_inside", 0))
+        return 12 * ntri + 48 * ntri + 8 * small_frags + 64 * st["binned_tris"]
+    if stage == "bin_scan":
+        tiles = -(-W // 16) * -(-H // 16)
+        return 8 * tiles
+    if stage == "bin_scatter":
+        return 64 * st["binned_tris"] + 4 * st["bin_entries"]
+    if stage == "tile_raster":
+        return 68 * st["bin_entries"] + 16 * npx
+    if stage == "resolve":
+        # key read + re-arm, planar RGB8 + depth written, and per covered pixel the winner's indices,
+        # vertices, normal indices and normals
+        return (8 + 8 + 3 + 4) * npx + st["written"] * (12 + 48 + 16 + 36)
+    return 0
+
+
+def load_traffic(kernel, workload):
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        d = json.load(fh)
+    e = d.get(workload, {}).get(kernel)
+    return None if e is None else float(e["dram_bytes_per_launch"])
+
+
+def cpu_baseline(frames, seconds, threads=1):
+    """The oracle port (C restatement of the reference's draw_frame) on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    port = oracle.Port()
+    done = []
+    lock = threading.Lock()
+    t0 = time.perf_counter()
+    stop = t0 + seconds
+
+    def worker(k):
+        i = k
+        while time.perf_counter() < stop:
+            sc, cam, nm, lights = frames[i % len(frames)]
+            port.draw(sc, cam, nm, lights, want_ids=False)
+            with lock:
+                done.append(i)
+            i += threads
+
+    ts = [threading.Thread(target=worker, args=(k,)) for k in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    dt = time.perf_counter() - t0
+    return len(done) / dt, len(done), dt
+
+
+def parallel_steps(frames, steps, threads, first=0):
+    """`steps` rounds; in each, `threads` threads render one frame each of the spin (the port
+    releases the GIL inside its C call). Returns the wall seconds of all rounds."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    port = oracle.Port()
+
+    def render(i):
+        sc, cam, nm, lights = frames[i % len(frames)]
+        port.draw(sc, cam, nm, lights, want_ids=False)
+
+    t0 = time.perf_counter()
+    for s in range(steps):
+        ts = [threading.Thread(target=render, args=(first + s * threads + k,)) for k in range(threads)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    scene, workload = make_scene(args.workload)
+    frames = frame_inputs(scene, SPIN_FRAMES)
+    threads = os.cpu_count() or 1
+    warm = parallel_steps(frames, max(1, min(args.warmup, 2)), threads)
+    per_step = warm / max(1, min(args.warmup, 2))
+    # bounded sample: at most ~90 s of timed work whatever --steps asks for
+    steps = max(1, min(args.steps, int(90.0 / max(per_step, 1e-3))))
+    dt = parallel_steps(frames, steps, threads, first=threads)
+    value = steps * threads / dt
+    line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus, "steps": steps,
+            "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": workload, "width": scene.width, "height": scene.height, "triangles": scene.ntri},
+            "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": f"{steps} steps x {threads} threads, one full frame of the 60-frame spin per "
+                                       f"thread per step, {dt:.1f} s"},
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    from rasteriser_gb300 import abi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    scene, workload = make_scene(args.workload)
+    n_frames = SPIN_FRAMES if args.workload == "displaced_sphere" else 1
+    frames = frame_inputs(scene, n_frames)
+    W, H = scene.width, scene.height
+
+    r = abi.Renderer(local)
+    stream = torch.cuda.current_stream()
+    r.set_stream(stream.cuda_stream)
+    if args.small_max:
+        r.set_option(abi.OPT_SMALL_MAX_PIXELS, args.small_max)
+    if args.tile:
+        r.set_option(abi.OPT_TILE_SIZE, args.tile)
+    r.upload_scene_mesh(scene)
+    r.set_lights(frames[0][3])  # the view is a fixed translation: the lights are the same each frame
+    d_rgb = torch.empty(3 * W * H, dtype=torch.uint8, device="cuda")
+    d_depth = torch.empty(W * H, dtype=torch.float32, device="cuda")
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def frame_of(k):
+        return frames[(rank + k * world) % n_frames]
+
+    def step(k):
+        _, cam, nm, _ = frame_of(k)
+        r.draw_device(cam, nm, W, H, abi.CLEAR, d_rgb.data_ptr(), d_depth.data_ptr())
+
+    for k in range(args.warmup):
+        step(k)
+        flush.zero_()
+    r.sync()
+    stats = r.stats()
+
+    # timed region: K steps, each bracketed by events; L2 flushed between steps, outside the events
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    with sampler:
+        # keep the GPU busy for >= 0.5 s so the 100 ms clock samples see the load
+        t_soak = time.perf_counter()
+        while not args.no_soak and time.perf_counter() - t_soak < 0.5:
+            step(0)
+            flush.zero_()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            starts[k].record(stream)
+            step(k)
+            ends[k].record(stream)
+            flush.zero_()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    r.sync()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) / 1000.0
+    if dist is not None:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * args.steps / total_s
+    launches_per_step = stats["launches"]
+
+    if args.device_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "frames/s", "steps": args.steps,
+                              "ms_per_step": 1000 * total_s / args.steps, "device_only": True}))
+        return
+
+    # per-stage device times (CUDA events recorded by librast between its kernels)
+    r.set_option(abi.OPT_STAGE_TIMING, 1)
+    n_st = min(args.steps, 200)
+    acc = {}
+    for k in range(n_st):
+        step(k)
+        r.sync()
+        for name, ms in r.stage_times().items():
+            acc[name] = acc.get(name, 0.0) + ms
+        flush.zero_()
+    r.set_option(abi.OPT_STAGE_TIMING, 0)
+    stage_ms = {k: v / n_st for k, v in acc.items()}
+
+    # end to end through the C ABI with host buffers (pinned), mesh resident
+    h_rgb = torch.zeros(3 * W * H, dtype=torch.uint8).pin_memory().numpy().reshape(3, H, W)
+    h_depth = torch.ones(W * H, dtype=torch.float32).pin_memory().numpy().reshape(H, W)
+    n_e2e = min(args.steps, 500)
+    e2e_s = 0.0
+    for k in range(n_e2e + 3):
+        h_rgb[...] = 0
+        h_depth[...] = 1.0
+        flush.zero_()
+        torch.cuda.synchronize()
+        _, cam, nm, _ = frame_of(k)
+        t0 = time.perf_counter()
+        r.draw(cam, nm, W, H, 0, h_rgb, h_depth)
+        if k >= 3:
+            e2e_s += time.perf_counter() - t0
+    e2e_value = world * n_e2e / e2e_s if dist is None else None
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_value = world * n_e2e / float(t.item())
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel
+    peak, peak_kind = peaks()
+    stage_names = ["vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve"]
+    dom = max(stage_names, key=lambda s: stage_ms.get(s, 0.0))
+    sc0 = frames[0][0]
+    alg = algorithmic_bytes(dom, sc0, stats)
+    achieved = alg / (stage_ms[dom] / 1000.0) / 1e9
+    kernel_names = {"vertex": "k_vertex", "setup_raster": "k_setup_raster", "bin_scan": "k_bin_scan",
+                    "bin_scatter": "k_bin_scatter", "tile_raster": "k_tile_raster", "resolve": "k_resolve"}
+    traffic = load_traffic(kernel_names[dom], workload)
+
+    cpu = None
+    if world == 1 or rank == 0:
+        v, n, dt = cpu_baseline(frames, args.cpu_seconds, 1)
+        cpu = {"value": v, "unit": "frames/s", "cores": 1, "kind": "port",
+               "sample": f"{n} frames of the same spin ({W}x{H}, {scene.ntri} triangles) in {dt:.1f} s, one thread"}
+
+    clocks = sampler.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload, "width": W, "height": H, "triangles": scene.ntri,
+                   "vertices": int(scene.pos.shape[0]), "lights": int(frames[0][3].shape[0]),
+                   "frames_cycled": n_frames, "l2": "flushed between steps (256 MiB write, outside the timed events)",
+                   "parallelism": f"replicas x{world}", "mode": "RAST_CLEAR (spin-loop clear + draw_frame)"},
+        "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": 7 * W * H, "d2h_bytes_per_step": 7 * W * H,
+                "path": "rast_draw with pinned host frame (planar RGB8) and depth buffers; mesh resident"},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"kernel": kernel_names[dom], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg, "launch_ms": stage_ms[dom]},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "wall_s_timed_loop": wall,
+        "stage_ms": stage_ms,
+        "frame_stats": {k: stats[k] for k in ("front", "tested", "inside", "written", "binned_tris", "bin_entries")},
+        "fragments_per_s": stats["inside"] * value,
+    }
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -150,8 +150,15 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
                                          the per-triangle path; larger ones are binned (1..65536) */
 #define RAST_OPT_TILE_SIZE 2          /* tile edge for binning: 8, 16 or 32 */
 #define RAST_OPT_BIN_CAPACITY 3       /* initial tile-bin pool, entries */
+#define RAST_OPT_STAGE_TIMING 4       /* 1: record CUDA events between the kernels of each draw */
 rast_status rast_set_option(rast_ctx* ctx, int option, int64_t value);
 rast_status rast_get_option(rast_ctx* ctx, int option, int64_t* value);
+
+/* Device time of each stage of the last draw in milliseconds, from CUDA events recorded on the
+ * context's stream between its kernels (needs RAST_OPT_STAGE_TIMING = 1; waits for the stream):
+ *   [0] key arming   [1] vertex        [2] setup + per-triangle raster   [3] bin scan
+ *   [4] bin scatter  [5] tile raster   [6] resolve + shade                [7] whole draw */
+rast_status rast_get_stage_times(rast_ctx* ctx, float out_ms[8]);
 
 #ifdef __cplusplus
 }

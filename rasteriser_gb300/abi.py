@@ -20,7 +20,8 @@ STATUS_NAMES = {0: "RAST_OK", 1: "RAST_ERR_INVALID_ARG", 2: "RAST_ERR_BAD_INDEX"
                 4: "RAST_ERR_CUDA", 5: "RAST_ERR_OUT_OF_MEMORY", 6: "RAST_ERR_BIN_OVERFLOW",
                 7: "RAST_ERR_TIMEOUT", 8: "RAST_ERR_NO_DEVICE"}
 WIND_CLOCKWISE, CLEAR, FLAT = 1, 2, 4
-OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY = 1, 2, 3
+OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY, OPT_STAGE_TIMING = 1, 2, 3, 4
+STAGES = ["arm", "vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve", "total"]
 NO_TRIANGLE = 0xFFFFFFFF
 
 # Every function include/rast.h declares, with its ctypes signature.
@@ -44,6 +45,7 @@ SIGNATURES = {
     "rast_get_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "rast_set_option": (C.c_int, [_P, C.c_int, _I64]),
     "rast_get_option": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
+    "rast_get_stage_times": (C.c_int, [_P, _F]),
 }
 
 _lib = None
@@ -201,6 +203,12 @@ class Renderer:
         self._check(self.lib.rast_get_stats(self.h, out), "rast_get_stats")
         keys = ["front", "tested", "inside", "written", "binned_tris", "bin_entries", "launches", "reserved"]
         return dict(zip(keys, list(out)))
+
+    def stage_times(self):
+        """Per-stage device milliseconds of the last draw (RAST_OPT_STAGE_TIMING must be on)."""
+        out = np.zeros(8, np.float32)
+        self._check(self.lib.rast_get_stage_times(self.h, _fp(out)), "rast_get_stage_times")
+        return dict(zip(STAGES, [float(v) for v in out]))
 
     def draw_scene(self, scene, frame=None, depth=None, want_ids=True, clear=False):
         """draw_frame for a Scene: uploads its mesh if it changed, sets its lights, renders."""

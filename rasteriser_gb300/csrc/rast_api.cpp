@@ -67,6 +67,12 @@ struct rast_ctx {
     int64_t bin_capacity = 0;  // 0: sized from the mesh
 
     uint64_t last_launches = 0;
+
+    // stage timing
+    bool timing = false;
+    cudaEvent_t ev[8] = {};
+    bool ev_made = false;
+    bool ev_recorded = false;
 };
 
 namespace {
@@ -194,7 +200,12 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     p.rgb = d_rgb;
     p.depth = d_depth;
     p.tri_id = d_ids;
-    const int n = rast::launch_draw(c->mesh, s, p, c->stream);
+    if (c->timing && !c->ev_made) {
+        for (auto& e : c->ev) RAST_CUDA(c, cudaEventCreate(&e));
+        c->ev_made = true;
+    }
+    const int n = rast::launch_draw(c->mesh, s, p, c->stream, c->timing ? c->ev : nullptr);
+    c->ev_recorded = c->timing;
     if (n < 0) return cuda_fail(c, cudaGetLastError(), "launch draw");
     c->last_launches = (uint64_t)n;
     c->keys_armed_clear = clear;
@@ -279,6 +290,8 @@ void rast_destroy(rast_ctx* c) {
                       &c->large, &c->counters, &c->tile_offset, &c->entries, &c->stats, &c->d_rgb, &c->d_depth,
                       &c->d_ids})
         b->release();
+    if (c->ev_made)
+        for (auto& e : c->ev) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -419,6 +432,10 @@ rast_status rast_set_option(rast_ctx* c, int option, int64_t value) {
             if (value != 8 && value != 16 && value != 32) return fail(c, RAST_ERR_INVALID_ARG, "tile must be 8, 16 or 32");
             c->tile = (uint32_t)value;
             return RAST_OK;
+        case RAST_OPT_STAGE_TIMING:
+            if (value != 0 && value != 1) return fail(c, RAST_ERR_INVALID_ARG, "stage timing is 0 or 1");
+            c->timing = value == 1;
+            return RAST_OK;
         case RAST_OPT_BIN_CAPACITY:
             if (value < 0 || value > (int64_t)1 << 31) return fail(c, RAST_ERR_INVALID_ARG, "bin capacity out of range");
             c->bin_capacity = value;
@@ -434,8 +451,20 @@ rast_status rast_get_option(rast_ctx* c, int option, int64_t* value) {
         case RAST_OPT_SMALL_MAX_PIXELS: *value = c->small_max; return RAST_OK;
         case RAST_OPT_TILE_SIZE: *value = c->tile; return RAST_OK;
         case RAST_OPT_BIN_CAPACITY: *value = c->cap_entries ? c->cap_entries : c->bin_capacity; return RAST_OK;
+        case RAST_OPT_STAGE_TIMING: *value = c->timing ? 1 : 0; return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
+}
+
+rast_status rast_get_stage_times(rast_ctx* c, float out_ms[8]) {
+    if (!c || !out_ms) return RAST_ERR_INVALID_ARG;
+    for (int i = 0; i < 8; ++i) out_ms[i] = 0.f;
+    if (!c->ev_recorded) return fail(c, RAST_ERR_INVALID_ARG, "no timed draw (set RAST_OPT_STAGE_TIMING first)");
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, cudaEventSynchronize(c->ev[7]));
+    for (int i = 0; i < 7; ++i) RAST_CUDA(c, cudaEventElapsedTime(&out_ms[i], c->ev[i], c->ev[i + 1]));
+    RAST_CUDA(c, cudaEventElapsedTime(&out_ms[7], c->ev[0], c->ev[7]));
+    return RAST_OK;
 }
 
 }  // extern "C"

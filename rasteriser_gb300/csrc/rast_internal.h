@@ -69,7 +69,10 @@ constexpr int kCounterHeader = 4;
 
 // Launches every kernel of one draw on `stream`. Returns the number of kernel launches made
 // (memsets excluded) or -1 with cudaGetLastError() set.
-int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams& p, cudaStream_t stream);
+// With `events` (8 events, nullable) it records events[0] before the first kernel and
+// events[1..7] after key arming, vertex, setup, scan, scatter, tile raster and resolve.
+int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams& p, cudaStream_t stream,
+                cudaEvent_t* events = nullptr);
 
 // Fills keys[0, n) with the value a cleared depth buffer (1.0) arms them with.
 int launch_arm_keys_clear(unsigned long long* keys, int64_t n, cudaStream_t stream);

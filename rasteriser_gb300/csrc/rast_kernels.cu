@@ -722,7 +722,11 @@ int launch_arm_keys_clear(unsigned long long* keys, int64_t n, cudaStream_t stre
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
-int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams& p, cudaStream_t stream) {
+int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams& p, cudaStream_t stream,
+                cudaEvent_t* events) {
+    auto mark = [&](int i) {
+        if (events) cudaEventRecord(events[i], stream);
+    };
     const bool clear = (p.flags & 2u) != 0;  // RAST_CLEAR
     const bool cw = (p.flags & 1u) != 0;     // RAST_WIND_CLOCKWISE
     const int64_t npx = (int64_t)p.width * p.height;
@@ -730,13 +734,16 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     const uint32_t shift = p.tile == 8 ? 3u : (p.tile == 16 ? 4u : 5u);
     int launches = 0;
 
+    mark(0);
     if (!clear) {
         k_arm_from_depth<<<grid_for(npx, 256, 1 << 16), 256, 0, stream>>>(p.depth, npx, s.keys);
         ++launches;
     }
+    mark(1);
     k_vertex<<<grid_for(mesh.nv, 256, 1 << 16), 256, 0, stream>>>(mesh.pos, mesh.nv, p.camera, (float)(int)p.width,
                                                                    (float)(int)p.height, s.rv);
     ++launches;
+    mark(2);
 
     SetupArgs sa;
     sa.tri_v = mesh.tri_v;
@@ -760,9 +767,11 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
         k_setup_raster<<<(unsigned)((mesh.ntri + kSetupThreads - 1) / kSetupThreads), kSetupThreads, 0, stream>>>(sa);
         ++launches;
     }
+    mark(3);
 
     k_bin_scan<<<1, 1024, 0, stream>>>(s.counters, n_tiles, s.tile_offset, s.cap_entries, s.counters + 1, s.stats);
     ++launches;
+    mark(4);
 
     ScatterArgs sc;
     sc.large = s.large;
@@ -778,6 +787,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     sc.stats = s.stats;
     k_bin_scatter<<<grid_for(s.cap_large, 256, 4 * 152), 256, 0, stream>>>(sc);
     ++launches;
+    mark(5);
 
     TileArgs ta;
     ta.large = s.large;
@@ -794,6 +804,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     else if (p.tile == 16) launch_tile<16>(ta, n_tiles, stream);
     else launch_tile<32>(ta, n_tiles, stream);
     ++launches;
+    mark(6);
 
     ResolveArgs ra;
     ra.keys = s.keys;
@@ -816,6 +827,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.stats = s.stats;
     k_resolve<<<grid_for(npx, 256, 152 * 16), 256, 0, stream>>>(ra);
     ++launches;
+    mark(7);
 
     return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
 }

@@ -185,11 +185,19 @@ def test_invalid_arguments(renderer):
     sc = S.square_scene()
     renderer.upload_scene_mesh(sc)
     cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    import ctypes
+    buf_f = np.zeros(3 * 40000 * 10, np.uint8)
+    buf_d = np.ones(40000 * 10, np.float32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    c, n = np.ascontiguousarray(cam), np.ascontiguousarray(nm)
     for w, h in [(0, 10), (10, 0), (40000, 10)]:
-        with pytest.raises(abi.RastError) as ei:
-            renderer.draw(cam, nm, w, h, 0, np.zeros((3, max(h, 1), max(w, 1)), np.uint8),
-                          np.ones((max(h, 1), max(w, 1)), np.float32))
-        assert ei.value.status == 1
+        st = renderer.lib.rast_draw(renderer.h, c.ctypes.data_as(fp), n.ctypes.data_as(fp), w, h, 0,
+                                    buf_f.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), buf_d.ctypes.data_as(fp),
+                                    None)
+        assert st == 1
+    st = renderer.lib.rast_draw(renderer.h, None, n.ctypes.data_as(fp), 10, 10, 0,
+                                buf_f.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), buf_d.ctypes.data_as(fp), None)
+    assert st == 1
     with pytest.raises(abi.RastError):
         renderer.set_option(abi.OPT_TILE_SIZE, 12)
     with pytest.raises(abi.RastError):
