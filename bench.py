@@ -254,7 +254,10 @@ def run_ours(args):
     W, H = scene.width, scene.height
 
     r = abi.Renderer(local)
-    stream = torch.cuda.current_stream()
+    # A created stream: librast and the timing events, L2 flushes and copies all run on it, in order.
+    # (Handle 0, torch's default stream, would select librast's own stream instead.)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     r.set_stream(stream.cuda_stream)
     if args.small_max:
         r.set_option(abi.OPT_SMALL_MAX_PIXELS, args.small_max)

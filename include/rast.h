@@ -84,7 +84,8 @@ const char* rast_last_error(const rast_ctx* ctx);
 const char* rast_status_string(rast_status s);
 int rast_abi_version(void);
 
-/* Makes the context launch on `stream` (a cudaStream_t; NULL restores its own stream). */
+/* Makes the context launch on `stream` (a created cudaStream_t). NULL restores the context's own
+ * stream; the legacy default stream cannot be selected. */
 rast_status rast_set_stream(rast_ctx* ctx, void* stream);
 void* rast_get_stream(const rast_ctx* ctx);
 

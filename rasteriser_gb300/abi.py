@@ -173,6 +173,11 @@ class Renderer:
         return v.value
 
     def set_stream(self, stream_handle):
+        """Launch on a created CUDA stream (an integer cudaStream_t), or None for the context's own.
+        Handle 0 is refused: in the C ABI it means the context's own stream, not the legacy default
+        stream, and work timed on the default stream would not see the draws."""
+        if stream_handle == 0:
+            raise ValueError("stream handle 0 is ambiguous; pass a created stream or None")
         self._check(self.lib.rast_set_stream(self.h, _P(stream_handle) if stream_handle else None), "rast_set_stream")
 
     # drawing --------------------------------------------------------------------------------

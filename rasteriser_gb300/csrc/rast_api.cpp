@@ -153,7 +153,7 @@ rast_status ensure_scratch(rast_ctx* c, uint32_t w, uint32_t h, uint32_t tiles) 
     if (c->cap_entries == 0)
         c->cap_entries = c->bin_capacity > 0 ? c->bin_capacity : std::max<int64_t>(1 << 20, 2 * c->mesh.ntri);
     RAST_CUDA(c, c->entries.reserve(sizeof(uint32_t) * (size_t)c->cap_entries));
-    RAST_CUDA(c, c->stats.reserve(sizeof(unsigned long long) * 8));
+    RAST_CUDA(c, c->stats.reserve(sizeof(unsigned long long) * rast::kStatWords));
     return RAST_OK;
 }
 
@@ -172,7 +172,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     }
     RAST_CUDA(c, cudaMemsetAsync(c->counters.ptr, 0, sizeof(uint32_t) * (rast::kCounterHeader + 2 * (size_t)n_tiles),
                                  c->stream));
-    RAST_CUDA(c, cudaMemsetAsync(c->stats.ptr, 0, sizeof(unsigned long long) * 8, c->stream));
+    RAST_CUDA(c, cudaMemsetAsync(c->stats.ptr, 0, sizeof(unsigned long long) * rast::kStatWords, c->stream));
 
     rast::FrameScratch s;
     s.rv = c->rv.as<float4>();
@@ -220,8 +220,8 @@ rast_status collect_status(rast_ctx* c) {
     RAST_CUDA(c, cudaMemcpy(&status, c->counters.as<uint32_t>() + 1, sizeof status, cudaMemcpyDeviceToHost));
     if (status & rast::STATUS_BIN_OVERFLOW) {
         unsigned long long need = 0;
-        RAST_CUDA(c, cudaMemcpy(&need, c->stats.as<unsigned long long>() + rast::STAT_BIN_ENTRIES, sizeof need,
-                                cudaMemcpyDeviceToHost));
+        RAST_CUDA(c, cudaMemcpy(&need, c->stats.as<unsigned long long>() + rast::STAT_BIN_ENTRIES * rast::kStatStride,
+                                sizeof need, cudaMemcpyDeviceToHost));
         c->cap_entries = std::max<int64_t>((int64_t)need + (int64_t)need / 4, 2 * c->cap_entries);
         RAST_CUDA(c, c->entries.reserve(sizeof(uint32_t) * (size_t)c->cap_entries));
         uint32_t zero = 0;
@@ -414,9 +414,9 @@ rast_status rast_get_stats(rast_ctx* c, uint64_t out[8]) {
     if (!c->stats.ptr) return RAST_OK;
     DeviceGuard g(c->device);
     RAST_CUDA(c, cudaStreamSynchronize(c->stream));
-    unsigned long long s[8];
+    unsigned long long s[rast::kStatWords];
     RAST_CUDA(c, cudaMemcpy(s, c->stats.ptr, sizeof s, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < 8; ++i) out[i] = s[i];
+    for (int i = 0; i < 8; ++i) out[i] = s[i * rast::kStatStride];
     out[rast::STAT_LAUNCHES] = c->last_launches;
     return RAST_OK;
 }

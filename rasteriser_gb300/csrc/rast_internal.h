@@ -20,6 +20,11 @@ struct alignas(16) BinnedTri {
 
 struct Mat4 { float m[16]; };  // column major, m[c*4 + r]
 
+// Stats counters live kStatStride 64-bit words apart (128 bytes) so that blocks adding to
+// different counters do not queue on one L2 line.
+constexpr int kStatStride = 16;
+constexpr int kStatWords = 8 * kStatStride;
+
 enum StatIndex : int {
     STAT_FRONT = 0, STAT_TESTED = 1, STAT_INSIDE = 2, STAT_WRITTEN = 3,
     STAT_BINNED_TRIS = 4, STAT_BIN_ENTRIES = 5, STAT_LAUNCHES = 6, STAT_RESERVED = 7
@@ -46,7 +51,7 @@ struct FrameScratch {
     uint32_t* counters = nullptr;       // [0] n_large, [1] status, [2..] tile counts, then cursors
     uint32_t* tile_offset = nullptr;    // n_tiles + 1
     uint32_t* entries = nullptr;        // bin entries, capacity cap_entries
-    unsigned long long* stats = nullptr;  // 8 counters
+    unsigned long long* stats = nullptr;  // 8 counters, kStatStride words apart
     int64_t cap_large = 0, cap_entries = 0;
 };
 

@@ -158,6 +158,17 @@ __device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
     return v;
 }
 
+__device__ __forceinline__ unsigned long long* stat(unsigned long long* stats, int i) {
+    return stats + i * kStatStride;
+}
+
+// Adds a per-thread value to a block-wide counter in shared memory (warp-reduced first). The block
+// then makes one global atomic per counter, so thousands of warps do not queue on one address.
+__device__ __forceinline__ void block_accumulate(unsigned long long* s_counter, unsigned long long v) {
+    v = warp_sum64(v);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(s_counter, v);
+}
+
 // First lane j whose inclusive prefix exceeds k (the owner of work item k).
 __device__ __forceinline__ int owner_of(const uint32_t* incl, uint32_t k) {
     int lo = 0, hi = 31;
@@ -225,14 +236,20 @@ __global__ void __launch_bounds__(256) k_split_triangles(const int32_t* __restri
 constexpr int kSetupThreads = 256;
 constexpr int kSetupWarps = kSetupThreads / 32;
 
-// Per-warp staging of 32 triangles for the cooperative pixel loop (structure of arrays, so lanes
-// reading different triangles hit different banks).
+// Per-warp staging of 32 triangles. rec[j] holds lane j's triangle as five float4s so a lane
+// working on another lane's triangle loads it with five 16-byte shared loads:
+//   rec[j][0] = x0 y0 x1 y1      rec[j][1] = x2 y2 area nthr
+//   rec[j][2] = d12x d12y d20x d20y
+//   rec[j][3] = d01x d01y sgn (tlx | brx << 16)      rec[j][4] = z0 z1 z2 tly
 struct SetupStage {
-    float x0[32], y0[32], x1[32], y1[32], x2[32], y2[32];
-    float d12x[32], d12y[32], d20x[32], d20y[32], d01x[32], d01y[32];
-    float z0[32], z1[32], z2[32], area[32], nthr[32], sgn[32], rbw[32];
+    float4 rec[32][5];
     uint32_t tlx[32], tly[32], bw[32], incl[32];
+    float rbw[32];
+    int slot[32];
 };
+
+// Bounding boxes at most this many pixels wide take the per-triangle path; wider ones are binned.
+constexpr uint32_t kSmallMaxRow = 32;
 
 struct SetupArgs {
     const int32_t* tri_v;
@@ -257,7 +274,11 @@ struct SetupArgs {
 // go to the binned list, and their warp adds them to the tile counts the same way.
 __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
     __shared__ SetupStage stage[kSetupWarps];
+    __shared__ uint32_t s_large[kSetupWarps];
+    __shared__ uint32_t s_large_base;
+    __shared__ unsigned long long s_stat[3];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < 3) s_stat[threadIdx.x] = 0;
     SetupStage& S = stage[warp];
     const int64_t t = blockIdx.x * (int64_t)kSetupThreads + threadIdx.x;
 
@@ -275,7 +296,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
             const uint32_t bw = brx - tlx + 1u, bh = bry - tly + 1u;
             const unsigned long long npx = (unsigned long long)bw * bh;
             make_edge_tri(v0, v1, v2, T);
-            if (npx <= a.small_max) {
+            if (npx <= a.small_max && bw <= kSmallMaxRow) {
                 n_small = (uint32_t)npx;
             } else {
                 large = true;
@@ -283,12 +304,22 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
         }
     }
 
-    // Binned path: append, and count the tiles the box overlaps.
+    // Binned path: append (one atomic per block), and count the tiles the box overlaps.
     const unsigned lmask = __ballot_sync(kFull, large);
+    if (lane == 0) s_large[warp] = __popc(lmask);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (int w = 0; w < kSetupWarps; ++w) {
+            const uint32_t c = s_large[w];
+            s_large[w] = tot;
+            tot += c;
+        }
+        s_large_base = tot ? atomicAdd(&a.counters[0], tot) : 0u;
+    }
+    __syncthreads();
     if (lmask) {
-        uint32_t base = 0;
-        if (lane == __ffs(lmask) - 1) base = atomicAdd(&a.counters[0], (uint32_t)__popc(lmask));
-        base = __shfl_sync(kFull, base, __ffs(lmask) - 1);
+        const uint32_t base = s_large_base + s_large[warp];
         if (large) {
             const uint32_t slot = base + __popc(lmask & ((1u << lane) - 1u));
             if (slot < a.cap_large) {
@@ -309,46 +340,63 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
 
     unsigned long long c_tested = 0, c_inside = 0;
 
-    // Cooperative pixel loop over the warp's small triangles.
+    // Cooperative raster of the warp's small triangles. A work item is one bounding-box row of one
+    // triangle; the warp's rows are laid end to end and taken 32 at a time, so lanes stay busy
+    // whatever the box sizes. The owner of an item is found from a ballot of the triangles whose
+    // rows start in the current window. Each edge function
+    //   e = (b.x - a.x)*(py - a.y) - (b.y - a.y)*(px - a.x)     (drawing.cpp:36-39)
+    // is evaluated as the reference does, with its first product taken once per row.
     {
-        const uint32_t incl = warp_inclusive_scan(n_small, lane);
+        const uint32_t n_rows = n_small ? (bry - tly + 1u) : 0u;
+        const uint32_t incl = warp_inclusive_scan(n_rows, lane);
         const uint32_t total = __shfl_sync(kFull, incl, 31);
         if (total) {
-            S.x0[lane] = T.x0; S.y0[lane] = T.y0; S.x1[lane] = T.x1; S.y1[lane] = T.y1;
-            S.x2[lane] = T.x2; S.y2[lane] = T.y2;
-            S.d12x[lane] = T.d12x; S.d12y[lane] = T.d12y; S.d20x[lane] = T.d20x; S.d20y[lane] = T.d20y;
-            S.d01x[lane] = T.d01x; S.d01y[lane] = T.d01y;
-            S.z0[lane] = T.z0; S.z1[lane] = T.z1; S.z2[lane] = T.z2;
-            S.area[lane] = T.area; S.nthr[lane] = T.nthr; S.sgn[lane] = T.sgn;
-            const uint32_t bw = brx - tlx + 1u;
-            S.tlx[lane] = tlx; S.tly[lane] = tly; S.bw[lane] = bw;
-            S.rbw[lane] = __frcp_rn((float)bw);
-            S.incl[lane] = incl;
+            const uint32_t start = incl - n_rows;
+            S.rec[lane][0] = make_float4(T.x0, T.y0, T.x1, T.y1);
+            S.rec[lane][1] = make_float4(T.x2, T.y2, T.area, T.nthr);
+            S.rec[lane][2] = make_float4(T.d12x, T.d12y, T.d20x, T.d20y);
+            S.rec[lane][3] = make_float4(T.d01x, T.d01y, T.sgn, __uint_as_float(tlx | (brx << 16)));
+            S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, __uint_as_float(tly));
             __syncwarp();
             const uint32_t tri_base = (uint32_t)(blockIdx.x * (int64_t)kSetupThreads + warp * 32);
+            int carry = 0;
             for (uint32_t base = 0; base < total; base += 32) {
+                const bool opens = n_rows != 0u && start >= base && start < base + 32u;
+                if (opens) S.slot[start - base] = lane;
+                const unsigned starts = __ballot_sync(kFull, opens);
+                __syncwarp();
+                const unsigned upto = starts & (0xFFFFFFFFu >> (31 - lane));
+                const int owner = upto ? S.slot[31 - __clz(upto)] : carry;
+                const uint32_t ostart = __shfl_sync(kFull, start, owner);
+                carry = __shfl_sync(kFull, owner, 31);
+                __syncwarp();
                 const uint32_t k = base + lane;
                 if (k < total) {
-                    const int j = owner_of(S.incl, k);
-                    const uint32_t start = j ? S.incl[j - 1] : 0u;
-                    const uint32_t local = k - start;
-                    const uint32_t w = S.bw[j];
-                    const uint32_t dy = div_small(local, w, S.rbw[j]);
-                    const uint32_t x = S.tlx[j] + (local - dy * w), y = S.tly[j] + dy;
-                    EdgeTri U;
-                    U.x0 = S.x0[j]; U.y0 = S.y0[j]; U.x1 = S.x1[j]; U.y1 = S.y1[j]; U.x2 = S.x2[j]; U.y2 = S.y2[j];
-                    U.d12x = S.d12x[j]; U.d12y = S.d12y[j]; U.d20x = S.d20x[j]; U.d20y = S.d20y[j];
-                    U.d01x = S.d01x[j]; U.d01y = S.d01y[j];
-                    U.area = S.area[j]; U.nthr = S.nthr[j]; U.sgn = S.sgn[j];
-                    float b0, b1, b2;
-                    ++c_tested;
-                    if (inside_test(U, (float)x, (float)y, b0, b1, b2)) {
+                    const float4 q0 = S.rec[owner][0], q1 = S.rec[owner][1], q2 = S.rec[owner][2],
+                                 q3 = S.rec[owner][3];
+                    const uint32_t xr = __float_as_uint(q3.w);
+                    const uint32_t x_lo = xr & 0xFFFFu, x_hi = xr >> 16;
+                    const uint32_t y = __float_as_uint(S.rec[owner][4].w) + (k - ostart);
+                    const float py = (float)y;
+                    const float p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
+                    const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
+                    const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
+                    const float sg = q3.z, nt = q1.w, area = q1.z;
+                    for (uint32_t x = x_lo; x <= x_hi; ++x) {
+                        const float px = (float)x;
+                        const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));  // - d12y * (px - x1)
+                        const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));  // - d20y * (px - x2)
+                        const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));  // - d01y * (px - x0)
+                        if (mul(sg, e0) < nt || mul(sg, e1) < nt || mul(sg, e2) < nt) continue;
+                        const float b0 = dvd(e0, area), b1 = dvd(e1, area), b2 = dvd(e2, area);
+                        if (!(b0 >= 0.f && b1 >= 0.f && b2 >= 0.f)) continue;
                         ++c_inside;
-                        U.z0 = S.z0[j]; U.z1 = S.z1[j]; U.z2 = S.z2[j];
-                        const float z = interp_depth(U, b0, b1, b2);
+                        const float4 q4 = S.rec[owner][4];
+                        const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
                         if (z == z && x < a.width && y < a.height)
-                            atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + (uint32_t)j));
+                            atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + (uint32_t)owner));
                     }
+                    c_tested += x_hi - x_lo + 1u;
                 }
             }
             __syncwarp();
@@ -380,13 +428,14 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
         }
     }
 
-    c_front = warp_sum64(c_front);
-    c_tested = warp_sum64(c_tested);
-    c_inside = warp_sum64(c_inside);
-    if (lane == 0) {
-        if (c_front) atomicAdd(&a.stats[STAT_FRONT], c_front);
-        if (c_tested) atomicAdd(&a.stats[STAT_TESTED], c_tested);
-        if (c_inside) atomicAdd(&a.stats[STAT_INSIDE], c_inside);
+    block_accumulate(&s_stat[0], c_front);
+    block_accumulate(&s_stat[1], c_tested);
+    block_accumulate(&s_stat[2], c_inside);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_stat[0]) atomicAdd(stat(a.stats, STAT_FRONT), s_stat[0]);
+        if (s_stat[1]) atomicAdd(stat(a.stats, STAT_TESTED), s_stat[1]);
+        if (s_stat[2]) atomicAdd(stat(a.stats, STAT_INSIDE), s_stat[2]);
     }
 }
 
@@ -431,7 +480,7 @@ __global__ void __launch_bounds__(1024) k_bin_scan(const uint32_t* __restrict__ 
     }
     if (tid == 0) {
         offset[n_tiles] = carry_s;
-        stats[STAT_BIN_ENTRIES] = carry_s;
+        *stat(stats, STAT_BIN_ENTRIES) = carry_s;
         if ((int64_t)carry_s > cap_entries) atomicOr(status, STATUS_BIN_OVERFLOW);
     }
 }
@@ -455,7 +504,7 @@ __global__ void __launch_bounds__(256) k_bin_scatter(ScatterArgs a) {
     __shared__ float s_rtw[8][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t n_large = (uint32_t)min((int64_t)a.counters[0], a.cap_large);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.stats[STAT_BINNED_TRIS] = n_large;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *stat(a.stats, STAT_BINNED_TRIS) = n_large;
     for (uint32_t wb = (blockIdx.x * 256u + warp * 32u); wb < n_large; wb += gridDim.x * 256u) {
         const uint32_t i = wb + lane;
         uint32_t n = 0, tx0 = 0, ty0 = 0, tw = 1;
@@ -585,7 +634,7 @@ __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
                 }
                 // Coverage mask of the warp's 8x4 block for this triangle.
                 const unsigned mask = __ballot_sync(kFull, covered);
-                if (lane == 0) c_inside += __popc(mask);
+                if (lane == 0) c_inside += (unsigned)__popc(mask);
             }
         }
     }
@@ -593,10 +642,15 @@ __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
     for (int s = 0; s < kPPT; ++s)
         if (valid[s] && best[s] != orig[s]) a.keys[(size_t)py[s] * a.width + px[s]] = best[s];
 
-    c_tested = warp_sum64(c_tested);
-    if (lane == 0) {
-        atomicAdd(&a.stats[STAT_TESTED], c_tested);
-        atomicAdd(&a.stats[STAT_INSIDE], c_inside);
+    __shared__ unsigned long long s_stat[2];
+    if (threadIdx.x < 2) s_stat[threadIdx.x] = 0;
+    __syncthreads();
+    block_accumulate(&s_stat[0], c_tested);
+    block_accumulate(&s_stat[1], c_inside);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_stat[0]) atomicAdd(stat(a.stats, STAT_TESTED), s_stat[0]);
+        if (s_stat[1]) atomicAdd(stat(a.stats, STAT_INSIDE), s_stat[1]);
     }
 }
 
@@ -694,8 +748,12 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a) {
         a.rgb[p + plane] = (uint8_t)__float2uint_rz(gmin(accg, 255.f));
         a.rgb[p + 2 * plane] = (uint8_t)__float2uint_rz(gmin(accb, 255.f));
     }
-    written = warp_sum64(written);
-    if ((threadIdx.x & 31) == 0 && written) atomicAdd(&a.stats[STAT_WRITTEN], written);
+    __shared__ unsigned long long s_written;
+    if (threadIdx.x == 0) s_written = 0;
+    __syncthreads();
+    block_accumulate(&s_written, written);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_written) atomicAdd(stat(a.stats, STAT_WRITTEN), s_written);
 }
 
 int grid_for(int64_t n, int threads, int max_blocks) {
