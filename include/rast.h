@@ -34,7 +34,9 @@ typedef enum rast_status {
     RAST_ERR_BIN_OVERFLOW = 6,  /* a device draw overflowed the tile-bin pool; the pool has been
                                    grown, draw the frame again */
     RAST_ERR_TIMEOUT = 7,       /* a bounded device-side wait gave up */
-    RAST_ERR_NO_DEVICE = 8
+    RAST_ERR_NO_DEVICE = 8,
+    RAST_ERR_INTERNAL = 9       /* a device-side consistency check failed; the access was skipped
+                                   and the frame is not trustworthy (rast_get_device_status) */
 } rast_status;
 
 typedef struct rast_ctx rast_ctx;
@@ -154,6 +156,12 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 #define RAST_OPT_STAGE_TIMING 4       /* 1: record CUDA events between the kernels of each draw */
 rast_status rast_set_option(rast_ctx* ctx, int option, int64_t value);
 rast_status rast_get_option(rast_ctx* ctx, int option, int64_t* value);
+
+/* Device status words of the last draw (waits for the stream): [0] triangles on the binned path,
+ * [1] status bits (1 bin-pool overflow, 2 binned-list overflow, 4 failed consistency check),
+ * [2] code of the first failed check (0 none), [3] its detail. Kernels built with RAST_CHECKED
+ * bounds-check every derived index; the default build checks the ones that index other arrays. */
+rast_status rast_get_device_status(rast_ctx* ctx, uint32_t out[4]);
 
 /* Device time of each stage of the last draw in milliseconds, from CUDA events recorded on the
  * context's stream between its kernels (needs RAST_OPT_STAGE_TIMING = 1; waits for the stream):

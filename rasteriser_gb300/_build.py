@@ -17,6 +17,10 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIB_DIR, "librast.so")
+
+
+def lib_path(checked=False):
+    return os.path.join(LIB_DIR, "librast_checked.so" if checked else "librast.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -27,11 +31,13 @@ def nvcc_path():
     return cand
 
 
-def _units():
+def _units(checked=False):
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-I" + os.path.join(PKG, "compat")]
     host = ["-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-std=c++17", "-O3"]
     kern = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                    "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v"]
+    if checked:
+        kern = kern + ["-DRAST_CHECKED"]
     return [
         ("rast_kernels.cu", kern + inc),
         ("rast_api.cpp", host + inc),
@@ -55,16 +61,18 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose=False, force=False):
-    """Compile librast.so if anything changed; returns its path."""
+def build(verbose=False, force=False, checked=False):
+    """Compile librast.so (or, with checked, librast_checked.so, whose kernels bounds-check every
+    derived index) if anything changed; returns its path."""
     nvcc = nvcc_path()
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     headers = _headers()
     jobs, objs = [], []
-    for src, flags in _units():
+    lib = lib_path(checked)
+    for src, flags in _units(checked):
         s = os.path.join(CSRC, src)
-        o = os.path.join(OBJ, src + ".o")
+        o = os.path.join(OBJ, src + (".checked.o" if checked else ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append([nvcc, "-c", s, "-o", o] + flags)
@@ -80,11 +88,11 @@ def build(verbose=False, force=False):
     if verbose:
         for lg in logs:
             print(lg)
-    if force or jobs or _stale(LIB, objs):
-        run([nvcc, "-shared", "-o", LIB] + ARCH + objs + ["-Xcompiler", "-fPIC"])
-    return LIB
+    if force or jobs or _stale(lib, objs):
+        run([nvcc, "-shared", "-o", lib] + ARCH + objs + ["-Xcompiler", "-fPIC"])
+    return lib
 
 
 if __name__ == "__main__":
-    build(verbose=True)
-    print(LIB)
+    import sys
+    print(build(verbose=True, checked="--checked" in sys.argv))

@@ -18,7 +18,7 @@ from . import _build
 RAST_OK = 0
 STATUS_NAMES = {0: "RAST_OK", 1: "RAST_ERR_INVALID_ARG", 2: "RAST_ERR_BAD_INDEX", 3: "RAST_ERR_NO_MESH",
                 4: "RAST_ERR_CUDA", 5: "RAST_ERR_OUT_OF_MEMORY", 6: "RAST_ERR_BIN_OVERFLOW",
-                7: "RAST_ERR_TIMEOUT", 8: "RAST_ERR_NO_DEVICE"}
+                7: "RAST_ERR_TIMEOUT", 8: "RAST_ERR_NO_DEVICE", 9: "RAST_ERR_INTERNAL"}
 WIND_CLOCKWISE, CLEAR, FLAT = 1, 2, 4
 OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY, OPT_STAGE_TIMING = 1, 2, 3, 4
 STAGES = ["arm", "vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve", "total"]
@@ -46,13 +46,15 @@ SIGNATURES = {
     "rast_set_option": (C.c_int, [_P, C.c_int, _I64]),
     "rast_get_option": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
     "rast_get_stage_times": (C.c_int, [_P, _F]),
+    "rast_get_device_status": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
 }
 
 _lib = None
 
 
 def library_path():
-    return _build.LIB
+    """librast.so, or its self-checking build librast_checked.so when RAST_CHECKED=1."""
+    return _build.lib_path(checked=os.environ.get("RAST_CHECKED") == "1")
 
 
 def load(build_if_missing=True):
@@ -64,7 +66,7 @@ def load(build_if_missing=True):
     if not os.path.exists(path):
         if not build_if_missing:
             raise RuntimeError(f"librast is not built ({path}); run __graft_entry__.build()")
-        _build.build()
+        _build.build(checked=os.environ.get("RAST_CHECKED") == "1")
     lib = C.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)
@@ -208,6 +210,11 @@ class Renderer:
         self._check(self.lib.rast_get_stats(self.h, out), "rast_get_stats")
         keys = ["front", "tested", "inside", "written", "binned_tris", "bin_entries", "launches", "reserved"]
         return dict(zip(keys, list(out)))
+
+    def device_status(self):
+        out = (C.c_uint32 * 4)()
+        self._check(self.lib.rast_get_device_status(self.h, out), "rast_get_device_status")
+        return list(out)
 
     def stage_times(self):
         """Per-stage device milliseconds of the last draw (RAST_OPT_STAGE_TIMING must be on)."""

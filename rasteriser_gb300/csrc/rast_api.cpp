@@ -230,7 +230,13 @@ rast_status collect_status(rast_ctx* c) {
         return fail(c, RAST_ERR_BIN_OVERFLOW, "tile-bin pool overflowed; it was grown to " +
                                                   std::to_string(c->cap_entries) + " entries, draw again");
     }
-    if (status) return fail(c, RAST_ERR_CUDA, "device status " + std::to_string(status));
+    if (status & rast::STATUS_CHECK_FAILED) {
+        uint32_t w[2] = {0, 0};
+        RAST_CUDA(c, cudaMemcpy(w, c->counters.as<uint32_t>() + 2, sizeof w, cudaMemcpyDeviceToHost));
+        return fail(c, RAST_ERR_INTERNAL, "device check " + std::to_string(w[0]) + " failed (detail " +
+                                              std::to_string(w[1]) + ")");
+    }
+    if (status) return fail(c, RAST_ERR_INTERNAL, "device status " + std::to_string(status));
     return RAST_OK;
 }
 
@@ -253,6 +259,7 @@ const char* rast_status_string(rast_status s) {
         case RAST_ERR_BIN_OVERFLOW: return "tile-bin pool overflow";
         case RAST_ERR_TIMEOUT: return "device wait timed out";
         case RAST_ERR_NO_DEVICE: return "no CUDA device";
+        case RAST_ERR_INTERNAL: return "device consistency check failed";
     }
     return "unknown status";
 }
@@ -454,6 +461,16 @@ rast_status rast_get_option(rast_ctx* c, int option, int64_t* value) {
         case RAST_OPT_STAGE_TIMING: *value = c->timing ? 1 : 0; return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
+}
+
+rast_status rast_get_device_status(rast_ctx* c, uint32_t out[4]) {
+    if (!c || !out) return RAST_ERR_INVALID_ARG;
+    for (int i = 0; i < 4; ++i) out[i] = 0;
+    if (!c->counters.ptr) return RAST_OK;
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    RAST_CUDA(c, cudaMemcpy(out, c->counters.ptr, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return RAST_OK;
 }
 
 rast_status rast_get_stage_times(rast_ctx* c, float out_ms[8]) {

@@ -31,7 +31,9 @@ enum StatIndex : int {
 };
 
 // Device status word bits.
-enum StatusBits : uint32_t { STATUS_BIN_OVERFLOW = 1u, STATUS_LARGE_OVERFLOW = 2u };
+// Device status word bits (counters[1]); counters[2] and [3] hold the code and detail of the
+// first failed internal check.
+enum StatusBits : uint32_t { STATUS_BIN_OVERFLOW = 1u, STATUS_LARGE_OVERFLOW = 2u, STATUS_CHECK_FAILED = 4u };
 
 struct DeviceMesh {
     const float* pos = nullptr;      // nv * 3
@@ -48,7 +50,8 @@ struct FrameScratch {
     float4* rv = nullptr;               // nv raster vertices
     unsigned long long* keys = nullptr; // W*H packed (order-preserving depth << 32 | triangle)
     BinnedTri* large = nullptr;         // binned triangles, capacity cap_large
-    uint32_t* counters = nullptr;       // [0] n_large, [1] status, [2..] tile counts, then cursors
+    uint32_t* counters = nullptr;       // [0] n_large, [1] status, [2] check code, [3] check detail,
+                                        // then tile counts, then tile cursors
     uint32_t* tile_offset = nullptr;    // n_tiles + 1
     uint32_t* entries = nullptr;        // bin entries, capacity cap_entries
     unsigned long long* stats = nullptr;  // 8 counters, kStatStride words apart

@@ -158,6 +158,13 @@ __device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
     return v;
 }
 
+// Records a failed internal check: sets STATUS_CHECK_FAILED and keeps the first failure's code
+// and detail in counters[2..3]. The caller skips the access that failed the check.
+__device__ __noinline__ void report(uint32_t* counters, uint32_t code, uint32_t detail) {
+    atomicOr(&counters[1], STATUS_CHECK_FAILED);
+    if (atomicCAS(&counters[2], 0u, code) == 0u) atomicExch(&counters[3], detail);
+}
+
 __device__ __forceinline__ unsigned long long* stat(unsigned long long* stats, int i) {
     return stats + i * kStatStride;
 }
@@ -240,9 +247,12 @@ constexpr int kSetupWarps = kSetupThreads / 32;
 // working on another lane's triangle loads it with five 16-byte shared loads:
 //   rec[j][0] = x0 y0 x1 y1      rec[j][1] = x2 y2 area nthr
 //   rec[j][2] = d12x d12y d20x d20y
-//   rec[j][3] = d01x d01y sgn (tlx | brx << 16)      rec[j][4] = z0 z1 z2 tly
+//   rec[j][3] = d01x d01y sgn -   rec[j][4] = z0 z1 z2 -
+// Its integer data (column range packed as tlx | brx << 16, first row, row count) is kept in
+// integer arrays.
 struct SetupStage {
     float4 rec[32][5];
+    uint32_t xr[32], ty[32], nrows[32];
     uint32_t tlx[32], tly[32], bw[32], incl[32];
     float rbw[32];
     int slot[32];
@@ -342,8 +352,9 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
 
     // Cooperative raster of the warp's small triangles. A work item is one bounding-box row of one
     // triangle; the warp's rows are laid end to end and taken 32 at a time, so lanes stay busy
-    // whatever the box sizes. The owner of an item is found from a ballot of the triangles whose
-    // rows start in the current window. Each edge function
+    // whatever the box sizes. The owner of an item is the last triangle whose rows start at or
+    // before it in the current window (an OR-reduction of start positions), else the owner of the
+    // window's first item carried over from the previous window. Each edge function
     //   e = (b.x - a.x)*(py - a.y) - (b.y - a.y)*(px - a.x)     (drawing.cpp:36-39)
     // is evaluated as the reference does, with its first product taken once per row.
     {
@@ -355,15 +366,20 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
             S.rec[lane][0] = make_float4(T.x0, T.y0, T.x1, T.y1);
             S.rec[lane][1] = make_float4(T.x2, T.y2, T.area, T.nthr);
             S.rec[lane][2] = make_float4(T.d12x, T.d12y, T.d20x, T.d20y);
-            S.rec[lane][3] = make_float4(T.d01x, T.d01y, T.sgn, __uint_as_float(tlx | (brx << 16)));
-            S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, __uint_as_float(tly));
+            S.rec[lane][3] = make_float4(T.d01x, T.d01y, T.sgn, 0.f);
+            S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, 0.f);
+            S.xr[lane] = tlx | (brx << 16);
+            S.ty[lane] = tly;
+            S.nrows[lane] = n_rows;
             __syncwarp();
             const uint32_t tri_base = (uint32_t)(blockIdx.x * (int64_t)kSetupThreads + warp * 32);
             int carry = 0;
             for (uint32_t base = 0; base < total; base += 32) {
+                // Bit b of `starts` is set when a triangle's rows begin at item base + b; that
+                // triangle's lane is in slot[b].
                 const bool opens = n_rows != 0u && start >= base && start < base + 32u;
                 if (opens) S.slot[start - base] = lane;
-                const unsigned starts = __ballot_sync(kFull, opens);
+                const unsigned starts = __reduce_or_sync(kFull, opens ? (1u << (start - base)) : 0u);
                 __syncwarp();
                 const unsigned upto = starts & (0xFFFFFFFFu >> (31 - lane));
                 const int owner = upto ? S.slot[31 - __clz(upto)] : carry;
@@ -372,11 +388,19 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                 __syncwarp();
                 const uint32_t k = base + lane;
                 if (k < total) {
+#ifdef RAST_CHECKED
+                    if (owner < 0 || owner > 31 || k < ostart || k - ostart >= S.nrows[owner] ||
+                        (S.xr[owner] & 0xFFFFu) > (S.xr[owner] >> 16) || (S.xr[owner] >> 16) >= a.width ||
+                        S.ty[owner] + (k - ostart) >= a.height) {
+                        report(a.counters, 1u, (uint32_t)owner);
+                        continue;
+                    }
+#endif
                     const float4 q0 = S.rec[owner][0], q1 = S.rec[owner][1], q2 = S.rec[owner][2],
                                  q3 = S.rec[owner][3];
-                    const uint32_t xr = __float_as_uint(q3.w);
+                    const uint32_t xr = S.xr[owner];
                     const uint32_t x_lo = xr & 0xFFFFu, x_hi = xr >> 16;
-                    const uint32_t y = __float_as_uint(S.rec[owner][4].w) + (k - ostart);
+                    const uint32_t y = S.ty[owner] + (k - ostart);
                     const float py = (float)y;
                     const float p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
                     const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
@@ -551,10 +575,10 @@ struct TileStage {
 
 struct TileArgs {
     const BinnedTri* large;
-    const uint32_t* counters;  // tile counts after kCounterHeader
+    uint32_t* counters;        // [0] binned triangles, [1..3] status, then tile counts
     const uint32_t* offset;
     const uint32_t* entries;
-    int64_t cap_entries;
+    int64_t cap_entries, cap_large;
     unsigned long long* keys;
     uint32_t width, height, tiles_x;
     unsigned long long* stats;
@@ -594,9 +618,16 @@ __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
     for (uint32_t c0 = 0; c0 < count; c0 += kTileChunk) {
         const uint32_t n = min((uint32_t)kTileChunk, count - c0);
         __syncthreads();
+        const uint32_t n_large = a.counters[0];
         for (uint32_t i = threadIdx.x; i < n; i += kThreads) {
             const uint32_t e = first + c0 + i;
-            const BinnedTri r = a.large[(int64_t)e < a.cap_entries ? a.entries[e] : 0];
+            uint32_t idx = (int64_t)e < a.cap_entries ? a.entries[e] : 0u;
+            if (idx >= n_large || (int64_t)idx >= a.cap_large) {
+                // Only a pool overflow (already flagged) can leave an entry unwritten.
+                report(a.counters, 2u, idx);
+                idx = 0;
+            }
+            const BinnedTri r = a.large[idx];
             S.x0[i] = r.x0; S.y0[i] = r.y0; S.x1[i] = r.x1; S.y1[i] = r.y1; S.x2[i] = r.x2; S.y2[i] = r.y2;
             S.d12x[i] = sub(r.x2, r.x1); S.d12y[i] = sub(r.y2, r.y1);
             S.d20x[i] = sub(r.x0, r.x2); S.d20y[i] = sub(r.y0, r.y2);
@@ -655,6 +686,8 @@ __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
 }
 
 struct ResolveArgs {
+    uint32_t* counters;
+    int64_t ntri;
     const unsigned long long* keys;
     unsigned long long* keys_rearm;  // non-null in clear mode: keys are re-armed for the next frame
     const int32_t* tri_v;
@@ -696,6 +729,10 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a) {
                 a.depth[p] = 1.0f;
             }
             if (a.tri_id) a.tri_id[p] = 0xFFFFFFFFu;
+            continue;
+        }
+        if ((int64_t)t >= a.ntri) {
+            report(a.counters, 3u, t);
             continue;
         }
         ++written;
@@ -853,6 +890,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ta.offset = s.tile_offset;
     ta.entries = s.entries;
     ta.cap_entries = s.cap_entries;
+    ta.cap_large = s.cap_large;
     ta.keys = s.keys;
     ta.width = p.width;
     ta.height = p.height;
@@ -865,6 +903,8 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     mark(6);
 
     ResolveArgs ra;
+    ra.counters = s.counters;
+    ra.ntri = mesh.ntri;
     ra.keys = s.keys;
     ra.keys_rearm = clear ? s.keys : nullptr;
     ra.tri_v = mesh.tri_v;
