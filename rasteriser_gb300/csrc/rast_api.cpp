@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "rast.h"
 #include "rast_internal.h"
@@ -67,6 +68,7 @@ struct rast_ctx {
     int64_t bin_capacity = 0;  // 0: sized from the mesh
 
     uint64_t last_launches = 0;
+    int n_sm = 1;
 
     // stage timing
     bool timing = false;
@@ -149,7 +151,7 @@ rast_status ensure_scratch(rast_ctx* c, uint32_t w, uint32_t h, uint32_t tiles) 
     c->cap_large = std::max<int64_t>(c->mesh.ntri, 1);
     RAST_CUDA(c, c->large.reserve(sizeof(rast::BinnedTri) * (size_t)c->cap_large));
     RAST_CUDA(c, c->counters.reserve(sizeof(uint32_t) * (rast::kCounterHeader + 2 * (size_t)tiles)));
-    RAST_CUDA(c, c->tile_offset.reserve(sizeof(uint32_t) * ((size_t)tiles + 1)));
+    RAST_CUDA(c, c->tile_offset.reserve(sizeof(uint32_t) * 2 * ((size_t)tiles + 1)));
     if (c->cap_entries == 0)
         c->cap_entries = c->bin_capacity > 0 ? c->bin_capacity : std::max<int64_t>(1 << 20, 2 * c->mesh.ntri);
     RAST_CUDA(c, c->entries.reserve(sizeof(uint32_t) * (size_t)c->cap_entries));
@@ -195,6 +197,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     p.tile = c->tile;
     p.tiles_x = tiles_x;
     p.tiles_y = tiles_y;
+    p.n_sm = c->n_sm;
     p.nl = c->nl;
     p.lights = c->lights.as<float>();
     p.rgb = d_rgb;
@@ -220,7 +223,9 @@ rast_status collect_status(rast_ctx* c) {
     RAST_CUDA(c, cudaMemcpy(&status, c->counters.as<uint32_t>() + 1, sizeof status, cudaMemcpyDeviceToHost));
     if (status & rast::STATUS_BIN_OVERFLOW) {
         unsigned long long need = 0;
-        RAST_CUDA(c, cudaMemcpy(&need, c->stats.as<unsigned long long>() + rast::STAT_BIN_ENTRIES * rast::kStatStride,
+        RAST_CUDA(c, cudaMemcpy(&need,
+                                c->stats.as<unsigned long long>() +
+                                    (size_t)rast::STAT_BIN_ENTRIES * rast::kStatSlots * rast::kSlotWords,
                                 sizeof need, cudaMemcpyDeviceToHost));
         c->cap_entries = std::max<int64_t>((int64_t)need + (int64_t)need / 4, 2 * c->cap_entries);
         RAST_CUDA(c, c->entries.reserve(sizeof(uint32_t) * (size_t)c->cap_entries));
@@ -285,6 +290,8 @@ rast_status rast_create(rast_ctx** out, int device) {
         return fail(nullptr, RAST_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
     }
     c->stream = c->own_stream;
+    if (cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || c->n_sm < 1)
+        c->n_sm = 1;
     *out = c;
     return RAST_OK;
 }
@@ -421,9 +428,10 @@ rast_status rast_get_stats(rast_ctx* c, uint64_t out[8]) {
     if (!c->stats.ptr) return RAST_OK;
     DeviceGuard g(c->device);
     RAST_CUDA(c, cudaStreamSynchronize(c->stream));
-    unsigned long long s[rast::kStatWords];
-    RAST_CUDA(c, cudaMemcpy(s, c->stats.ptr, sizeof s, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < 8; ++i) out[i] = s[i * rast::kStatStride];
+    std::vector<unsigned long long> s(rast::kStatWords);
+    RAST_CUDA(c, cudaMemcpy(s.data(), c->stats.ptr, sizeof(unsigned long long) * s.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 8; ++i)
+        for (int k = 0; k < rast::kStatSlots; ++k) out[i] += s[((size_t)i * rast::kStatSlots + k) * rast::kSlotWords];
     out[rast::STAT_LAUNCHES] = c->last_launches;
     return RAST_OK;
 }

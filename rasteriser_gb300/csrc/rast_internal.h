@@ -20,20 +20,30 @@ struct alignas(16) BinnedTri {
 
 struct Mat4 { float m[16]; };  // column major, m[c*4 + r]
 
-// Stats counters live kStatStride 64-bit words apart (128 bytes) so that blocks adding to
-// different counters do not queue on one L2 line.
-constexpr int kStatStride = 16;
-constexpr int kStatWords = 8 * kStatStride;
+// Statistics counters. Each counter is spread over kStatSlots slots, kSlotWords 64-bit words
+// (128 bytes) apart; warps add into slot (warp id mod kStatSlots), so no counter is a single hot
+// address and no kernel needs a block barrier to reduce them. The host sums the slots.
+constexpr int kStatCounters = 8;
+constexpr int kStatSlots = 32;
+constexpr int kSlotWords = 16;
+constexpr int kStatWords = kStatCounters * kStatSlots * kSlotWords;
 
 enum StatIndex : int {
     STAT_FRONT = 0, STAT_TESTED = 1, STAT_INSIDE = 2, STAT_WRITTEN = 3,
     STAT_BINNED_TRIS = 4, STAT_BIN_ENTRIES = 5, STAT_LAUNCHES = 6, STAT_RESERVED = 7
 };
 
-// Device status word bits.
 // Device status word bits (counters[1]); counters[2] and [3] hold the code and detail of the
 // first failed internal check.
 enum StatusBits : uint32_t { STATUS_BIN_OVERFLOW = 1u, STATUS_LARGE_OVERFLOW = 2u, STATUS_CHECK_FAILED = 4u };
+
+// Words of FrameScratch::counters before the per-tile counts:
+//   [0] binned triangles   [1] status bits   [2] first failed check   [3] its detail
+//   [4] next tile-raster work item           [5..7] unused
+constexpr int kCounterHeader = 8;
+
+// Binned triangles per tile-raster work item.
+constexpr int kTileChunk = 64;
 
 struct DeviceMesh {
     const float* pos = nullptr;      // nv * 3
@@ -50,11 +60,10 @@ struct FrameScratch {
     float4* rv = nullptr;               // nv raster vertices
     unsigned long long* keys = nullptr; // W*H packed (order-preserving depth << 32 | triangle)
     BinnedTri* large = nullptr;         // binned triangles, capacity cap_large
-    uint32_t* counters = nullptr;       // [0] n_large, [1] status, [2] check code, [3] check detail,
-                                        // then tile counts, then tile cursors
-    uint32_t* tile_offset = nullptr;    // n_tiles + 1
+    uint32_t* counters = nullptr;       // kCounterHeader words, n_tiles counts, n_tiles cursors
+    uint32_t* tile_offset = nullptr;    // n_tiles + 1 entry offsets, then n_tiles + 1 work-item offsets
     uint32_t* entries = nullptr;        // bin entries, capacity cap_entries
-    unsigned long long* stats = nullptr;  // 8 counters, kStatStride words apart
+    unsigned long long* stats = nullptr;  // kStatWords
     int64_t cap_large = 0, cap_entries = 0;
 };
 
@@ -65,15 +74,13 @@ struct DrawParams {
     uint32_t small_max;     // bounding boxes up to this many pixels take the per-triangle path
     uint32_t tile;          // tile edge: 8, 16, 32
     uint32_t tiles_x, tiles_y;
+    int32_t n_sm;           // streaming multiprocessors of the device
     int32_t nl;
     const float* lights;    // device, nl * 7
     uint8_t* rgb;           // device planar RGB8
     float* depth;           // device
     uint32_t* tri_id;       // device, nullable
 };
-
-// Number of counter words before the per-tile counts in FrameScratch::counters.
-constexpr int kCounterHeader = 4;
 
 // Launches every kernel of one draw on `stream`. Returns the number of kernel launches made
 // (memsets excluded) or -1 with cudaGetLastError() set.

@@ -10,10 +10,11 @@
 //   k_setup_raster  per triangle: de-index, signed_area_2d cull, bounding_box (drawing.cpp:77-93,
 //                   160-188); triangles with small boxes are rasterised here by their warp, the
 //                   rest are appended to the binned list and counted into 16x16 (8/32) tiles
-//   k_bin_scan      exclusive scan of the tile counts
+//   k_bin_scan      exclusive scans of the tile counts and of the tile work items
 //   k_bin_scatter   binned triangles into per-tile lists
-//   k_tile_raster   one CTA per tile; each thread owns a pixel and keeps its minimum key in a
-//                   register; warp ballots skip triangles that miss a warp's 8x4 block
+//   k_tile_raster   persistent CTAs take (tile, up to 64 binned triangles) work items; each thread
+//                   owns pixels of the tile and keeps their minimum keys in registers; warp
+//                   ballots give the coverage masks and skip triangles that miss a warp's block
 //   k_resolve       per pixel: decode the winner, recompute its barycentrics, perspective-correct
 //                   normal, Lambert shading over the lights (shading.cpp:20-34), planar RGB8 +
 //                   depth writes
@@ -143,6 +144,14 @@ __device__ __forceinline__ bool front_facing(float4 a, float4 b, float4 c, bool 
     return (sa > 0.f) != cw;
 }
 
+// transform_direction with the normal matrix (geometry.cpp:35-42, 97-108).
+__device__ __forceinline__ float3 camera_normal(const Mat4& M, float x, float y, float z) {
+    return make_float3(mrow(M, 0, x, y, z, 0.f), mrow(M, 1, x, y, z, 0.f), mrow(M, 2, x, y, z, 0.f));
+}
+
+// ---------------------------------------------------------------------------------------------
+// warp and bookkeeping helpers
+// ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v, int lane) {
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -165,15 +174,18 @@ __device__ __noinline__ void report(uint32_t* counters, uint32_t code, uint32_t 
     if (atomicCAS(&counters[2], 0u, code) == 0u) atomicExch(&counters[3], detail);
 }
 
-__device__ __forceinline__ unsigned long long* stat(unsigned long long* stats, int i) {
-    return stats + i * kStatStride;
+// Adds the warp's sum of v to statistics counter `which`, in the slot of this warp. Must be
+// called by all 32 lanes.
+__device__ __forceinline__ void stat_add(unsigned long long* stats, int which, unsigned long long v) {
+    v = warp_sum64(v);
+    if ((threadIdx.x & 31) == 0 && v) {
+        const uint32_t warp_id = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) + blockIdx.y * 977u;
+        atomicAdd(stats + ((size_t)which * kStatSlots + (warp_id % kStatSlots)) * kSlotWords, v);
+    }
 }
 
-// Adds a per-thread value to a block-wide counter in shared memory (warp-reduced first). The block
-// then makes one global atomic per counter, so thousands of warps do not queue on one address.
-__device__ __forceinline__ void block_accumulate(unsigned long long* s_counter, unsigned long long v) {
-    v = warp_sum64(v);
-    if ((threadIdx.x & 31) == 0 && v) atomicAdd(s_counter, v);
+__device__ __forceinline__ unsigned long long* stat_slot0(unsigned long long* stats, int which) {
+    return stats + (size_t)which * kStatSlots * kSlotWords;
 }
 
 // First lane j whose inclusive prefix exceeds k (the owner of work item k).
@@ -242,24 +254,24 @@ __global__ void __launch_bounds__(256) k_split_triangles(const int32_t* __restri
 
 constexpr int kSetupThreads = 256;
 constexpr int kSetupWarps = kSetupThreads / 32;
+// Bounding boxes at most this many pixels wide take the per-triangle path; wider ones are binned.
+constexpr uint32_t kSmallMaxRow = 32;
+// Pixels of one bounding-box row handled by one work item of the per-triangle path.
+constexpr uint32_t kRowChunk = 4;
 
 // Per-warp staging of 32 triangles. rec[j] holds lane j's triangle as five float4s so a lane
 // working on another lane's triangle loads it with five 16-byte shared loads:
 //   rec[j][0] = x0 y0 x1 y1      rec[j][1] = x2 y2 area nthr
 //   rec[j][2] = d12x d12y d20x d20y
 //   rec[j][3] = d01x d01y sgn -   rec[j][4] = z0 z1 z2 -
-// Its integer data (column range packed as tlx | brx << 16, first row, row count) is kept in
-// integer arrays.
+// Its integer data (bounding box, items per row) is kept in integer arrays.
 struct SetupStage {
     float4 rec[32][5];
-    uint32_t xr[32], ty[32], nrows[32];
-    uint32_t tlx[32], tly[32], bw[32], incl[32];
-    float rbw[32];
+    uint32_t tlx[32], tly[32], brx[32], cpr[32];
+    float rcpr[32];
+    uint32_t incl[32];
     int slot[32];
 };
-
-// Bounding boxes at most this many pixels wide take the per-triangle path; wider ones are binned.
-constexpr uint32_t kSmallMaxRow = 32;
 
 struct SetupArgs {
     const int32_t* tri_v;
@@ -274,25 +286,31 @@ struct SetupArgs {
     unsigned long long* keys;
     BinnedTri* large;
     int64_t cap_large;
-    uint32_t* counters;  // [0] n_large, [1] status, then tile counts
+    uint32_t* counters;
     unsigned long long* stats;
 };
 
-// One thread per triangle. Front-facing triangles whose bounding box holds at most small_max
-// pixels are rasterised by their warp: the 32 boxes are laid end to end and the warp walks the
-// concatenation 32 pixels at a time, so lanes stay busy whatever the box sizes. Larger triangles
-// go to the binned list, and their warp adds them to the tile counts the same way.
+// One thread per triangle: load, cull and bound it. Front-facing triangles whose bounding box is
+// at most small_max pixels and kSmallMaxRow pixels wide are rasterised by their warp; the others
+// are appended to the binned list (one atomic per block) and counted into the tiles their box
+// overlaps.
+//
+// The warp's raster work is split into items of up to kRowChunk pixels of one bounding-box row.
+// The items of its 32 triangles are laid end to end and taken 32 at a time, so every lane has at
+// most kRowChunk pixels whatever the box sizes. The owner of an item is the last triangle whose
+// items start at or before it in the current window (an OR-reduction of start positions), else
+// the owner of the window's first item, carried over from the previous window. Each edge function
+//   e = (b.x - a.x)*(py - a.y) - (b.y - a.y)*(px - a.x)     (drawing.cpp:36-39)
+// is evaluated as the reference does, its first product taken once per item.
 __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
     __shared__ SetupStage stage[kSetupWarps];
     __shared__ uint32_t s_large[kSetupWarps];
     __shared__ uint32_t s_large_base;
-    __shared__ unsigned long long s_stat[3];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x < 3) s_stat[threadIdx.x] = 0;
     SetupStage& S = stage[warp];
     const int64_t t = blockIdx.x * (int64_t)kSetupThreads + threadIdx.x;
 
-    uint32_t n_small = 0, n_tiles = 0;
+    uint32_t n_items = 0, n_tiles = 0, cpr = 1;
     uint32_t tlx = 0, tly = 0, brx = 0, bry = 0;
     EdgeTri T;
     unsigned long long c_front = 0;
@@ -307,7 +325,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
             const unsigned long long npx = (unsigned long long)bw * bh;
             make_edge_tri(v0, v1, v2, T);
             if (npx <= a.small_max && bw <= kSmallMaxRow) {
-                n_small = (uint32_t)npx;
+                cpr = (bw + kRowChunk - 1u) / kRowChunk;
+                n_items = bh * cpr;
             } else {
                 large = true;
             }
@@ -328,99 +347,92 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
         s_large_base = tot ? atomicAdd(&a.counters[0], tot) : 0u;
     }
     __syncthreads();
-    if (lmask) {
-        const uint32_t base = s_large_base + s_large[warp];
-        if (large) {
-            const uint32_t slot = base + __popc(lmask & ((1u << lane) - 1u));
-            if (slot < a.cap_large) {
-                BinnedTri r;
-                r.x0 = T.x0; r.y0 = T.y0; r.x1 = T.x1; r.y1 = T.y1;
-                r.x2 = T.x2; r.y2 = T.y2; r.z0 = T.z0; r.z1 = T.z1;
-                r.z2 = T.z2; r.area = T.area; r.thr = T.nthr; r.sgn = T.sgn;
-                r.tri = (uint32_t)t; r.tl = tlx | (tly << 16); r.br = brx | (bry << 16); r.pad = 0;
-                a.large[slot] = r;
-                const uint32_t tx0 = tlx >> a.tile_shift, tx1 = brx >> a.tile_shift;
-                const uint32_t ty0 = tly >> a.tile_shift, ty1 = bry >> a.tile_shift;
-                n_tiles = (tx1 - tx0 + 1u) * (ty1 - ty0 + 1u);
-            } else {
-                atomicOr(&a.counters[1], STATUS_LARGE_OVERFLOW);
-            }
+    if (large) {
+        const uint32_t slot = s_large_base + s_large[warp] + __popc(lmask & ((1u << lane) - 1u));
+        if (slot < a.cap_large) {
+            BinnedTri r;
+            r.x0 = T.x0; r.y0 = T.y0; r.x1 = T.x1; r.y1 = T.y1;
+            r.x2 = T.x2; r.y2 = T.y2; r.z0 = T.z0; r.z1 = T.z1;
+            r.z2 = T.z2; r.area = T.area; r.thr = T.nthr; r.sgn = T.sgn;
+            r.tri = (uint32_t)t; r.tl = tlx | (tly << 16); r.br = brx | (bry << 16); r.pad = 0;
+            a.large[slot] = r;
+            const uint32_t tx0 = tlx >> a.tile_shift, tx1 = brx >> a.tile_shift;
+            const uint32_t ty0 = tly >> a.tile_shift, ty1 = bry >> a.tile_shift;
+            n_tiles = (tx1 - tx0 + 1u) * (ty1 - ty0 + 1u);
+        } else {
+            atomicOr(&a.counters[1], STATUS_LARGE_OVERFLOW);
         }
     }
 
     unsigned long long c_tested = 0, c_inside = 0;
 
-    // Cooperative raster of the warp's small triangles. A work item is one bounding-box row of one
-    // triangle; the warp's rows are laid end to end and taken 32 at a time, so lanes stay busy
-    // whatever the box sizes. The owner of an item is the last triangle whose rows start at or
-    // before it in the current window (an OR-reduction of start positions), else the owner of the
-    // window's first item carried over from the previous window. Each edge function
-    //   e = (b.x - a.x)*(py - a.y) - (b.y - a.y)*(px - a.x)     (drawing.cpp:36-39)
-    // is evaluated as the reference does, with its first product taken once per row.
+    // Cooperative raster of the warp's small triangles.
     {
-        const uint32_t n_rows = n_small ? (bry - tly + 1u) : 0u;
-        const uint32_t incl = warp_inclusive_scan(n_rows, lane);
+        const uint32_t incl = warp_inclusive_scan(n_items, lane);
         const uint32_t total = __shfl_sync(kFull, incl, 31);
         if (total) {
-            const uint32_t start = incl - n_rows;
+            const uint32_t start = incl - n_items;
             S.rec[lane][0] = make_float4(T.x0, T.y0, T.x1, T.y1);
             S.rec[lane][1] = make_float4(T.x2, T.y2, T.area, T.nthr);
             S.rec[lane][2] = make_float4(T.d12x, T.d12y, T.d20x, T.d20y);
             S.rec[lane][3] = make_float4(T.d01x, T.d01y, T.sgn, 0.f);
             S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, 0.f);
-            S.xr[lane] = tlx | (brx << 16);
-            S.ty[lane] = tly;
-            S.nrows[lane] = n_rows;
+            S.tlx[lane] = tlx;
+            S.tly[lane] = tly;
+            S.brx[lane] = brx;
+            S.cpr[lane] = cpr;
+            S.rcpr[lane] = __frcp_rn((float)cpr);
+            S.incl[lane] = incl;
             __syncwarp();
             const uint32_t tri_base = (uint32_t)(blockIdx.x * (int64_t)kSetupThreads + warp * 32);
             int carry = 0;
             for (uint32_t base = 0; base < total; base += 32) {
-                // Bit b of `starts` is set when a triangle's rows begin at item base + b; that
+                // Bit b of `starts` is set when a triangle's items begin at item base + b; that
                 // triangle's lane is in slot[b].
-                const bool opens = n_rows != 0u && start >= base && start < base + 32u;
+                const bool opens = n_items != 0u && start >= base && start < base + 32u;
                 if (opens) S.slot[start - base] = lane;
                 const unsigned starts = __reduce_or_sync(kFull, opens ? (1u << (start - base)) : 0u);
                 __syncwarp();
                 const unsigned upto = starts & (0xFFFFFFFFu >> (31 - lane));
                 const int owner = upto ? S.slot[31 - __clz(upto)] : carry;
-                const uint32_t ostart = __shfl_sync(kFull, start, owner);
                 carry = __shfl_sync(kFull, owner, 31);
                 __syncwarp();
                 const uint32_t k = base + lane;
-                if (k < total) {
+                if (k >= total) continue;
+                const uint32_t ostart = owner ? S.incl[owner - 1] : 0u;
+                const uint32_t local = k - ostart;
+                const uint32_t ocpr = S.cpr[owner];
+                const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
+                const uint32_t x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
+                const uint32_t x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
+                const uint32_t y = S.tly[owner] + row;
 #ifdef RAST_CHECKED
-                    if (owner < 0 || owner > 31 || k < ostart || k - ostart >= S.nrows[owner] ||
-                        (S.xr[owner] & 0xFFFFu) > (S.xr[owner] >> 16) || (S.xr[owner] >> 16) >= a.width ||
-                        S.ty[owner] + (k - ostart) >= a.height) {
-                        report(a.counters, 1u, (uint32_t)owner);
-                        continue;
-                    }
+                if (owner < 0 || owner > 31 || local >= S.incl[owner] - ostart || x_lo > x_hi || x_hi >= a.width ||
+                    y >= a.height) {
+                    report(a.counters, 1u, (uint32_t)owner);
+                    continue;
+                }
 #endif
-                    const float4 q0 = S.rec[owner][0], q1 = S.rec[owner][1], q2 = S.rec[owner][2],
-                                 q3 = S.rec[owner][3];
-                    const uint32_t xr = S.xr[owner];
-                    const uint32_t x_lo = xr & 0xFFFFu, x_hi = xr >> 16;
-                    const uint32_t y = S.ty[owner] + (k - ostart);
-                    const float py = (float)y;
-                    const float p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
-                    const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
-                    const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
-                    const float sg = q3.z, nt = q1.w, area = q1.z;
-                    for (uint32_t x = x_lo; x <= x_hi; ++x) {
-                        const float px = (float)x;
-                        const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));  // - d12y * (px - x1)
-                        const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));  // - d20y * (px - x2)
-                        const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));  // - d01y * (px - x0)
-                        if (mul(sg, e0) < nt || mul(sg, e1) < nt || mul(sg, e2) < nt) continue;
-                        const float b0 = dvd(e0, area), b1 = dvd(e1, area), b2 = dvd(e2, area);
-                        if (!(b0 >= 0.f && b1 >= 0.f && b2 >= 0.f)) continue;
-                        ++c_inside;
-                        const float4 q4 = S.rec[owner][4];
-                        const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
-                        if (z == z && x < a.width && y < a.height)
-                            atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + (uint32_t)owner));
-                    }
-                    c_tested += x_hi - x_lo + 1u;
+                const float4 q0 = S.rec[owner][0], q1 = S.rec[owner][1], q2 = S.rec[owner][2], q3 = S.rec[owner][3];
+                const float py = (float)y;
+                const float p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
+                const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
+                const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
+                const float sg = q3.z, nt = q1.w, area = q1.z;
+                c_tested += x_hi - x_lo + 1u;
+                for (uint32_t x = x_lo; x <= x_hi; ++x) {
+                    const float px = (float)x;
+                    const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));  // - d12y * (px - x1)
+                    const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));  // - d20y * (px - x2)
+                    const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));  // - d01y * (px - x0)
+                    if (mul(sg, e0) < nt || mul(sg, e1) < nt || mul(sg, e2) < nt) continue;
+                    const float b0 = dvd(e0, area), b1 = dvd(e1, area), b2 = dvd(e2, area);
+                    if (!(b0 >= 0.f && b1 >= 0.f && b2 >= 0.f)) continue;
+                    ++c_inside;
+                    const float4 q4 = S.rec[owner][4];
+                    const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
+                    if (z == z && x < a.width && y < a.height)
+                        atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + (uint32_t)owner));
                 }
             }
             __syncwarp();
@@ -433,9 +445,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
         const uint32_t total = __shfl_sync(kFull, incl, 31);
         if (total) {
             const uint32_t tx0 = tlx >> a.tile_shift, tx1 = brx >> a.tile_shift;
-            S.tlx[lane] = tx0; S.tly[lane] = tly >> a.tile_shift;
-            S.bw[lane] = tx1 - tx0 + 1u;
-            S.rbw[lane] = __frcp_rn((float)(tx1 - tx0 + 1u));
+            const uint32_t tw = tx1 - tx0 + 1u;
+            S.tlx[lane] = tx0;
+            S.tly[lane] = tly >> a.tile_shift;
+            S.cpr[lane] = tw;
+            S.rcpr[lane] = __frcp_rn((float)tw);
             S.incl[lane] = incl;
             __syncwarp();
             for (uint32_t base = 0; base < total; base += 32) {
@@ -443,8 +457,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                 if (k < total) {
                     const int j = owner_of(S.incl, k);
                     const uint32_t local = k - (j ? S.incl[j - 1] : 0u);
-                    const uint32_t w = S.bw[j];
-                    const uint32_t dy = div_small(local, w, S.rbw[j]);
+                    const uint32_t w = S.cpr[j];
+                    const uint32_t dy = div_small(local, w, S.rcpr[j]);
                     const uint32_t tile = (S.tly[j] + dy) * a.tiles_x + S.tlx[j] + (local - dy * w);
                     if (tile < a.n_tiles) atomicAdd(&a.counters[kCounterHeader + tile], 1u);
                 }
@@ -452,60 +466,72 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
         }
     }
 
-    block_accumulate(&s_stat[0], c_front);
-    block_accumulate(&s_stat[1], c_tested);
-    block_accumulate(&s_stat[2], c_inside);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        if (s_stat[0]) atomicAdd(stat(a.stats, STAT_FRONT), s_stat[0]);
-        if (s_stat[1]) atomicAdd(stat(a.stats, STAT_TESTED), s_stat[1]);
-        if (s_stat[2]) atomicAdd(stat(a.stats, STAT_INSIDE), s_stat[2]);
-    }
+    stat_add(a.stats, STAT_FRONT, c_front);
+    stat_add(a.stats, STAT_TESTED, c_tested);
+    stat_add(a.stats, STAT_INSIDE, c_inside);
 }
 
-// Exclusive scan of the per-tile counts into tile_offset[0..n_tiles]; one CTA of 1024 threads
-// walks the counts 4096 at a time. Flags an overflow of the bin pool.
+// Exclusive scans over the tiles: entry offsets (the tile counts) into offset[0..n_tiles] and
+// work-item offsets (ceil(count / kTileChunk)) into offset[n_tiles+1 .. 2*n_tiles+1]. One CTA of
+// 1024 threads walks the tiles 4096 at a time. Flags an overflow of the bin pool.
 __global__ void __launch_bounds__(1024) k_bin_scan(const uint32_t* __restrict__ counters, uint32_t n_tiles,
                                                    uint32_t* __restrict__ offset, int64_t cap_entries,
                                                    uint32_t* __restrict__ status, unsigned long long* stats) {
-    __shared__ uint32_t warp_tot[32];
-    __shared__ uint32_t carry_s;
+    __shared__ uint32_t warp_tot[2][32];
+    __shared__ uint32_t carry_s[2];
     const uint32_t* cnt = counters + kCounterHeader;
+    uint32_t* chunk_offset = offset + n_tiles + 1;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) carry_s = 0;
+    if (tid < 2) carry_s[tid] = 0;
     __syncthreads();
     for (uint32_t base = 0; base < n_tiles; base += 4096) {
-        uint32_t v[4];
-        uint32_t s = 0;
+        uint32_t v[4], c[4];
+        uint32_t s = 0, sc = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const uint32_t i = base + tid * 4 + k;
             v[k] = i < n_tiles ? cnt[i] : 0u;
+            c[k] = (v[k] + kTileChunk - 1) / kTileChunk;
             s += v[k];
+            sc += c[k];
         }
         const uint32_t incl = warp_inclusive_scan(s, lane);
-        if (lane == 31) warp_tot[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            const uint32_t w = warp_tot[lane];
-            warp_tot[lane] = warp_inclusive_scan(w, lane) - w;
+        const uint32_t incl_c = warp_inclusive_scan(sc, lane);
+        if (lane == 31) {
+            warp_tot[0][warp] = incl;
+            warp_tot[1][warp] = incl_c;
         }
         __syncthreads();
-        uint32_t run = carry_s + warp_tot[warp] + incl - s;
+        if (warp == 0) {
+            const uint32_t w = warp_tot[0][lane], wc = warp_tot[1][lane];
+            warp_tot[0][lane] = warp_inclusive_scan(w, lane) - w;
+            warp_tot[1][lane] = warp_inclusive_scan(wc, lane) - wc;
+        }
+        __syncthreads();
+        uint32_t run = carry_s[0] + warp_tot[0][warp] + incl - s;
+        uint32_t run_c = carry_s[1] + warp_tot[1][warp] + incl_c - sc;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const uint32_t i = base + tid * 4 + k;
-            if (i < n_tiles) offset[i] = run;
+            if (i < n_tiles) {
+                offset[i] = run;
+                chunk_offset[i] = run_c;
+            }
             run += v[k];
+            run_c += c[k];
         }
         __syncthreads();
-        if (tid == 1023) carry_s = run;
+        if (tid == 1023) {
+            carry_s[0] = run;
+            carry_s[1] = run_c;
+        }
         __syncthreads();
     }
     if (tid == 0) {
-        offset[n_tiles] = carry_s;
-        *stat(stats, STAT_BIN_ENTRIES) = carry_s;
-        if ((int64_t)carry_s > cap_entries) atomicOr(status, STATUS_BIN_OVERFLOW);
+        offset[n_tiles] = carry_s[0];
+        chunk_offset[n_tiles] = carry_s[1];
+        *stat_slot0(stats, STAT_BIN_ENTRIES) = carry_s[0];
+        if ((int64_t)carry_s[0] > cap_entries) atomicOr(status, STATUS_BIN_OVERFLOW);
     }
 }
 
@@ -528,7 +554,7 @@ __global__ void __launch_bounds__(256) k_bin_scatter(ScatterArgs a) {
     __shared__ float s_rtw[8][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t n_large = (uint32_t)min((int64_t)a.counters[0], a.cap_large);
-    if (blockIdx.x == 0 && threadIdx.x == 0) *stat(a.stats, STAT_BINNED_TRIS) = n_large;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *stat_slot0(a.stats, STAT_BINNED_TRIS) = n_large;
     for (uint32_t wb = (blockIdx.x * 256u + warp * 32u); wb < n_large; wb += gridDim.x * 256u) {
         const uint32_t i = wb + lane;
         uint32_t n = 0, tx0 = 0, ty0 = 0, tw = 1;
@@ -563,8 +589,6 @@ __global__ void __launch_bounds__(256) k_bin_scatter(ScatterArgs a) {
     }
 }
 
-constexpr int kTileChunk = 256;
-
 struct TileStage {
     float x0[kTileChunk], y0[kTileChunk], x1[kTileChunk], y1[kTileChunk], x2[kTileChunk], y2[kTileChunk];
     float d12x[kTileChunk], d12y[kTileChunk], d20x[kTileChunk], d20y[kTileChunk], d01x[kTileChunk],
@@ -575,52 +599,58 @@ struct TileStage {
 
 struct TileArgs {
     const BinnedTri* large;
-    uint32_t* counters;        // [0] binned triangles, [1..3] status, then tile counts
-    const uint32_t* offset;
+    uint32_t* counters;        // [0] binned triangles, [1..3] status, [4] work counter, then tile counts
+    const uint32_t* offset;    // entry offsets (n_tiles + 1), then work-item offsets (n_tiles + 1)
     const uint32_t* entries;
     int64_t cap_entries, cap_large;
     unsigned long long* keys;
-    uint32_t width, height, tiles_x;
+    uint32_t width, height, tiles_x, n_tiles;
     unsigned long long* stats;
 };
 
-// One CTA per TS x TS tile; each thread owns PPT pixels (a warp covers an 8x4 block per pixel
-// slot) and keeps their minimum keys in registers, so the tile needs no atomics. The per-triangle
-// pass of k_setup_raster ran earlier on the stream, so the tile's keys are final apart from this
-// CTA and are read and written back plainly.
+// Persistent CTAs take work items (a tile and up to kTileChunk of its binned triangles) from a
+// counter until none are left, so a tile crowded with triangles is shared out among CTAs. Each
+// thread owns kPPT pixels of the tile (a warp covers an 8x4 block per pixel slot) and keeps their
+// minimum keys in registers; the item ends with one 64-bit atomicMin per pixel it improved (items
+// of one tile may run at once, and the per-triangle pass wrote its keys earlier on the stream).
 template <int TS>
 __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
     constexpr int kThreads = (TS * TS < 256) ? TS * TS : 256;
     constexpr int kPPT = (TS * TS) / kThreads;  // pixels per thread
     constexpr int kBlocksX = TS / 8;             // 8x4 blocks across a tile
     __shared__ TileStage S;
-    const uint32_t tile = blockIdx.x;
-    const uint32_t count = a.counters[kCounterHeader + tile];
-    if (count == 0) return;
-    const uint32_t first = a.offset[tile];
-    const uint32_t tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+    __shared__ uint32_t s_item, s_tile;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-    uint32_t px[kPPT], py[kPPT];
-    bool valid[kPPT];
-    unsigned long long best[kPPT], orig[kPPT];
-#pragma unroll
-    for (int s = 0; s < kPPT; ++s) {
-        const int blk = warp + s * (kThreads / 32);
-        px[s] = tx * TS + (blk % kBlocksX) * 8 + (lane & 7);
-        py[s] = ty * TS + (blk / kBlocksX) * 4 + (lane >> 3);
-        valid[s] = px[s] < a.width && py[s] < a.height;
-        orig[s] = valid[s] ? a.keys[(size_t)py[s] * a.width + px[s]] : ~0ull;
-        best[s] = orig[s];
-    }
+    const uint32_t* chunk_offset = a.offset + a.n_tiles + 1;
+    const uint32_t total_items = chunk_offset[a.n_tiles];
+    const uint32_t n_large = a.counters[0];
     unsigned long long c_tested = 0, c_inside = 0;
 
-    for (uint32_t c0 = 0; c0 < count; c0 += kTileChunk) {
-        const uint32_t n = min((uint32_t)kTileChunk, count - c0);
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t item = atomicAdd(&a.counters[4], 1u);
+            uint32_t tile = 0;
+            if (item < total_items) {
+                // last tile whose first work item is <= item
+                uint32_t lo = 0, hi = a.n_tiles - 1u;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1u) >> 1;
+                    if (chunk_offset[mid] <= item) lo = mid; else hi = mid - 1u;
+                }
+                tile = lo;
+            }
+            s_item = item;
+            s_tile = tile;
+        }
         __syncthreads();
-        const uint32_t n_large = a.counters[0];
+        const uint32_t item = s_item, tile = s_tile;
+        if (item >= total_items) break;
+        const uint32_t count = a.counters[kCounterHeader + tile];
+        const uint32_t c0 = (item - chunk_offset[tile]) * kTileChunk;
+        const uint32_t n = min((uint32_t)kTileChunk, count - c0);
+        const uint32_t first = a.offset[tile] + c0;
         for (uint32_t i = threadIdx.x; i < n; i += kThreads) {
-            const uint32_t e = first + c0 + i;
+            const uint32_t e = first + i;
             uint32_t idx = (int64_t)e < a.cap_entries ? a.entries[e] : 0u;
             if (idx >= n_large || (int64_t)idx >= a.cap_large) {
                 // Only a pool overflow (already flagged) can leave an entry unwritten.
@@ -637,6 +667,19 @@ __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
             S.tri[i] = r.tri; S.tl[i] = r.tl; S.br[i] = r.br;
         }
         __syncthreads();
+
+        const uint32_t tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+        uint32_t px[kPPT], py[kPPT];
+        bool valid[kPPT];
+        unsigned long long best[kPPT];
+#pragma unroll
+        for (int s = 0; s < kPPT; ++s) {
+            const int blk = warp + s * (kThreads / 32);
+            px[s] = tx * TS + (blk % kBlocksX) * 8 + (lane & 7);
+            py[s] = ty * TS + (blk / kBlocksX) * 4 + (lane >> 3);
+            valid[s] = px[s] < a.width && py[s] < a.height;
+            best[s] = ~0ull;
+        }
         for (uint32_t j = 0; j < n; ++j) {
             const uint32_t tl = S.tl[j], br = S.br[j];
             const uint32_t tlx = tl & 0xFFFFu, tly = tl >> 16, brx = br & 0xFFFFu, bry = br >> 16;
@@ -668,21 +711,13 @@ __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
                 if (lane == 0) c_inside += (unsigned)__popc(mask);
             }
         }
-    }
 #pragma unroll
-    for (int s = 0; s < kPPT; ++s)
-        if (valid[s] && best[s] != orig[s]) a.keys[(size_t)py[s] * a.width + px[s]] = best[s];
-
-    __shared__ unsigned long long s_stat[2];
-    if (threadIdx.x < 2) s_stat[threadIdx.x] = 0;
-    __syncthreads();
-    block_accumulate(&s_stat[0], c_tested);
-    block_accumulate(&s_stat[1], c_inside);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        if (s_stat[0]) atomicAdd(stat(a.stats, STAT_TESTED), s_stat[0]);
-        if (s_stat[1]) atomicAdd(stat(a.stats, STAT_INSIDE), s_stat[1]);
+        for (int s = 0; s < kPPT; ++s)
+            if (valid[s] && best[s] != ~0ull) atomicMin(&a.keys[(size_t)py[s] * a.width + px[s]], best[s]);
+        __syncthreads();  // the stage and s_item are rewritten by the next item
     }
+    stat_add(a.stats, STAT_TESTED, c_tested);
+    stat_add(a.stats, STAT_INSIDE, c_inside);
 }
 
 struct ResolveArgs {
@@ -698,99 +733,179 @@ struct ResolveArgs {
     const float* lights;
     int32_t nl;
     Mat4 normal;
-    uint32_t width;
-    int64_t npx;
+    uint32_t width, height;
     bool cw, clear;
+    bool vec_ok;  // width % 4 == 0, rgb 4-byte and depth 16-byte aligned: 4-pixel vector access
     uint8_t* rgb;
     float* depth;
     uint32_t* tri_id;
     unsigned long long* stats;
 };
 
-// transform_direction with the normal matrix (geometry.cpp:35-42, 97-108).
-__device__ __forceinline__ float3 camera_normal(const Mat4& M, const float* n) {
-    const float x = n[0], y = n[1], z = n[2];
-    return make_float3(mrow(M, 0, x, y, z, 0.f), mrow(M, 1, x, y, z, 0.f), mrow(M, 2, x, y, z, 0.f));
+constexpr int kResolveThreads = 64;
+constexpr int kResolvePx = 4;  // consecutive pixels of one row per thread
+
+// Shades one winning fragment exactly as update_pixel does (drawing.cpp:108-146,
+// shading.cpp:20-34): barycentrics at the integer pixel, NDC depth, perspective-correct normal,
+// normalise, clockwise flip, Lambert sum over the lights, clamp to 255 and truncate.
+__device__ __forceinline__ void shade_fragment(const ResolveArgs& a, uint32_t x, uint32_t y, float4 v0, float4 v1,
+                                               float4 v2, float3 n0, float3 n1, float3 n2, int mat, float& depth,
+                                               uint32_t& rgb) {
+    EdgeTri T;
+    make_edge_tri(v0, v1, v2, T);
+    const float pxf = (float)x, pyf = (float)y;
+    const float e0 = sub(mul(T.d12x, sub(pyf, T.y1)), mul(T.d12y, sub(pxf, T.x1)));
+    const float e1 = sub(mul(T.d20x, sub(pyf, T.y2)), mul(T.d20y, sub(pxf, T.x2)));
+    const float e2 = sub(mul(T.d01x, sub(pyf, T.y0)), mul(T.d01y, sub(pxf, T.x0)));
+    const float b0 = dvd(e0, T.area), b1 = dvd(e1, T.area), b2 = dvd(e2, T.area);
+    depth = interp_depth(T, b0, b1, b2);
+
+    const float i0 = mul(v0.w, b0), i1 = mul(v1.w, b1), i2 = mul(v2.w, b2);
+    const float dd = dvd(1.f, add(add(i0, i1), i2));
+    float sx = add(add(mul(i0, n0.x), mul(i1, n1.x)), mul(i2, n2.x));
+    float sy = add(add(mul(i0, n0.y), mul(i1, n1.y)), mul(i2, n2.y));
+    float sz = add(add(mul(i0, n0.z), mul(i1, n1.z)), mul(i2, n2.z));
+    sx = mul(dd, sx); sy = mul(dd, sy); sz = mul(dd, sz);
+    const float inv = dvd(1.0f, __fsqrt_rn(add(add(mul(sx, sx), mul(sy, sy)), mul(sz, sz))));
+    float nx = mul(sx, inv), ny = mul(sy, inv), nz = mul(sz, inv);
+    if (a.cw) { nx = -nx; ny = -ny; nz = -nz; }
+
+    const float* kd = a.kd + 3 * (int64_t)mat;
+    const float ar = __ldg(kd), ag = __ldg(kd + 1), ab = __ldg(kd + 2);
+    const float one_over_pi = 0.318309886183790671537767526745028724f;
+    float accr = 0.f, accg = 0.f, accb = 0.f;
+    for (int l = 0; l < a.nl; ++l) {
+        const float* L = a.lights + 7 * l;
+        const float I = __ldg(L + 3);
+        float cr = mul(I, __ldg(L + 4)), cg = mul(I, __ldg(L + 5)), cb = mul(I, __ldg(L + 6));
+        cr = mul(cr, ar); cg = mul(cg, ag); cb = mul(cb, ab);
+        const float d = add(add(mul(nx, -__ldg(L)), mul(ny, -__ldg(L + 1))), mul(nz, -__ldg(L + 2)));
+        const float m = gmax(0.f, d);
+        cr = mul(mul(cr, m), one_over_pi);
+        cg = mul(mul(cg, m), one_over_pi);
+        cb = mul(mul(cb, m), one_over_pi);
+        accr = add(accr, cr); accg = add(accg, cg); accb = add(accb, cb);
+    }
+    const uint32_t r = __float2uint_rz(gmin(accr, 255.f)) & 0xFFu;
+    const uint32_t g = __float2uint_rz(gmin(accg, 255.f)) & 0xFFu;
+    const uint32_t b = __float2uint_rz(gmin(accb, 255.f)) & 0xFFu;
+    rgb = r | (g << 8) | (b << 16);
 }
 
-// Per pixel: the winning triangle's fragment is recomputed and shaded exactly as update_pixel
-// shades it (drawing.cpp:108-146, shading.cpp:20-34).
-__global__ void __launch_bounds__(256) k_resolve(ResolveArgs a) {
-    const unsigned long long rearm = arm_key(1.0f);
+// Per pixel: the winning triangle's fragment is recomputed and shaded. Each thread takes
+// kResolvePx consecutive pixels of one row (grid: x blocks across a row, one block row per image
+// row). The winners' index loads, then their vertex and normal loads, are issued together before
+// any shading, so a thread has several memory requests in flight.
+__global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
+    const uint32_t y = blockIdx.y;
+    const uint32_t x0 = (blockIdx.x * kResolveThreads + threadIdx.x) * kResolvePx;
+    const uint32_t W = a.width;
     unsigned long long written = 0;
-    const int64_t plane = a.npx;
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.npx; p += (int64_t)gridDim.x * blockDim.x) {
-        const unsigned long long key = a.keys[p];
-        if (a.keys_rearm) a.keys_rearm[p] = rearm;
-        const uint32_t t = (uint32_t)(key & 0xFFFFFFFFull);
-        if (t == 0xFFFFFFFFu) {
-            if (a.clear) {
-                a.rgb[p] = 0; a.rgb[p + plane] = 0; a.rgb[p + 2 * plane] = 0;
-                a.depth[p] = 1.0f;
+    if (x0 < W) {
+        const size_t p0 = (size_t)y * W + x0;
+        const size_t plane = (size_t)W * a.height;
+        const uint32_t n = min((uint32_t)kResolvePx, W - x0);
+        const bool vec = a.vec_ok;  // then p0 is a multiple of 4 and every vector access is aligned
+        unsigned long long key[kResolvePx];
+        if (vec) {
+            const ulonglong2 k01 = *reinterpret_cast<const ulonglong2*>(a.keys + p0);
+            const ulonglong2 k23 = *reinterpret_cast<const ulonglong2*>(a.keys + p0 + 2);
+            key[0] = k01.x; key[1] = k01.y; key[2] = k23.x; key[3] = k23.y;
+        } else {
+#pragma unroll
+            for (int k = 0; k < kResolvePx; ++k) key[k] = (uint32_t)k < n ? a.keys[p0 + k] : kNoWinner;
+        }
+        if (a.keys_rearm) {
+            const unsigned long long r = arm_key(1.0f);
+            if (vec) {
+                *reinterpret_cast<ulonglong2*>(a.keys_rearm + p0) = make_ulonglong2(r, r);
+                *reinterpret_cast<ulonglong2*>(a.keys_rearm + p0 + 2) = make_ulonglong2(r, r);
+            } else {
+                for (uint32_t k = 0; k < n; ++k) a.keys_rearm[p0 + k] = r;
             }
-            if (a.tri_id) a.tri_id[p] = 0xFFFFFFFFu;
-            continue;
         }
-        if ((int64_t)t >= a.ntri) {
-            report(a.counters, 3u, t);
-            continue;
+        uint32_t t[kResolvePx];
+        bool win[kResolvePx];
+#pragma unroll
+        for (int k = 0; k < kResolvePx; ++k) {
+            t[k] = (uint32_t)(key[k] & 0xFFFFFFFFull);
+            win[k] = t[k] != 0xFFFFFFFFu;
+            if (win[k] && (int64_t)t[k] >= a.ntri) {
+                report(a.counters, 3u, t[k]);
+                win[k] = false;
+            }
         }
-        ++written;
-        const uint32_t y = (uint32_t)(p / a.width), x = (uint32_t)(p - (int64_t)y * a.width);
-        const float4 v0 = a.rv[a.tri_v[3 * (int64_t)t]], v1 = a.rv[a.tri_v[3 * (int64_t)t + 1]],
-                     v2 = a.rv[a.tri_v[3 * (int64_t)t + 2]];
-        EdgeTri T;
-        make_edge_tri(v0, v1, v2, T);
-        const float pxf = (float)x, pyf = (float)y;
-        const float e0 = sub(mul(T.d12x, sub(pyf, T.y1)), mul(T.d12y, sub(pxf, T.x1)));
-        const float e1 = sub(mul(T.d20x, sub(pyf, T.y2)), mul(T.d20y, sub(pxf, T.x2)));
-        const float e2 = sub(mul(T.d01x, sub(pyf, T.y0)), mul(T.d01y, sub(pxf, T.x0)));
-        const float b0 = dvd(e0, T.area), b1 = dvd(e1, T.area), b2 = dvd(e2, T.area);
-        a.depth[p] = interp_depth(T, b0, b1, b2);
-        if (a.tri_id) a.tri_id[p] = t;
-
-        // drawing.cpp:125-132: perspective-correct, normalised normal.
-        const int4 nm = a.tri_nm[t];
-        const float3 n0 = camera_normal(a.normal, a.nrm + 3 * (int64_t)nm.x);
-        const float3 n1 = camera_normal(a.normal, a.nrm + 3 * (int64_t)nm.y);
-        const float3 n2 = camera_normal(a.normal, a.nrm + 3 * (int64_t)nm.z);
-        const float i0 = mul(v0.w, b0), i1 = mul(v1.w, b1), i2 = mul(v2.w, b2);
-        const float dd = dvd(1.f, add(add(i0, i1), i2));
-        float sx = add(add(mul(i0, n0.x), mul(i1, n1.x)), mul(i2, n2.x));
-        float sy = add(add(mul(i0, n0.y), mul(i1, n1.y)), mul(i2, n2.y));
-        float sz = add(add(mul(i0, n0.z), mul(i1, n1.z)), mul(i2, n2.z));
-        sx = mul(dd, sx); sy = mul(dd, sy); sz = mul(dd, sz);
-        const float inv = dvd(1.0f, __fsqrt_rn(add(add(mul(sx, sx), mul(sy, sy)), mul(sz, sz))));
-        float nx = mul(sx, inv), ny = mul(sy, inv), nz = mul(sz, inv);
-        if (a.cw) { nx = -nx; ny = -ny; nz = -nz; }
-
-        // shading.cpp:20-34 with the material's constant albedo (material.cpp:24).
-        const float* kd = a.kd + 3 * (int64_t)nm.w;
-        const float ar = kd[0], ag = kd[1], ab = kd[2];
-        const float one_over_pi = 0.318309886183790671537767526745028724f;
-        float accr = 0.f, accg = 0.f, accb = 0.f;
-        for (int l = 0; l < a.nl; ++l) {
-            const float* L = a.lights + 7 * l;
-            const float I = __ldg(L + 3);
-            float cr = mul(I, __ldg(L + 4)), cg = mul(I, __ldg(L + 5)), cb = mul(I, __ldg(L + 6));
-            cr = mul(cr, ar); cg = mul(cg, ag); cb = mul(cb, ab);
-            const float d = add(add(mul(nx, -__ldg(L)), mul(ny, -__ldg(L + 1))), mul(nz, -__ldg(L + 2)));
-            const float m = gmax(0.f, d);
-            cr = mul(mul(cr, m), one_over_pi);
-            cg = mul(mul(cg, m), one_over_pi);
-            cb = mul(mul(cb, m), one_over_pi);
-            accr = add(accr, cr); accg = add(accg, cg); accb = add(accb, cb);
+        // indices
+        int32_t vi[kResolvePx][3];
+        int4 nm[kResolvePx];
+#pragma unroll
+        for (int k = 0; k < kResolvePx; ++k) {
+            if (win[k]) {
+                const int64_t tt = t[k];
+                vi[k][0] = __ldg(a.tri_v + 3 * tt);
+                vi[k][1] = __ldg(a.tri_v + 3 * tt + 1);
+                vi[k][2] = __ldg(a.tri_v + 3 * tt + 2);
+                nm[k] = __ldg(a.tri_nm + tt);
+            }
         }
-        a.rgb[p] = (uint8_t)__float2uint_rz(gmin(accr, 255.f));
-        a.rgb[p + plane] = (uint8_t)__float2uint_rz(gmin(accg, 255.f));
-        a.rgb[p + 2 * plane] = (uint8_t)__float2uint_rz(gmin(accb, 255.f));
+        // vertices and normals
+        float4 v[kResolvePx][3];
+        float3 nv[kResolvePx][3];
+#pragma unroll
+        for (int k = 0; k < kResolvePx; ++k) {
+            if (win[k]) {
+#pragma unroll
+                for (int j = 0; j < 3; ++j) v[k][j] = __ldg(a.rv + vi[k][j]);
+                const int ni[3] = {nm[k].x, nm[k].y, nm[k].z};
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const float* q = a.nrm + 3 * (int64_t)ni[j];
+                    nv[k][j] = make_float3(__ldg(q), __ldg(q + 1), __ldg(q + 2));
+                }
+            }
+        }
+        float dep[kResolvePx];
+        uint32_t col[kResolvePx];
+#pragma unroll
+        for (int k = 0; k < kResolvePx; ++k) {
+            dep[k] = 1.0f;
+            col[k] = 0u;
+            if (win[k]) {
+                ++written;
+                const float3 n0 = camera_normal(a.normal, nv[k][0].x, nv[k][0].y, nv[k][0].z);
+                const float3 n1 = camera_normal(a.normal, nv[k][1].x, nv[k][1].y, nv[k][1].z);
+                const float3 n2 = camera_normal(a.normal, nv[k][2].x, nv[k][2].y, nv[k][2].z);
+                shade_fragment(a, x0 + k, y, v[k][0], v[k][1], v[k][2], n0, n1, n2, nm[k].w, dep[k], col[k]);
+            }
+        }
+        if (a.clear && vec) {
+            // every pixel is written: background 0 / 1.0 where nothing won
+            *reinterpret_cast<float4*>(a.depth + p0) = make_float4(dep[0], dep[1], dep[2], dep[3]);
+            uint32_t pr = 0, pg = 0, pb = 0;
+#pragma unroll
+            for (int k = 0; k < kResolvePx; ++k) {
+                pr |= (col[k] & 0xFFu) << (8 * k);
+                pg |= ((col[k] >> 8) & 0xFFu) << (8 * k);
+                pb |= ((col[k] >> 16) & 0xFFu) << (8 * k);
+            }
+            *reinterpret_cast<uint32_t*>(a.rgb + p0) = pr;
+            *reinterpret_cast<uint32_t*>(a.rgb + plane + p0) = pg;
+            *reinterpret_cast<uint32_t*>(a.rgb + 2 * plane + p0) = pb;
+        } else {
+            for (uint32_t k = 0; k < n; ++k) {
+                if (win[k] || a.clear) {
+                    a.depth[p0 + k] = dep[k];
+                    a.rgb[p0 + k] = (uint8_t)(col[k] & 0xFFu);
+                    a.rgb[plane + p0 + k] = (uint8_t)((col[k] >> 8) & 0xFFu);
+                    a.rgb[2 * plane + p0 + k] = (uint8_t)((col[k] >> 16) & 0xFFu);
+                }
+            }
+        }
+        if (a.tri_id) {
+            for (uint32_t k = 0; k < n; ++k) a.tri_id[p0 + k] = win[k] ? t[k] : 0xFFFFFFFFu;
+        }
     }
-    __shared__ unsigned long long s_written;
-    if (threadIdx.x == 0) s_written = 0;
-    __syncthreads();
-    block_accumulate(&s_written, written);
-    __syncthreads();
-    if (threadIdx.x == 0 && s_written) atomicAdd(stat(a.stats, STAT_WRITTEN), s_written);
+    stat_add(a.stats, STAT_WRITTEN, written);
 }
 
 int grid_for(int64_t n, int threads, int max_blocks) {
@@ -800,9 +915,10 @@ int grid_for(int64_t n, int threads, int max_blocks) {
 }
 
 template <int TS>
-void launch_tile(const TileArgs& ta, uint32_t n_tiles, cudaStream_t stream) {
+void launch_tile(const TileArgs& ta, int n_sm, cudaStream_t stream) {
     constexpr int kThreads = (TS * TS < 256) ? TS * TS : 256;
-    k_tile_raster<TS><<<n_tiles, kThreads, 0, stream>>>(ta);
+    const int per_sm = 2048 / kThreads < 8 ? 2048 / kThreads : 8;
+    k_tile_raster<TS><<<n_sm * per_sm, kThreads, 0, stream>>>(ta);
 }
 
 }  // namespace
@@ -880,7 +996,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     sc.tile_shift = shift;
     sc.tiles_x = p.tiles_x;
     sc.stats = s.stats;
-    k_bin_scatter<<<grid_for(s.cap_large, 256, 4 * 152), 256, 0, stream>>>(sc);
+    k_bin_scatter<<<grid_for(s.cap_large, 256, 4 * p.n_sm), 256, 0, stream>>>(sc);
     ++launches;
     mark(5);
 
@@ -895,10 +1011,11 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ta.width = p.width;
     ta.height = p.height;
     ta.tiles_x = p.tiles_x;
+    ta.n_tiles = n_tiles;
     ta.stats = s.stats;
-    if (p.tile == 8) launch_tile<8>(ta, n_tiles, stream);
-    else if (p.tile == 16) launch_tile<16>(ta, n_tiles, stream);
-    else launch_tile<32>(ta, n_tiles, stream);
+    if (p.tile == 8) launch_tile<8>(ta, p.n_sm, stream);
+    else if (p.tile == 16) launch_tile<16>(ta, p.n_sm, stream);
+    else launch_tile<32>(ta, p.n_sm, stream);
     ++launches;
     mark(6);
 
@@ -916,14 +1033,17 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.nl = p.nl;
     ra.normal = p.normal;
     ra.width = p.width;
-    ra.npx = npx;
+    ra.height = p.height;
     ra.cw = cw;
     ra.clear = clear;
+    ra.vec_ok = (p.width % kResolvePx) == 0 && (reinterpret_cast<uintptr_t>(p.rgb) % 4u) == 0 &&
+                (reinterpret_cast<uintptr_t>(p.depth) % 16u) == 0;
     ra.rgb = p.rgb;
     ra.depth = p.depth;
     ra.tri_id = p.tri_id;
     ra.stats = s.stats;
-    k_resolve<<<grid_for(npx, 256, 152 * 16), 256, 0, stream>>>(ra);
+    const dim3 rgrid((p.width + kResolveThreads * kResolvePx - 1) / (kResolveThreads * kResolvePx), p.height);
+    k_resolve<<<rgrid, kResolveThreads, 0, stream>>>(ra);
     ++launches;
     mark(7);
 
