@@ -149,8 +149,9 @@ rast_status rast_sync(rast_ctx* ctx);
 rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 
 /* Tuning knobs (see rast_set_option keys). Values outside the supported set are refused. */
-#define RAST_OPT_SMALL_MAX_PIXELS 1   /* bounding boxes up to this many pixels are rasterised by
-                                         the per-triangle path; larger ones are binned (1..65536) */
+#define RAST_OPT_SMALL_MAX_PIXELS 1   /* bounding boxes up to this many pixels (default 4096) and
+                                         at most 32 pixels wide are rasterised by the per-triangle
+                                         path; the others are binned into tiles (1..65536) */
 #define RAST_OPT_TILE_SIZE 2          /* tile edge for binning: 8, 16 or 32 */
 #define RAST_OPT_BIN_CAPACITY 3       /* initial tile-bin pool, entries */
 #define RAST_OPT_STAGE_TIMING 4       /* 1: record CUDA events between the kernels of each draw */

@@ -63,7 +63,7 @@ struct rast_ctx {
     DevBuf d_rgb, d_depth, d_ids;
 
     // options
-    uint32_t small_max = 256;
+    uint32_t small_max = 4096;
     uint32_t tile = 16;
     int64_t bin_capacity = 0;  // 0: sized from the mesh
 

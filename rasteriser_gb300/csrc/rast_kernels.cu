@@ -271,6 +271,10 @@ struct SetupStage {
     float rcpr[32];
     uint32_t incl[32];
     int slot[32];
+    // Ring of pixels that passed the early reject and still need the exact test: pixel (x | y << 16),
+    // owning lane, and the three edge values.
+    uint32_t q_xy[64], q_owner[64];
+    float q_e0[64], q_e1[64], q_e2[64];
 };
 
 struct SetupArgs {
@@ -366,7 +370,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
 
     unsigned long long c_tested = 0, c_inside = 0;
 
-    // Cooperative raster of the warp's small triangles.
+    // Cooperative raster of the warp's small triangles. Each lane evaluates the three edge
+    // functions of up to kRowChunk pixels of its item; pixels that the early reject cannot rule
+    // out are pushed to a per-warp ring, and whenever the ring holds 32 of them the whole warp takes
+    // one each for the exact test (the reference's three divisions), the depth and the atomic. The
+    // divisions thus run on full warps although only about one tested pixel in ten is inside.
     {
         const uint32_t incl = warp_inclusive_scan(n_items, lane);
         const uint32_t total = __shfl_sync(kFull, incl, 31);
@@ -385,6 +393,25 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
             S.incl[lane] = incl;
             __syncwarp();
             const uint32_t tri_base = (uint32_t)(blockIdx.x * (int64_t)kSetupThreads + warp * 32);
+            const unsigned lt_mask = (1u << lane) - 1u;
+            uint32_t q_head = 0, q_count = 0;  // warp-uniform
+
+            // Exact test, depth and atomic for ring entry `e` (drawing.cpp:108-121).
+            auto finish = [&](uint32_t e) {
+                const uint32_t j = S.q_owner[e];
+                const uint32_t xy = S.q_xy[e];
+                const float area = S.rec[j][1].z;
+                const float b0 = dvd(S.q_e0[e], area), b1 = dvd(S.q_e1[e], area), b2 = dvd(S.q_e2[e], area);
+                if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
+                    ++c_inside;
+                    const float4 q4 = S.rec[j][4];
+                    const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
+                    const uint32_t x = xy & 0xFFFFu, y = xy >> 16;
+                    if (z == z && x < a.width && y < a.height)
+                        atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + j));
+                }
+            };
+
             int carry = 0;
             for (uint32_t base = 0; base < total; base += 32) {
                 // Bit b of `starts` is set when a triangle's items begin at item base + b; that
@@ -398,43 +425,70 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                 carry = __shfl_sync(kFull, owner, 31);
                 __syncwarp();
                 const uint32_t k = base + lane;
-                if (k >= total) continue;
-                const uint32_t ostart = owner ? S.incl[owner - 1] : 0u;
-                const uint32_t local = k - ostart;
-                const uint32_t ocpr = S.cpr[owner];
-                const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
-                const uint32_t x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
-                const uint32_t x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
-                const uint32_t y = S.tly[owner] + row;
+                bool live = k < total;
+                uint32_t x_lo = 1u, x_hi = 0u, y = 0u;
+                float p0 = 0.f, p1 = 0.f, p2 = 0.f;
+                float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0, q3 = q0;
+                if (live) {
+                    const uint32_t ostart = owner ? S.incl[owner - 1] : 0u;
+                    const uint32_t local = k - ostart;
+                    const uint32_t ocpr = S.cpr[owner];
+                    const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
+                    x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
+                    x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
+                    y = S.tly[owner] + row;
 #ifdef RAST_CHECKED
-                if (owner < 0 || owner > 31 || local >= S.incl[owner] - ostart || x_lo > x_hi || x_hi >= a.width ||
-                    y >= a.height) {
-                    report(a.counters, 1u, (uint32_t)owner);
-                    continue;
-                }
+                    if (owner < 0 || owner > 31 || local >= S.incl[owner] - ostart || x_lo > x_hi ||
+                        x_hi >= a.width || y >= a.height) {
+                        report(a.counters, 1u, (uint32_t)owner);
+                        live = false;
+                        x_lo = 1u;
+                        x_hi = 0u;
+                    }
 #endif
-                const float4 q0 = S.rec[owner][0], q1 = S.rec[owner][1], q2 = S.rec[owner][2], q3 = S.rec[owner][3];
-                const float py = (float)y;
-                const float p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
-                const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
-                const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
-                const float sg = q3.z, nt = q1.w, area = q1.z;
-                c_tested += x_hi - x_lo + 1u;
-                for (uint32_t x = x_lo; x <= x_hi; ++x) {
-                    const float px = (float)x;
-                    const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));  // - d12y * (px - x1)
-                    const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));  // - d20y * (px - x2)
-                    const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));  // - d01y * (px - x0)
-                    if (mul(sg, e0) < nt || mul(sg, e1) < nt || mul(sg, e2) < nt) continue;
-                    const float b0 = dvd(e0, area), b1 = dvd(e1, area), b2 = dvd(e2, area);
-                    if (!(b0 >= 0.f && b1 >= 0.f && b2 >= 0.f)) continue;
-                    ++c_inside;
-                    const float4 q4 = S.rec[owner][4];
-                    const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
-                    if (z == z && x < a.width && y < a.height)
-                        atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + (uint32_t)owner));
+                    if (live) {
+                        q0 = S.rec[owner][0]; q1 = S.rec[owner][1]; q2 = S.rec[owner][2]; q3 = S.rec[owner][3];
+                        const float py = (float)y;
+                        p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
+                        p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
+                        p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
+                        c_tested += x_hi - x_lo + 1u;
+                    }
+                }
+#pragma unroll
+                for (uint32_t sx = 0; sx < kRowChunk; ++sx) {
+                    const uint32_t x = x_lo + sx;
+                    bool cand = false;
+                    float e0 = 0.f, e1 = 0.f, e2 = 0.f;
+                    if (x <= x_hi) {
+                        const float px = (float)x;
+                        e0 = sub(p0, mul(q2.y, sub(px, q0.z)));  // - d12y * (px - x1)
+                        e1 = sub(p1, mul(q2.w, sub(px, q1.x)));  // - d20y * (px - x2)
+                        e2 = sub(p2, mul(q3.y, sub(px, q0.x)));  // - d01y * (px - x0)
+                        const float sg = q3.z, nt = q1.w;
+                        cand = !(mul(sg, e0) < nt || mul(sg, e1) < nt || mul(sg, e2) < nt);
+                    }
+                    const unsigned m = __ballot_sync(kFull, cand);
+                    if (cand) {
+                        const uint32_t e = (q_head + q_count + __popc(m & lt_mask)) & 63u;
+                        S.q_xy[e] = x | (y << 16);
+                        S.q_owner[e] = (uint32_t)owner;
+                        S.q_e0[e] = e0;
+                        S.q_e1[e] = e1;
+                        S.q_e2[e] = e2;
+                    }
+                    q_count += __popc(m);
+                    if (q_count >= 32u) {
+                        __syncwarp();
+                        finish((q_head + lane) & 63u);
+                        __syncwarp();
+                        q_head = (q_head + 32u) & 63u;
+                        q_count -= 32u;
+                    }
                 }
             }
+            __syncwarp();
+            if ((uint32_t)lane < q_count) finish((q_head + lane) & 63u);
             __syncwarp();
         }
     }
@@ -735,15 +789,16 @@ struct ResolveArgs {
     Mat4 normal;
     uint32_t width, height;
     bool cw, clear;
-    bool vec_ok;  // width % 4 == 0, rgb 4-byte and depth 16-byte aligned: 4-pixel vector access
+    bool vec_ok;  // npx % 4 == 0 (planes stay 4-byte aligned), rgb 4-byte and depth 16-byte aligned
     uint8_t* rgb;
     float* depth;
     uint32_t* tri_id;
     unsigned long long* stats;
 };
 
-constexpr int kResolveThreads = 64;
-constexpr int kResolvePx = 4;  // consecutive pixels of one row per thread
+constexpr int kResolveThreads = 256;
+constexpr int kResolveWarps = kResolveThreads / 32;
+constexpr int kSpan = 128;  // consecutive pixels per warp, 4 per lane
 
 // Shades one winning fragment exactly as update_pixel does (drawing.cpp:108-146,
 // shading.cpp:20-34): barycentrics at the integer pixel, NDC depth, perspective-correct normal,
@@ -792,98 +847,106 @@ __device__ __forceinline__ void shade_fragment(const ResolveArgs& a, uint32_t x,
     rgb = r | (g << 8) | (b << 16);
 }
 
-// Per pixel: the winning triangle's fragment is recomputed and shaded. Each thread takes
-// kResolvePx consecutive pixels of one row (grid: x blocks across a row, one block row per image
-// row). The winners' index loads, then their vertex and normal loads, are issued together before
-// any shading, so a thread has several memory requests in flight.
+struct ResolveStage {
+    uint32_t win_px[kSpan], win_tri[kSpan];  // compacted winners: pixel offset in the span, triangle
+    float depth[kSpan];                      // per pixel offset: shaded depth and packed RGB
+    uint32_t rgb[kSpan];
+};
+
+// Each warp takes kSpan consecutive pixels (4 per lane) of the flattened frame: it loads their keys
+// (16-byte loads), re-arms them in clear mode, compacts the pixels that have a winner, shades the
+// winners one per lane so the gathers of 32 fragments are in flight together, and writes the
+// frame and depth buffers 4 pixels per lane.
 __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
-    const uint32_t y = blockIdx.y;
-    const uint32_t x0 = (blockIdx.x * kResolveThreads + threadIdx.x) * kResolvePx;
-    const uint32_t W = a.width;
+    __shared__ ResolveStage stage[kResolveWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    ResolveStage& S = stage[warp];
+    const int64_t npx = (int64_t)a.width * a.height;
+    const int64_t span0 = ((int64_t)blockIdx.x * kResolveWarps + warp) * kSpan;
     unsigned long long written = 0;
-    if (x0 < W) {
-        const size_t p0 = (size_t)y * W + x0;
-        const size_t plane = (size_t)W * a.height;
-        const uint32_t n = min((uint32_t)kResolvePx, W - x0);
-        const bool vec = a.vec_ok;  // then p0 is a multiple of 4 and every vector access is aligned
-        unsigned long long key[kResolvePx];
-        if (vec) {
+    if (span0 < npx) {
+        const int64_t p0 = span0 + 4 * lane;
+        const bool full = p0 + 3 < npx;
+        const bool vec = a.vec_ok && full;
+        unsigned long long key[4];
+        if (full) {
             const ulonglong2 k01 = *reinterpret_cast<const ulonglong2*>(a.keys + p0);
             const ulonglong2 k23 = *reinterpret_cast<const ulonglong2*>(a.keys + p0 + 2);
             key[0] = k01.x; key[1] = k01.y; key[2] = k23.x; key[3] = k23.y;
         } else {
 #pragma unroll
-            for (int k = 0; k < kResolvePx; ++k) key[k] = (uint32_t)k < n ? a.keys[p0 + k] : kNoWinner;
+            for (int k = 0; k < 4; ++k) key[k] = p0 + k < npx ? a.keys[p0 + k] : kNoWinner;
         }
         if (a.keys_rearm) {
             const unsigned long long r = arm_key(1.0f);
-            if (vec) {
+            if (full) {
                 *reinterpret_cast<ulonglong2*>(a.keys_rearm + p0) = make_ulonglong2(r, r);
                 *reinterpret_cast<ulonglong2*>(a.keys_rearm + p0 + 2) = make_ulonglong2(r, r);
             } else {
-                for (uint32_t k = 0; k < n; ++k) a.keys_rearm[p0 + k] = r;
+                for (int k = 0; k < 4; ++k)
+                    if (p0 + k < npx) a.keys_rearm[p0 + k] = r;
             }
         }
-        uint32_t t[kResolvePx];
-        bool win[kResolvePx];
+        // compact the winners of the span
+        bool win[4];
+        uint32_t n_win = 0;
+        const unsigned lt_mask = (1u << lane) - 1u;
 #pragma unroll
-        for (int k = 0; k < kResolvePx; ++k) {
-            t[k] = (uint32_t)(key[k] & 0xFFFFFFFFull);
-            win[k] = t[k] != 0xFFFFFFFFu;
-            if (win[k] && (int64_t)t[k] >= a.ntri) {
-                report(a.counters, 3u, t[k]);
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t t = (uint32_t)(key[k] & 0xFFFFFFFFull);
+            win[k] = t != 0xFFFFFFFFu;
+            if (win[k] && (int64_t)t >= a.ntri) {
+                report(a.counters, 3u, t);
                 win[k] = false;
             }
-        }
-        // indices
-        int32_t vi[kResolvePx][3];
-        int4 nm[kResolvePx];
-#pragma unroll
-        for (int k = 0; k < kResolvePx; ++k) {
+            const unsigned m = __ballot_sync(kFull, win[k]);
             if (win[k]) {
-                const int64_t tt = t[k];
-                vi[k][0] = __ldg(a.tri_v + 3 * tt);
-                vi[k][1] = __ldg(a.tri_v + 3 * tt + 1);
-                vi[k][2] = __ldg(a.tri_v + 3 * tt + 2);
-                nm[k] = __ldg(a.tri_nm + tt);
+                const uint32_t pos = n_win + __popc(m & lt_mask);
+                S.win_px[pos] = 4u * lane + k;
+                S.win_tri[pos] = t;
             }
+            n_win += __popc(m);
         }
-        // vertices and normals
-        float4 v[kResolvePx][3];
-        float3 nv[kResolvePx][3];
-#pragma unroll
-        for (int k = 0; k < kResolvePx; ++k) {
-            if (win[k]) {
-#pragma unroll
-                for (int j = 0; j < 3; ++j) v[k][j] = __ldg(a.rv + vi[k][j]);
-                const int ni[3] = {nm[k].x, nm[k].y, nm[k].z};
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    const float* q = a.nrm + 3 * (int64_t)ni[j];
-                    nv[k][j] = make_float3(__ldg(q), __ldg(q + 1), __ldg(q + 2));
-                }
-            }
+        __syncwarp();
+        for (uint32_t i = lane; i < n_win; i += 32) {
+            const uint32_t off = S.win_px[i];
+            const int64_t tt = S.win_tri[i];
+            const uint32_t p = (uint32_t)(span0 + off);  // < 2^30: width, height <= 32768
+            const uint32_t y = p / a.width, x = p - y * a.width;
+            const int32_t i0 = __ldg(a.tri_v + 3 * tt), i1 = __ldg(a.tri_v + 3 * tt + 1), i2 = __ldg(a.tri_v + 3 * tt + 2);
+            const int4 nm = __ldg(a.tri_nm + tt);
+            const float4 v0 = __ldg(a.rv + i0), v1 = __ldg(a.rv + i1), v2 = __ldg(a.rv + i2);
+            const float* q0 = a.nrm + 3 * (int64_t)nm.x;
+            const float* q1 = a.nrm + 3 * (int64_t)nm.y;
+            const float* q2 = a.nrm + 3 * (int64_t)nm.z;
+            const float3 m0 = make_float3(__ldg(q0), __ldg(q0 + 1), __ldg(q0 + 2));
+            const float3 m1 = make_float3(__ldg(q1), __ldg(q1 + 1), __ldg(q1 + 2));
+            const float3 m2 = make_float3(__ldg(q2), __ldg(q2 + 1), __ldg(q2 + 2));
+            const float3 n0 = camera_normal(a.normal, m0.x, m0.y, m0.z);
+            const float3 n1 = camera_normal(a.normal, m1.x, m1.y, m1.z);
+            const float3 n2 = camera_normal(a.normal, m2.x, m2.y, m2.z);
+            float dep;
+            uint32_t col;
+            shade_fragment(a, x, y, v0, v1, v2, n0, n1, n2, nm.w, dep, col);
+            S.depth[off] = dep;
+            S.rgb[off] = col;
         }
-        float dep[kResolvePx];
-        uint32_t col[kResolvePx];
+        written = n_win;
+        __syncwarp();
+        float dep[4];
+        uint32_t col[4];
 #pragma unroll
-        for (int k = 0; k < kResolvePx; ++k) {
-            dep[k] = 1.0f;
-            col[k] = 0u;
-            if (win[k]) {
-                ++written;
-                const float3 n0 = camera_normal(a.normal, nv[k][0].x, nv[k][0].y, nv[k][0].z);
-                const float3 n1 = camera_normal(a.normal, nv[k][1].x, nv[k][1].y, nv[k][1].z);
-                const float3 n2 = camera_normal(a.normal, nv[k][2].x, nv[k][2].y, nv[k][2].z);
-                shade_fragment(a, x0 + k, y, v[k][0], v[k][1], v[k][2], n0, n1, n2, nm[k].w, dep[k], col[k]);
-            }
+        for (int k = 0; k < 4; ++k) {
+            dep[k] = win[k] ? S.depth[4 * lane + k] : 1.0f;
+            col[k] = win[k] ? S.rgb[4 * lane + k] : 0u;
         }
+        const int64_t plane = npx;
         if (a.clear && vec) {
             // every pixel is written: background 0 / 1.0 where nothing won
             *reinterpret_cast<float4*>(a.depth + p0) = make_float4(dep[0], dep[1], dep[2], dep[3]);
             uint32_t pr = 0, pg = 0, pb = 0;
 #pragma unroll
-            for (int k = 0; k < kResolvePx; ++k) {
+            for (int k = 0; k < 4; ++k) {
                 pr |= (col[k] & 0xFFu) << (8 * k);
                 pg |= ((col[k] >> 8) & 0xFFu) << (8 * k);
                 pb |= ((col[k] >> 16) & 0xFFu) << (8 * k);
@@ -892,8 +955,9 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             *reinterpret_cast<uint32_t*>(a.rgb + plane + p0) = pg;
             *reinterpret_cast<uint32_t*>(a.rgb + 2 * plane + p0) = pb;
         } else {
-            for (uint32_t k = 0; k < n; ++k) {
-                if (win[k] || a.clear) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (p0 + k < npx && (win[k] || a.clear)) {
                     a.depth[p0 + k] = dep[k];
                     a.rgb[p0 + k] = (uint8_t)(col[k] & 0xFFu);
                     a.rgb[plane + p0 + k] = (uint8_t)((col[k] >> 8) & 0xFFu);
@@ -902,8 +966,12 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             }
         }
         if (a.tri_id) {
-            for (uint32_t k = 0; k < n; ++k) a.tri_id[p0 + k] = win[k] ? t[k] : 0xFFFFFFFFu;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (p0 + k < npx) a.tri_id[p0 + k] = win[k] ? (uint32_t)(key[k] & 0xFFFFFFFFull) : 0xFFFFFFFFu;
         }
+        // lane 0 counts for the warp
+        if (lane != 0) written = 0;
     }
     stat_add(a.stats, STAT_WRITTEN, written);
 }
@@ -1036,14 +1104,14 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.height = p.height;
     ra.cw = cw;
     ra.clear = clear;
-    ra.vec_ok = (p.width % kResolvePx) == 0 && (reinterpret_cast<uintptr_t>(p.rgb) % 4u) == 0 &&
+    ra.vec_ok = (reinterpret_cast<uintptr_t>(p.rgb) % 4u) == 0 && (npx % 4) == 0 &&
                 (reinterpret_cast<uintptr_t>(p.depth) % 16u) == 0;
     ra.rgb = p.rgb;
     ra.depth = p.depth;
     ra.tri_id = p.tri_id;
     ra.stats = s.stats;
-    const dim3 rgrid((p.width + kResolveThreads * kResolvePx - 1) / (kResolveThreads * kResolvePx), p.height);
-    k_resolve<<<rgrid, kResolveThreads, 0, stream>>>(ra);
+    const int64_t spans = (npx + kSpan - 1) / kSpan;
+    k_resolve<<<(unsigned)((spans + kResolveWarps - 1) / kResolveWarps), kResolveThreads, 0, stream>>>(ra);
     ++launches;
     mark(7);
 

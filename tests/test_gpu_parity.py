@@ -64,7 +64,7 @@ def random_scenes():
 
 
 @pytest.mark.parametrize("idx", range(len(random_scenes())))
-@pytest.mark.parametrize("tile,small_max", [(16, 256), (8, 1), (32, 65536), (16, 16)])
+@pytest.mark.parametrize("tile,small_max", [(16, 4096), (8, 1), (32, 65536), (16, 16)])
 def test_against_port(renderer, port, idx, tile, small_max):
     sc = random_scenes()[idx]
     renderer.set_option(abi.OPT_TILE_SIZE, tile)
@@ -79,7 +79,7 @@ def test_against_port(renderer, port, idx, tile, small_max):
         assert s["written"] == int((ip != abi.NO_TRIANGLE).sum())
     finally:
         renderer.set_option(abi.OPT_TILE_SIZE, 16)
-        renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, 256)
+        renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, 4096)
 
 
 def test_read_modify_write_buffers(renderer, port):
