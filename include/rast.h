@@ -170,6 +170,30 @@ rast_status rast_get_device_status(rast_ctx* ctx, uint32_t out[4]);
  *   [4] bin scatter  [5] tile raster   [6] resolve + shade                [7] whole draw */
 rast_status rast_get_stage_times(rast_ctx* ctx, float out_ms[8]);
 
+/* ------------------------------------------------------------------------------------------ */
+/* drawing without device allocation (no counterpart in the reference)                         */
+/* ------------------------------------------------------------------------------------------ */
+
+/* One frame like rast_draw_device, for callers that must not allocate device memory: a host
+ * application that gives all device memory to its own pool and allows no allocation it does not
+ * own, or a frame loop that cannot take the device-wide synchronisation of cudaMalloc / cudaFree.
+ * No context is needed and nothing is allocated: the mesh (in the layouts of rast_upload_mesh),
+ * the lights (as for rast_set_lights) and the outputs are the caller's device buffers, and every
+ * intermediate buffer lives in one fixed 64 MiB array inside the library, which each GPU that
+ * loads the library holds until the process exits. A frame whose buffers do not fit is refused
+ * with RAST_ERR_INVALID_ARG: about 100 bytes per triangle, 16 per vertex and 8 per pixel must
+ * fit, e.g. a closed mesh of about 590 k triangles at 640x480 or 460 k at 1920x1080. Indices are checked on the device (RAST_ERR_BAD_INDEX); uv indices are not read. The
+ * first call on a device looks up the array's device address (with that device current); make
+ * that first call before any stream capture. All calls share the array and it keeps the last
+ * call's contents; each call clears what it needs. Calls that overlap on the GPU race on the
+ * array: serialise them. Runs on `stream` (a cudaStream_t, NULL for the legacy default stream)
+ * and returns when the frame is complete. Errors: rast_last_error(NULL). */
+rast_status rast_draw_noalloc(const float* d_pos, int64_t nv, const float* d_nrm, int64_t nn,
+                              const int32_t* d_tris, int64_t ntri, const float* d_kd, int32_t nmat,
+                              const float* d_lights7, int32_t nl, const float camera[16],
+                              const float normal[16], uint32_t width, uint32_t height, uint32_t flags,
+                              uint8_t* d_rgb_planar, float* d_depth, uint32_t* d_tri_id, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

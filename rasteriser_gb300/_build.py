@@ -40,6 +40,7 @@ def _units(checked=False):
         kern = kern + ["-DRAST_CHECKED"]
     return [
         ("rast_kernels.cu", kern + inc),
+        ("rast_noalloc.cu", kern + inc),
         ("rast_api.cpp", host + inc),
         ("rast_host_math.cpp", host + inc),
     ]

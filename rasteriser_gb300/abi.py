@@ -47,6 +47,8 @@ SIGNATURES = {
     "rast_get_option": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
     "rast_get_stage_times": (C.c_int, [_P, _F]),
     "rast_get_device_status": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    "rast_draw_noalloc": (C.c_int, [_P, _I64, _P, _I64, _P, _I64, _P, _I32, _P, _I32, _F, _F, _U32, _U32, _U32,
+                                    _P, _P, _P, _P]),
 }
 
 _lib = None

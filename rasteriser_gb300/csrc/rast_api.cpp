@@ -77,6 +77,10 @@ struct rast_ctx {
     bool ev_recorded = false;
 };
 
+namespace rast {
+void set_thread_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace rast
+
 namespace {
 
 rast_status fail(rast_ctx* c, rast_status s, const std::string& msg) {

@@ -3,6 +3,8 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
+
 #include <cuda_runtime.h>
 
 namespace rast {
@@ -91,6 +93,9 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
 
 // Fills keys[0, n) with the value a cleared depth buffer (1.0) arms them with.
 int launch_arm_keys_clear(unsigned long long* keys, int64_t n, cudaStream_t stream);
+
+// Sets the text rast_last_error(NULL) returns on this thread.
+void set_thread_error(const std::string& msg);
 
 // Splits the reference's Triangle records (10 int32 each) into tri_v and tri_nm on the device.
 int launch_split_triangles(const int32_t* tris10, int64_t ntri, int32_t* tri_v, int4* tri_nm, cudaStream_t stream);
