@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-soak", action="store_true", help="skip the clock-sampling soak loop (profiling)")
     ap.add_argument("--small-max", type=int, default=None)
     ap.add_argument("--tile", type=int, default=None)
+    ap.add_argument("--row-chunk", type=int, default=None)
     return ap.parse_args()
 
 
@@ -263,6 +264,8 @@ def run_ours(args):
         r.set_option(abi.OPT_SMALL_MAX_PIXELS, args.small_max)
     if args.tile:
         r.set_option(abi.OPT_TILE_SIZE, args.tile)
+    if args.row_chunk:
+        r.set_option(abi.OPT_ROW_CHUNK, args.row_chunk)
     r.upload_scene_mesh(scene)
     r.set_lights(frames[0][3])  # the view is a fixed translation: the lights are the same each frame
     d_rgb = torch.empty(3 * W * H, dtype=torch.uint8, device="cuda")

@@ -20,7 +20,7 @@ STATUS_NAMES = {0: "RAST_OK", 1: "RAST_ERR_INVALID_ARG", 2: "RAST_ERR_BAD_INDEX"
                 4: "RAST_ERR_CUDA", 5: "RAST_ERR_OUT_OF_MEMORY", 6: "RAST_ERR_BIN_OVERFLOW",
                 7: "RAST_ERR_TIMEOUT", 8: "RAST_ERR_NO_DEVICE", 9: "RAST_ERR_INTERNAL"}
 WIND_CLOCKWISE, CLEAR, FLAT = 1, 2, 4
-OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY, OPT_STAGE_TIMING = 1, 2, 3, 4
+OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY, OPT_STAGE_TIMING, OPT_ROW_CHUNK = 1, 2, 3, 4, 5
 STAGES = ["arm", "vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve", "total"]
 NO_TRIANGLE = 0xFFFFFFFF
 

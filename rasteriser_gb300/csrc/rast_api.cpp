@@ -65,6 +65,7 @@ struct rast_ctx {
     // options
     uint32_t small_max = 4096;
     uint32_t tile = 16;
+    uint32_t row_chunk = 4;
     int64_t bin_capacity = 0;  // 0: sized from the mesh
 
     uint64_t last_launches = 0;
@@ -199,6 +200,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     p.flags = flags;
     p.small_max = c->small_max;
     p.tile = c->tile;
+    p.row_chunk = c->row_chunk;
     p.tiles_x = tiles_x;
     p.tiles_y = tiles_y;
     p.n_sm = c->n_sm;
@@ -451,6 +453,10 @@ rast_status rast_set_option(rast_ctx* c, int option, int64_t value) {
             if (value != 8 && value != 16 && value != 32) return fail(c, RAST_ERR_INVALID_ARG, "tile must be 8, 16 or 32");
             c->tile = (uint32_t)value;
             return RAST_OK;
+        case RAST_OPT_ROW_CHUNK:
+            if (value != 4 && value != 8) return fail(c, RAST_ERR_INVALID_ARG, "row chunk must be 4 or 8");
+            c->row_chunk = (uint32_t)value;
+            return RAST_OK;
         case RAST_OPT_STAGE_TIMING:
             if (value != 0 && value != 1) return fail(c, RAST_ERR_INVALID_ARG, "stage timing is 0 or 1");
             c->timing = value == 1;
@@ -471,6 +477,7 @@ rast_status rast_get_option(rast_ctx* c, int option, int64_t* value) {
         case RAST_OPT_TILE_SIZE: *value = c->tile; return RAST_OK;
         case RAST_OPT_BIN_CAPACITY: *value = c->cap_entries ? c->cap_entries : c->bin_capacity; return RAST_OK;
         case RAST_OPT_STAGE_TIMING: *value = c->timing ? 1 : 0; return RAST_OK;
+        case RAST_OPT_ROW_CHUNK: *value = c->row_chunk; return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
 }

@@ -229,6 +229,36 @@ __global__ void __launch_bounds__(256) k_vertex(const float* __restrict__ pos, i
     }
 }
 
+__device__ __forceinline__ float4 raster_vertex(const Mat4& cam, float x, float y, float z, float wf, float hf) {
+    const float cx = mrow(cam, 0, x, y, z, 1.f);
+    const float cy = mrow(cam, 1, x, y, z, 1.f);
+    const float cz = mrow(cam, 2, x, y, z, 1.f);
+    const float cw = mrow(cam, 3, x, y, z, 1.f);
+    const float nx = dvd(cx, cw), ny = dvd(cy, cw), nz = dvd(cz, cw), iw = dvd(1.f, cw);
+    return make_float4(mul(mul(0.5f, add(nx, 1.0f)), wf), mul(mul(0.5f, add(-ny, 1.0f)), hf), nz, iw);
+}
+
+// The same for four consecutive vertices per thread, read as three 16-byte loads (positions must
+// be 16-byte aligned); the last nv % 4 vertices are done one by one.
+__global__ void __launch_bounds__(256) k_vertex4(const float* __restrict__ pos, int64_t nv, Mat4 cam, float wf,
+                                                 float hf, float4* __restrict__ rv) {
+    const int64_t groups = nv / 4;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups + (nv % 4); g += (int64_t)gridDim.x * blockDim.x) {
+        if (g < groups) {
+            const float4* q = reinterpret_cast<const float4*>(pos) + 3 * g;
+            const float4 a = q[0], b = q[1], c = q[2];
+            float4* o = rv + 4 * g;
+            o[0] = raster_vertex(cam, a.x, a.y, a.z, wf, hf);
+            o[1] = raster_vertex(cam, a.w, b.x, b.y, wf, hf);
+            o[2] = raster_vertex(cam, b.z, b.w, c.x, wf, hf);
+            o[3] = raster_vertex(cam, c.y, c.z, c.w, wf, hf);
+        } else {
+            const int64_t i = 4 * groups + (g - groups);
+            rv[i] = raster_vertex(cam, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], wf, hf);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) k_arm_from_depth(const float* __restrict__ depth, int64_t n,
                                                         unsigned long long* __restrict__ keys) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -256,8 +286,6 @@ constexpr int kSetupThreads = 256;
 constexpr int kSetupWarps = kSetupThreads / 32;
 // Bounding boxes at most this many pixels wide take the per-triangle path; wider ones are binned.
 constexpr uint32_t kSmallMaxRow = 32;
-// Pixels of one bounding-box row handled by one work item of the per-triangle path.
-constexpr uint32_t kRowChunk = 4;
 
 // Per-warp staging of 32 triangles. rec[j] holds lane j's triangle as five float4s so a lane
 // working on another lane's triangle loads it with five 16-byte shared loads:
@@ -306,6 +334,7 @@ struct SetupArgs {
 // the owner of the window's first item, carried over from the previous window. Each edge function
 //   e = (b.x - a.x)*(py - a.y) - (b.y - a.y)*(px - a.x)     (drawing.cpp:36-39)
 // is evaluated as the reference does, its first product taken once per item.
+template <uint32_t kRowChunk>  // pixels of one bounding-box row per work item
 __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
     __shared__ SetupStage stage[kSetupWarps];
     __shared__ uint32_t s_large[kSetupWarps];
@@ -380,10 +409,13 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
         const uint32_t total = __shfl_sync(kFull, incl, 31);
         if (total) {
             const uint32_t start = incl - n_items;
+            // The edge coefficients are staged multiplied by sgn (+-1, exact), so the staged edge
+            // values are f = sgn*e bit for bit, and f / (sgn*area) is e / area exactly.
+            const float sg = T.sgn;
             S.rec[lane][0] = make_float4(T.x0, T.y0, T.x1, T.y1);
-            S.rec[lane][1] = make_float4(T.x2, T.y2, T.area, T.nthr);
-            S.rec[lane][2] = make_float4(T.d12x, T.d12y, T.d20x, T.d20y);
-            S.rec[lane][3] = make_float4(T.d01x, T.d01y, T.sgn, 0.f);
+            S.rec[lane][1] = make_float4(T.x2, T.y2, mul(sg, T.area), T.nthr);
+            S.rec[lane][2] = make_float4(mul(sg, T.d12x), mul(sg, T.d12y), mul(sg, T.d20x), mul(sg, T.d20y));
+            S.rec[lane][3] = make_float4(mul(sg, T.d01x), mul(sg, T.d01y), 0.f, 0.f);
             S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, 0.f);
             S.tlx[lane] = tlx;
             S.tly[lane] = tly;
@@ -465,8 +497,9 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                         e0 = sub(p0, mul(q2.y, sub(px, q0.z)));  // - d12y * (px - x1)
                         e1 = sub(p1, mul(q2.w, sub(px, q1.x)));  // - d20y * (px - x2)
                         e2 = sub(p2, mul(q3.y, sub(px, q0.x)));  // - d01y * (px - x0)
-                        const float sg = q3.z, nt = q1.w;
-                        cand = !(mul(sg, e0) < nt || mul(sg, e1) < nt || mul(sg, e2) < nt);
+                        // Early reject on the smallest edge value; a NaN stays a candidate and the
+                        // exact test decides it.
+                        cand = fminf(fminf(e0, e1), e2) >= q1.w;
                     }
                     const unsigned m = __ballot_sync(kFull, cand);
                     if (cand) {
@@ -1019,8 +1052,12 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
         ++launches;
     }
     mark(1);
-    k_vertex<<<grid_for(mesh.nv, 256, 1 << 16), 256, 0, stream>>>(mesh.pos, mesh.nv, p.camera, (float)(int)p.width,
-                                                                   (float)(int)p.height, s.rv);
+    if ((reinterpret_cast<uintptr_t>(mesh.pos) % 16u) == 0)
+        k_vertex4<<<grid_for(mesh.nv / 4 + mesh.nv % 4, 256, 1 << 16), 256, 0, stream>>>(
+            mesh.pos, mesh.nv, p.camera, (float)(int)p.width, (float)(int)p.height, s.rv);
+    else
+        k_vertex<<<grid_for(mesh.nv, 256, 1 << 16), 256, 0, stream>>>(mesh.pos, mesh.nv, p.camera, (float)(int)p.width,
+                                                                       (float)(int)p.height, s.rv);
     ++launches;
     mark(2);
 
@@ -1043,7 +1080,9 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     sa.counters = s.counters;
     sa.stats = s.stats;
     if (mesh.ntri > 0) {
-        k_setup_raster<<<(unsigned)((mesh.ntri + kSetupThreads - 1) / kSetupThreads), kSetupThreads, 0, stream>>>(sa);
+        const unsigned blocks = (unsigned)((mesh.ntri + kSetupThreads - 1) / kSetupThreads);
+        if (p.row_chunk == 8) k_setup_raster<8><<<blocks, kSetupThreads, 0, stream>>>(sa);
+        else k_setup_raster<4><<<blocks, kSetupThreads, 0, stream>>>(sa);
         ++launches;
     }
     mark(3);

@@ -64,11 +64,12 @@ def random_scenes():
 
 
 @pytest.mark.parametrize("idx", range(len(random_scenes())))
-@pytest.mark.parametrize("tile,small_max", [(16, 4096), (8, 1), (32, 65536), (16, 16)])
-def test_against_port(renderer, port, idx, tile, small_max):
+@pytest.mark.parametrize("tile,small_max,row_chunk", [(16, 4096, 4), (8, 1, 4), (32, 65536, 8), (16, 16, 8)])
+def test_against_port(renderer, port, idx, tile, small_max, row_chunk):
     sc = random_scenes()[idx]
     renderer.set_option(abi.OPT_TILE_SIZE, tile)
     renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, small_max)
+    renderer.set_option(abi.OPT_ROW_CHUNK, row_chunk)
     try:
         cam, nm, lights, _ = abi.scene_frame_inputs(sc)
         out = gpu_draw(renderer, sc, cam, nm, lights)
@@ -80,6 +81,7 @@ def test_against_port(renderer, port, idx, tile, small_max):
     finally:
         renderer.set_option(abi.OPT_TILE_SIZE, 16)
         renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, 4096)
+        renderer.set_option(abi.OPT_ROW_CHUNK, 4)
 
 
 def test_read_modify_write_buffers(renderer, port):
