@@ -160,6 +160,52 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 rast_status rast_set_option(rast_ctx* ctx, int option, int64_t value);
 rast_status rast_get_option(rast_ctx* ctx, int option, int64_t* value);
 
+/* ------------------------------------------------------------------------------------------ */
+/* batches: many frames of different meshes, sizes, transforms and light rigs                   */
+/* ------------------------------------------------------------------------------------------ */
+
+/* One frame of a batch. Everything a single rast_draw_device takes, per frame. */
+typedef struct rast_frame_desc {
+    int32_t mesh;            /* 0: the mesh of rast_upload_mesh; otherwise an id from rast_add_mesh */
+    uint32_t width, height;  /* 1..32768 */
+    uint32_t flags;          /* RAST_WIND_CLOCKWISE, RAST_CLEAR */
+    float camera[16];        /* as rast_draw */
+    float normal[16];
+    const float* d_lights7;  /* device: nl records as rast_set_lights takes them */
+    int32_t nl;
+    int32_t reserved;
+    uint8_t* d_rgb_planar;   /* device outputs, as rast_draw_device */
+    float* d_depth;
+    uint32_t* d_tri_id;      /* nullable */
+} rast_frame_desc;
+
+/* Uploads another mesh (same layouts and checks as rast_upload_mesh) for use by batches;
+ * *mesh_id receives its id (1, 2, ...). Synchronous. */
+rast_status rast_add_mesh(rast_ctx* ctx, const float* pos, int64_t nv, const float* nrm, int64_t nn,
+                          const float* uv, int64_t nuv, const int32_t* tris, int64_t ntri, const float* kd,
+                          int32_t nmat, int32_t* mesh_id);
+
+#define RAST_BATCH_GRAPH 1u /* record the batch as one CUDA graph and launch that; while the frames'
+                               descriptors, the options and the stream stay the same, later calls
+                               launch the recorded graph again without recording */
+
+/* Draws n frames, frame i on stream i % lanes (1..64 lanes, each with its own scratch), forked from
+ * and joined back into the context's stream; asynchronous. Each frame's result equals that of
+ * rast_draw_device with the same arguments. Call rast_sync to wait and to collect device status
+ * (RAST_ERR_BIN_OVERFLOW: a lane's bin pool was grown, draw the batch again). */
+rast_status rast_draw_batch(rast_ctx* ctx, const rast_frame_desc* frames, int32_t n, int32_t lanes,
+                            uint32_t batch_flags);
+
+/* Per-frame counters of the last batch (waits for the stream): out[8*i + k] as rast_get_stats. */
+rast_status rast_get_batch_stats(rast_ctx* ctx, uint64_t* out);
+
+/* Autotuner: draws the batch (as a CUDA graph) `repeats` times for each tile size (8, 16, 32),
+ * per-triangle-path limit (256, 1024, 4096 pixels) and row chunk (4, 8), keeps the fastest as the
+ * context's options, and sizes the bin pools to what the batch needed. out: tile, small_max,
+ * row_chunk, bin capacity (entries). */
+rast_status rast_autotune(rast_ctx* ctx, const rast_frame_desc* frames, int32_t n, int32_t lanes,
+                          int32_t repeats, int64_t out[4]);
+
 /* Device status words of the last draw (waits for the stream): [0] triangles on the binned path,
  * [1] status bits (1 bin-pool overflow, 2 binned-list overflow, 4 failed consistency check),
  * [2] code of the first failed check (0 none), [3] its detail. Kernels built with RAST_CHECKED

@@ -42,6 +42,7 @@ def _units(checked=False):
         ("rast_kernels.cu", kern + inc),
         ("rast_noalloc.cu", kern + inc),
         ("rast_api.cpp", host + inc),
+        ("rast_batch.cpp", host + inc),
         ("rast_host_math.cpp", host + inc),
     ]
 

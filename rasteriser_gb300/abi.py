@@ -24,6 +24,16 @@ OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY, OPT_STAGE_TIMING, OPT_ROW
 STAGES = ["arm", "vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve", "total"]
 NO_TRIANGLE = 0xFFFFFFFF
 
+class FrameDesc(C.Structure):
+    """rast_frame_desc of include/rast.h."""
+    _fields_ = [("mesh", C.c_int32), ("width", C.c_uint32), ("height", C.c_uint32), ("flags", C.c_uint32),
+                ("camera", C.c_float * 16), ("normal", C.c_float * 16), ("d_lights7", C.c_void_p),
+                ("nl", C.c_int32), ("reserved", C.c_int32), ("d_rgb_planar", C.c_void_p),
+                ("d_depth", C.c_void_p), ("d_tri_id", C.c_void_p)]
+
+
+BATCH_GRAPH = 1
+
 # Every function include/rast.h declares, with its ctypes signature.
 _F, _I32, _I64, _U32, _P = C.POINTER(C.c_float), C.c_int32, C.c_int64, C.c_uint32, C.c_void_p
 SIGNATURES = {
@@ -47,6 +57,11 @@ SIGNATURES = {
     "rast_get_option": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int64)]),
     "rast_get_stage_times": (C.c_int, [_P, _F]),
     "rast_get_device_status": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    "rast_add_mesh": (C.c_int, [_P, _F, _I64, _F, _I64, _F, _I64, C.POINTER(C.c_int32), _I64, _F, _I32,
+                                C.POINTER(C.c_int32)]),
+    "rast_draw_batch": (C.c_int, [_P, C.POINTER(FrameDesc), _I32, _I32, _U32]),
+    "rast_get_batch_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "rast_autotune": (C.c_int, [_P, C.POINTER(FrameDesc), _I32, _I32, _I32, C.POINTER(C.c_int64)]),
     "rast_draw_noalloc": (C.c_int, [_P, _I64, _P, _I64, _P, _I64, _P, _I32, _P, _I32, _F, _F, _U32, _U32, _U32,
                                     _P, _P, _P, _P]),
 }
@@ -206,6 +221,45 @@ class Renderer:
 
     def sync(self):
         self._check(self.lib.rast_sync(self.h), "rast_sync")
+
+    # batches ---------------------------------------------------------------------------------
+    def add_mesh(self, pos, nrm, uv, tris, kd):
+        pos, nrm, uv, kd = _f32(pos), _f32(nrm), _f32(uv), _f32(kd)
+        tris = np.ascontiguousarray(tris, np.int32)
+        mid = C.c_int32()
+        st = self.lib.rast_add_mesh(self.h, _fp(pos), pos.shape[0], _fp(nrm), nrm.shape[0],
+                                    _fp(uv) if uv.size else None, uv.shape[0],
+                                    tris.ctypes.data_as(C.POINTER(C.c_int32)), tris.shape[0], _fp(kd), kd.shape[0],
+                                    C.byref(mid))
+        self._check(st, "rast_add_mesh")
+        return mid.value
+
+    @staticmethod
+    def frame_desc(mesh, width, height, flags, camera, normal, d_lights, nl, d_rgb, d_depth, d_ids=0):
+        f = FrameDesc()
+        f.mesh, f.width, f.height, f.flags = mesh, width, height, flags
+        f.camera[:] = [float(v) for v in np.asarray(camera, np.float32)]
+        f.normal[:] = [float(v) for v in np.asarray(normal, np.float32)]
+        f.d_lights7, f.nl = d_lights or None, nl
+        f.d_rgb_planar, f.d_depth, f.d_tri_id = d_rgb, d_depth, d_ids or None
+        return f
+
+    def draw_batch(self, frames, lanes=8, graph=True):
+        arr = (FrameDesc * len(frames))(*frames)
+        self._check(self.lib.rast_draw_batch(self.h, arr, len(frames), lanes, BATCH_GRAPH if graph else 0),
+                    "rast_draw_batch")
+        self._batch_keepalive = arr
+
+    def batch_stats(self, n):
+        out = (C.c_uint64 * (8 * n))()
+        self._check(self.lib.rast_get_batch_stats(self.h, out), "rast_get_batch_stats")
+        return np.frombuffer(out, np.uint64).reshape(n, 8).copy()
+
+    def autotune(self, frames, lanes=8, repeats=3):
+        arr = (FrameDesc * len(frames))(*frames)
+        out = (C.c_int64 * 4)()
+        self._check(self.lib.rast_autotune(self.h, arr, len(frames), lanes, repeats, out), "rast_autotune")
+        return dict(zip(["tile", "small_max", "row_chunk", "bin_capacity"], list(out)))
 
     def stats(self):
         out = (C.c_uint64 * 8)()

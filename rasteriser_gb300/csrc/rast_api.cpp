@@ -8,142 +8,17 @@
 #include <string>
 #include <vector>
 
-#include "rast.h"
-#include "rast_internal.h"
 
-namespace {
-
-thread_local std::string g_create_error;
-
-// A device allocation that grows and never shrinks.
-struct DevBuf {
-    void* ptr = nullptr;
-    size_t bytes = 0;
-    cudaError_t reserve(size_t want) {
-        if (want <= bytes) return cudaSuccess;
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMalloc(&ptr, want);
-        if (e == cudaSuccess) bytes = want;
-        return e;
-    }
-    void release() {
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        bytes = 0;
-    }
-    template <typename T> T* as() const { return static_cast<T*>(ptr); }
-};
-
-}  // namespace
-
-struct rast_ctx {
-    int device = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    std::string err;
-
-    // mesh
-    DevBuf pos, tris10, tri_v, tri_nm, nrm, kd;
-    rast::DeviceMesh mesh;
-    bool has_mesh = false;
-
-    // lights
-    DevBuf lights;
-    int32_t nl = 0;
-
-    // per-draw scratch
-    DevBuf rv, keys, large, counters, tile_offset, entries, stats;
-    int64_t cap_large = 0, cap_entries = 0;
-    bool keys_armed_clear = false;
-    int64_t keys_px = 0;
-
-    // host-pointer draws stage through these
-    DevBuf d_rgb, d_depth, d_ids;
-
-    // options
-    uint32_t small_max = 4096;
-    uint32_t tile = 16;
-    uint32_t row_chunk = 4;
-    int64_t bin_capacity = 0;  // 0: sized from the mesh
-
-    uint64_t last_launches = 0;
-    int n_sm = 1;
-
-    // stage timing
-    bool timing = false;
-    cudaEvent_t ev[8] = {};
-    bool ev_made = false;
-    bool ev_recorded = false;
-};
+#include "rast_context.h"
 
 namespace rast {
+thread_local std::string g_create_error;
 void set_thread_error(const std::string& msg) { g_create_error = msg; }
 }  // namespace rast
 
+using namespace rast;
+
 namespace {
-
-rast_status fail(rast_ctx* c, rast_status s, const std::string& msg) {
-    if (c) c->err = msg;
-    else g_create_error = msg;
-    return s;
-}
-
-rast_status cuda_fail(rast_ctx* c, cudaError_t e, const char* what) {
-    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
-    return fail(c, e == cudaErrorMemoryAllocation ? RAST_ERR_OUT_OF_MEMORY : RAST_ERR_CUDA, m);
-}
-
-#define RAST_CUDA(ctx, call)                                      \
-    do {                                                          \
-        cudaError_t e_ = (call);                                  \
-        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
-    } while (0)
-
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
-
-constexpr uint32_t kMaxDim = 32768;
-constexpr int32_t kMaxLights = 4096;
-
-rast_status check_index(const int32_t* tris, int64_t ntri, int64_t nv, int64_t nn, int64_t nuv, int32_t nmat,
-                        std::string& msg) {
-    if (ntri >= 0xFFFFFFFFll) {
-        msg = "too many triangles (the triangle index must fit in 32 bits)";
-        return RAST_ERR_INVALID_ARG;
-    }
-    for (int64_t i = 0; i < ntri; ++i) {
-        const int32_t* t = tris + 10 * i;
-        for (int k = 0; k < 3; ++k) {
-            if (t[k] < 0 || t[k] >= nv) {
-                msg = "triangle " + std::to_string(i) + " vertex index " + std::to_string(t[k]) + " out of range";
-                return RAST_ERR_BAD_INDEX;
-            }
-            if (t[3 + k] < 0 || t[3 + k] >= nn) {
-                msg = "triangle " + std::to_string(i) + " normal index " + std::to_string(t[3 + k]) + " out of range";
-                return RAST_ERR_BAD_INDEX;
-            }
-            if (t[6 + k] >= nuv) {
-                msg = "triangle " + std::to_string(i) + " uv index " + std::to_string(t[6 + k]) + " out of range";
-                return RAST_ERR_BAD_INDEX;
-            }
-        }
-        if (t[9] < 0 || t[9] >= nmat) {
-            msg = "triangle " + std::to_string(i) + " material " + std::to_string(t[9]) + " out of range";
-            return RAST_ERR_BAD_INDEX;
-        }
-    }
-    return RAST_OK;
-}
 
 uint32_t tile_shift(uint32_t tile) { return tile == 8 ? 3u : (tile == 16 ? 4u : 5u); }
 
@@ -312,6 +187,16 @@ void rast_destroy(rast_ctx* c) {
         b->release();
     if (c->ev_made)
         for (auto& e : c->ev) cudaEventDestroy(e);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    for (auto& l : c->lanes) {
+        for (DevBuf* b : {&l->rv, &l->keys, &l->large, &l->counters, &l->tile_offset, &l->entries}) b->release();
+        if (l->done) cudaEventDestroy(l->done);
+        if (l->stream) cudaStreamDestroy(l->stream);
+    }
+    for (auto& m : c->meshes)
+        for (DevBuf* b : {&m->pos, &m->tris10, &m->tri_v, &m->tri_nm, &m->nrm, &m->kd}) b->release();
+    c->batch_stats.release();
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -336,6 +221,11 @@ rast_status rast_upload_mesh(rast_ctx* c, const float* pos, int64_t nv, const fl
     DeviceGuard g(c->device);
     RAST_CUDA(c, cudaStreamSynchronize(c->stream));
     c->has_mesh = false;
+    if (c->graph_exec) {  // a recorded batch may refer to the mesh being replaced
+        cudaGraphExecDestroy(c->graph_exec);
+        c->graph_exec = nullptr;
+        c->graph_key.clear();
+    }
     RAST_CUDA(c, c->pos.reserve(sizeof(float) * 3 * (size_t)std::max<int64_t>(nv, 1)));
     RAST_CUDA(c, c->nrm.reserve(sizeof(float) * 3 * (size_t)std::max<int64_t>(nn, 1)));
     RAST_CUDA(c, c->kd.reserve(sizeof(float) * 3 * (size_t)std::max<int32_t>(nmat, 1)));
@@ -425,7 +315,9 @@ rast_status rast_sync(rast_ctx* c) {
     if (!c) return RAST_ERR_INVALID_ARG;
     DeviceGuard g(c->device);
     RAST_CUDA(c, cudaStreamSynchronize(c->stream));
-    return collect_status(c);
+    const rast_status st = collect_status(c);
+    const rast_status sb = c->lanes.empty() ? RAST_OK : collect_batch_status(c);
+    return st != RAST_OK ? st : sb;
 }
 
 rast_status rast_get_stats(rast_ctx* c, uint64_t out[8]) {
