@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--small-max", type=int, default=None)
     ap.add_argument("--tile", type=int, default=None)
     ap.add_argument("--row-chunk", type=int, default=None)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the extra workloads (4M-triangle soup, 256-frame batch) reported beside the line")
     return ap.parse_args()
 
 
@@ -232,6 +234,131 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def time_scene_device(torch, abi, r, stream, frames_in, steps, warmup, flush):
+    """Device-resident loop over one scene's frames (clear + draw), L2 flushed between frames, each
+    frame timed with CUDA events on the draw's stream. Returns (frames/s, stats, stage ms)."""
+    sc0 = frames_in[0][0]
+    W, H = sc0.width, sc0.height
+    r.upload_scene_mesh(sc0)
+    r.set_lights(frames_in[0][3])
+    d_rgb = torch.empty(3 * W * H, dtype=torch.uint8, device="cuda")
+    d_depth = torch.empty(W * H, dtype=torch.float32, device="cuda")
+
+    def step(k):
+        _, cam, nm, _ = frames_in[k % len(frames_in)]
+        r.draw_device(cam, nm, W, H, abi.CLEAR, d_rgb.data_ptr(), d_depth.data_ptr())
+
+    for k in range(warmup):
+        step(k)
+        flush.zero_()
+    r.sync()
+    stats = r.stats()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        ev[k][0].record(stream)
+        step(k)
+        ev[k][1].record(stream)
+        flush.zero_()
+    r.sync()
+    total = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
+    r.set_option(abi.OPT_STAGE_TIMING, 1)
+    acc = {}
+    for k in range(min(steps, 20)):
+        step(k)
+        r.sync()
+        for name, ms in r.stage_times().items():
+            acc[name] = acc.get(name, 0.0) + ms
+        flush.zero_()
+    r.set_option(abi.OPT_STAGE_TIMING, 0)
+    n = min(steps, 20)
+    return steps / total, stats, {k: v / n for k, v in acc.items()}
+
+
+def extra_soup(torch, abi, stream, flush, steps=30):
+    """configs[2]: 4M-triangle soup at 3840x2160 (one frame drawn repeatedly)."""
+    from rasteriser_gb300 import scenes as S
+    sc = S.config_soup()
+    fr = frame_inputs(sc, 1)
+    r = abi.Renderer(0)
+    r.set_stream(stream.cuda_stream)
+    try:
+        fps, st, stage = time_scene_device(torch, abi, r, stream, fr, steps, 3, flush)
+    finally:
+        r.close()
+    return {"workload": "triangle_soup_4M_2160p", "frames_per_s": fps, "fragments_per_s": st["inside"] * fps,
+            "ms_per_frame": 1000.0 / fps, "stage_ms": stage,
+            "frame_stats": {k: st[k] for k in ("front", "tested", "inside", "written", "binned_tris", "bin_entries")}}
+
+
+def batch_workload(seed=3, n_frames=256, n_soups=16):
+    """configs[3]: icospheres L2-L7 and seeded soups of 1k-500k triangles (log-uniform sizes); each
+    frame picks a mesh uniformly, a resolution from {256x256, 640x480, 1280x720, 1920x1080}, random
+    rx/ry and a 1-8 light rig."""
+    from rasteriser_gb300 import scenes as S
+    rng = np.random.default_rng(seed)
+    meshes = [S.icosphere(l) for l in range(2, 8)]
+    for k in range(n_soups):
+        n = int(round(float(S.det_exp(np.log(1000.0) + (np.log(500000.0) - np.log(1000.0)) * rng.random()))))
+        meshes.append(S.soup(n, 1280, 720, seed=1000 + k))
+    sizes = [(256, 256), (640, 480), (1280, 720), (1920, 1080)]
+    frames = []
+    for i in range(n_frames):
+        mi = int(rng.integers(len(meshes)))
+        W, H = sizes[int(rng.integers(4))]
+        nl = int(rng.integers(1, 9))
+        angles = (float(rng.uniform(-np.pi, np.pi)), float(rng.uniform(-np.pi, np.pi)), 0.0)
+        frames.append((mi, W, H, angles, S.rig_random(nl, seed=10_000 + i)))
+    return meshes, frames
+
+
+def extra_batch(torch, abi, stream, steps=10):
+    """configs[3]: the 256-frame batch as one CUDA graph over 8 lanes after autotuning, against the
+    same frames drawn one after another on one stream."""
+    meshes, frames = batch_workload()
+    r = abi.Renderer(0)
+    r.set_stream(stream.cuda_stream)
+    keep = []
+    try:
+        ids = [r.add_mesh(m.pos, m.nrm, m.uv, m.tris, m.kd) for m in meshes]
+        descs = []
+        for mi, W, H, angles, lights in frames:
+            sc = meshes[mi].with_view(width=W, height=H, angles=angles, lights=lights, fovy_deg=60.0, z_near=0.1,
+                                      z_far=100.0)
+            cam, nm, l7, _ = abi.scene_frame_inputs(sc)
+            d = (torch.from_numpy(l7).cuda(), torch.empty(3 * W * H, dtype=torch.uint8, device="cuda"),
+                 torch.empty(W * H, dtype=torch.float32, device="cuda"))
+            keep.append(d)
+            descs.append(r.frame_desc(ids[mi], W, H, abi.CLEAR, cam, nm, d[0].data_ptr(), l7.shape[0],
+                                      d[1].data_ptr(), d[2].data_ptr()))
+        tuned = r.autotune(descs, lanes=8, repeats=2)
+
+        def timed(lanes, graph):
+            r.draw_batch(descs, lanes=lanes, graph=graph)
+            r.sync()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(steps):
+                r.draw_batch(descs, lanes=lanes, graph=graph)
+            b.record(stream)
+            r.sync()
+            return a.elapsed_time(b) / 1000.0 / steps
+
+        t_graph = timed(8, True)
+        st = r.batch_stats(len(descs))
+        t_serial = timed(1, False)
+    finally:
+        r.close()
+    n = len(descs)
+    frags = int(st[:, 2].sum())
+    return {"workload": "batch_256_frames_uneven", "frames": n, "meshes": len(meshes),
+            "triangles_per_batch": int(sum(meshes[f[0]].ntri for f in frames)),
+            "autotuned": tuned, "lanes": 8,
+            "graph_frames_per_s": n / t_graph, "graph_fragments_per_s": frags / t_graph,
+            "serial_frames_per_s": n / t_serial, "speedup_vs_frame_by_frame": t_serial / t_graph,
+            "ms_per_batch_graph": 1000 * t_graph, "ms_per_batch_serial": 1000 * t_serial,
+            "l2": "not flushed (the batch's working set exceeds L2)"}
+
+
 def run_ours(args):
     import torch
     from rasteriser_gb300 import abi
@@ -402,6 +529,8 @@ def run_ours(args):
         "frame_stats": {k: stats[k] for k in ("front", "tested", "inside", "written", "binned_tris", "bin_entries")},
         "fragments_per_s": stats["inside"] * value,
     }
+    if not args.no_extras and world == 1 and args.workload == "displaced_sphere":
+        line["extras"] = {"soup": extra_soup(torch, abi, stream, flush), "batch": extra_batch(torch, abi, stream)}
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
