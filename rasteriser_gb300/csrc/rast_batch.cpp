@@ -254,7 +254,14 @@ rast_status rast::collect_batch_status(rast_ctx* c) {
         const uint32_t zero[3] = {0, 0, 0};
         RAST_CUDA(c, cudaMemcpy(L.counters.as<uint32_t>() + 1, zero, sizeof zero, cudaMemcpyHostToDevice));
         if (w[0] & STATUS_BIN_OVERFLOW) {
-            L.cap_entries *= 4;
+            // Grow to what the largest frame of the batch needed, with a quarter in reserve.
+            int64_t need = 0;
+            if (c->batch_frames > 0) {
+                std::vector<uint64_t> st((size_t)8 * c->batch_frames);
+                if (rast_get_batch_stats(c, st.data()) == RAST_OK)
+                    for (int32_t f = 0; f < c->batch_frames; ++f) need = std::max<int64_t>(need, (int64_t)st[8 * f + 5]);
+            }
+            L.cap_entries = std::max<int64_t>(need + need / 4, 2 * L.cap_entries);
             RAST_CUDA(c, L.entries.reserve(sizeof(uint32_t) * (size_t)L.cap_entries));
             drop_graph(c);
             result = fail(c, RAST_ERR_BIN_OVERFLOW, "a lane's tile-bin pool overflowed; it was grown, draw again");

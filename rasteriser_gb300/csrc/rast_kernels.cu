@@ -439,8 +439,13 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                     const float4 q4 = S.rec[j][4];
                     const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
                     const uint32_t x = xy & 0xFFFFu, y = xy >> 16;
-                    if (z == z && x < a.width && y < a.height)
-                        atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + j));
+                    if (z == z && x < a.width && y < a.height) {
+                        // Keys only decrease, so a stale read is never below the true key: skipping
+                        // the atomic when the read already beats this fragment is exact.
+                        unsigned long long* kp = &a.keys[(size_t)y * a.width + x];
+                        const unsigned long long k = frag_key(z, tri_base + j);
+                        if (k < __ldcg(kp)) atomicMin(kp, k);
+                    }
                 }
             };
 
@@ -800,7 +805,10 @@ __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
         }
 #pragma unroll
         for (int s = 0; s < kPPT; ++s)
-            if (valid[s] && best[s] != ~0ull) atomicMin(&a.keys[(size_t)py[s] * a.width + px[s]], best[s]);
+            if (valid[s] && best[s] != ~0ull) {
+                unsigned long long* kp = &a.keys[(size_t)py[s] * a.width + px[s]];
+                if (best[s] < __ldcg(kp)) atomicMin(kp, best[s]);  // exact: keys only decrease
+            }
         __syncthreads();  // the stage and s_item are rewritten by the next item
     }
     stat_add(a.stats, STAT_TESTED, c_tested);
