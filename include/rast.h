@@ -156,7 +156,7 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 #define RAST_OPT_BIN_CAPACITY 3       /* initial tile-bin pool, entries */
 #define RAST_OPT_STAGE_TIMING 4       /* 1: record CUDA events between the kernels of each draw */
 #define RAST_OPT_ROW_CHUNK 5          /* pixels of a bounding-box row per work item of the
-                                         per-triangle path: 4 (default) or 8 */
+                                         per-triangle path: 4 or 8 (default) */
 rast_status rast_set_option(rast_ctx* ctx, int option, int64_t value);
 rast_status rast_get_option(rast_ctx* ctx, int option, int64_t* value);
 

@@ -299,10 +299,9 @@ struct SetupStage {
     float rcpr[32];
     uint32_t incl[32];
     int slot[32];
-    // Ring of pixels that passed the early reject and still need the exact test: pixel (x | y << 16),
-    // owning lane, and the three edge values.
-    uint32_t q_xy[64], q_owner[64];
-    float q_e0[64], q_e1[64], q_e2[64];
+    // Ring of work items with pixels the early reject could not rule out: first pixel
+    // (x | y << 16), and owning lane | candidate mask << 8.
+    uint32_t q_xy[64], q_om[64];
 };
 
 struct SetupArgs {
@@ -400,10 +399,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
     unsigned long long c_tested = 0, c_inside = 0;
 
     // Cooperative raster of the warp's small triangles. Each lane evaluates the three edge
-    // functions of up to kRowChunk pixels of its item; pixels that the early reject cannot rule
-    // out are pushed to a per-warp ring, and whenever the ring holds 32 of them the whole warp takes
-    // one each for the exact test (the reference's three divisions), the depth and the atomic. The
-    // divisions thus run on full warps although only about one tested pixel in ten is inside.
+    // functions of the kRowChunk pixels of its item and keeps a mask of the pixels the early reject
+    // cannot rule out; items with a nonzero mask go to a per-warp ring, and whenever the ring holds
+    // 32 of them the whole warp takes one each for the exact test of its masked pixels (the
+    // reference's three divisions), the depth and the atomic. The tested pixels cost only the edge
+    // evaluations, and the divisions run on full warps.
     {
         const uint32_t incl = warp_inclusive_scan(n_items, lane);
         const uint32_t total = __shfl_sync(kFull, incl, 31);
@@ -428,23 +428,30 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
             const unsigned lt_mask = (1u << lane) - 1u;
             uint32_t q_head = 0, q_count = 0;  // warp-uniform
 
-            // Exact test, depth and atomic for ring entry `e` (drawing.cpp:108-121).
+            // Exact test, depth and atomic for the masked pixels of ring entry `e`
+            // (drawing.cpp:108-121).
             auto finish = [&](uint32_t e) {
-                const uint32_t j = S.q_owner[e];
-                const uint32_t xy = S.q_xy[e];
-                const float area = S.rec[j][1].z;
-                const float b0 = dvd(S.q_e0[e], area), b1 = dvd(S.q_e1[e], area), b2 = dvd(S.q_e2[e], area);
-                if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
-                    ++c_inside;
-                    const float4 q4 = S.rec[j][4];
-                    const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
-                    const uint32_t x = xy & 0xFFFFu, y = xy >> 16;
-                    if (z == z && x < a.width && y < a.height) {
-                        // Keys only decrease, so a stale read is never below the true key: skipping
-                        // the atomic when the read already beats this fragment is exact.
-                        unsigned long long* kp = &a.keys[(size_t)y * a.width + x];
-                        const unsigned long long k = frag_key(z, tri_base + j);
-                        if (k < __ldcg(kp)) atomicMin(kp, k);
+                const uint32_t om = S.q_om[e], xy = S.q_xy[e];
+                const uint32_t j = om & 31u;
+                uint32_t mask = om >> 8;
+                const uint32_t x0 = xy & 0xFFFFu, y = xy >> 16;
+                const float4 q0 = S.rec[j][0], q1 = S.rec[j][1], q2 = S.rec[j][2], q3 = S.rec[j][3], q4 = S.rec[j][4];
+                const float py = (float)y;
+                const float p0 = mul(q2.x, sub(py, q0.w)), p1 = mul(q2.z, sub(py, q1.y)), p2 = mul(q3.x, sub(py, q0.y));
+                while (mask) {
+                    const uint32_t b = __ffs(mask) - 1u;
+                    mask &= mask - 1u;
+                    const uint32_t x = x0 + b;
+                    const float px = (float)x;
+                    const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));
+                    const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));
+                    const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));
+                    const float b0 = dvd(e0, q1.z), b1 = dvd(e1, q1.z), b2 = dvd(e2, q1.z);
+                    if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
+                        ++c_inside;
+                        const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
+                        if (z == z && x < a.width && y < a.height)
+                            atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + j));
                     }
                 }
             };
@@ -462,67 +469,58 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                 carry = __shfl_sync(kFull, owner, 31);
                 __syncwarp();
                 const uint32_t k = base + lane;
-                bool live = k < total;
-                uint32_t x_lo = 1u, x_hi = 0u, y = 0u;
-                float p0 = 0.f, p1 = 0.f, p2 = 0.f;
-                float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0, q3 = q0;
-                if (live) {
+                uint32_t x_lo = 0u, y = 0u, mask = 0u;
+                if (k < total) {
                     const uint32_t ostart = owner ? S.incl[owner - 1] : 0u;
                     const uint32_t local = k - ostart;
                     const uint32_t ocpr = S.cpr[owner];
                     const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
                     x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
-                    x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
+                    const uint32_t x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
                     y = S.tly[owner] + row;
+                    bool live = true;
 #ifdef RAST_CHECKED
                     if (owner < 0 || owner > 31 || local >= S.incl[owner] - ostart || x_lo > x_hi ||
                         x_hi >= a.width || y >= a.height) {
                         report(a.counters, 1u, (uint32_t)owner);
                         live = false;
-                        x_lo = 1u;
-                        x_hi = 0u;
                     }
 #endif
                     if (live) {
-                        q0 = S.rec[owner][0]; q1 = S.rec[owner][1]; q2 = S.rec[owner][2]; q3 = S.rec[owner][3];
-                        const float py = (float)y;
-                        p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
-                        p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
-                        p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
-                        c_tested += x_hi - x_lo + 1u;
+                        const float4 q0 = S.rec[owner][0], q1 = S.rec[owner][1], q2 = S.rec[owner][2],
+                                     q3 = S.rec[owner][3];
+                        const float py = (float)y, px_lo = (float)x_lo;
+                        const float p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
+                        const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
+                        const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
+                        const uint32_t n_px = x_hi - x_lo + 1u;
+                        c_tested += n_px;
+#pragma unroll
+                        for (uint32_t sx = 0; sx < kRowChunk; ++sx) {
+                            const float px = add(px_lo, (float)sx);  // exact: integers below 2^24
+                            const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));  // - d12y * (px - x1)
+                            const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));  // - d20y * (px - x2)
+                            const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));  // - d01y * (px - x0)
+                            // Early reject on the smallest edge value; a NaN stays a candidate.
+                            const bool cand = sx < n_px && fminf(fminf(e0, e1), e2) >= q1.w;
+                            mask |= (uint32_t)cand << sx;
+                        }
                     }
                 }
-#pragma unroll
-                for (uint32_t sx = 0; sx < kRowChunk; ++sx) {
-                    const uint32_t x = x_lo + sx;
-                    bool cand = false;
-                    float e0 = 0.f, e1 = 0.f, e2 = 0.f;
-                    if (x <= x_hi) {
-                        const float px = (float)x;
-                        e0 = sub(p0, mul(q2.y, sub(px, q0.z)));  // - d12y * (px - x1)
-                        e1 = sub(p1, mul(q2.w, sub(px, q1.x)));  // - d20y * (px - x2)
-                        e2 = sub(p2, mul(q3.y, sub(px, q0.x)));  // - d01y * (px - x0)
-                        // Early reject on the smallest edge value; a NaN stays a candidate and the
-                        // exact test decides it.
-                        cand = fminf(fminf(e0, e1), e2) >= q1.w;
-                    }
-                    const unsigned m = __ballot_sync(kFull, cand);
-                    if (cand) {
-                        const uint32_t e = (q_head + q_count + __popc(m & lt_mask)) & 63u;
-                        S.q_xy[e] = x | (y << 16);
-                        S.q_owner[e] = (uint32_t)owner;
-                        S.q_e0[e] = e0;
-                        S.q_e1[e] = e1;
-                        S.q_e2[e] = e2;
-                    }
-                    q_count += __popc(m);
-                    if (q_count >= 32u) {
-                        __syncwarp();
-                        finish((q_head + lane) & 63u);
-                        __syncwarp();
-                        q_head = (q_head + 32u) & 63u;
-                        q_count -= 32u;
-                    }
+                const bool has = mask != 0u;
+                const unsigned m = __ballot_sync(kFull, has);
+                if (has) {
+                    const uint32_t e = (q_head + q_count + __popc(m & lt_mask)) & 63u;
+                    S.q_xy[e] = x_lo | (y << 16);
+                    S.q_om[e] = (uint32_t)owner | (mask << 8);
+                }
+                q_count += __popc(m);
+                if (q_count >= 32u) {
+                    __syncwarp();
+                    finish((q_head + lane) & 63u);
+                    __syncwarp();
+                    q_head = (q_head + 32u) & 63u;
+                    q_count -= 32u;
                 }
             }
             __syncwarp();
@@ -805,10 +803,7 @@ __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
         }
 #pragma unroll
         for (int s = 0; s < kPPT; ++s)
-            if (valid[s] && best[s] != ~0ull) {
-                unsigned long long* kp = &a.keys[(size_t)py[s] * a.width + px[s]];
-                if (best[s] < __ldcg(kp)) atomicMin(kp, best[s]);  // exact: keys only decrease
-            }
+            if (valid[s] && best[s] != ~0ull) atomicMin(&a.keys[(size_t)py[s] * a.width + px[s]], best[s]);
         __syncthreads();  // the stage and s_item are rewritten by the next item
     }
     stat_add(a.stats, STAT_TESTED, c_tested);

@@ -167,7 +167,7 @@ extern "C" rast_status rast_draw_noalloc(const float* d_pos, int64_t nv, const f
     p.flags = flags;
     p.small_max = 4096;
     p.tile = tile;
-    p.row_chunk = 4;
+    p.row_chunk = 8;
     p.tiles_x = tiles_x;
     p.tiles_y = tiles_y;
     int n_sm = 1;

@@ -81,7 +81,7 @@ def test_against_port(renderer, port, idx, tile, small_max, row_chunk):
     finally:
         renderer.set_option(abi.OPT_TILE_SIZE, 16)
         renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, 4096)
-        renderer.set_option(abi.OPT_ROW_CHUNK, 4)
+        renderer.set_option(abi.OPT_ROW_CHUNK, 8)
 
 
 def test_read_modify_write_buffers(renderer, port):
