@@ -495,15 +495,28 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                         const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
                         const uint32_t n_px = x_hi - x_lo + 1u;
                         c_tested += n_px;
+                        // Two pixels per instruction: __fadd2_rn / __fmul2_rn round each component
+                        // exactly as __fadd_rn / __fmul_rn, and a - b is a + (-b) bit for bit, so
+                        //   e = p - d.y * (px - a.x)  ==  p + -(d.y * (px + -a.x)).
+                        const float2 P0 = make_float2(p0, p0), P1 = make_float2(p1, p1), P2 = make_float2(p2, p2);
+                        const float2 NX1 = make_float2(-q0.z, -q0.z), NX2 = make_float2(-q1.x, -q1.x),
+                                     NX0 = make_float2(-q0.x, -q0.x);
+                        const float2 B0 = make_float2(q2.y, q2.y), B1 = make_float2(q2.w, q2.w),
+                                     B2 = make_float2(q3.y, q3.y);
 #pragma unroll
-                        for (uint32_t sx = 0; sx < kRowChunk; ++sx) {
-                            const float px = add(px_lo, (float)sx);  // exact: integers below 2^24
-                            const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));  // - d12y * (px - x1)
-                            const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));  // - d20y * (px - x2)
-                            const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));  // - d01y * (px - x0)
+                        for (uint32_t sx = 0; sx < kRowChunk; sx += 2) {
+                            // pixel centres px_lo + sx, + sx + 1: exact, integers below 2^24
+                            const float2 px = make_float2(add(px_lo, (float)sx), add(px_lo, (float)(sx + 1)));
+                            const float2 t0 = __fmul2_rn(B0, __fadd2_rn(px, NX1));
+                            const float2 t1 = __fmul2_rn(B1, __fadd2_rn(px, NX2));
+                            const float2 t2 = __fmul2_rn(B2, __fadd2_rn(px, NX0));
+                            const float2 e0 = __fadd2_rn(P0, make_float2(-t0.x, -t0.y));
+                            const float2 e1 = __fadd2_rn(P1, make_float2(-t1.x, -t1.y));
+                            const float2 e2 = __fadd2_rn(P2, make_float2(-t2.x, -t2.y));
                             // Early reject on the smallest edge value; a NaN stays a candidate.
-                            const bool cand = sx < n_px && fminf(fminf(e0, e1), e2) >= q1.w;
-                            mask |= (uint32_t)cand << sx;
+                            const bool ca = sx < n_px && fminf(fminf(e0.x, e1.x), e2.x) >= q1.w;
+                            const bool cb = sx + 1 < n_px && fminf(fminf(e0.y, e1.y), e2.y) >= q1.w;
+                            mask |= ((uint32_t)ca | ((uint32_t)cb << 1)) << sx;
                         }
                     }
                 }
