@@ -110,6 +110,13 @@ rast_status rast_upload_mesh(rast_ctx* ctx, const float* pos, int64_t nv, const 
                              const float* uv, int64_t nuv, const int32_t* tris, int64_t ntri,
                              const float* kd, int32_t nmat);
 
+/* Per-vertex albedo for the uploaded mesh (no counterpart in the reference, whose materials are
+ * constant): nv * 3 floats, interpolated perspective-correctly like the normals
+ * (drawing.cpp:64-75) and used in place of the material's Kd (Material::sample). nv must equal
+ * the mesh's vertex count; rgb3 = NULL with nv = 0 returns to the materials' Kd. A new
+ * rast_upload_mesh drops it. Synchronous. */
+rast_status rast_upload_vertex_albedo(rast_ctx* ctx, const float* rgb3, int64_t nv);
+
 /* Sets the frame's lights: n records of 7 floats (trans_dir xyz, intensity, colour rgb), i.e.
  * already transformed (rast_transform_lights). Shading sums them in this order
  * (shading.cpp:24-34). 0 <= n <= 4096. */
@@ -145,7 +152,7 @@ rast_status rast_sync(rast_ctx* ctx);
  *   [0] front-facing triangles      [1] bounding-box pixels tested
  *   [2] inside fragments            [3] pixels written
  *   [4] triangles on the binned path [5] tile-bin entries
- *   [6] kernel launches of the draw  [7] reserved */
+ *   [6] kernel launches of the draw  [7] reserved (0) */
 rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 
 /* Tuning knobs (see rast_set_option keys). Values outside the supported set are refused. */
@@ -157,6 +164,24 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 #define RAST_OPT_STAGE_TIMING 4       /* 1: record CUDA events between the kernels of each draw */
 #define RAST_OPT_ROW_CHUNK 5          /* pixels of a bounding-box row per work item of the
                                          per-triangle path: 4 or 8 (default) */
+#define RAST_OPT_SHADER 6             /* RAST_SHADER_* (default RAST_SHADER_EXACT) */
+#define RAST_OPT_MLP_SAMPLES 7        /* learned shader: fragments of each 128-fragment tile that
+                                         are also shaded exactly to check it, 0..4 (default 2) */
+#define RAST_OPT_MLP_BOUND_MILLI 8    /* learned shader: a tile whose checked fragments differ from
+                                         the exact shader by more than this many thousandths of
+                                         1/255 in a channel is shaded exactly (default 500) */
+/* Shading (RAST_OPT_SHADER). Coverage, depth and triangle ids are the same in every mode.
+ *   EXACT: shading.cpp's per-light sum inside the resolve pass (the reference's colour, bit for bit)
+ *   EXACT_DEFERRED: the resolve pass stores the winning fragments (normal, albedo, pixel); a
+ *     separate pass shades them with the same per-light sum (same colour as EXACT)
+ *   LEARNED: the stored fragments are shaded by the context's MLP (rast_mlp_train / rast_mlp_load)
+ *     on the tensor cores; RAST_OPT_MLP_SAMPLES fragments per 128-fragment tile are also shaded
+ *     exactly and a tile whose sampled error exceeds RAST_OPT_MLP_BOUND_MILLI is shaded exactly
+ *     in full. Needs weights trained or loaded for the current lights (RAST_ERR_INVALID_ARG
+ *     otherwise). Single draws only: batches always use EXACT. */
+#define RAST_SHADER_EXACT 0
+#define RAST_SHADER_EXACT_DEFERRED 1
+#define RAST_SHADER_LEARNED 2
 rast_status rast_set_option(rast_ctx* ctx, int option, int64_t value);
 rast_status rast_get_option(rast_ctx* ctx, int option, int64_t* value);
 
@@ -207,7 +232,8 @@ rast_status rast_autotune(rast_ctx* ctx, const rast_frame_desc* frames, int32_t 
                           int32_t repeats, int64_t out[4]);
 
 /* Device status words of the last draw (waits for the stream): [0] triangles on the binned path,
- * [1] status bits (1 bin-pool overflow, 2 binned-list overflow, 4 failed consistency check),
+ * [1] status bits (1 bin-pool overflow, 2 binned-list overflow, 4 failed consistency check,
+ * 8 the learned shader timed out waiting for the tensor cores),
  * [2] code of the first failed check (0 none), [3] its detail. Kernels built with RAST_CHECKED
  * bounds-check every derived index; the default build checks the ones that index other arrays. */
 rast_status rast_get_device_status(rast_ctx* ctx, uint32_t out[4]);
@@ -215,8 +241,52 @@ rast_status rast_get_device_status(rast_ctx* ctx, uint32_t out[4]);
 /* Device time of each stage of the last draw in milliseconds, from CUDA events recorded on the
  * context's stream between its kernels (needs RAST_OPT_STAGE_TIMING = 1; waits for the stream):
  *   [0] key arming   [1] vertex        [2] setup + per-triangle raster   [3] bin scan
- *   [4] bin scatter  [5] tile raster   [6] resolve + shade                [7] whole draw */
-rast_status rast_get_stage_times(rast_ctx* ctx, float out_ms[8]);
+ *   [4] bin scatter  [5] tile raster   [6] resolve (+ shade in EXACT mode)
+ *   [7] deferred shading (fragment scan + shading kernel; 0 in EXACT mode)   [8] whole draw */
+rast_status rast_get_stage_times(rast_ctx* ctx, float out_ms[9]);
+
+/* ------------------------------------------------------------------------------------------ */
+/* learned many-light shading (no counterpart in the reference)                                 */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Training of the context's MLP for its current lights (rast_set_lights). Samples are normals
+ * uniform on the sphere and albedos uniform in [0,1]^3, labelled on the GPU with the exact
+ * per-light shader's float radiance; training is Adam on the mean squared error with the
+ * forward pass rounded as the tensor-core kernel rounds it (BF16 weights and activations). */
+typedef struct rast_mlp_train_desc {
+    int64_t samples;   /* training samples (default 4194304) */
+    int64_t holdout;   /* held-out samples for the error report (default 65536) */
+    int32_t epochs;    /* passes over the samples (default 12) */
+    int32_t ctas;      /* CTAs per step, 64 samples each (default: the SM count) */
+    float lr;          /* peak learning rate (default 0.003), cosine decay to lr/100 */
+    uint64_t seed;     /* samples and initial weights (default 1) */
+} rast_mlp_train_desc;
+
+/* Trains (desc NULL: defaults; zero fields take their default). out (nullable): [0] mean squared
+ * error of the last epoch (1/255 units squared), [1] mean and [2] largest absolute channel error
+ * of the tensor-core kernel on the held-out samples (1/255 units, before clamping), [3] seconds.
+ * Synchronous. */
+rast_status rast_mlp_train(rast_ctx* ctx, const rast_mlp_train_desc* desc, float out[4]);
+
+/* The weights as a versioned blob ("RMLP", see rasteriser_gb300/csrc/rast_mlp.h: header with the
+ * light rig's hash and the output scale, BF16 weights, FP32 biases). *size receives the blob size;
+ * buf may be NULL to query it. RAST_ERR_INVALID_ARG if cap is too small or nothing is trained. */
+rast_status rast_mlp_save(rast_ctx* ctx, void* buf, size_t cap, size_t* size);
+
+/* Loads a blob from rast_mlp_save. It is used only while the context's lights hash to the rig it
+ * was trained for. */
+rast_status rast_mlp_load(rast_ctx* ctx, const void* buf, size_t size);
+
+/* Evaluates n (normal, albedo) pairs (host buffers, 3 floats each) through the tensor-core kernel
+ * (exact = 0) or the exact shader (exact = 1); out: n * 3 radiance floats before clamping and
+ * truncation (1/255 units). Synchronous. */
+rast_status rast_mlp_eval(rast_ctx* ctx, const float* normals3, const float* albedo3, int64_t n, int32_t exact,
+                          float* out3);
+
+/* Learned-shader counters of the last draw (waits for the stream): [0] tiles, [1] tiles shaded
+ * exactly after their check failed, [2] fragments checked, [3] largest checked channel error in
+ * millionths of 1/255. */
+rast_status rast_get_shade_stats(rast_ctx* ctx, uint64_t out[4]);
 
 /* ------------------------------------------------------------------------------------------ */
 /* drawing without device allocation (no counterpart in the reference)                         */

@@ -51,7 +51,8 @@ class _OracleFrame(C.Structure):
                 ("kd", C.POINTER(C.c_float)), ("nmat", C.c_int32),
                 ("camera", C.POINTER(C.c_float)), ("normal_matrix", C.POINTER(C.c_float)),
                 ("lights", C.POINTER(C.c_float)), ("nl", C.c_int32),
-                ("width", C.c_uint32), ("height", C.c_uint32), ("wind_clockwise", C.c_int32)]
+                ("width", C.c_uint32), ("height", C.c_uint32), ("wind_clockwise", C.c_int32),
+                ("vcol", C.POINTER(C.c_float))]
 
 
 class Port:
@@ -78,10 +79,12 @@ class Port:
         ids = np.full((H, W), 0xFFFFFFFF, np.uint32) if want_ids else None
         keep = [_f32(scene.pos), _i32(scene.tris), _f32(scene.nrm), _f32(scene.uv), _f32(scene.kd),
                 _f32(camera), _f32(normal_matrix), _f32(lights7)]
+        vcol = getattr(scene, "vertex_albedo", None)
+        vcol = _f32(vcol) if vcol is not None else None
         f = _OracleFrame(_p(keep[0]), scene.pos.shape[0], _p(keep[1], C.c_int32), scene.tris.shape[0],
                          _p(keep[2]), scene.nrm.shape[0], _p(keep[3]), scene.uv.shape[0],
                          _p(keep[4]), scene.kd.shape[0], _p(keep[5]), _p(keep[6]), _p(keep[7]),
-                         keep[7].shape[0], W, H, int(scene.wind_clockwise))
+                         keep[7].shape[0], W, H, int(scene.wind_clockwise), _p(vcol))
         stats = np.zeros(4, np.uint64)
         rc = self.lib.oracle_draw_frame(C.byref(f), _p(frame, C.c_uint8), _p(depth),
                                         _p(ids, C.c_uint32), _p(stats, C.c_uint64))

@@ -122,6 +122,15 @@ int oracle_draw_frame(const oracle_frame* f, uint8_t* frame, float* depth, uint3
         v3 n0 = cn[tri[3]], n1 = cn[tri[4]], n2 = cn[tri[5]];
         const float* kd = f->kd + 3 * tri[9];
         v3 albedo = {kd[0], kd[1], kd[2]};
+        v3 c0 = {0, 0, 0}, c1 = {0, 0, 0}, c2 = {0, 0, 0};
+        if (f->vcol) {
+            const float* a = f->vcol + 3 * tri[0];
+            const float* b = f->vcol + 3 * tri[1];
+            const float* c = f->vcol + 3 * tri[2];
+            c0 = (v3){a[0], a[1], a[2]};
+            c1 = (v3){b[0], b[1], b[2]};
+            c2 = (v3){c[0], c[1], c[2]};
+        }
 
         /* geometry.cpp:76-83 signed_area_2d, drawing.cpp:176-178 culling */
         float sa = -0.5f * (v0.x * v1.y - v1.x * v0.y + v1.x * v2.y - v2.x * v1.y + v2.x * v0.y - v0.x * v2.y);
@@ -168,6 +177,15 @@ int oracle_draw_frame(const oracle_frame* f, uint8_t* frame, float* depth, uint3
                 float inv = 1.0f / sqrtf((s.x * s.x + s.y * s.y) + s.z * s.z);
                 v3 nrm = {s.x * inv, s.y * inv, s.z * inv};
                 if (cw) { nrm.x = -nrm.x; nrm.y = -nrm.y; nrm.z = -nrm.z; }
+                if (f->vcol) {  /* per-vertex albedo, interpolated as the normal is */
+                    v3 u;
+                    u.x = i0 * c0.x + i1 * c1.x + i2 * c2.x;
+                    u.y = i0 * c0.y + i1 * c1.y + i2 * c2.y;
+                    u.z = i0 * c0.z + i1 * c1.z + i2 * c2.z;
+                    albedo.x = dd * u.x;
+                    albedo.y = dd * u.y;
+                    albedo.z = dd * u.z;
+                }
                 /* drawing.cpp:138-146 shade and write planar RGB */
                 uint32_t rgb[3];
                 shade(nrm, albedo, f->lights, f->nl, rgb);

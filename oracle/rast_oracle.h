@@ -32,6 +32,10 @@ typedef struct oracle_frame {
     int32_t nl;
     uint32_t width, height;
     int32_t wind_clockwise;
+    /* Per-vertex albedo (nv * 3, nullable). The reference's materials are constant per material;
+     * the many-light workload adds a colour per vertex, interpolated perspective-correctly exactly
+     * as the normals are (drawing.cpp:64-75, 131), in place of Material::sample. */
+    const float* vcol;
 } oracle_frame;
 
 /* stats (nullable) receives: [0] front-facing triangles, [1] bounding-box pixels tested,

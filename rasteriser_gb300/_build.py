@@ -40,9 +40,11 @@ def _units(checked=False):
         kern = kern + ["-DRAST_CHECKED"]
     return [
         ("rast_kernels.cu", kern + inc),
+        ("rast_shade.cu", kern + inc),
         ("rast_noalloc.cu", kern + inc),
         ("rast_api.cpp", host + inc),
         ("rast_batch.cpp", host + inc),
+        ("rast_mlp.cpp", host + inc),
         ("rast_host_math.cpp", host + inc),
     ]
 

@@ -21,7 +21,9 @@ STATUS_NAMES = {0: "RAST_OK", 1: "RAST_ERR_INVALID_ARG", 2: "RAST_ERR_BAD_INDEX"
                 7: "RAST_ERR_TIMEOUT", 8: "RAST_ERR_NO_DEVICE", 9: "RAST_ERR_INTERNAL"}
 WIND_CLOCKWISE, CLEAR, FLAT = 1, 2, 4
 OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY, OPT_STAGE_TIMING, OPT_ROW_CHUNK = 1, 2, 3, 4, 5
-STAGES = ["arm", "vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve", "total"]
+OPT_SHADER, OPT_MLP_SAMPLES, OPT_MLP_BOUND_MILLI = 6, 7, 8
+SHADER_EXACT, SHADER_EXACT_DEFERRED, SHADER_LEARNED = 0, 1, 2
+STAGES = ["arm", "vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve", "shade", "total"]
 NO_TRIANGLE = 0xFFFFFFFF
 
 class FrameDesc(C.Structure):
@@ -33,6 +35,12 @@ class FrameDesc(C.Structure):
 
 
 BATCH_GRAPH = 1
+
+
+class MlpTrainDesc(C.Structure):
+    """rast_mlp_train_desc of include/rast.h (zero fields take their defaults)."""
+    _fields_ = [("samples", C.c_int64), ("holdout", C.c_int64), ("epochs", C.c_int32), ("ctas", C.c_int32),
+                ("lr", C.c_float), ("seed", C.c_uint64)]
 
 # Every function include/rast.h declares, with its ctypes signature.
 _F, _I32, _I64, _U32, _P = C.POINTER(C.c_float), C.c_int32, C.c_int64, C.c_uint32, C.c_void_p
@@ -64,6 +72,12 @@ SIGNATURES = {
     "rast_autotune": (C.c_int, [_P, C.POINTER(FrameDesc), _I32, _I32, _I32, C.POINTER(C.c_int64)]),
     "rast_draw_noalloc": (C.c_int, [_P, _I64, _P, _I64, _P, _I64, _P, _I32, _P, _I32, _F, _F, _U32, _U32, _U32,
                                     _P, _P, _P, _P]),
+    "rast_upload_vertex_albedo": (C.c_int, [_P, _F, _I64]),
+    "rast_mlp_train": (C.c_int, [_P, C.POINTER(MlpTrainDesc), _F]),
+    "rast_mlp_save": (C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "rast_mlp_load": (C.c_int, [_P, _P, C.c_size_t]),
+    "rast_mlp_eval": (C.c_int, [_P, _F, _F, _I64, _I32, _F]),
+    "rast_get_shade_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
 }
 
 _lib = None
@@ -177,7 +191,19 @@ class Renderer:
         dg = scene.mesh_digest()
         if dg != self._mesh_digest:
             self.upload_mesh(scene.pos, scene.nrm, scene.uv, scene.tris, scene.kd)
+            va = getattr(scene, "vertex_albedo", None)
+            if va is not None:
+                self.upload_vertex_albedo(va)
             self._mesh_digest = dg
+
+    def upload_vertex_albedo(self, rgb):
+        """Per-vertex albedo (nv, 3) in place of the materials' Kd; None returns to Kd."""
+        if rgb is None:
+            self._check(self.lib.rast_upload_vertex_albedo(self.h, None, 0), "rast_upload_vertex_albedo")
+        else:
+            a = _f32(rgb).reshape(-1, 3)
+            self._check(self.lib.rast_upload_vertex_albedo(self.h, _fp(a), a.shape[0]), "rast_upload_vertex_albedo")
+        self._mesh_digest = None
 
     def set_lights(self, lights7):
         li = _f32(lights7).reshape(-1, 7)
@@ -274,9 +300,44 @@ class Renderer:
 
     def stage_times(self):
         """Per-stage device milliseconds of the last draw (RAST_OPT_STAGE_TIMING must be on)."""
-        out = np.zeros(8, np.float32)
+        out = np.zeros(len(STAGES), np.float32)
         self._check(self.lib.rast_get_stage_times(self.h, _fp(out)), "rast_get_stage_times")
         return dict(zip(STAGES, [float(v) for v in out]))
+
+    # learned shading ------------------------------------------------------------------------
+    def mlp_train(self, samples=0, holdout=0, epochs=0, ctas=0, lr=0.0, seed=0):
+        """Train the context's MLP for its current lights. Returns dict(mse, mean_err, max_err, seconds)."""
+        d = MlpTrainDesc(samples, holdout, epochs, ctas, lr, seed)
+        out = np.zeros(4, np.float32)
+        self._check(self.lib.rast_mlp_train(self.h, C.byref(d), _fp(out)), "rast_mlp_train")
+        return dict(zip(["mse", "mean_err", "max_err", "seconds"], [float(v) for v in out]))
+
+    def mlp_save(self):
+        size = C.c_size_t()
+        self._check(self.lib.rast_mlp_save(self.h, None, 0, C.byref(size)), "rast_mlp_save")
+        buf = (C.c_uint8 * size.value)()
+        self._check(self.lib.rast_mlp_save(self.h, buf, size.value, C.byref(size)), "rast_mlp_save")
+        return bytes(buf)
+
+    def mlp_load(self, blob):
+        buf = (C.c_uint8 * len(blob)).from_buffer_copy(blob)
+        self._check(self.lib.rast_mlp_load(self.h, buf, len(blob)), "rast_mlp_load")
+
+    def mlp_eval(self, normals, albedo, exact=False):
+        """Radiance (n, 3) float32 of (normal, albedo) pairs through the tensor-core kernel or the
+        exact shader, before clamping."""
+        nv, al = _f32(normals).reshape(-1, 3), _f32(albedo).reshape(-1, 3)
+        assert nv.shape == al.shape
+        out = np.zeros_like(nv)
+        self._check(self.lib.rast_mlp_eval(self.h, _fp(nv), _fp(al), nv.shape[0], 1 if exact else 0, _fp(out)),
+                    "rast_mlp_eval")
+        return out
+
+    def shade_stats(self):
+        out = (C.c_uint64 * 4)()
+        self._check(self.lib.rast_get_shade_stats(self.h, out), "rast_get_shade_stats")
+        return {"tiles": int(out[0]), "fallback_tiles": int(out[1]), "checked": int(out[2]),
+                "max_checked_err": out[3] / 1e6}
 
     def draw_scene(self, scene, frame=None, depth=None, want_ids=True, clear=False):
         """draw_frame for a Scene: uploads its mesh if it changed, sets its lights, renders."""

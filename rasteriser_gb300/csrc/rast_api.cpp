@@ -36,12 +36,24 @@ rast_status ensure_scratch(rast_ctx* c, uint32_t w, uint32_t h, uint32_t tiles) 
         c->cap_entries = c->bin_capacity > 0 ? c->bin_capacity : std::max<int64_t>(1 << 20, 2 * c->mesh.ntri);
     RAST_CUDA(c, c->entries.reserve(sizeof(uint32_t) * (size_t)c->cap_entries));
     RAST_CUDA(c, c->stats.reserve(sizeof(unsigned long long) * rast::kStatWords));
+    if (c->shader != RAST_SHADER_EXACT) {
+        const int64_t blocks = (npx + rast::kShadeBlock - 1) / rast::kShadeBlock;
+        RAST_CUDA(c, c->gbuf.reserve(2 * sizeof(float4) * (size_t)blocks * rast::kShadeBlock));
+        RAST_CUDA(c, c->gbuf_count.reserve(sizeof(uint32_t) * (size_t)blocks));
+        RAST_CUDA(c, c->shade_index.reserve(sizeof(uint32_t) * (size_t)rast::kShadeIndexWords(blocks)));
+        RAST_CUDA(c, c->shade_stats.reserve(sizeof(unsigned long long) * rast::kShadeStats));
+    }
     return RAST_OK;
 }
 
 rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, uint32_t w, uint32_t h,
                          uint32_t flags, uint8_t* d_rgb, float* d_depth, uint32_t* d_ids) {
     if (!c->has_mesh) return fail(c, RAST_ERR_NO_MESH, "no mesh uploaded");
+    if (c->shader == RAST_SHADER_LEARNED) {
+        if (!c->mlp_ready) return fail(c, RAST_ERR_INVALID_ARG, "learned shading needs trained or loaded weights");
+        if (c->mlp_nl != c->nl || c->mlp_lights_hash != rast::lights_hash(c->lights_host.data(), c->nl))
+            return fail(c, RAST_ERR_INVALID_ARG, "the MLP was trained for another light rig");
+    }
     const uint32_t tiles_x = (w + c->tile - 1) / c->tile, tiles_y = (h + c->tile - 1) / c->tile;
     const uint32_t n_tiles = tiles_x * tiles_y;
     rast_status st = ensure_scratch(c, w, h, n_tiles);
@@ -55,6 +67,8 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     RAST_CUDA(c, cudaMemsetAsync(c->counters.ptr, 0, sizeof(uint32_t) * (rast::kCounterHeader + 2 * (size_t)n_tiles),
                                  c->stream));
     RAST_CUDA(c, cudaMemsetAsync(c->stats.ptr, 0, sizeof(unsigned long long) * rast::kStatWords, c->stream));
+    if (c->shader != RAST_SHADER_EXACT)
+        RAST_CUDA(c, cudaMemsetAsync(c->shade_stats.ptr, 0, sizeof(unsigned long long) * rast::kShadeStats, c->stream));
 
     rast::FrameScratch s;
     s.rv = c->rv.as<float4>();
@@ -66,6 +80,12 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     s.stats = c->stats.as<unsigned long long>();
     s.cap_large = c->cap_large;
     s.cap_entries = c->cap_entries;
+    if (c->shader != RAST_SHADER_EXACT) {
+        s.gbuf = c->gbuf.as<float4>();
+        s.gbuf_count = c->gbuf_count.as<uint32_t>();
+        s.shade_index = c->shade_index.as<uint32_t>();
+        s.shade_stats = c->shade_stats.as<unsigned long long>();
+    }
 
     rast::DrawParams p;
     std::memcpy(p.camera.m, camera, sizeof p.camera.m);
@@ -84,6 +104,10 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     p.rgb = d_rgb;
     p.depth = d_depth;
     p.tri_id = d_ids;
+    p.shader = c->shader;
+    p.mlp = c->mlp_image.ptr;
+    p.mlp_samples = c->mlp_samples;
+    p.mlp_bound = (float)c->mlp_bound_milli * 1e-3f;
     if (c->timing && !c->ev_made) {
         for (auto& e : c->ev) RAST_CUDA(c, cudaEventCreate(&e));
         c->ev_made = true;
@@ -115,6 +139,11 @@ rast_status collect_status(rast_ctx* c) {
         c->keys_armed_clear = false;
         return fail(c, RAST_ERR_BIN_OVERFLOW, "tile-bin pool overflowed; it was grown to " +
                                                   std::to_string(c->cap_entries) + " entries, draw again");
+    }
+    if (status & rast::STATUS_SHADE_TIMEOUT) {
+        uint32_t zero = 0;
+        RAST_CUDA(c, cudaMemcpy(c->counters.as<uint32_t>() + 1, &zero, sizeof zero, cudaMemcpyHostToDevice));
+        return fail(c, RAST_ERR_INTERNAL, "learned shader: a tensor-core MMA did not complete in time");
     }
     if (status & rast::STATUS_CHECK_FAILED) {
         uint32_t w[2] = {0, 0};
@@ -183,7 +212,8 @@ void rast_destroy(rast_ctx* c) {
     cudaStreamSynchronize(c->stream);
     for (DevBuf* b : {&c->pos, &c->tris10, &c->tri_v, &c->tri_nm, &c->nrm, &c->kd, &c->lights, &c->rv, &c->keys,
                       &c->large, &c->counters, &c->tile_offset, &c->entries, &c->stats, &c->d_rgb, &c->d_depth,
-                      &c->d_ids})
+                      &c->d_ids, &c->vcol, &c->gbuf, &c->gbuf_count, &c->shade_index, &c->shade_stats,
+                      &c->mlp_image})
         b->release();
     if (c->ev_made)
         for (auto& e : c->ev) cudaEventDestroy(e);
@@ -221,6 +251,8 @@ rast_status rast_upload_mesh(rast_ctx* c, const float* pos, int64_t nv, const fl
     DeviceGuard g(c->device);
     RAST_CUDA(c, cudaStreamSynchronize(c->stream));
     c->has_mesh = false;
+    c->has_vcol = false;
+    c->mesh.vcol = nullptr;
     if (c->graph_exec) {  // a recorded batch may refer to the mesh being replaced
         cudaGraphExecDestroy(c->graph_exec);
         c->graph_exec = nullptr;
@@ -256,6 +288,24 @@ rast_status rast_upload_mesh(rast_ctx* c, const float* pos, int64_t nv, const fl
     return RAST_OK;
 }
 
+rast_status rast_upload_vertex_albedo(rast_ctx* c, const float* rgb3, int64_t nv) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    if (!c->has_mesh) return fail(c, RAST_ERR_NO_MESH, "no mesh uploaded");
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (!rgb3 && nv == 0) {
+        c->has_vcol = false;
+        c->mesh.vcol = nullptr;
+        return RAST_OK;
+    }
+    if (!rgb3 || nv != c->mesh.nv) return fail(c, RAST_ERR_INVALID_ARG, "vertex albedo needs one rgb per mesh vertex");
+    RAST_CUDA(c, c->vcol.reserve(sizeof(float) * 3 * (size_t)std::max<int64_t>(nv, 1)));
+    if (nv) RAST_CUDA(c, cudaMemcpy(c->vcol.ptr, rgb3, sizeof(float) * 3 * nv, cudaMemcpyHostToDevice));
+    c->has_vcol = true;
+    c->mesh.vcol = c->vcol.as<float>();
+    return RAST_OK;
+}
+
 rast_status rast_set_lights(rast_ctx* c, const float* lights7, int32_t n) {
     if (!c) return RAST_ERR_INVALID_ARG;
     if (n < 0 || n > kMaxLights || (n && !lights7)) return fail(c, RAST_ERR_INVALID_ARG, "bad light count or pointer");
@@ -266,6 +316,7 @@ rast_status rast_set_lights(rast_ctx* c, const float* lights7, int32_t n) {
     // The host array may be reused by the caller as soon as this returns.
     RAST_CUDA(c, cudaStreamSynchronize(c->stream));
     c->nl = n;
+    c->lights_host.assign(lights7, lights7 + 7 * (size_t)n);
     return RAST_OK;
 }
 
@@ -358,6 +409,19 @@ rast_status rast_set_option(rast_ctx* c, int option, int64_t value) {
             c->bin_capacity = value;
             c->cap_entries = 0;
             return RAST_OK;
+        case RAST_OPT_SHADER:
+            if (value != RAST_SHADER_EXACT && value != RAST_SHADER_EXACT_DEFERRED && value != RAST_SHADER_LEARNED)
+                return fail(c, RAST_ERR_INVALID_ARG, "unknown shader");
+            c->shader = (int32_t)value;
+            return RAST_OK;
+        case RAST_OPT_MLP_SAMPLES:
+            if (value < 0 || value > 4) return fail(c, RAST_ERR_INVALID_ARG, "MLP check samples must be 0..4");
+            c->mlp_samples = (int32_t)value;
+            return RAST_OK;
+        case RAST_OPT_MLP_BOUND_MILLI:
+            if (value < 0 || value > 255000) return fail(c, RAST_ERR_INVALID_ARG, "MLP bound out of range");
+            c->mlp_bound_milli = (int32_t)value;
+            return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
 }
@@ -370,6 +434,9 @@ rast_status rast_get_option(rast_ctx* c, int option, int64_t* value) {
         case RAST_OPT_BIN_CAPACITY: *value = c->cap_entries ? c->cap_entries : c->bin_capacity; return RAST_OK;
         case RAST_OPT_STAGE_TIMING: *value = c->timing ? 1 : 0; return RAST_OK;
         case RAST_OPT_ROW_CHUNK: *value = c->row_chunk; return RAST_OK;
+        case RAST_OPT_SHADER: *value = c->shader; return RAST_OK;
+        case RAST_OPT_MLP_SAMPLES: *value = c->mlp_samples; return RAST_OK;
+        case RAST_OPT_MLP_BOUND_MILLI: *value = c->mlp_bound_milli; return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
 }
@@ -384,14 +451,32 @@ rast_status rast_get_device_status(rast_ctx* c, uint32_t out[4]) {
     return RAST_OK;
 }
 
-rast_status rast_get_stage_times(rast_ctx* c, float out_ms[8]) {
+rast_status rast_get_stage_times(rast_ctx* c, float out_ms[9]) {
     if (!c || !out_ms) return RAST_ERR_INVALID_ARG;
-    for (int i = 0; i < 8; ++i) out_ms[i] = 0.f;
+    for (int i = 0; i < 9; ++i) out_ms[i] = 0.f;
     if (!c->ev_recorded) return fail(c, RAST_ERR_INVALID_ARG, "no timed draw (set RAST_OPT_STAGE_TIMING first)");
     DeviceGuard g(c->device);
-    RAST_CUDA(c, cudaEventSynchronize(c->ev[7]));
-    for (int i = 0; i < 7; ++i) RAST_CUDA(c, cudaEventElapsedTime(&out_ms[i], c->ev[i], c->ev[i + 1]));
-    RAST_CUDA(c, cudaEventElapsedTime(&out_ms[7], c->ev[0], c->ev[7]));
+    RAST_CUDA(c, cudaEventSynchronize(c->ev[8]));
+    for (int i = 0; i < 8; ++i) RAST_CUDA(c, cudaEventElapsedTime(&out_ms[i], c->ev[i], c->ev[i + 1]));
+    RAST_CUDA(c, cudaEventElapsedTime(&out_ms[8], c->ev[0], c->ev[8]));
+    return RAST_OK;
+}
+
+rast_status rast_get_shade_stats(rast_ctx* c, uint64_t out[4]) {
+    if (!c || !out) return RAST_ERR_INVALID_ARG;
+    std::memset(out, 0, sizeof(uint64_t) * 4);
+    if (!c->shade_stats.ptr) return RAST_OK;
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    unsigned long long s[rast::kShadeStats];
+    RAST_CUDA(c, cudaMemcpy(s, c->shade_stats.ptr, sizeof s, cudaMemcpyDeviceToHost));
+    out[0] = s[0];
+    out[1] = s[1];
+    out[2] = s[2];
+    float e;
+    const uint32_t bits = (uint32_t)s[3];
+    std::memcpy(&e, &bits, sizeof e);
+    out[3] = (uint64_t)((double)e * 1e6 + 0.5);
     return RAST_OK;
 }
 

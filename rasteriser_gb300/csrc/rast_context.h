@@ -11,6 +11,7 @@
 
 #include "rast.h"
 #include "rast_internal.h"
+#include "rast_mlp.h"
 
 namespace rast {
 
@@ -65,9 +66,14 @@ struct rast_ctx {
     rast::DeviceMesh mesh;
     bool has_mesh = false;
 
+    // per-vertex albedo (rast_upload_vertex_albedo), nv * 3
+    DevBuf vcol;
+    bool has_vcol = false;
+
     // lights
     DevBuf lights;
     int32_t nl = 0;
+    std::vector<float> lights_host;  // the records last set, for the learned shader's rig check
 
     // per-draw scratch
     DevBuf rv, keys, large, counters, tile_offset, entries, stats;
@@ -78,10 +84,25 @@ struct rast_ctx {
     // host-pointer draws stage through these
     DevBuf d_rgb, d_depth, d_ids;
 
+    // deferred shading
+    int32_t shader = 0;           // RAST_SHADER_*
+    int32_t mlp_samples = 2;      // RAST_OPT_MLP_SAMPLES
+    int32_t mlp_bound_milli = 500;  // RAST_OPT_MLP_BOUND_MILLI
+    DevBuf gbuf, gbuf_count, shade_index, shade_stats;
+
+    // learned shader state (rast_mlp.cpp)
+    DevBuf mlp_image;             // rast::MlpImage
+    bool mlp_ready = false;
+    uint64_t mlp_lights_hash = 0;
+    int32_t mlp_nl = 0;
+    float mlp_scale = 1.f;
+    float mlp_loss = 0.f;
+    std::vector<float> mlp_q;     // rounded parameters of the current weights (rast::kMlpParams)
+
     // options
     uint32_t small_max = 4096;
     uint32_t tile = 16;
-    uint32_t row_chunk = 4;
+    uint32_t row_chunk = 8;
     int64_t bin_capacity = 0;  // 0: sized from the mesh
 
     uint64_t last_launches = 0;
@@ -98,7 +119,7 @@ struct rast_ctx {
 
     // stage timing
     bool timing = false;
-    cudaEvent_t ev[8] = {};
+    cudaEvent_t ev[9] = {};
     bool ev_made = false;
     bool ev_recorded = false;
 };

@@ -37,7 +37,10 @@ enum StatIndex : int {
 
 // Device status word bits (counters[1]); counters[2] and [3] hold the code and detail of the
 // first failed internal check.
-enum StatusBits : uint32_t { STATUS_BIN_OVERFLOW = 1u, STATUS_LARGE_OVERFLOW = 2u, STATUS_CHECK_FAILED = 4u };
+enum StatusBits : uint32_t {
+    STATUS_BIN_OVERFLOW = 1u, STATUS_LARGE_OVERFLOW = 2u, STATUS_CHECK_FAILED = 4u,
+    STATUS_SHADE_TIMEOUT = 8u  // the learned shader gave up waiting for a tensor-core MMA
+};
 
 // Words of FrameScratch::counters before the per-tile counts:
 //   [0] binned triangles   [1] status bits   [2] first failed check   [3] its detail
@@ -53,6 +56,7 @@ struct DeviceMesh {
     const int4* tri_nm = nullptr;    // ntri: normal indices 0..2, material
     const float* nrm = nullptr;      // nn * 3
     const float* kd = nullptr;       // nmat * 3
+    const float* vcol = nullptr;     // nv * 3 per-vertex albedo, or null
     int64_t nv = 0, ntri = 0, nn = 0;
     int32_t nmat = 0;
 };
@@ -67,7 +71,27 @@ struct FrameScratch {
     uint32_t* entries = nullptr;        // bin entries, capacity cap_entries
     unsigned long long* stats = nullptr;  // kStatWords
     int64_t cap_large = 0, cap_entries = 0;
+    // deferred shading (DrawParams::shader != 0)
+    float4* gbuf = nullptr;             // 2 float4 per record: (normal xyz, albedo r), (albedo gb, pixel, 0)
+    uint32_t* gbuf_count = nullptr;     // records per block of 1024 pixels
+    uint32_t* shade_index = nullptr;    // kShadeIndexWords(blocks): the tiles of the shading pass
+    unsigned long long* shade_stats = nullptr;  // kShadeStats counters of the learned shader
 };
+
+// Deferred shading. The resolve pass stores the winning fragments of each block of 1024 pixels
+// in the block's records (block * 1024 + i, raster order) with the block's count; the last block
+// to finish lists the shading tiles (rast_tiles.cuh), up to 128 records of one block each.
+constexpr int kShadeTile = 128;
+constexpr int kShadeBlock = 1024;
+// shade_index layout: [0] fragments, [1] tiles, [2..3] unused, then up to 8 tile entries per block.
+inline int64_t kShadeIndexWords(int64_t blocks) { return 4 + 8 * blocks; }
+// counters word counting the resolve blocks that finished (deferred shading)
+constexpr int kResolveTicket = 5;
+// counters word handing out the learned shader's tiles
+constexpr int kShadeTicket = 6;
+// shade_stats: [0] tiles shaded by the MLP, [1] tiles sent to the exact shader, [2] fragments
+// checked, [3] largest checked error (float bits of the channel error in 1/255 units).
+constexpr int kShadeStats = 4;
 
 struct DrawParams {
     Mat4 camera, normal;
@@ -83,12 +107,21 @@ struct DrawParams {
     uint8_t* rgb;           // device planar RGB8
     float* depth;           // device
     uint32_t* tri_id;       // device, nullable
+    int32_t shader = 0;     // 0 exact in the resolve pass, 1 exact deferred, 2 learned deferred
+    const void* mlp = nullptr;  // shader 2: the device MlpImage
+    int32_t mlp_samples = 2;    // shader 2: fragments per tile checked against the exact shader
+    float mlp_bound = 0.5f;     // shader 2: largest checked channel error (1/255 units) a tile may have
 };
+
+// The deferred shading pass over the resolve's fragment records (rast_shade.cu): the exact or
+// learned shading kernel over the tiles the resolve listed. Returns the number of launches, or -1.
+int launch_shade(const FrameScratch& s, const DrawParams& p, int64_t blocks, cudaStream_t stream);
 
 // Launches every kernel of one draw on `stream`. Returns the number of kernel launches made
 // (memsets excluded) or -1 with cudaGetLastError() set.
-// With `events` (8 events, nullable) it records events[0] before the first kernel and
-// events[1..7] after key arming, vertex, setup, scan, scatter, tile raster and resolve.
+// With `events` (9 events, nullable) it records events[0] before the first kernel and
+// events[1..8] after key arming, vertex, setup, scan, scatter, tile raster, resolve and the
+// deferred shading pass.
 int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams& p, cudaStream_t stream,
                 cudaEvent_t* events = nullptr);
 

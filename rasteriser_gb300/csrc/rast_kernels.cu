@@ -27,24 +27,15 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "rast_exact.cuh"
 #include "rast_internal.h"
+#include "rast_tiles.cuh"
 
 namespace rast {
 namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr unsigned long long kNoWinner = 0xFFFFFFFFull;  // low word of a key with no fragment
-
-// ---------------------------------------------------------------------------------------------
-// exact arithmetic helpers
-// ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ float dvd(float a, float b) { return __fdiv_rn(a, b); }
-// glm::min / glm::max on scalars: x < y ? x : y and x > y ? x : y (NaN and -0 follow from this).
-__device__ __forceinline__ float gmin(float x, float y) { return x < y ? x : y; }
-__device__ __forceinline__ float gmax(float x, float y) { return x > y ? x : y; }
 
 // Row r of mat4 * vec4, summed (c0*x + c1*y) + (c2*z + c3*w).
 __device__ __forceinline__ float mrow(const Mat4& M, int r, float x, float y, float z, float w) {
@@ -843,18 +834,25 @@ struct ResolveArgs {
     float* depth;
     uint32_t* tri_id;
     unsigned long long* stats;
+    const float* vcol;    // per-vertex albedo (nv * 3) or null for the material's Kd
+    float4* gbuf;         // deferred shading: 2 float4 per fragment record, or null to shade here
+    uint32_t* gbuf_count; // deferred shading: records per block (1024 pixels)
+    uint32_t* shade_index;  // deferred shading: the tile list build_shade_tiles writes
 };
 
 constexpr int kResolveThreads = 256;
 constexpr int kResolveWarps = kResolveThreads / 32;
 constexpr int kSpan = 128;  // consecutive pixels per warp, 4 per lane
+static_assert(kResolveWarps * kSpan == kShadeBlock, "a resolve block is one block of shading records");
 
-// Shades one winning fragment exactly as update_pixel does (drawing.cpp:108-146,
-// shading.cpp:20-34): barycentrics at the integer pixel, NDC depth, perspective-correct normal,
-// normalise, clockwise flip, Lambert sum over the lights, clamp to 255 and truncate.
-__device__ __forceinline__ void shade_fragment(const ResolveArgs& a, uint32_t x, uint32_t y, float4 v0, float4 v1,
-                                               float4 v2, float3 n0, float3 n1, float3 n2, int mat, float& depth,
-                                               uint32_t& rgb) {
+// The winning fragment's attributes as update_pixel computes them (drawing.cpp:108-140):
+// barycentrics at the integer pixel, NDC depth, perspective-correct normal, normalised and flipped
+// for clockwise winding, and the albedo (the material's Kd, or the perspective-correct per-vertex
+// colour when the mesh has one).
+__device__ __forceinline__ void fragment_attributes(const ResolveArgs& a, uint32_t x, uint32_t y, float4 v0, float4 v1,
+                                                    float4 v2, float3 n0, float3 n1, float3 n2, int mat,
+                                                    int32_t i0, int32_t i1, int32_t i2, float& depth, float3& nrm,
+                                                    float3& alb) {
     EdgeTri T;
     make_edge_tri(v0, v1, v2, T);
     const float pxf = (float)x, pyf = (float)y;
@@ -864,36 +862,28 @@ __device__ __forceinline__ void shade_fragment(const ResolveArgs& a, uint32_t x,
     const float b0 = dvd(e0, T.area), b1 = dvd(e1, T.area), b2 = dvd(e2, T.area);
     depth = interp_depth(T, b0, b1, b2);
 
-    const float i0 = mul(v0.w, b0), i1 = mul(v1.w, b1), i2 = mul(v2.w, b2);
-    const float dd = dvd(1.f, add(add(i0, i1), i2));
-    float sx = add(add(mul(i0, n0.x), mul(i1, n1.x)), mul(i2, n2.x));
-    float sy = add(add(mul(i0, n0.y), mul(i1, n1.y)), mul(i2, n2.y));
-    float sz = add(add(mul(i0, n0.z), mul(i1, n1.z)), mul(i2, n2.z));
+    const float i0w = mul(v0.w, b0), i1w = mul(v1.w, b1), i2w = mul(v2.w, b2);
+    const float dd = dvd(1.f, add(add(i0w, i1w), i2w));
+    float sx = add(add(mul(i0w, n0.x), mul(i1w, n1.x)), mul(i2w, n2.x));
+    float sy = add(add(mul(i0w, n0.y), mul(i1w, n1.y)), mul(i2w, n2.y));
+    float sz = add(add(mul(i0w, n0.z), mul(i1w, n1.z)), mul(i2w, n2.z));
     sx = mul(dd, sx); sy = mul(dd, sy); sz = mul(dd, sz);
     const float inv = dvd(1.0f, __fsqrt_rn(add(add(mul(sx, sx), mul(sy, sy)), mul(sz, sz))));
-    float nx = mul(sx, inv), ny = mul(sy, inv), nz = mul(sz, inv);
-    if (a.cw) { nx = -nx; ny = -ny; nz = -nz; }
+    nrm = make_float3(mul(sx, inv), mul(sy, inv), mul(sz, inv));
+    if (a.cw) nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
 
-    const float* kd = a.kd + 3 * (int64_t)mat;
-    const float ar = __ldg(kd), ag = __ldg(kd + 1), ab = __ldg(kd + 2);
-    const float one_over_pi = 0.318309886183790671537767526745028724f;
-    float accr = 0.f, accg = 0.f, accb = 0.f;
-    for (int l = 0; l < a.nl; ++l) {
-        const float* L = a.lights + 7 * l;
-        const float I = __ldg(L + 3);
-        float cr = mul(I, __ldg(L + 4)), cg = mul(I, __ldg(L + 5)), cb = mul(I, __ldg(L + 6));
-        cr = mul(cr, ar); cg = mul(cg, ag); cb = mul(cb, ab);
-        const float d = add(add(mul(nx, -__ldg(L)), mul(ny, -__ldg(L + 1))), mul(nz, -__ldg(L + 2)));
-        const float m = gmax(0.f, d);
-        cr = mul(mul(cr, m), one_over_pi);
-        cg = mul(mul(cg, m), one_over_pi);
-        cb = mul(mul(cb, m), one_over_pi);
-        accr = add(accr, cr); accg = add(accg, cg); accb = add(accb, cb);
+    if (a.vcol) {
+        const float* c0 = a.vcol + 3 * (int64_t)i0;
+        const float* c1 = a.vcol + 3 * (int64_t)i1;
+        const float* c2 = a.vcol + 3 * (int64_t)i2;
+        float ux = add(add(mul(i0w, __ldg(c0)), mul(i1w, __ldg(c1))), mul(i2w, __ldg(c2)));
+        float uy = add(add(mul(i0w, __ldg(c0 + 1)), mul(i1w, __ldg(c1 + 1))), mul(i2w, __ldg(c2 + 1)));
+        float uz = add(add(mul(i0w, __ldg(c0 + 2)), mul(i1w, __ldg(c1 + 2))), mul(i2w, __ldg(c2 + 2)));
+        alb = make_float3(mul(dd, ux), mul(dd, uy), mul(dd, uz));
+    } else {
+        const float* kd = a.kd + 3 * (int64_t)mat;
+        alb = make_float3(__ldg(kd), __ldg(kd + 1), __ldg(kd + 2));
     }
-    const uint32_t r = __float2uint_rz(gmin(accr, 255.f)) & 0xFFu;
-    const uint32_t g = __float2uint_rz(gmin(accg, 255.f)) & 0xFFu;
-    const uint32_t b = __float2uint_rz(gmin(accb, 255.f)) & 0xFFu;
-    rgb = r | (g << 8) | (b << 16);
 }
 
 struct ResolveStage {
@@ -908,14 +898,19 @@ struct ResolveStage {
 // frame and depth buffers 4 pixels per lane.
 __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
     __shared__ ResolveStage stage[kResolveWarps];
+    __shared__ uint32_t s_count[kResolveWarps];
+    // Deferred shading: the shading kernel may be launched once every block of this grid has
+    // started (it waits for this grid's completion before it reads the records).
+    if (a.gbuf) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     ResolveStage& S = stage[warp];
     const int64_t npx = (int64_t)a.width * a.height;
     const int64_t span0 = ((int64_t)blockIdx.x * kResolveWarps + warp) * kSpan;
     unsigned long long written = 0;
-    if (span0 < npx) {
+    const bool in_range = span0 < npx;
+    {
         const int64_t p0 = span0 + 4 * lane;
-        const bool full = p0 + 3 < npx;
+        const bool full = in_range && p0 + 3 < npx;
         const bool vec = a.vec_ok && full;
         unsigned long long key[4];
         if (full) {
@@ -924,9 +919,9 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             key[0] = k01.x; key[1] = k01.y; key[2] = k23.x; key[3] = k23.y;
         } else {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) key[k] = p0 + k < npx ? a.keys[p0 + k] : kNoWinner;
+            for (int k = 0; k < 4; ++k) key[k] = in_range && p0 + k < npx ? a.keys[p0 + k] : kNoWinner;
         }
-        if (a.keys_rearm) {
+        if (a.keys_rearm && in_range) {
             const unsigned long long r = arm_key(1.0f);
             if (full) {
                 *reinterpret_cast<ulonglong2*>(a.keys_rearm + p0) = make_ulonglong2(r, r);
@@ -957,6 +952,22 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             n_win += __popc(m);
         }
         __syncwarp();
+        // deferred shading: the block's winners go to its records in raster order; this warp's
+        // start is the count of the warps before it
+        uint32_t rec_base = 0;
+        if (a.gbuf) {
+            if (lane == 0) s_count[warp] = n_win;
+            __syncthreads();
+            uint32_t before = 0, total = 0;
+#pragma unroll
+            for (int w = 0; w < kResolveWarps; ++w) {
+                const uint32_t c = s_count[w];
+                before += w < warp ? c : 0u;
+                total += c;
+            }
+            rec_base = blockIdx.x * (uint32_t)(kResolveWarps * kSpan) + before;
+            if (threadIdx.x == 0) a.gbuf_count[blockIdx.x] = total;
+        }
         for (uint32_t i = lane; i < n_win; i += 32) {
             const uint32_t off = S.win_px[i];
             const int64_t tt = S.win_tri[i];
@@ -975,13 +986,22 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             const float3 n1 = camera_normal(a.normal, m1.x, m1.y, m1.z);
             const float3 n2 = camera_normal(a.normal, m2.x, m2.y, m2.z);
             float dep;
-            uint32_t col;
-            shade_fragment(a, x, y, v0, v1, v2, n0, n1, n2, nm.w, dep, col);
+            float3 nrm, alb;
+            fragment_attributes(a, x, y, v0, v1, v2, n0, n1, n2, nm.w, i0, i1, i2, dep, nrm, alb);
             S.depth[off] = dep;
-            S.rgb[off] = col;
+            if (a.gbuf) {
+                // deferred: the span's i-th record; the shading pass writes the colour
+                const size_t slot = (size_t)rec_base + i;
+                a.gbuf[2 * slot] = make_float4(nrm.x, nrm.y, nrm.z, alb.x);
+                a.gbuf[2 * slot + 1] = make_float4(alb.y, alb.z, __uint_as_float(p), 0.f);
+                S.rgb[off] = 0u;
+            } else {
+                S.rgb[off] = shade_lights(a.lights, a.nl, nrm, alb);
+            }
         }
         written = n_win;
         __syncwarp();
+        if (in_range) {
         float dep[4];
         uint32_t col[4];
 #pragma unroll
@@ -1019,10 +1039,24 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             for (int k = 0; k < 4; ++k)
                 if (p0 + k < npx) a.tri_id[p0 + k] = win[k] ? (uint32_t)(key[k] & 0xFFFFFFFFull) : 0xFFFFFFFFu;
         }
+        }
         // lane 0 counts for the warp
         if (lane != 0) written = 0;
     }
     stat_add(a.stats, STAT_WRITTEN, written);
+    if (a.gbuf) {
+        // the last block to finish lists the shading tiles of all blocks
+        __shared__ bool s_last;
+        if (threadIdx.x == 0) {
+            __threadfence();  // this block's count is visible before its ticket
+            s_last = atomicAdd(&a.counters[kResolveTicket], 1u) == gridDim.x - 1;
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            build_shade_tiles(a.gbuf_count, gridDim.x, a.shade_index);
+        }
+    }
 }
 
 int grid_for(int64_t n, int threads, int max_blocks) {
@@ -1165,10 +1199,21 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.depth = p.depth;
     ra.tri_id = p.tri_id;
     ra.stats = s.stats;
+    ra.vcol = mesh.vcol;
+    const bool deferred = p.shader != 0;
+    ra.gbuf = deferred ? s.gbuf : nullptr;
+    ra.gbuf_count = deferred ? s.gbuf_count : nullptr;
+    ra.shade_index = deferred ? s.shade_index : nullptr;
     const int64_t spans = (npx + kSpan - 1) / kSpan;
     k_resolve<<<(unsigned)((spans + kResolveWarps - 1) / kResolveWarps), kResolveThreads, 0, stream>>>(ra);
     ++launches;
     mark(7);
+    if (p.shader != 0) {
+        const int n = launch_shade(s, p, (spans + kResolveWarps - 1) / kResolveWarps, stream);
+        if (n < 0) return -1;
+        launches += n;
+    }
+    mark(8);
 
     return cudaPeekAtLastError() == cudaSuccess ? launches : -1;
 }

@@ -106,6 +106,7 @@ class Scene:
     fovy_deg: float = 45.0
     z_near: float = 0.1
     z_far: float = 6.0
+    vertex_albedo: object = None      # (nv, 3) float32 per-vertex albedo in place of Kd, or None
 
     def with_view(self, **kw):
         return dataclasses.replace(self, **kw)
@@ -118,6 +119,10 @@ class Scene:
         h = hashlib.sha256()
         for a in (self.pos, self.tris, self.nrm, self.uv, self.kd, self.lights):
             h.update(np.ascontiguousarray(a).tobytes())
+        va = getattr(self, "vertex_albedo", None)
+        if va is not None:
+            h.update(b"vertex_albedo")
+            h.update(np.ascontiguousarray(va).tobytes())
         return h.hexdigest()
 
 
@@ -353,3 +358,11 @@ def spin_angles(frame, step=1.0 / 60.0):
 def config_soup(n_tris=4_000_000, width=3840, height=2160, seed=2):
     """Overdraw-heavy triangle soup (4M triangles at 3840x2160)."""
     return soup(n_tris, width, height, seed=seed)
+
+
+def config_many_lights(n_lon=1024, n_lat=512, width=1920, height=1080, n_lights=256, seed=4, light_seed=5):
+    """Many-light shading workload: the displaced sphere with smooth normals (the normalised unit
+    positions), per-vertex albedo uniform in [0,1]^3 and ``n_lights`` directional lights from
+    rig_random (directions uniform on the sphere, intensity Exp(1)/n * 255, colours uniform)."""
+    sc = uv_sphere(n_lon, n_lat, seed=seed, flat=False, vertex_albedo=True)
+    return sc.with_view(width=width, height=height, lights=rig_random(n_lights, light_seed), **CAMERA)

@@ -1,0 +1,257 @@
+"""Deferred and learned shading through the C ABI.
+
+- EXACT_DEFERRED gives the reference's colour bit for bit (oracle port), like the fused EXACT mode.
+- Per-vertex albedo (the many-light workload's material) matches the oracle port bit for bit.
+- The tensor-core MLP kernel matches a float64 numpy forward pass of the same BF16 network.
+- LEARNED keeps depth and triangle ids bit-exact and the colour within the error bound.
+"""
+import numpy as np
+import pytest
+
+import mlp_ref
+from rasteriser_gb300 import abi
+from rasteriser_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+RGB_TOL = 1          # per channel, 1/255 units, for the learned shader's frame
+MEAN_TOL = 0.5       # mean absolute channel error over covered pixels, learned shader
+
+
+@pytest.fixture(scope="module")
+def rnd():
+    r = abi.Renderer(0)
+    yield r
+    r.close()
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def draw(r, sc, shader, clear=True):
+    r.set_option(abi.OPT_SHADER, shader)
+    try:
+        return r.draw_scene(sc, clear=clear)
+    finally:
+        r.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+
+
+def oracle_frame(port, sc):
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    f, d, ids, _ = port.draw(sc, cam, nm, lights)
+    return f, d, ids
+
+
+def small_many_lights(n_lights=16, w=320, h=240, seg=(96, 48)):
+    return S.config_many_lights(seg[0], seg[1], w, h, n_lights).with_view(angles=(0.2, 0.7, 0.0))
+
+
+SCENES = {
+    "icosphere4": lambda: S.config_icosphere_small(),
+    "soup": lambda: S.soup(20000, 320, 200, seed=31, area_range=(0.5, 2000.0)),
+    "many_lights16": lambda: small_many_lights(16),
+    "sphere_cw": lambda: S.config_displaced_sphere(128, 64, 257, 131).with_view(wind_clockwise=True),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+@pytest.mark.parametrize("shader", [abi.SHADER_EXACT, abi.SHADER_EXACT_DEFERRED])
+def test_exact_modes_match_oracle(rnd, port, name, shader):
+    sc = SCENES[name]()
+    f, d, ids = draw(rnd, sc, shader)
+    of, od, oids = oracle_frame(port, sc)
+    assert np.array_equal(bits(d), bits(od))
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(f, of), f"RGB differs at {np.argwhere(f != of)[:5]}"
+
+
+def test_deferred_read_modify_write(rnd, port):
+    """Without RAST_CLEAR the frame and depth coming in are kept where nothing wins."""
+    sc = small_many_lights(8)
+    rng = np.random.default_rng(3)
+    frame0 = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
+    depth0 = np.where(rng.random((sc.height, sc.width)) < 0.5, 1.0, 0.97).astype(np.float32)
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT_DEFERRED)
+    try:
+        f, d, ids = rnd.draw_scene(sc, frame=frame0.copy(), depth=depth0.copy())
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    of, od, oids, _ = port.draw(sc, cam, nm, lights, frame=frame0, depth=depth0)
+    assert np.array_equal(bits(d), bits(od))
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(f, of)
+
+
+def test_vertex_albedo_removed(rnd, port):
+    sc = small_many_lights(4)
+    rnd.upload_scene_mesh(sc)
+    rnd.upload_vertex_albedo(None)  # back to Kd
+    plain = sc.with_view(vertex_albedo=None)
+    cam, nm, lights, _ = abi.scene_frame_inputs(plain)
+    rnd.set_lights(lights)
+    f, d, ids = rnd.draw(cam, nm, plain.width, plain.height, abi.CLEAR, want_ids=True)
+    of, od, oids = oracle_frame(port, plain)
+    assert np.array_equal(f, of) and np.array_equal(bits(d), bits(od))
+    rnd._mesh_digest = None
+
+
+def test_vertex_albedo_size_checked(rnd):
+    sc = small_many_lights(4)
+    rnd.upload_scene_mesh(sc)
+    with pytest.raises(abi.RastError):
+        rnd.upload_vertex_albedo(np.zeros((sc.pos.shape[0] - 1, 3), np.float32))
+    rnd._mesh_digest = None
+
+
+def test_options_validated(rnd):
+    for opt, bad in [(abi.OPT_SHADER, 3), (abi.OPT_MLP_SAMPLES, 5), (abi.OPT_MLP_SAMPLES, -1),
+                     (abi.OPT_MLP_BOUND_MILLI, -1)]:
+        with pytest.raises(abi.RastError):
+            rnd.set_option(opt, bad)
+    assert rnd.get_option(abi.OPT_SHADER) == abi.SHADER_EXACT
+    assert rnd.get_option(abi.OPT_MLP_SAMPLES) == 2
+    assert rnd.get_option(abi.OPT_MLP_BOUND_MILLI) == 500
+
+
+def test_mlp_kernel_matches_numpy(rnd):
+    """The tcgen05 path against a float64 forward pass of the same BF16 weights."""
+    w = mlp_ref.random_weights(7)
+    rnd.mlp_load(mlp_ref.make_blob(w))
+    rng = np.random.default_rng(11)
+    n = 5000  # 40 tiles, the last one partial
+    v = rng.normal(size=(n, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    nv = v.astype(np.float32)
+    alb = rng.random((n, 3)).astype(np.float32)
+    got = rnd.mlp_eval(nv, alb)
+    want = mlp_ref.forward(w, nv, alb)
+    err = np.abs(got - want)
+    scale = float(w["scale"])
+    # Sums agree to FP32 rounding except where a feature or hidden value sits on a BF16 rounding
+    # boundary and the kernel's feature recurrence (hardware sine, FP32) rounds it the other way
+    # than numpy's float64 sine: one BF16 step in one input moves the output by ~1e-2 * scale.
+    tight = err <= 1e-4 * scale + 1e-4 * np.abs(want)
+    assert tight.mean() > 0.95, f"only {tight.mean():.4f} of the outputs agree to FP32 rounding"
+    tol = 0.02 * np.abs(want) + 0.01 * scale
+    assert np.all(err <= tol), f"max err {err.max()} at {np.unravel_index(err.argmax(), err.shape)}"
+
+
+def test_mlp_blob_round_trip(rnd):
+    w = mlp_ref.random_weights(8)
+    blob = mlp_ref.make_blob(w, n_lights=3, lights_hash=12345, loss=0.25)
+    rnd.mlp_load(blob)
+    assert rnd.mlp_save() == blob
+    back = mlp_ref.parse_blob(rnd.mlp_save())
+    for k in ("w1", "w2", "w3"):
+        assert np.array_equal(back[k], np.asarray(w[k], np.float32))
+
+
+def test_mlp_blob_refused(rnd):
+    blob = bytearray(mlp_ref.make_blob(mlp_ref.random_weights(9)))
+    with pytest.raises(abi.RastError):
+        rnd.mlp_load(bytes(blob[:-4]))
+    bad = bytearray(blob)
+    bad[0:4] = b"XMLP"
+    with pytest.raises(abi.RastError):
+        rnd.mlp_load(bytes(bad))
+    other = bytearray(blob)
+    other[8:12] = (102).to_bytes(4, "little")  # n_in of another network
+    with pytest.raises(abi.RastError):
+        rnd.mlp_load(bytes(other))
+
+
+def test_exact_eval_matches_oracle_shade(rnd, port):
+    lights = S.rig_random(256, 21)
+    rnd.set_lights(lights)
+    rng = np.random.default_rng(5)
+    n = 700
+    v = rng.normal(size=(n, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    nv = v.astype(np.float32)
+    alb = rng.random((n, 3)).astype(np.float32)
+    got = rnd.mlp_eval(nv, alb, exact=True)
+    gb = np.minimum(got, 255.0).astype(np.uint32)
+    for i in range(n):
+        assert np.array_equal(gb[i], port.shade(nv[i], alb[i], lights)), i
+
+
+@pytest.fixture(scope="module")
+def trained(rnd):
+    """A learned shader for a 256-light rig, trained on 1M samples."""
+    sc = small_many_lights(256, 640, 480, (256, 128))
+    _, _, lights, _ = abi.scene_frame_inputs(sc)
+    rnd.set_lights(lights)
+    stats = rnd.mlp_train(samples=1 << 20, epochs=24, seed=3)
+    return sc, lights, stats, rnd.mlp_save()
+
+
+def test_training_converges(trained):
+    _, _, st, _ = trained
+    print("training:", st)
+    assert st["mean_err"] < 0.25, st
+    assert st["max_err"] < 2.0, st
+
+
+def test_learned_frame(rnd, port, trained):
+    sc, lights, _, blob = trained
+    rnd.mlp_load(blob)
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
+    try:
+        f, d, ids = rnd.draw_scene(sc, clear=True)
+        st = rnd.shade_stats()
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+    of, od, oids = oracle_frame(port, sc)
+    assert np.array_equal(bits(d), bits(od)), "depth must stay exact"
+    assert np.array_equal(ids, oids), "coverage must stay exact"
+    cov = oids != 0xFFFFFFFF
+    diff = np.abs(f.astype(np.int16) - of.astype(np.int16))
+    print("learned frame: max", diff.max(), "mean", diff[:, cov].mean(), "stats", st)
+    assert np.all(diff[:, ~cov] == 0)
+    assert diff.max() <= RGB_TOL
+    assert diff[:, cov].mean() <= MEAN_TOL
+    # tiles: up to 128 covered pixels of one 1024-pixel block (raster order) each
+    flat = np.concatenate([cov.ravel(), np.zeros(-cov.size % 1024, bool)]).reshape(-1, 1024)
+    assert st["tiles"] == int(((flat.sum(axis=1) + 127) // 128).sum())
+
+
+def test_learned_fallback_gives_exact_colour(rnd, port, trained):
+    """With a bound below any error every checked tile falls back: the exact colour everywhere."""
+    sc, lights, _, blob = trained
+    rnd.mlp_load(blob)
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
+    rnd.set_option(abi.OPT_MLP_BOUND_MILLI, 0)
+    rnd.set_option(abi.OPT_MLP_SAMPLES, 4)
+    try:
+        f, d, ids = rnd.draw_scene(sc, clear=True)
+        st = rnd.shade_stats()
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+        rnd.set_option(abi.OPT_MLP_BOUND_MILLI, 500)
+        rnd.set_option(abi.OPT_MLP_SAMPLES, 2)
+    of, _, _ = oracle_frame(port, sc)
+    # a tile keeps the MLP colour only where all four checked fragments match to the bit
+    fell = st["fallback_tiles"]
+    assert fell >= st["tiles"] - 2, st
+    diff = np.abs(f.astype(np.int16) - of.astype(np.int16))
+    assert diff.max() <= RGB_TOL
+
+
+def test_learned_needs_matching_rig(rnd, trained):
+    sc, lights, _, blob = trained
+    rnd.mlp_load(blob)
+    rnd.upload_scene_mesh(sc)
+    other = lights.copy()
+    other[0, 3] *= 1.5
+    rnd.set_lights(other)
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
+    try:
+        cam, nm, _, _ = abi.scene_frame_inputs(sc)
+        with pytest.raises(abi.RastError):
+            rnd.draw(cam, nm, sc.width, sc.height, abi.CLEAR)
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+    hdr = mlp_ref.parse_blob(blob)
+    assert hdr["lights_hash"] == mlp_ref.lights_hash(lights)
