@@ -290,6 +290,79 @@ def extra_soup(torch, abi, stream, flush, steps=30):
             "frame_stats": {k: st[k] for k in ("front", "tested", "inside", "written", "binned_tris", "bin_entries")}}
 
 
+def bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return float(json.load(fh)["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+def extra_many_lights(torch, abi, stream, flush, steps=30):
+    """configs[4]: the 1M-triangle displaced sphere with smooth normals and per-vertex albedo at
+    1920x1080 under 256 lights. The plain per-light shader (deferred exact; fused exact beside it)
+    against the learned shader, which is trained here on 4M samples the exact shader labels."""
+    from rasteriser_gb300 import scenes as S
+    sc = S.config_many_lights()
+    fr = frame_inputs(sc, 1)
+    _, cam, nm, lights = fr[0]
+    W, H = sc.width, sc.height
+    r = abi.Renderer(0)
+    r.set_stream(stream.cuda_stream)
+    out = {"workload": "displaced_sphere_1M_1080p_256_lights", "lights": int(lights.shape[0])}
+    try:
+        r.upload_scene_mesh(sc)
+        r.set_lights(lights)
+        t0 = time.perf_counter()
+        out["training"] = r.mlp_train(samples=4 << 20, epochs=24, seed=3)
+        out["training"]["wall_s"] = time.perf_counter() - t0
+        out["training"]["samples"] = 4 << 20
+        frames, modes = {}, {}
+        for name, shader, samples in (("exact_fused", abi.SHADER_EXACT, 2),
+                                      ("exact_deferred", abi.SHADER_EXACT_DEFERRED, 2),
+                                      ("learned", abi.SHADER_LEARNED, 2),
+                                      ("learned_unchecked", abi.SHADER_LEARNED, 0)):
+            r.set_option(abi.OPT_SHADER, shader)
+            r.set_option(abi.OPT_MLP_SAMPLES, samples)
+            fps, st, stage = time_scene_device(torch, abi, r, stream, fr, steps, 3, flush)
+            shade_ms = stage["resolve"] if shader == abi.SHADER_EXACT else stage["shade"]
+            m = {"frames_per_s": fps, "shade_ms": shade_ms, "stage_ms": stage}
+            if shader == abi.SHADER_LEARNED:
+                m["checks"] = r.shade_stats()
+                m["check_samples_per_tile"] = samples
+            f, _, ids = r.draw(cam, nm, W, H, abi.CLEAR, want_ids=True)
+            frames[name] = (f, ids)
+            modes[name] = m
+        r.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+        ref, ids = frames["exact_fused"]
+        cov = ids != abi.NO_TRIANGLE
+        covered = int(cov.sum())
+        peak, peak_kind = bf16_peak()
+        for name, m in modes.items():
+            f, fid = frames[name]
+            d = np.abs(f.astype(np.int16) - ref.astype(np.int16))
+            m["shade_px_per_s"] = covered / (m["shade_ms"] * 1e-3)
+            m["err_vs_exact"] = {"mean": float(d[:, cov].mean()), "max": int(d.max()),
+                                 "coverage_identical": bool(np.array_equal(fid, ids))}
+            if name.startswith("learned"):
+                ck = m["checks"]
+                m["fallback_tile_fraction"] = ck["fallback_tiles"] / max(ck["tiles"], 1)
+                # algorithmic tensor work: 2 * (103*64 + 64*64 + 64*3) FLOP per shaded pixel
+                alg = covered * 2.0 * (103 * 64 + 64 * 64 + 64 * 3)
+                executed = ck["tiles"] * 128 * 2.0 * (112 * 64 + 64 * 64 + 64 * 16)
+                tflops = alg / (m["shade_ms"] * 1e-3) / 1e12
+                m["tensor"] = {"algorithmic_flop": alg, "executed_flop": executed, "achieved_tflops": tflops,
+                               "peak_tflops": peak, "frac": tflops / peak, "peak_source": peak_kind}
+        plain = modes["exact_deferred"]["shade_ms"]
+        out["covered_px"] = covered
+        out["modes"] = modes
+        out["speedup_learned_vs_plain"] = plain / modes["learned"]["shade_ms"]
+        out["speedup_learned_unchecked_vs_plain"] = plain / modes["learned_unchecked"]["shade_ms"]
+    finally:
+        r.close()
+    return out
+
+
 def batch_workload(seed=3, n_frames=256, n_soups=16):
     """configs[3]: icospheres L2-L7 and seeded soups of 1k-500k triangles (log-uniform sizes); each
     frame picks a mesh uniformly, a resolution from {256x256, 640x480, 1280x720, 1920x1080}, random
@@ -530,7 +603,8 @@ def run_ours(args):
         "fragments_per_s": stats["inside"] * value,
     }
     if not args.no_extras and world == 1 and args.workload == "displaced_sphere":
-        line["extras"] = {"soup": extra_soup(torch, abi, stream, flush), "batch": extra_batch(torch, abi, stream)}
+        line["extras"] = {"soup": extra_soup(torch, abi, stream, flush), "batch": extra_batch(torch, abi, stream),
+                          "many_lights": extra_many_lights(torch, abi, stream, flush)}
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
