@@ -87,8 +87,6 @@ constexpr int kShadeBlock = 1024;
 inline int64_t kShadeIndexWords(int64_t blocks) { return 4 + 8 * blocks; }
 // counters word counting the resolve blocks that finished (deferred shading)
 constexpr int kResolveTicket = 5;
-// counters word handing out the learned shader's tiles
-constexpr int kShadeTicket = 6;
 // shade_stats: [0] tiles shaded by the MLP, [1] tiles sent to the exact shader, [2] fragments
 // checked, [3] largest checked error (float bits of the channel error in 1/255 units).
 constexpr int kShadeStats = 4;

@@ -351,8 +351,7 @@ struct MlpMisc {
     unsigned long long mbar;                     // MMA completion
     unsigned long long mbar_w;                   // the weights' bulk copy
     uint32_t tmem;
-    uint32_t tile;                               // the next tile, handed out by thread 0
-    uint32_t pad[2];
+    uint32_t pad[3];
     CheckBatch check;
 };
 constexpr uint32_t kMlpSmem = kSmMisc + ((sizeof(MlpMisc) + 127) / 128) * 128;
@@ -473,24 +472,26 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         bulk_copy_g2s(smem_addr(sm + kSmW), a.mlp, sizeof(MlpImage), mbar_w);
     }
     if (warp == 0) tmem_alloc(smem_addr(&M.tmem), kTmemCols);
+    const int n_samples = a.eval_out ? 0 : min(a.samples, (int)kMaxSamples);
     // the records and the tile list are the previous kernel's output
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
     const uint32_t n_tiles = a.index[1];
-    const int n_samples = a.eval_out ? 0 : min(a.samples, (int)kMaxSamples);
-    if (row == 0) M.tile = atomicAdd(&a.counters[kShadeTicket], 1u);
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    // this thread's record of the current tile, fetched one tile ahead
-    uint32_t t = M.tile;
+    // Tiles t = blockIdx.x + k * gridDim.x. This thread's record of the current tile is fetched
+    // one tile ahead and the tile list entry two tiles ahead, so neither load waits on the way.
+    const uint32_t stride = gridDim.x;
+    uint32_t t = blockIdx.x;
     uint32_t e = t < n_tiles ? a.index[4 + t] : 0u;
+    uint32_t e_next = t + stride < n_tiles ? a.index[4 + t + stride] : 0u;
     uint32_t count = t < n_tiles ? tile_count(e) : 0u;
     float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f), g1 = g0;
     if ((uint32_t)row < count) {
         g0 = a.gbuf[2 * ((size_t)tile_first(e) + row)];
         g1 = a.gbuf[2 * ((size_t)tile_first(e) + row) + 1];
     }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
     bool ok = __syncthreads_and(mbar_wait(mbar_w, 0));
     const bool weights_pending = !ok;
     const uint32_t tmem = M.tmem;
@@ -504,7 +505,14 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
     int nb = 0;  // tiles in the check batch
 
     while (ok && t < n_tiles) {
-        if (row == 0) M.tile = atomicAdd(&a.counters[kShadeTicket], 1u);  // read after the next barrier
+        const uint32_t t_next = t + stride;
+        const uint32_t count_next = t_next < n_tiles ? tile_count(e_next) : 0u;
+        float4 g0n = make_float4(0.f, 0.f, 0.f, 0.f), g1n = g0n;
+        if ((uint32_t)row < count_next) {
+            g0n = a.gbuf[2 * ((size_t)tile_first(e_next) + row)];
+            g1n = a.gbuf[2 * ((size_t)tile_first(e_next) + row) + 1];
+        }
+        const uint32_t e_next2 = t_next + stride < n_tiles ? a.index[4 + t_next + stride] : 0u;
         const bool valid = (uint32_t)row < count;
         const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
         const uint32_t pix = __float_as_uint(g1.z);
@@ -515,16 +523,6 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         // layer 1: D = X (128 x 112) * W1^T
         if (row == 0)
             issue_layer(tmem + kColD, tmem + kColA, sW1, kMlpHid * 16, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-
-        // while it runs: the next tile's records are fetched
-        const uint32_t t_next = M.tile;
-        const uint32_t e_next = t_next < n_tiles ? a.index[4 + t_next] : 0u;
-        const uint32_t count_next = t_next < n_tiles ? tile_count(e_next) : 0u;
-        float4 g0n = make_float4(0.f, 0.f, 0.f, 0.f), g1n = g0n;
-        if ((uint32_t)row < count_next) {
-            g0n = a.gbuf[2 * ((size_t)tile_first(e_next) + row)];
-            g1n = a.gbuf[2 * ((size_t)tile_first(e_next) + row) + 1];
-        }
 
         ok = __syncthreads_and(mbar_wait(mbar, phase));
         phase ^= 1u;
@@ -591,10 +589,12 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         }
         t = t_next;
         e = e_next;
+        e_next = e_next2;
         count = count_next;
         g0 = g0n;
         g1 = g1n;
     }
+
     if (ok && nb > 0) {
         run_checks(a, M.check, nb, n_samples, n_fallback, max_err);
         n_checked += (unsigned long long)nb * n_samples;
