@@ -312,6 +312,75 @@ rast_status rast_draw_noalloc(const float* d_pos, int64_t nv, const float* d_nrm
                               const float normal[16], uint32_t width, uint32_t height, uint32_t flags,
                               uint8_t* d_rgb_planar, float* d_depth, uint32_t* d_tri_id, void* stream);
 
+/* ------------------------------------------------------------------------------------------ */
+/* inputs from files (fileloader.cpp, material.h) and outputs (renderer.cpp)                    */
+/* ------------------------------------------------------------------------------------------ */
+
+/* A Wavefront OBJ model loaded as the reference's load_obj loads it (fileloader.cpp:81-118, with
+ * the vendored tinyobjloader): vertex positions, normals and uvs in file order, the triangles of
+ * every kept shape in order (polygons as fans), in the Triangle layout of rast_upload_mesh, and the
+ * MTL materials in file order. Missing uv / normal indices are -1; a face without `usemtl` gets
+ * material -1 (rast_upload_mesh refuses both normals and materials < 0, where the reference's
+ * draw_frame reads out of bounds). textures[i] is mats_dir + map_Kd of material i, or "". */
+typedef struct rast_obj rast_obj;
+typedef struct rast_obj_data {
+    const float* pos;     int64_t nv;
+    const float* nrm;     int64_t nn;
+    const float* uv;      int64_t nuv;
+    const int32_t* tris;  int64_t ntri;
+    const float* kd;      int32_t nmat;
+    const char* const* textures;
+} rast_obj_data;
+
+/* Loads obj_path; MTL files named by `mtllib` are read from mats_dir + name (the reference's
+ * --mats-dir, concatenated as given). Errors: rast_last_error(NULL). */
+rast_status rast_obj_load(const char* obj_path, const char* mats_dir, rast_obj** out);
+void rast_obj_free(rast_obj* obj);
+/* Pointers into the loaded model, valid until rast_obj_free. */
+rast_status rast_obj_view(const rast_obj* obj, rast_obj_data* out);
+
+/* The lights CSV (fileloader.cpp:121-132): one light per non-blank line, 7 comma-separated numbers
+ * (direction xyz, intensity, colour rgb) as rast_set_lights takes them once transformed
+ * (rast_transform_lights). Writes min(n, cap) records; *n receives the count. */
+rast_status rast_lights_load(const char* path, float* lights7, int32_t cap, int32_t* n);
+
+/* A raw image for a texture: binary or ASCII PGM / PPM (maxval up to 65535) or PFM, as floats in
+ * CImg's planar layout (x + y*w + c*w*h, rows top first), values as stored (0..maxval). With
+ * out = NULL only w, h and channels (1 or 3) are reported; otherwise cap >= w*h*channels floats. */
+rast_status rast_image_load(const char* path, uint32_t* w, uint32_t* h, uint32_t* channels, float* out,
+                            size_t cap);
+
+/* renderer.cpp:93 `depth_buffer.normalize(0,255)` for a device depth buffer: the smallest and
+ * largest depth m, M of the w*h values, each value v written as (uint8)((v - m) / (M - m) * 255)
+ * (0 everywhere when m == M), on the context's stream (asynchronous). */
+rast_status rast_depth_to_u8(rast_ctx* ctx, const float* d_depth, uint32_t width, uint32_t height,
+                             uint8_t* d_out);
+
+/* The same for host buffers (synchronous). */
+rast_status rast_depth_to_u8_host(rast_ctx* ctx, const float* depth, uint32_t width, uint32_t height,
+                                  uint8_t* out);
+
+/* The spin loop of renderer.cpp:94-125 without a window: `frames` frames drawn one after another
+ * on the device into buffers the context owns (each cleared first, as the loop fills the frame
+ * with 0 and the depth with 1), the model's ry advancing by `step` radians per frame (the
+ * reference advances it by each frame's wall-clock time). The lights are the world-space records
+ * of the lights CSV; they are transformed with the frames' view matrix (it does not depend on the
+ * rotation). The mesh is the context's. last_rgb / last_depth (nullable, host, planar RGB8 and
+ * floats) receive the last frame; *seconds (nullable) the wall-clock time of the loop, frames
+ * enqueued without waiting in between. */
+typedef struct rast_spin_desc {
+    uint32_t width, height;   /* 1..32768 */
+    uint32_t flags;           /* RAST_WIND_CLOCKWISE */
+    int32_t frames;           /* >= 1 */
+    float scale, disp[3], angles[3];
+    float step;               /* ry increment per frame, radians */
+    float fovy_deg, z_near, z_far;
+    const float* lights7;     /* nl records: direction xyz, intensity, colour rgb */
+    int32_t nl;
+} rast_spin_desc;
+rast_status rast_spin(rast_ctx* ctx, const rast_spin_desc* desc, uint8_t* last_rgb, float* last_depth,
+                      double* seconds);
+
 #ifdef __cplusplus
 }
 #endif

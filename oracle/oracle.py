@@ -128,6 +128,16 @@ class Reference:
         self.lib.ref_signed_area_2d.argtypes = [C.POINTER(C.c_float)]
         self.lib.ref_shade.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                        C.c_int, C.POINTER(C.c_uint32)]
+        self.lib.ref_draw_frame_tex.restype = C.c_int
+        self.lib.ref_draw_frame_tex.argtypes = self.lib.ref_draw_frame.argtypes[:12] + [C.POINTER(C.c_char_p)] + \
+            self.lib.ref_draw_frame.argtypes[12:]
+        self.lib.ref_load_obj.restype = C.c_int
+        self.lib.ref_load_obj.argtypes = [C.c_char_p, C.c_char_p]
+        self.lib.ref_obj_counts.argtypes = [C.POINTER(C.c_int64)]
+        self.lib.ref_obj_copy.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                          C.POINTER(C.c_int32), C.POINTER(C.c_float)]
+        self.lib.ref_load_lights.restype = C.c_int
+        self.lib.ref_load_lights.argtypes = [C.c_char_p, C.POINTER(C.c_float), C.c_int]
 
     def matrices(self, scene):
         """dict of model, view, modelview, camera, normal, camera45 (each (16,) float32, column major)."""
@@ -138,8 +148,25 @@ class Reference:
         names = ["model", "view", "modelview", "camera", "normal", "camera45"]
         return {k: out[16 * i:16 * (i + 1)].copy() for i, k in enumerate(names)}
 
-    def draw(self, scene, frame=None, depth=None):
-        """Returns (frame (3,H,W) uint8, depth (H,W) float32, trans_dirs (nl,3))."""
+    def load_obj(self, path, mats_dir=""):
+        """The reference's load_obj: dict of pos, nrm, uv, tris, kd (Material::sample at uv 0)."""
+        if self.lib.ref_load_obj(os.fsencode(path), os.fsencode(mats_dir)) != 0:
+            raise RuntimeError("reference load_obj raised")
+        n = np.zeros(5, np.int64)
+        self.lib.ref_obj_counts(_p(n, C.c_int64))
+        pos, nrm, uv = np.zeros((n[0], 3), np.float32), np.zeros((n[1], 3), np.float32), np.zeros((n[2], 2), np.float32)
+        tris, kd = np.zeros((n[3], 10), np.int32), np.zeros((n[4], 3), np.float32)
+        self.lib.ref_obj_copy(_p(pos), _p(nrm), _p(uv), _p(tris, C.c_int32), _p(kd))
+        return {"pos": pos, "nrm": nrm, "uv": uv, "tris": tris, "kd": kd}
+
+    def load_lights(self, path, cap=4096):
+        out = np.zeros((cap, 7), np.float32)
+        n = self.lib.ref_load_lights(os.fsencode(path), _p(out), cap)
+        return out[:min(n, cap)].copy()
+
+    def draw(self, scene, frame=None, depth=None, textures=None):
+        """Returns (frame (3,H,W) uint8, depth (H,W) float32, trans_dirs (nl,3)). textures: per
+        material an image path the reference's Material loads, or None."""
         W, H = scene.width, scene.height
         self.lib.ref_set_projection(scene.fovy_deg, scene.z_near, scene.z_far)
         frame = np.zeros((3, H, W), np.uint8) if frame is None else np.ascontiguousarray(frame, np.uint8).copy()
@@ -148,10 +175,13 @@ class Reference:
                                       _f32(scene.kd), _f32(scene.lights))
         td = np.zeros((li.shape[0], 3), np.float32)
         disp, ang = _f32(scene.disp), _f32(scene.angles)
-        rc = self.lib.ref_draw_frame(_p(pos), pos.shape[0], _p(tris, C.c_int32), tris.shape[0], _p(nrm),
-                                     nrm.shape[0], _p(uv), uv.shape[0], _p(li), li.shape[0], _p(kd), kd.shape[0],
-                                     W, H, int(scene.wind_clockwise), scene.scale, _p(disp), _p(ang),
-                                     _p(frame, C.c_uint8), _p(depth), _p(td))
+        tex = None
+        if textures is not None:
+            tex = (C.c_char_p * len(textures))(*[os.fsencode(t) if t else None for t in textures])
+        rc = self.lib.ref_draw_frame_tex(_p(pos), pos.shape[0], _p(tris, C.c_int32), tris.shape[0], _p(nrm),
+                                         nrm.shape[0], _p(uv), uv.shape[0], _p(li), li.shape[0], _p(kd),
+                                         kd.shape[0], tex, W, H, int(scene.wind_clockwise), scene.scale,
+                                         _p(disp), _p(ang), _p(frame, C.c_uint8), _p(depth), _p(td))
         if rc != 0:
             raise RuntimeError("reference draw_frame raised")
         return frame, depth, td

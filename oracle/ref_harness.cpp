@@ -1,6 +1,7 @@
 // Oracle test infrastructure. A C-ABI harness around canmom/rasteriser's own, unmodified
-// geometry.cpp, drawing.cpp, shading.cpp, material.cpp and arguments.cpp, compiled from the
-// reference tree by oracle/Makefile into oracle/_ref/libref.so. Tests and the golden-fixture script
+// geometry.cpp, drawing.cpp, shading.cpp, material.cpp, fileloader.cpp and arguments.cpp (with the
+// vendored CImg and tinyobjloader), compiled from the reference tree by oracle/Makefile into
+// oracle/_ref/libref.so. Tests and the golden-fixture script
 // load it with ctypes; nothing in the product links it.
 //
 // The reference hard-codes its projection to 45 deg / 0.1 / 6 (geometry.cpp:27-33). geometry.cpp is
@@ -19,6 +20,7 @@
 #include "arguments.h"
 #include "drawing.h"
 #include "face.h"
+#include "fileloader.h"
 #include "geometry.h"
 #include "light.h"
 #include "material.h"
@@ -134,10 +136,25 @@ void ref_shade(const float* normal3, const float* albedo3, const float* lights7,
 //   kd: nmat*3 (constant-albedo materials). frame: planar RGB8 (W*H*3), depth: W*H floats; both
 //   are read and written. trans_dirs (nullable): the lights' trans_dir after the call, nl*3.
 // Returns 0 on success, 1 on a C++ exception.
+// ref_draw_frame with textured materials: textures[i] (nullable, or "") is the image file material
+// i loads through the reference's Material (CImg, normalised to 0..1, material.h:20-22).
+int ref_draw_frame_tex(const float* verts, int64_t nv, const int32_t* tris, int64_t ntri, const float* normals,
+                       int64_t nn, const float* uvs, int64_t nuv, const float* lights7, int nl, const float* kd,
+                       int nmat, const char* const* textures, uint32_t w, uint32_t h, int cw, float scale,
+                       const float* disp, const float* angles, uint8_t* frame, float* depth, float* trans_dirs);
+
 int ref_draw_frame(const float* verts, int64_t nv, const int32_t* tris, int64_t ntri, const float* normals,
                    int64_t nn, const float* uvs, int64_t nuv, const float* lights7, int nl, const float* kd,
                    int nmat, uint32_t w, uint32_t h, int cw, float scale, const float* disp, const float* angles,
                    uint8_t* frame, float* depth, float* trans_dirs) {
+    return ref_draw_frame_tex(verts, nv, tris, ntri, normals, nn, uvs, nuv, lights7, nl, kd, nmat, nullptr, w, h, cw,
+                              scale, disp, angles, frame, depth, trans_dirs);
+}
+
+int ref_draw_frame_tex(const float* verts, int64_t nv, const int32_t* tris, int64_t ntri, const float* normals,
+                       int64_t nn, const float* uvs, int64_t nuv, const float* lights7, int nl, const float* kd,
+                       int nmat, const char* const* textures, uint32_t w, uint32_t h, int cw, float scale,
+                       const float* disp, const float* angles, uint8_t* frame, float* depth, float* trans_dirs) {
     try {
         Args args = make_args(w, h, cw, scale, disp, angles);
         std::vector<glm::vec3> mv((size_t)nv), mn((size_t)nn);
@@ -152,7 +169,11 @@ int ref_draw_frame(const float* verts, int64_t nv, const int32_t* tris, int64_t 
             faces.push_back(Triangle({t[0], t[1], t[2]}, {t[3], t[4], t[5]}, {t[6], t[7], t[8]}, t[9]));
         }
         std::vector<Material> mats;
-        for (int i = 0; i < nmat; ++i) mats.push_back(Material(glm::vec3(kd[3 * i], kd[3 * i + 1], kd[3 * i + 2])));
+        for (int i = 0; i < nmat; ++i) {
+            const glm::vec3 dc(kd[3 * i], kd[3 * i + 1], kd[3 * i + 2]);
+            if (textures && textures[i] && textures[i][0]) mats.push_back(Material(dc, textures[i]));
+            else mats.push_back(Material(dc));
+        }
         std::vector<Light> lights;
         for (int i = 0; i < nl; ++i) {
             const float* L = lights7 + 7 * i;
@@ -175,6 +196,82 @@ int ref_draw_frame(const float* verts, int64_t nv, const int32_t* tris, int64_t 
     } catch (...) {
         return 1;
     }
+}
+
+// The reference's load_obj (fileloader.cpp:81-118) on obj_path with --mats-dir mats_dir. The
+// arrays are kept until the next call: ref_obj_counts gives nv, nn, nuv, ntri, nmat and ref_obj_copy
+// copies them (positions, normals, uvs, Triangle records, and each material's Material::sample at
+// uv (0, 0): its Kd without a texture). Returns 0, or 1 on a C++ exception.
+namespace {
+std::vector<glm::vec3> g_v, g_n;
+std::vector<glm::vec2> g_uv;
+std::vector<Triangle> g_tris;
+std::vector<Material> g_mats;
+}  // namespace
+
+int ref_load_obj(const char* obj_path, const char* mats_dir) {
+    try {
+        std::string o(obj_path), d(mats_dir ? mats_dir : "");
+        char a0[] = "oracle", a1[] = "-l", a2[] = "unused.csv", a3[] = "-o", a5[] = "--mats-dir";
+        std::vector<char> a4(o.begin(), o.end()), a6(d.begin(), d.end());
+        a4.push_back('\0');
+        a6.push_back('\0');
+        char* argv[] = {a0, a1, a2, a3, a4.data(), a5, a6.data(), nullptr};
+        Args args(7, argv);
+        g_v.clear(); g_n.clear(); g_uv.clear(); g_tris.clear(); g_mats.clear();
+        load_obj(args, g_v, g_tris, g_n, g_uv, g_mats);
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+void ref_obj_counts(int64_t* out5) {
+    out5[0] = (int64_t)g_v.size();
+    out5[1] = (int64_t)g_n.size();
+    out5[2] = (int64_t)g_uv.size();
+    out5[3] = (int64_t)g_tris.size();
+    out5[4] = (int64_t)g_mats.size();
+}
+
+void ref_obj_copy(float* pos, float* nrm, float* uv, int32_t* tris, float* kd) {
+    for (size_t i = 0; i < g_v.size(); ++i)
+        for (int k = 0; k < 3; ++k) pos[3 * i + k] = g_v[i][k];
+    for (size_t i = 0; i < g_n.size(); ++i)
+        for (int k = 0; k < 3; ++k) nrm[3 * i + k] = g_n[i][k];
+    for (size_t i = 0; i < g_uv.size(); ++i)
+        for (int k = 0; k < 2; ++k) uv[2 * i + k] = g_uv[i][k];
+    for (size_t i = 0; i < g_tris.size(); ++i) {
+        const Triangle& t = g_tris[i];
+        for (int k = 0; k < 3; ++k) {
+            tris[10 * i + k] = t.vertices[k];
+            tris[10 * i + 3 + k] = t.normals[k];
+            tris[10 * i + 6 + k] = t.uvs[k];
+        }
+        tris[10 * i + 9] = t.material;
+    }
+    for (size_t i = 0; i < g_mats.size(); ++i) {
+        const glm::vec3 c = g_mats[i].sample(glm::vec2(0.f, 0.f));
+        for (int k = 0; k < 3; ++k) kd[3 * i + k] = c[k];
+    }
+}
+
+// The reference's load_lights (fileloader.cpp:121-132): up to cap records of 7 floats; returns the
+// number it read.
+int ref_load_lights(const char* path, float* out7, int cap) {
+    std::vector<Light> lights;
+    load_lights(path, lights);
+    int n = 0;
+    for (const Light& L : lights) {
+        if (n < cap) {
+            float* o = out7 + 7 * n;
+            o[0] = L.direction.x; o[1] = L.direction.y; o[2] = L.direction.z;
+            o[3] = L.intensity;
+            o[4] = L.colour.r; o[5] = L.colour.g; o[6] = L.colour.b;
+        }
+        ++n;
+    }
+    return n;
 }
 
 }  // extern "C"

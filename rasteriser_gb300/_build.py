@@ -41,10 +41,12 @@ def _units(checked=False):
     return [
         ("rast_kernels.cu", kern + inc),
         ("rast_shade.cu", kern + inc),
+        ("rast_view.cu", kern + inc),
         ("rast_noalloc.cu", kern + inc),
         ("rast_api.cpp", host + inc),
         ("rast_batch.cpp", host + inc),
         ("rast_mlp.cpp", host + inc),
+        ("rast_io.cpp", host + inc),
         ("rast_host_math.cpp", host + inc),
     ]
 
@@ -94,7 +96,19 @@ def build(verbose=False, force=False, checked=False):
             print(lg)
     if force or jobs or _stale(lib, objs):
         run([nvcc, "-shared", "-o", lib] + ARCH + objs + ["-Xcompiler", "-fPIC"])
+    if not checked:
+        cli_src = os.path.join(PKG, "cpp", "rast_render.cpp")
+        cli = cli_path()
+        if force or _stale(cli, [cli_src, lib, os.path.join(ROOT, "include", "rast.h")]):
+            cxx = shutil.which("g++") or "c++"
+            run([cxx, "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), cli_src, "-o", cli,
+                 "-L" + LIB_DIR, "-lrast", "-Wl,-rpath,$ORIGIN"])
     return lib
+
+
+def cli_path():
+    """The headless renderer rast_render (rasteriser_gb300/cpp/rast_render.cpp)."""
+    return os.path.join(LIB_DIR, "rast_render")
 
 
 if __name__ == "__main__":

@@ -42,6 +42,22 @@ class MlpTrainDesc(C.Structure):
     _fields_ = [("samples", C.c_int64), ("holdout", C.c_int64), ("epochs", C.c_int32), ("ctas", C.c_int32),
                 ("lr", C.c_float), ("seed", C.c_uint64)]
 
+class ObjData(C.Structure):
+    """rast_obj_data of include/rast.h."""
+    _fields_ = [("pos", C.POINTER(C.c_float)), ("nv", C.c_int64), ("nrm", C.POINTER(C.c_float)), ("nn", C.c_int64),
+                ("uv", C.POINTER(C.c_float)), ("nuv", C.c_int64), ("tris", C.POINTER(C.c_int32)),
+                ("ntri", C.c_int64), ("kd", C.POINTER(C.c_float)), ("nmat", C.c_int32),
+                ("textures", C.POINTER(C.c_char_p))]
+
+
+class SpinDesc(C.Structure):
+    """rast_spin_desc of include/rast.h."""
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("flags", C.c_uint32), ("frames", C.c_int32),
+                ("scale", C.c_float), ("disp", C.c_float * 3), ("angles", C.c_float * 3), ("step", C.c_float),
+                ("fovy_deg", C.c_float), ("z_near", C.c_float), ("z_far", C.c_float),
+                ("lights7", C.POINTER(C.c_float)), ("nl", C.c_int32)]
+
+
 # Every function include/rast.h declares, with its ctypes signature.
 _F, _I32, _I64, _U32, _P = C.POINTER(C.c_float), C.c_int32, C.c_int64, C.c_uint32, C.c_void_p
 SIGNATURES = {
@@ -78,6 +94,15 @@ SIGNATURES = {
     "rast_mlp_load": (C.c_int, [_P, _P, C.c_size_t]),
     "rast_mlp_eval": (C.c_int, [_P, _F, _F, _I64, _I32, _F]),
     "rast_get_shade_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "rast_obj_load": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(_P)]),
+    "rast_obj_free": (None, [_P]),
+    "rast_obj_view": (C.c_int, [_P, C.POINTER(ObjData)]),
+    "rast_lights_load": (C.c_int, [C.c_char_p, _F, _I32, C.POINTER(C.c_int32)]),
+    "rast_image_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                  _F, C.c_size_t]),
+    "rast_depth_to_u8": (C.c_int, [_P, _P, _U32, _U32, _P]),
+    "rast_depth_to_u8_host": (C.c_int, [_P, _F, _U32, _U32, C.POINTER(C.c_uint8)]),
+    "rast_spin": (C.c_int, [_P, C.POINTER(SpinDesc), C.POINTER(C.c_uint8), _F, C.POINTER(C.c_double)]),
 }
 
 _lib = None
@@ -141,6 +166,65 @@ def transform_lights(view, lights7):
     st = lib.rast_transform_lights(_fp(_f32(view)), _fp(li), li.shape[0], _fp(out))
     if st != RAST_OK:
         raise RastError(st, "rast_transform_lights")
+    return out
+
+
+def _io_error(st, what):
+    lib = load()
+    return RastError(st, f"{what}: {lib.rast_last_error(None).decode()}")
+
+
+def obj_load(path, mats_dir=""):
+    """A Wavefront OBJ as the reference's load_obj reads it: dict of pos (nv,3), nrm (nn,3),
+    uv (nuv,2), tris (ntri,10) int32, kd (nmat,3) and textures (list of str)."""
+    lib = load()
+    h = _P()
+    st = lib.rast_obj_load(os.fsencode(path), os.fsencode(mats_dir), C.byref(h))
+    if st != RAST_OK:
+        raise _io_error(st, "rast_obj_load")
+    try:
+        d = ObjData()
+        lib.rast_obj_view(h, C.byref(d))
+
+        def arr(ptr, n, cols, dtype):
+            if n == 0:
+                return np.zeros((0, cols), dtype)
+            return np.ctypeslib.as_array(ptr, shape=(n * cols,)).reshape(n, cols).astype(dtype, copy=True)
+
+        return {"pos": arr(d.pos, d.nv, 3, np.float32), "nrm": arr(d.nrm, d.nn, 3, np.float32),
+                "uv": arr(d.uv, d.nuv, 2, np.float32), "tris": arr(d.tris, d.ntri, 10, np.int32),
+                "kd": arr(d.kd, d.nmat, 3, np.float32),
+                "textures": [d.textures[i].decode() for i in range(d.nmat)]}
+    finally:
+        lib.rast_obj_free(h)
+
+
+def lights_load(path):
+    """The lights CSV as (n, 7) float32 records."""
+    lib = load()
+    n = C.c_int32()
+    st = lib.rast_lights_load(os.fsencode(path), None, 0, C.byref(n))
+    if st != RAST_OK:
+        raise _io_error(st, "rast_lights_load")
+    out = np.zeros((n.value, 7), np.float32)
+    if n.value:
+        st = lib.rast_lights_load(os.fsencode(path), _fp(out), n.value, C.byref(n))
+        if st != RAST_OK:
+            raise _io_error(st, "rast_lights_load")
+    return out
+
+
+def image_load(path):
+    """A PGM / PPM / PFM image as float32 (channels, height, width), values as stored."""
+    lib = load()
+    w, h, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    st = lib.rast_image_load(os.fsencode(path), C.byref(w), C.byref(h), C.byref(c), None, 0)
+    if st != RAST_OK:
+        raise _io_error(st, "rast_image_load")
+    out = np.zeros((c.value, h.value, w.value), np.float32)
+    st = lib.rast_image_load(os.fsencode(path), C.byref(w), C.byref(h), C.byref(c), _fp(out), out.size)
+    if st != RAST_OK:
+        raise _io_error(st, "rast_image_load")
     return out
 
 
@@ -332,6 +416,41 @@ class Renderer:
         self._check(self.lib.rast_mlp_eval(self.h, _fp(nv), _fp(al), nv.shape[0], 1 if exact else 0, _fp(out)),
                     "rast_mlp_eval")
         return out
+
+    def depth_to_u8(self, d_depth, width, height, d_out):
+        """renderer.cpp's depth view of a device depth buffer into device bytes (asynchronous)."""
+        self._check(self.lib.rast_depth_to_u8(self.h, _P(d_depth), width, height, _P(d_out)), "rast_depth_to_u8")
+
+    def depth_view(self, depth):
+        """The depth view of a host depth buffer (H, W) float32 -> (H, W) uint8."""
+        d = _f32(depth)
+        out = np.zeros(d.shape, np.uint8)
+        self._check(self.lib.rast_depth_to_u8_host(self.h, _fp(d), d.shape[1], d.shape[0],
+                                                   out.ctypes.data_as(C.POINTER(C.c_uint8))), "rast_depth_to_u8_host")
+        return out
+
+    def spin(self, scene, frames, step=1.0 / 60.0):
+        """The headless spin loop over the scene's mesh (uploaded if it changed): frames frames with
+        ry advancing by step. Returns (last frame (3,H,W), last depth (H,W), seconds)."""
+        self.upload_scene_mesh(scene)
+        li = _f32(scene.lights).reshape(-1, 7)
+        d = SpinDesc()
+        d.width, d.height = scene.width, scene.height
+        d.flags = WIND_CLOCKWISE if scene.wind_clockwise else 0
+        d.frames = frames
+        d.scale = scene.scale
+        d.disp[:] = [float(v) for v in scene.disp]
+        d.angles[:] = [float(v) for v in scene.angles]
+        d.step = step
+        d.fovy_deg, d.z_near, d.z_far = scene.fovy_deg, scene.z_near, scene.z_far
+        d.lights7 = _fp(li)
+        d.nl = li.shape[0]
+        frame = np.zeros((3, scene.height, scene.width), np.uint8)
+        depth = np.zeros((scene.height, scene.width), np.float32)
+        sec = C.c_double()
+        self._check(self.lib.rast_spin(self.h, C.byref(d), frame.ctypes.data_as(C.POINTER(C.c_uint8)), _fp(depth),
+                                       C.byref(sec)), "rast_spin")
+        return frame, depth, sec.value
 
     def shade_stats(self):
         out = (C.c_uint64 * 4)()

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -212,7 +213,7 @@ void rast_destroy(rast_ctx* c) {
     cudaStreamSynchronize(c->stream);
     for (DevBuf* b : {&c->pos, &c->tris10, &c->tri_v, &c->tri_nm, &c->nrm, &c->kd, &c->lights, &c->rv, &c->keys,
                       &c->large, &c->counters, &c->tile_offset, &c->entries, &c->stats, &c->d_rgb, &c->d_depth,
-                      &c->d_ids, &c->vcol, &c->gbuf, &c->gbuf_count, &c->shade_index, &c->shade_stats,
+                      &c->d_ids, &c->vcol, &c->gbuf, &c->gbuf_count, &c->shade_index, &c->shade_stats, &c->view_mm,
                       &c->mlp_image})
         b->release();
     if (c->ev_made)
@@ -459,6 +460,75 @@ rast_status rast_get_stage_times(rast_ctx* c, float out_ms[9]) {
     RAST_CUDA(c, cudaEventSynchronize(c->ev[8]));
     for (int i = 0; i < 8; ++i) RAST_CUDA(c, cudaEventElapsedTime(&out_ms[i], c->ev[i], c->ev[i + 1]));
     RAST_CUDA(c, cudaEventElapsedTime(&out_ms[8], c->ev[0], c->ev[8]));
+    return RAST_OK;
+}
+
+rast_status rast_depth_to_u8(rast_ctx* c, const float* d_depth, uint32_t w, uint32_t h, uint8_t* d_out) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    if (!d_depth || !d_out || w == 0 || h == 0 || w > kMaxDim || h > kMaxDim)
+        return fail(c, RAST_ERR_INVALID_ARG, "bad depth view arguments");
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, c->view_mm.reserve(2 * sizeof(uint32_t)));
+    if (rast::launch_depth_view(d_depth, (int64_t)w * h, c->view_mm.as<uint32_t>(), d_out, c->n_sm, c->stream) < 0)
+        return cuda_fail(c, cudaGetLastError(), "depth view");
+    return RAST_OK;
+}
+
+rast_status rast_depth_to_u8_host(rast_ctx* c, const float* depth, uint32_t w, uint32_t h, uint8_t* out) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    if (!depth || !out || w == 0 || h == 0 || w > kMaxDim || h > kMaxDim)
+        return fail(c, RAST_ERR_INVALID_ARG, "bad depth view arguments");
+    DeviceGuard g(c->device);
+    const size_t npx = (size_t)w * h;
+    RAST_CUDA(c, c->d_depth.reserve(sizeof(float) * npx));
+    RAST_CUDA(c, c->d_rgb.reserve(3 * npx));
+    RAST_CUDA(c, cudaMemcpyAsync(c->d_depth.ptr, depth, sizeof(float) * npx, cudaMemcpyHostToDevice, c->stream));
+    const rast_status st = rast_depth_to_u8(c, c->d_depth.as<float>(), w, h, c->d_rgb.as<uint8_t>());
+    if (st != RAST_OK) return st;
+    RAST_CUDA(c, cudaMemcpyAsync(out, c->d_rgb.ptr, npx, cudaMemcpyDeviceToHost, c->stream));
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    return RAST_OK;
+}
+
+rast_status rast_spin(rast_ctx* c, const rast_spin_desc* d, uint8_t* last_rgb, float* last_depth, double* seconds) {
+    if (!c || !d) return RAST_ERR_INVALID_ARG;
+    if (d->width == 0 || d->height == 0 || d->width > kMaxDim || d->height > kMaxDim || d->frames < 1 ||
+        d->nl < 0 || d->nl > kMaxLights || (d->nl && !d->lights7))
+        return fail(c, RAST_ERR_INVALID_ARG, "bad spin arguments");
+    DeviceGuard g(c->device);
+    const uint32_t w = d->width, h = d->height;
+    const size_t npx = (size_t)w * h;
+    float model[16], view[16], mv[16], cam[16], nm[16];
+    float angles[3] = {d->angles[0], d->angles[1], d->angles[2]};
+    rast_status st = rast_frame_matrices(w, h, d->scale, d->disp, angles, d->fovy_deg, d->z_near, d->z_far, model,
+                                         view, mv, cam, nm);
+    if (st != RAST_OK) return fail(c, st, "frame matrices");
+    std::vector<float> lt(7 * (size_t)std::max(d->nl, 1));
+    if (d->nl) {
+        st = rast_transform_lights(view, d->lights7, d->nl, lt.data());
+        if (st != RAST_OK) return fail(c, st, "lights");
+    }
+    st = rast_set_lights(c, lt.data(), d->nl);
+    if (st != RAST_OK) return st;
+    RAST_CUDA(c, c->d_rgb.reserve(3 * npx));
+    RAST_CUDA(c, c->d_depth.reserve(sizeof(float) * npx));
+    const uint32_t flags = (d->flags & RAST_WIND_CLOCKWISE) | RAST_CLEAR;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int32_t k = 0; k < d->frames; ++k) {
+        angles[1] = d->angles[1] + (float)k * d->step;
+        st = rast_frame_matrices(w, h, d->scale, d->disp, angles, d->fovy_deg, d->z_near, d->z_far, model, view, mv,
+                                 cam, nm);
+        if (st != RAST_OK) return fail(c, st, "frame matrices");
+        st = enqueue_draw(c, cam, nm, w, h, flags, c->d_rgb.as<uint8_t>(), c->d_depth.as<float>(), nullptr);
+        if (st != RAST_OK) return st;
+    }
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    st = collect_status(c);
+    if (st != RAST_OK) return st;
+    if (last_rgb) RAST_CUDA(c, cudaMemcpy(last_rgb, c->d_rgb.ptr, 3 * npx, cudaMemcpyDeviceToHost));
+    if (last_depth) RAST_CUDA(c, cudaMemcpy(last_depth, c->d_depth.ptr, sizeof(float) * npx, cudaMemcpyDeviceToHost));
+    if (seconds) *seconds = s;
     return RAST_OK;
 }
 

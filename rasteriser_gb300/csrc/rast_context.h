@@ -89,6 +89,7 @@ struct rast_ctx {
     int32_t mlp_samples = 2;      // RAST_OPT_MLP_SAMPLES
     int32_t mlp_bound_milli = 500;  // RAST_OPT_MLP_BOUND_MILLI
     DevBuf gbuf, gbuf_count, shade_index, shade_stats;
+    DevBuf view_mm;  // rast_depth_to_u8: the depth range
 
     // learned shader state (rast_mlp.cpp)
     DevBuf mlp_image;             // rast::MlpImage

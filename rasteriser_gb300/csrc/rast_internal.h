@@ -111,6 +111,10 @@ struct DrawParams {
     float mlp_bound = 0.5f;     // shader 2: largest checked channel error (1/255 units) a tile may have
 };
 
+// The depth view (rast_view.cu): min / max of n depths into mm[0..1] (order keys), then the bytes.
+// Returns the number of launches, or -1.
+int launch_depth_view(const float* depth, int64_t n, uint32_t* mm, uint8_t* out, int n_sm, cudaStream_t stream);
+
 // The deferred shading pass over the resolve's fragment records (rast_shade.cu): the exact or
 // learned shading kernel over the tiles the resolve listed. Returns the number of launches, or -1.
 int launch_shade(const FrameScratch& s, const DrawParams& p, int64_t blocks, cudaStream_t stream);
