@@ -98,7 +98,7 @@ void* rast_get_stream(const rast_ctx* ctx);
 /* Uploads a mesh in the reference's host layouts (the vectors draw_frame receives):
  *   pos: nv * 3 floats (vector<vec3> model_vertices)
  *   nrm: nn * 3 floats (vector<vec3> model_vertnormals)
- *   uv:  nuv * 2 floats (vector<vec2> vertuvs; may be NULL when nuv == 0)
+ *   uv:  nuv * 2 floats (vector<vec2> vertuvs; may be NULL when nuv == 0; read by textures)
  *   tris: ntri * 10 int32, the Triangle layout of face.h:6-13 (vertices[3], normals[3], uvs[3],
  *         material); vector<Triangle>::data() can be passed as is
  *   kd:  nmat * 3 floats, each material's constant albedo (Material::diffuse_colour,
@@ -116,6 +116,17 @@ rast_status rast_upload_mesh(rast_ctx* ctx, const float* pos, int64_t nv, const 
  * the mesh's vertex count; rgb3 = NULL with nv = 0 returns to the materials' Kd. A new
  * rast_upload_mesh drops it. Synchronous. */
 rast_status rast_upload_vertex_albedo(rast_ctx* ctx, const float* rgb3, int64_t nv);
+
+/* A texture for material `material` of the uploaded mesh (Material(dc, file), material.h:17-22):
+ * texels as CImg loads an image, planar (x + y*w + c*w*h, rows top first, e.g. rast_image_load),
+ * channels 3 or 4 (the first three are sampled). They are normalised as the reference's Material
+ * does (CImg normalize(0, 1) over every channel), and fragments of the material take the texture's
+ * colour at their perspective-correct uv (drawing.cpp:135, Material::sample: bilinear, coordinates
+ * clamped to the image, v flipped) in place of Kd. A uv index < 0 reads uv (0, 0), as in the
+ * reference. texels = NULL removes the texture. Per-vertex albedo, where set, takes precedence.
+ * A new rast_upload_mesh drops the textures. Synchronous. */
+rast_status rast_upload_texture(rast_ctx* ctx, int32_t material, const float* texels, uint32_t width,
+                                uint32_t height, uint32_t channels);
 
 /* Sets the frame's lights: n records of 7 floats (trans_dir xyz, intensity, colour rgb), i.e.
  * already transformed (rast_transform_lights). Shading sums them in this order

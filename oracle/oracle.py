@@ -52,7 +52,20 @@ class _OracleFrame(C.Structure):
                 ("camera", C.POINTER(C.c_float)), ("normal_matrix", C.POINTER(C.c_float)),
                 ("lights", C.POINTER(C.c_float)), ("nl", C.c_int32),
                 ("width", C.c_uint32), ("height", C.c_uint32), ("wind_clockwise", C.c_int32),
-                ("vcol", C.POINTER(C.c_float))]
+                ("vcol", C.POINTER(C.c_float)), ("tex", C.POINTER(C.c_float)), ("tex_off", C.POINTER(C.c_int64)),
+                ("tex_wh", C.POINTER(C.c_int32))]
+
+
+def cimg_normalize01(texels):
+    """material.h:21 `diffuse_texture.normalize(0.f, 1.f)` (CImg, float): m, M over every value;
+    (v - m) / (M - m) * (1 - 0) + 0, or 0 everywhere when m == M."""
+    t = np.ascontiguousarray(texels, np.float32)
+    m, M = np.float32(t.min()), np.float32(t.max())
+    if m == M:
+        return np.zeros_like(t)
+    if m == 0 and M == 1:
+        return t.copy()
+    return (((t - m) / (M - m)) * np.float32(1.0) + np.float32(0.0)).astype(np.float32)
 
 
 class Port:
@@ -71,8 +84,9 @@ class Port:
         self.lib.oracle_shade.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                           C.c_int32, C.POINTER(C.c_uint32)]
 
-    def draw(self, scene, camera, normal_matrix, lights7, frame=None, depth=None, want_ids=True):
-        """Returns (frame (3,H,W) uint8, depth (H,W) float32, ids (H,W) uint32 or None, stats)."""
+    def draw(self, scene, camera, normal_matrix, lights7, frame=None, depth=None, want_ids=True, textures=None):
+        """Returns (frame (3,H,W) uint8, depth (H,W) float32, ids (H,W) uint32 or None, stats).
+        textures: per material a normalised (c>=3, h, w) float32 texture or None."""
         W, H = scene.width, scene.height
         frame = np.zeros((3, H, W), np.uint8) if frame is None else np.ascontiguousarray(frame, np.uint8).copy()
         depth = np.ones((H, W), np.float32) if depth is None else _f32(depth).copy()
@@ -81,10 +95,22 @@ class Port:
                 _f32(camera), _f32(normal_matrix), _f32(lights7)]
         vcol = getattr(scene, "vertex_albedo", None)
         vcol = _f32(vcol) if vcol is not None else None
+        tex = off = wh = None
+        if textures is not None:
+            parts, off, wh, at = [], np.full(len(textures), -1, np.int64), np.zeros(2 * len(textures), np.int32), 0
+            for i, t in enumerate(textures):
+                if t is None:
+                    continue
+                t = _f32(t)
+                off[i], wh[2 * i], wh[2 * i + 1] = at, t.shape[2], t.shape[1]
+                parts.append(t[:3].ravel())
+                at += parts[-1].size
+            tex = np.concatenate(parts) if parts else np.zeros(1, np.float32)
         f = _OracleFrame(_p(keep[0]), scene.pos.shape[0], _p(keep[1], C.c_int32), scene.tris.shape[0],
                          _p(keep[2]), scene.nrm.shape[0], _p(keep[3]), scene.uv.shape[0],
                          _p(keep[4]), scene.kd.shape[0], _p(keep[5]), _p(keep[6]), _p(keep[7]),
-                         keep[7].shape[0], W, H, int(scene.wind_clockwise), _p(vcol))
+                         keep[7].shape[0], W, H, int(scene.wind_clockwise), _p(vcol), _p(tex),
+                         _p(off, C.c_int64), _p(wh, C.c_int32))
         stats = np.zeros(4, np.uint64)
         rc = self.lib.oracle_draw_frame(C.byref(f), _p(frame, C.c_uint8), _p(depth),
                                         _p(ids, C.c_uint32), _p(stats, C.c_uint64))

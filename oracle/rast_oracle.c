@@ -96,6 +96,21 @@ void oracle_shade(const float* normal3, const float* albedo3, const float* light
     shade(n, a, lights7, nl, out3);
 }
 
+/* CImg's linear_atXY(fx, fy, 0, c) with Neumann boundaries: the coordinates clamped to the image
+ * (cimg::cut), the integer corner, and the bilinear blend in CImg's order of operations. */
+static float cimg_linear_xy(const float* img, int w, int h, int c, float fx, float fy) {
+    const float wm = (float)(w - 1), hm = (float)(h - 1);
+    const float nfx = fx < 0.f ? 0.f : (fx > wm ? wm : fx);
+    const float nfy = fy < 0.f ? 0.f : (fy > hm ? hm : fy);
+    const unsigned x = (unsigned)nfx, y = (unsigned)nfy;
+    const float dx = nfx - (float)x, dy = nfy - (float)y;
+    const unsigned nx = dx > 0 ? x + 1 : x, ny = dy > 0 ? y + 1 : y;
+    const size_t plane = (size_t)w * h, co = (size_t)c * plane;
+    const float Icc = img[co + x + (size_t)y * w], Inc = img[co + nx + (size_t)y * w];
+    const float Icn = img[co + x + (size_t)ny * w], Inn = img[co + nx + (size_t)ny * w];
+    return Icc + dx * (Inc - Icc + dy * (Icc + Inn - Icn - Inc)) + dy * (Icn - Icc);
+}
+
 int oracle_draw_frame(const oracle_frame* f, uint8_t* frame, float* depth, uint32_t* tri_id,
                       uint64_t* stats) {
     if (!f || !frame || !depth || f->width == 0 || f->height == 0) return -1;
@@ -123,6 +138,15 @@ int oracle_draw_frame(const oracle_frame* f, uint8_t* frame, float* depth, uint3
         const float* kd = f->kd + 3 * tri[9];
         v3 albedo = {kd[0], kd[1], kd[2]};
         v3 c0 = {0, 0, 0}, c1 = {0, 0, 0}, c2 = {0, 0, 0};
+        /* drawing.cpp:166-170: a face's uvs, (0, 0) where the index is < 0 */
+        const int textured = !f->vcol && f->tex && f->tex_off && f->tex_off[tri[9]] >= 0;
+        float uvx[3] = {0.f, 0.f, 0.f}, uvy[3] = {0.f, 0.f, 0.f};
+        if (textured)
+            for (int k = 0; k < 3; ++k)
+                if (tri[6 + k] >= 0) {
+                    uvx[k] = f->uv[2 * tri[6 + k]];
+                    uvy[k] = f->uv[2 * tri[6 + k] + 1];
+                }
         if (f->vcol) {
             const float* a = f->vcol + 3 * tri[0];
             const float* b = f->vcol + 3 * tri[1];
@@ -185,6 +209,16 @@ int oracle_draw_frame(const oracle_frame* f, uint8_t* frame, float* depth, uint3
                     albedo.x = dd * u.x;
                     albedo.y = dd * u.y;
                     albedo.z = dd * u.z;
+                }
+                if (textured) {  /* drawing.cpp:135, material.cpp:18-21 */
+                    const float ux = dd * (i0 * uvx[0] + i1 * uvx[1] + i2 * uvx[2]);
+                    const float uy = dd * (i0 * uvy[0] + i1 * uvy[1] + i2 * uvy[2]);
+                    const int tw = f->tex_wh[2 * tri[9]], th = f->tex_wh[2 * tri[9] + 1];
+                    const float* img = f->tex + f->tex_off[tri[9]];
+                    const float u = ux * (float)tw, v = (1.f - uy) * (float)th;
+                    albedo.x = cimg_linear_xy(img, tw, th, 0, u, v);
+                    albedo.y = cimg_linear_xy(img, tw, th, 1, u, v);
+                    albedo.z = cimg_linear_xy(img, tw, th, 2, u, v);
                 }
                 /* drawing.cpp:138-146 shade and write planar RGB */
                 uint32_t rgb[3];

@@ -36,6 +36,13 @@ typedef struct oracle_frame {
      * the many-light workload adds a colour per vertex, interpolated perspective-correctly exactly
      * as the normals are (drawing.cpp:64-75, 131), in place of Material::sample. */
     const float* vcol;
+    /* Textures (nullable; ignored where vcol is given): for material m with tex_off[m] >= 0, its
+     * texels normalised to 0..1 as material.h:20-22 does (CImg normalize over all channels), three
+     * planes of tex_wh[2m] * tex_wh[2m+1] floats from tex + tex_off[m] (x + y*w + c*w*h), sampled at
+     * the perspective-correct uv as Material::sample does (material.cpp:11-26, CImg linear_atXY). */
+    const float* tex;
+    const int64_t* tex_off;
+    const int32_t* tex_wh;
 } oracle_frame;
 
 /* stats (nullable) receives: [0] front-facing triangles, [1] bounding-box pixels tested,

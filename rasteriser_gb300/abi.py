@@ -89,6 +89,7 @@ SIGNATURES = {
     "rast_draw_noalloc": (C.c_int, [_P, _I64, _P, _I64, _P, _I64, _P, _I32, _P, _I32, _F, _F, _U32, _U32, _U32,
                                     _P, _P, _P, _P]),
     "rast_upload_vertex_albedo": (C.c_int, [_P, _F, _I64]),
+    "rast_upload_texture": (C.c_int, [_P, _I32, _F, _U32, _U32, _U32]),
     "rast_mlp_train": (C.c_int, [_P, C.POINTER(MlpTrainDesc), _F]),
     "rast_mlp_save": (C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "rast_mlp_load": (C.c_int, [_P, _P, C.c_size_t]),
@@ -288,6 +289,15 @@ class Renderer:
             a = _f32(rgb).reshape(-1, 3)
             self._check(self.lib.rast_upload_vertex_albedo(self.h, _fp(a), a.shape[0]), "rast_upload_vertex_albedo")
         self._mesh_digest = None
+
+    def upload_texture(self, material, texels):
+        """Texture of a material: texels (c, h, w) as loaded (e.g. image_load), or None to remove."""
+        if texels is None:
+            self._check(self.lib.rast_upload_texture(self.h, material, None, 0, 0, 0), "rast_upload_texture")
+            return
+        t = _f32(texels)
+        self._check(self.lib.rast_upload_texture(self.h, material, _fp(t), t.shape[2], t.shape[1], t.shape[0]),
+                    "rast_upload_texture")
 
     def set_lights(self, lights7):
         li = _f32(lights7).reshape(-1, 7)

@@ -141,6 +141,7 @@ int main(int argc, char** argv) {
     // model: the OBJ, or renderer.cpp's add_square
     std::vector<float> pos, nrm, uv, kd;
     std::vector<int32_t> tris;
+    std::vector<std::string> textures;
     if (!o.obj.empty()) {
         rast_obj* obj = nullptr;
         check(rast_obj_load(o.obj.c_str(), o.mats_dir.c_str(), &obj), nullptr, "obj");
@@ -151,9 +152,7 @@ int main(int argc, char** argv) {
         uv.assign(d.uv, d.uv + 2 * d.nuv);
         tris.assign(d.tris, d.tris + 10 * d.ntri);
         kd.assign(d.kd, d.kd + 3 * d.nmat);
-        for (int32_t i = 0; i < d.nmat; ++i)
-            if (d.textures[i][0])
-                std::fprintf(stderr, "note: material %d texture %s is drawn with its Kd\n", i, d.textures[i]);
+        for (int32_t i = 0; i < d.nmat; ++i) textures.push_back(d.textures[i]);
         rast_obj_free(obj);
         std::printf("Loaded model %s: %zu triangles.\n", o.obj.c_str(), tris.size() / 10);
     } else {
@@ -170,6 +169,19 @@ int main(int argc, char** argv) {
                            uv.empty() ? nullptr : uv.data(), (int64_t)uv.size() / 2, tris.data(),
                            (int64_t)tris.size() / 10, kd.data(), (int32_t)kd.size() / 3),
           ctx, "upload");
+    // textures: raw images (PPM / PGM / PFM); other formats are drawn with the material's Kd
+    for (size_t i = 0; i < textures.size(); ++i) {
+        if (textures[i].empty()) continue;
+        uint32_t tw = 0, th = 0, tc = 0;
+        if (rast_image_load(textures[i].c_str(), &tw, &th, &tc, nullptr, 0) != RAST_OK || tc < 3) {
+            std::fprintf(stderr, "note: texture %s is not a 3-channel PPM / PFM; material %zu uses its Kd\n",
+                         textures[i].c_str(), i);
+            continue;
+        }
+        std::vector<float> texels((size_t)tw * th * tc);
+        check(rast_image_load(textures[i].c_str(), &tw, &th, &tc, texels.data(), texels.size()), nullptr, "texture");
+        check(rast_upload_texture(ctx, (int32_t)i, texels.data(), tw, th, tc), ctx, "texture");
+    }
     if (o.deferred) check(rast_set_option(ctx, RAST_OPT_SHADER, RAST_SHADER_EXACT_DEFERRED), ctx, "option");
 
     const unsigned W = o.width, H = o.height;

@@ -213,7 +213,7 @@ void rast_destroy(rast_ctx* c) {
     cudaStreamSynchronize(c->stream);
     for (DevBuf* b : {&c->pos, &c->tris10, &c->tri_v, &c->tri_nm, &c->nrm, &c->kd, &c->lights, &c->rv, &c->keys,
                       &c->large, &c->counters, &c->tile_offset, &c->entries, &c->stats, &c->d_rgb, &c->d_depth,
-                      &c->d_ids, &c->vcol, &c->gbuf, &c->gbuf_count, &c->shade_index, &c->shade_stats, &c->view_mm,
+                      &c->d_ids, &c->vcol, &c->uvbuf, &c->texbuf, &c->tex_offbuf, &c->tex_whbuf, &c->gbuf, &c->gbuf_count, &c->shade_index, &c->shade_stats, &c->view_mm,
                       &c->mlp_image})
         b->release();
     if (c->ev_made)
@@ -275,6 +275,15 @@ rast_status rast_upload_mesh(rast_ctx* c, const float* pos, int64_t nv, const fl
             return cuda_fail(c, cudaGetLastError(), "split triangles");
     }
     RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    RAST_CUDA(c, c->uvbuf.reserve(sizeof(float) * 2 * (size_t)std::max<int64_t>(nuv, 1)));
+    if (nuv) RAST_CUDA(c, cudaMemcpy(c->uvbuf.ptr, uv, sizeof(float) * 2 * nuv, cudaMemcpyHostToDevice));
+    c->tex_host.assign((size_t)nmat, std::vector<float>());
+    c->tex_dims.assign((size_t)nmat, make_int2(0, 0));
+    c->mesh.tex = nullptr;
+    c->mesh.tex_off = nullptr;
+    c->mesh.tex_wh = nullptr;
+    c->mesh.uv = c->uvbuf.as<float>();
+    c->mesh.tris10 = c->tris10.as<int32_t>();
     c->mesh.pos = c->pos.as<float>();
     c->mesh.tri_v = c->tri_v.as<int32_t>();
     c->mesh.tri_nm = c->tri_nm.as<int4>();
@@ -304,6 +313,64 @@ rast_status rast_upload_vertex_albedo(rast_ctx* c, const float* rgb3, int64_t nv
     if (nv) RAST_CUDA(c, cudaMemcpy(c->vcol.ptr, rgb3, sizeof(float) * 3 * nv, cudaMemcpyHostToDevice));
     c->has_vcol = true;
     c->mesh.vcol = c->vcol.as<float>();
+    return RAST_OK;
+}
+
+rast_status rast_upload_texture(rast_ctx* c, int32_t material, const float* texels, uint32_t w, uint32_t h,
+                                uint32_t channels) {
+    if (!c) return RAST_ERR_INVALID_ARG;
+    if (!c->has_mesh) return fail(c, RAST_ERR_NO_MESH, "no mesh uploaded");
+    if (material < 0 || material >= c->mesh.nmat) return fail(c, RAST_ERR_INVALID_ARG, "material out of range");
+    if (texels && (w == 0 || h == 0 || w > 65536 || h > 65536 || channels < 3 || channels > 4))
+        return fail(c, RAST_ERR_INVALID_ARG, "texture needs 3 or 4 channels and 1..65536 pixels a side");
+    DeviceGuard g(c->device);
+    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<float>& t = c->tex_host[(size_t)material];
+    if (!texels) {
+        t.clear();
+        c->tex_dims[(size_t)material] = make_int2(0, 0);
+    } else {
+        // material.h:21, diffuse_texture.normalize(0.f, 1.f): CImg takes the smallest and largest
+        // value over every channel (with < and >), fills with 0 when they are equal, leaves an image
+        // already spanning 0..1 as it is, and otherwise maps v to (v - m) / (M - m) * (1 - 0) + 0.
+        const size_t plane = (size_t)w * h, n = plane * channels;
+        float m = texels[0], M = texels[0];
+        for (size_t i = 1; i < n; ++i) {
+            if (texels[i] < m) m = texels[i];
+            if (texels[i] > M) M = texels[i];
+        }
+        t.assign(3 * plane, 0.f);
+        if (!(m == M))
+            for (size_t i = 0; i < 3 * plane; ++i)
+                t[i] = (m != 0.f || M != 1.f) ? (texels[i] - m) / (M - m) * (1.f - 0.f) + 0.f : texels[i];
+        c->tex_dims[(size_t)material] = make_int2((int)w, (int)h);
+    }
+    // device tables
+    std::vector<long long> off((size_t)c->mesh.nmat, -1);
+    size_t total = 0;
+    for (size_t i = 0; i < c->tex_host.size(); ++i)
+        if (!c->tex_host[i].empty()) {
+            off[i] = (long long)total;
+            total += c->tex_host[i].size();
+        }
+    if (total == 0) {
+        c->mesh.tex = nullptr;
+        c->mesh.tex_off = nullptr;
+        c->mesh.tex_wh = nullptr;
+        return RAST_OK;
+    }
+    RAST_CUDA(c, c->texbuf.reserve(sizeof(float) * total));
+    RAST_CUDA(c, c->tex_offbuf.reserve(sizeof(long long) * off.size()));
+    RAST_CUDA(c, c->tex_whbuf.reserve(sizeof(int2) * off.size()));
+    for (size_t i = 0; i < c->tex_host.size(); ++i)
+        if (off[i] >= 0)
+            RAST_CUDA(c, cudaMemcpy(c->texbuf.as<float>() + off[i], c->tex_host[i].data(),
+                                    sizeof(float) * c->tex_host[i].size(), cudaMemcpyHostToDevice));
+    RAST_CUDA(c, cudaMemcpy(c->tex_offbuf.ptr, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice));
+    RAST_CUDA(c, cudaMemcpy(c->tex_whbuf.ptr, c->tex_dims.data(), sizeof(int2) * off.size(), cudaMemcpyHostToDevice));
+    c->mesh.tex = c->texbuf.as<float>();
+    c->mesh.tex_off = c->tex_offbuf.as<long long>();
+    c->mesh.tex_wh = c->tex_whbuf.as<int2>();
     return RAST_OK;
 }
 

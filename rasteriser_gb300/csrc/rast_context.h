@@ -70,6 +70,12 @@ struct rast_ctx {
     DevBuf vcol;
     bool has_vcol = false;
 
+    // uvs and textures (rast_upload_texture): normalised planes per material, on the device
+    // concatenated with per-material offsets and sizes
+    DevBuf uvbuf, texbuf, tex_offbuf, tex_whbuf;
+    std::vector<std::vector<float>> tex_host;
+    std::vector<int2> tex_dims;
+
     // lights
     DevBuf lights;
     int32_t nl = 0;

@@ -57,6 +57,13 @@ struct DeviceMesh {
     const float* nrm = nullptr;      // nn * 3
     const float* kd = nullptr;       // nmat * 3
     const float* vcol = nullptr;     // nv * 3 per-vertex albedo, or null
+    // textures (null when no material has one): per material the offset of its normalised texels
+    // in tex (-1: none) and its width, height; the uvs and the triangles' uv indices
+    const float* tex = nullptr;
+    const long long* tex_off = nullptr;
+    const int2* tex_wh = nullptr;
+    const float* uv = nullptr;       // nuv * 2
+    const int32_t* tris10 = nullptr; // ntri * 10, the Triangle records (uv indices at 6..8)
     int64_t nv = 0, ntri = 0, nn = 0;
     int32_t nmat = 0;
 };

@@ -834,7 +834,12 @@ struct ResolveArgs {
     float* depth;
     uint32_t* tri_id;
     unsigned long long* stats;
-    const float* vcol;    // per-vertex albedo (nv * 3) or null for the material's Kd
+    const float* vcol;    // per-vertex albedo (nv * 3) or null for the material's Kd / texture
+    const float* tex;     // textures (null: none), see DeviceMesh
+    const long long* tex_off;
+    const int2* tex_wh;
+    const float* uv;
+    const int32_t* tris10;
     float4* gbuf;         // deferred shading: 2 float4 per fragment record, or null to shade here
     uint32_t* gbuf_count; // deferred shading: records per block (1024 pixels)
     uint32_t* shade_index;  // deferred shading: the tile list build_shade_tiles writes
@@ -845,14 +850,37 @@ constexpr int kResolveWarps = kResolveThreads / 32;
 constexpr int kSpan = 128;  // consecutive pixels per warp, 4 per lane
 static_assert(kResolveWarps * kSpan == kShadeBlock, "a resolve block is one block of shading records");
 
+// CImg's linear_atXY(fx, fy, 0, c) for c = 0, 1, 2 on a normalised planar texture: the coordinates
+// clamped to [0, w-1] x [0, h-1] (cimg::cut), the integer corner by truncation, and the blend
+// Icc + dx*(Inc - Icc + dy*(Icc + Inn - Icn - Inc)) + dy*(Icn - Icc) in CImg's order.
+__device__ __forceinline__ float3 texture_sample(const float* img, int w, int h, float fx, float fy) {
+    const float wm = (float)(w - 1), hm = (float)(h - 1);
+    const float nfx = fx < 0.f ? 0.f : (fx > wm ? wm : fx);
+    const float nfy = fy < 0.f ? 0.f : (fy > hm ? hm : fy);
+    const uint32_t x = min(__float2uint_rz(nfx), (uint32_t)(w - 1)), y = min(__float2uint_rz(nfy), (uint32_t)(h - 1));
+    const float dx = sub(nfx, (float)x), dy = sub(nfy, (float)y);
+    const uint32_t nx = dx > 0.f ? x + 1 : x, ny = dy > 0.f ? y + 1 : y;
+    const size_t plane = (size_t)w * h;
+    float r[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float* P = img + c * plane;
+        const float Icc = __ldg(P + x + (size_t)y * w), Inc = __ldg(P + nx + (size_t)y * w);
+        const float Icn = __ldg(P + x + (size_t)ny * w), Inn = __ldg(P + nx + (size_t)ny * w);
+        const float t = add(sub(Inc, Icc), mul(dy, sub(sub(add(Icc, Inn), Icn), Inc)));
+        r[c] = add(add(Icc, mul(dx, t)), mul(dy, sub(Icn, Icc)));
+    }
+    return make_float3(r[0], r[1], r[2]);
+}
+
 // The winning fragment's attributes as update_pixel computes them (drawing.cpp:108-140):
 // barycentrics at the integer pixel, NDC depth, perspective-correct normal, normalised and flipped
 // for clockwise winding, and the albedo (the material's Kd, or the perspective-correct per-vertex
 // colour when the mesh has one).
 __device__ __forceinline__ void fragment_attributes(const ResolveArgs& a, uint32_t x, uint32_t y, float4 v0, float4 v1,
                                                     float4 v2, float3 n0, float3 n1, float3 n2, int mat,
-                                                    int32_t i0, int32_t i1, int32_t i2, float& depth, float3& nrm,
-                                                    float3& alb) {
+                                                    int32_t i0, int32_t i1, int32_t i2, int64_t tri, float& depth,
+                                                    float3& nrm, float3& alb) {
     EdgeTri T;
     make_edge_tri(v0, v1, v2, T);
     const float pxf = (float)x, pyf = (float)y;
@@ -880,6 +908,22 @@ __device__ __forceinline__ void fragment_attributes(const ResolveArgs& a, uint32
         float uy = add(add(mul(i0w, __ldg(c0 + 1)), mul(i1w, __ldg(c1 + 1))), mul(i2w, __ldg(c2 + 1)));
         float uz = add(add(mul(i0w, __ldg(c0 + 2)), mul(i1w, __ldg(c1 + 2))), mul(i2w, __ldg(c2 + 2)));
         alb = make_float3(mul(dd, ux), mul(dd, uy), mul(dd, uz));
+    } else if (a.tex && __ldg(a.tex_off + mat) >= 0) {
+        // drawing.cpp:166-170 (uv (0, 0) where the index is < 0) and 135, material.cpp:18-21
+        float ux[3] = {0.f, 0.f, 0.f}, uy[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int32_t ui = __ldg(a.tris10 + 10 * tri + 6 + k);
+            if (ui >= 0) {
+                ux[k] = __ldg(a.uv + 2 * (int64_t)ui);
+                uy[k] = __ldg(a.uv + 2 * (int64_t)ui + 1);
+            }
+        }
+        const float u = mul(dd, add(add(mul(i0w, ux[0]), mul(i1w, ux[1])), mul(i2w, ux[2])));
+        const float v = mul(dd, add(add(mul(i0w, uy[0]), mul(i1w, uy[1])), mul(i2w, uy[2])));
+        const int2 wh = __ldg(a.tex_wh + mat);
+        alb = texture_sample(a.tex + __ldg(a.tex_off + mat), wh.x, wh.y, mul(u, (float)wh.x),
+                             mul(sub(1.f, v), (float)wh.y));
     } else {
         const float* kd = a.kd + 3 * (int64_t)mat;
         alb = make_float3(__ldg(kd), __ldg(kd + 1), __ldg(kd + 2));
@@ -987,7 +1031,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             const float3 n2 = camera_normal(a.normal, m2.x, m2.y, m2.z);
             float dep;
             float3 nrm, alb;
-            fragment_attributes(a, x, y, v0, v1, v2, n0, n1, n2, nm.w, i0, i1, i2, dep, nrm, alb);
+            fragment_attributes(a, x, y, v0, v1, v2, n0, n1, n2, nm.w, i0, i1, i2, tt, dep, nrm, alb);
             S.depth[off] = dep;
             if (a.gbuf) {
                 // deferred: the span's i-th record; the shading pass writes the colour
@@ -1200,6 +1244,11 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.tri_id = p.tri_id;
     ra.stats = s.stats;
     ra.vcol = mesh.vcol;
+    ra.tex = mesh.tex;
+    ra.tex_off = mesh.tex_off;
+    ra.tex_wh = mesh.tex_wh;
+    ra.uv = mesh.uv;
+    ra.tris10 = mesh.tris10;
     const bool deferred = p.shader != 0;
     ra.gbuf = deferred ? s.gbuf : nullptr;
     ra.gbuf_count = deferred ? s.gbuf_count : nullptr;

@@ -360,6 +360,21 @@ def config_soup(n_tris=4_000_000, width=3840, height=2160, seed=2):
     return soup(n_tris, width, height, seed=seed)
 
 
+def with_spherical_uvs(sc, scale=1.0, offset=0.0):
+    """The scene with one uv per vertex from its direction (u = atan2(z, x) / 2pi + 1/2,
+    v = asin(y / |p|) / pi + 1/2, times `scale` plus `offset`, so uvs outside 0..1 can be asked for)
+    and every triangle's uv indices equal to its vertex indices."""
+    p = sc.pos.astype(np.float64)
+    r = np.sqrt((p * p).sum(axis=1))
+    r[r == 0] = 1.0
+    u = np.arctan2(p[:, 2], p[:, 0]) / _TWO_PI + 0.5
+    v = np.arcsin(np.clip(p[:, 1] / r, -1.0, 1.0)) / _PI + 0.5
+    uv = (np.stack([u, v], axis=1) * scale + offset).astype(np.float32)
+    tris = sc.tris.copy()
+    tris[:, 6:9] = tris[:, 0:3]
+    return dataclasses.replace(sc, uv=uv, tris=tris)
+
+
 def config_many_lights(n_lon=1024, n_lat=512, width=1920, height=1080, n_lights=256, seed=4, light_seed=5):
     """Many-light shading workload: the displaced sphere with smooth normals (the normalised unit
     positions), per-vertex albedo uniform in [0,1]^3 and ``n_lights`` directional lights from
