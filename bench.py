@@ -42,7 +42,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["displaced_sphere", "soup", "icosphere"], default="displaced_sphere")
+    ap.add_argument("--workload", choices=["displaced_sphere", "soup", "icosphere", "many_lights"],
+                    default="displaced_sphere")
+    ap.add_argument("--shader", choices=["exact", "deferred", "learned"], default="exact",
+                    help="shading mode (learned: the MLP is trained on 4M samples first)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--device-only", action="store_true", help="only the device-resident timed loop (profiling)")
     ap.add_argument("--no-soak", action="store_true", help="skip the clock-sampling soak loop (profiling)")
@@ -60,7 +63,25 @@ def make_scene(name):
         return S.config_displaced_sphere(), "displaced_sphere_1024x512_1080p_spin60"
     if name == "soup":
         return S.config_soup(), "triangle_soup_4M_2160p"
+    if name == "many_lights":
+        return S.config_many_lights(), "displaced_sphere_1M_1080p_256_lights"
     return S.config_icosphere_small(), "icosphere_l4_480p"
+
+
+def rank_frame(rank, world, k, n_frames):
+    """The spin frame that rank `rank` of `world` draws at its step k: the ranks take consecutive
+    frames of the spin (replicas, no exchange between them)."""
+    return (rank + k * world) % n_frames
+
+
+def max_over_ranks(dist, seconds, device):
+    """The slowest rank's time (the job's time), or the time itself without a process group."""
+    if dist is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def frame_inputs(scene, n_frames):
@@ -143,6 +164,9 @@ def algorithmic_bytes(stage, sc, st):
         return 64 * st["binned_tris"] + 4 * st["bin_entries"]
     if stage == "tile_raster":
         return 68 * st["bin_entries"] + 16 * npx
+    if stage == "shade":
+        # the deferred pass: one 32-byte record read and an RGB8 pixel written per covered pixel
+        return (32 + 3) * st["written"]
     if stage == "resolve":
         # key read + re-arm, planar RGB8 + depth written, and per covered pixel the winner's indices,
         # vertices, normal indices and normals
@@ -275,7 +299,7 @@ def time_scene_device(torch, abi, r, stream, frames_in, steps, warmup, flush):
 
 
 def extra_soup(torch, abi, stream, flush, steps=30):
-    """configs[2]: 4M-triangle soup at 3840x2160 (one frame drawn repeatedly)."""
+    """The 4M-triangle soup at 3840x2160 (one frame drawn repeatedly)."""
     from rasteriser_gb300 import scenes as S
     sc = S.config_soup()
     fr = frame_inputs(sc, 1)
@@ -299,7 +323,7 @@ def bf16_peak():
 
 
 def extra_many_lights(torch, abi, stream, flush, steps=30):
-    """configs[4]: the 1M-triangle displaced sphere with smooth normals and per-vertex albedo at
+    """The 1M-triangle displaced sphere with smooth normals and per-vertex albedo at
     1920x1080 under 256 lights. The plain per-light shader (deferred exact; fused exact beside it)
     against the learned shader, which is trained here on 4M samples the exact shader labels."""
     from rasteriser_gb300 import scenes as S
@@ -364,7 +388,7 @@ def extra_many_lights(torch, abi, stream, flush, steps=30):
 
 
 def batch_workload(seed=3, n_frames=256, n_soups=16):
-    """configs[3]: icospheres L2-L7 and seeded soups of 1k-500k triangles (log-uniform sizes); each
+    """The uneven batch: icospheres L2-L7 and seeded soups of 1k-500k triangles (log-uniform sizes); each
     frame picks a mesh uniformly, a resolution from {256x256, 640x480, 1280x720, 1920x1080}, random
     rx/ry and a 1-8 light rig."""
     from rasteriser_gb300 import scenes as S
@@ -385,7 +409,7 @@ def batch_workload(seed=3, n_frames=256, n_soups=16):
 
 
 def extra_batch(torch, abi, stream, steps=10):
-    """configs[3]: the 256-frame batch as one CUDA graph over 8 lanes after autotuning, against the
+    """The 256-frame batch as one CUDA graph over 8 lanes after autotuning, against the
     same frames drawn one after another on one stream."""
     meshes, frames = batch_workload()
     r = abi.Renderer(0)
@@ -468,12 +492,17 @@ def run_ours(args):
         r.set_option(abi.OPT_ROW_CHUNK, args.row_chunk)
     r.upload_scene_mesh(scene)
     r.set_lights(frames[0][3])  # the view is a fixed translation: the lights are the same each frame
+    training = None
+    if args.shader == "learned":
+        training = r.mlp_train(samples=4 << 20, epochs=24, seed=3)
+    r.set_option(abi.OPT_SHADER, {"exact": abi.SHADER_EXACT, "deferred": abi.SHADER_EXACT_DEFERRED,
+                                  "learned": abi.SHADER_LEARNED}[args.shader])
     d_rgb = torch.empty(3 * W * H, dtype=torch.uint8, device="cuda")
     d_depth = torch.empty(W * H, dtype=torch.float32, device="cuda")
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
     def frame_of(k):
-        return frames[(rank + k * world) % n_frames]
+        return frames[rank_frame(rank, world, k, n_frames)]
 
     def step(k):
         _, cam, nm, _ = frame_of(k)
@@ -510,11 +539,7 @@ def run_ours(args):
         wall = time.perf_counter() - wall0
     r.sync()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_s = sum(step_ms) / 1000.0
-    if dist is not None:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(dist, sum(step_ms) / 1000.0, "cuda")
     value = world * args.steps / total_s
     launches_per_step = stats["launches"]
 
@@ -552,11 +577,7 @@ def run_ours(args):
         r.draw(cam, nm, W, H, 0, h_rgb, h_depth)
         if k >= 3:
             e2e_s += time.perf_counter() - t0
-    e2e_value = world * n_e2e / e2e_s if dist is None else None
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_value = world * n_e2e / float(t.item())
+    e2e_value = world * n_e2e / max_over_ranks(dist, e2e_s, "cuda")
 
     if rank != 0:
         if dist is not None:
@@ -566,12 +587,15 @@ def run_ours(args):
     # roofline of the dominant kernel
     peak, peak_kind = peaks()
     stage_names = ["vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve"]
+    if args.shader != "exact":
+        stage_names.append("shade")
     dom = max(stage_names, key=lambda s: stage_ms.get(s, 0.0))
     sc0 = frames[0][0]
     alg = algorithmic_bytes(dom, sc0, stats)
     achieved = alg / (stage_ms[dom] / 1000.0) / 1e9
     kernel_names = {"vertex": "k_vertex", "setup_raster": "k_setup_raster", "bin_scan": "k_bin_scan",
-                    "bin_scatter": "k_bin_scatter", "tile_raster": "k_tile_raster", "resolve": "k_resolve"}
+                    "bin_scatter": "k_bin_scatter", "tile_raster": "k_tile_raster", "resolve": "k_resolve",
+                    "shade": "k_shade_mlp" if args.shader == "learned" else "k_shade_exact"}
     traffic = load_traffic(kernel_names[dom], workload)
 
     cpu = None
@@ -588,7 +612,8 @@ def run_ours(args):
         "config": {"workload": workload, "width": W, "height": H, "triangles": scene.ntri,
                    "vertices": int(scene.pos.shape[0]), "lights": int(frames[0][3].shape[0]),
                    "frames_cycled": n_frames, "l2": "flushed between steps (256 MiB write, outside the timed events)",
-                   "parallelism": f"replicas x{world}", "mode": "RAST_CLEAR (spin-loop clear + draw_frame)"},
+                   "parallelism": f"replicas x{world}", "mode": "RAST_CLEAR (spin-loop clear + draw_frame)",
+                   "shader": args.shader},
         "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": 7 * W * H, "d2h_bytes_per_step": 7 * W * H,
                 "path": "rast_draw with pinned host frame (planar RGB8) and depth buffers; mesh resident"},
         "gpu_launches": launches_per_step * args.steps,
@@ -602,6 +627,9 @@ def run_ours(args):
         "frame_stats": {k: stats[k] for k in ("front", "tested", "inside", "written", "binned_tris", "bin_entries")},
         "fragments_per_s": stats["inside"] * value,
     }
+    if training is not None:
+        line["training"] = training
+        line["shade_checks"] = r.shade_stats()
     if not args.no_extras and world == 1 and args.workload == "displaced_sphere":
         line["extras"] = {"soup": extra_soup(torch, abi, stream, flush), "batch": extra_batch(torch, abi, stream),
                           "many_lights": extra_many_lights(torch, abi, stream, flush)}
