@@ -280,7 +280,8 @@ typedef struct rast_mlp_train_desc {
 rast_status rast_mlp_train(rast_ctx* ctx, const rast_mlp_train_desc* desc, float out[4]);
 
 /* The weights as a versioned blob ("RMLP", see rasteriser_gb300/csrc/rast_mlp.h: header with the
- * light rig's hash and the output scale, BF16 weights, FP32 biases). *size receives the blob size;
+ * light rig's hash and the output scale, then the BF16 weights; the biases are weights of constant
+ * inputs). *size receives the blob size;
  * buf may be NULL to query it. RAST_ERR_INVALID_ARG if cap is too small or nothing is trained. */
 rast_status rast_mlp_save(rast_ctx* ctx, void* buf, size_t cap, size_t* size);
 

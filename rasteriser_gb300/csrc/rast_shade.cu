@@ -78,19 +78,25 @@ __device__ __forceinline__ void stage_lights(const float* lights, int l0, int n,
     }
 }
 
+// One staged light's term of shading.cpp:24-31 for normal nv and albedo alb.
+__device__ __forceinline__ float3 light_term(const float4* sl, int l, float3 nv, float3 alb) {
+    const float4 A = sl[2 * l], B = sl[2 * l + 1];
+    float cr = mul(A.w, alb.x), cg = mul(B.x, alb.y), cb = mul(B.y, alb.z);
+    const float d = add(add(mul(nv.x, A.x), mul(nv.y, A.y)), mul(nv.z, A.z));
+    const float m = gmax(0.f, d);
+    cr = mul(mul(cr, m), kOneOverPi);
+    cg = mul(mul(cg, m), kOneOverPi);
+    cb = mul(mul(cb, m), kOneOverPi);
+    return make_float3(cr, cg, cb);
+}
+
 __device__ __forceinline__ void accumulate_lights(const float4* sl, int n, float3 nv, float3 alb, float3& acc) {
 #pragma unroll 4
     for (int l = 0; l < n; ++l) {
-        const float4 A = sl[2 * l], B = sl[2 * l + 1];
-        float cr = mul(A.w, alb.x), cg = mul(B.x, alb.y), cb = mul(B.y, alb.z);
-        const float d = add(add(mul(nv.x, A.x), mul(nv.y, A.y)), mul(nv.z, A.z));
-        const float m = gmax(0.f, d);
-        cr = mul(mul(cr, m), kOneOverPi);
-        cg = mul(mul(cg, m), kOneOverPi);
-        cb = mul(mul(cb, m), kOneOverPi);
-        acc.x = add(acc.x, cr);
-        acc.y = add(acc.y, cg);
-        acc.z = add(acc.z, cb);
+        const float3 c = light_term(sl, l, nv, alb);
+        acc.x = add(acc.x, c.x);
+        acc.y = add(acc.y, c.y);
+        acc.z = add(acc.z, c.z);
     }
 }
 
@@ -198,8 +204,8 @@ __device__ __forceinline__ void mlp_feature_pairs(float3 n, float3 alb, uint32_t
 }
 
 // The same features, written as they are made into this thread's TMEM lane from column taddr on
-// (56 columns, two BF16 features each; zeros when !valid): the A operand of the first layer.
-__device__ __forceinline__ void store_features(float3 n, float3 alb, bool valid, uint32_t taddr);
+// (56 columns, two BF16 features each): the A operand of the first layer.
+__device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t taddr);
 
 // ---------------------------------------------------------------------------------------------
 // learned shader: tcgen05 helpers
@@ -337,7 +343,9 @@ constexpr uint32_t kSmW2 = kSmW1 + kMlpHid * kMlpIn * 2;
 constexpr uint32_t kSmW3 = kSmW2 + kMlpHid * kMlpHid * 2;
 constexpr uint32_t kSmMisc = kSmW + sizeof(MlpImage);
 constexpr uint32_t kMaxSamples = 4;
-constexpr int kCheckTiles = 16;   // tiles whose checks a CTA batches before running them
+constexpr int kMlpSmemLights = 512;  // lights staged in shared memory (32 bytes each) for the checks
+
+constexpr int kCheckTiles = 16;  // tiles whose checks a CTA batches before running them
 
 // The checked records of the tiles a CTA shaded since its last check batch: the record, the MLP's
 // clamped radiance, then the exact radiance.
@@ -354,10 +362,17 @@ struct MlpMisc {
     uint32_t pad[3];
     CheckBatch check;
 };
-constexpr uint32_t kMlpSmem = kSmMisc + ((sizeof(MlpMisc) + 127) / 128) * 128;
+constexpr uint32_t kSmLights = kSmMisc + ((sizeof(MlpMisc) + 127) / 128) * 128;
+constexpr uint32_t kMlpSmem = kSmLights;  // without staged lights
 static_assert(kSmW1 % 16 == 0 && kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmMisc % 16 == 0, "operand alignment");
-static_assert(kMlpCtasPerSm * (kMlpSmem + 1024) <= 228 * 1024, "four CTAs per SM");
+static_assert(kMlpCtasPerSm * (kMlpSmem + 32 * kMlpSmemLights + 1024) <= 228 * 1024, "four CTAs per SM");
 static_assert(sizeof(MlpImage) % 16 == 0 && kSmW % 16 == 0, "bulk copy alignment");
+
+// Whether a launch stages its lights in shared memory, and its dynamic shared memory.
+RAST_HD inline bool mlp_lights_staged(int nl, int samples) { return samples > 0 && nl > 0 && nl <= kMlpSmemLights; }
+inline uint32_t mlp_smem_bytes(int nl, int samples) {
+    return kMlpSmem + (mlp_lights_staged(nl, samples) ? 32u * (uint32_t)nl : 0u);
+}
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
@@ -392,13 +407,31 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a) {
     tmem_wait_st();
 }
 
+// A tile whose check failed, shaded exactly (shading.cpp:20-34 in its order) by its rows.
+__device__ __forceinline__ void reshade_tile(const ShadeArgs& a, const float4* sl, uint32_t e) {
+    if (threadIdx.x >= tile_count(e)) return;
+    const size_t slot = (size_t)tile_first(e) + threadIdx.x;
+    const float4 g0 = a.gbuf[2 * slot], g1 = a.gbuf[2 * slot + 1];
+    const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
+    uint32_t col;
+    if (sl) {
+        float3 acc = make_float3(0.f, 0.f, 0.f);
+        accumulate_lights(sl, a.nl, nv, alb, acc);
+        col = pack_rgb(acc);
+    } else {
+        col = shade_lights(a.lights, a.nl, nv, alb);
+    }
+    write_rgb(a.rgb, a.npx, __float_as_uint(g1.z), col);
+}
+
 // The checked records of a batch through the exact shader: warp w takes the pairs (tile, sample)
-// p = w, w + 4, ...; its lanes split the lights and add their partial sums in a tree (the per-light
-// terms of shading.cpp:24-34 summed in another order: the check only estimates the error, it
-// never produces a colour). Then each tile's largest channel error decides whether it is shaded
-// exactly, which the whole CTA does for the failing tiles. Ends synchronised.
-__device__ void run_checks(const ShadeArgs& a, CheckBatch& B, int nb, int n_samples, unsigned long long& n_fallback,
-                           float& max_err) {
+// p = w, w + 4, ...; its lanes split the lights, read from shared memory when staged (sl), and add
+// their partial sums in a tree (the per-light terms of shading.cpp:24-31 summed in another order:
+// the check only estimates the error, it never produces a colour). Then each tile's largest channel
+// error decides whether it is shaded exactly, which the whole CTA does for the failing tiles. Ends
+// synchronised.
+__device__ void run_checks(const ShadeArgs& a, const float4* sl, CheckBatch& B, int nb, int n_samples,
+                           unsigned long long& n_fallback, float& max_err) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __syncthreads();
     for (int p = warp; p < nb * n_samples; p += kMlpThreads / 32) {
@@ -406,7 +439,7 @@ __device__ void run_checks(const ShadeArgs& a, CheckBatch& B, int nb, int n_samp
         const float3 n = make_float3(R[0], R[1], R[2]), alb = make_float3(R[3], R[4], R[5]);
         float x = 0.f, y = 0.f, z = 0.f;
         for (int l = lane; l < a.nl; l += 32) {
-            const float3 c = light_sum(a.lights + 7 * (int64_t)l, 1, n, alb);
+            const float3 c = sl ? light_term(sl, l, n, alb) : light_sum(a.lights + 7 * (int64_t)l, 1, n, alb);
             x += c.x; y += c.y; z += c.z;
         }
 #pragma unroll
@@ -431,21 +464,15 @@ __device__ void run_checks(const ShadeArgs& a, CheckBatch& B, int nb, int n_samp
     __syncthreads();
     for (int i = 0; i < nb; ++i) {
         if (!B.fail[i]) continue;  // uniform: every thread reads the same flag
-        const uint32_t e = B.entry[i];
         if (threadIdx.x == 0) ++n_fallback;
-        if (threadIdx.x < tile_count(e)) {
-            const size_t slot = (size_t)tile_first(e) + threadIdx.x;
-            const float4 g0 = a.gbuf[2 * slot], g1 = a.gbuf[2 * slot + 1];
-            write_rgb(a.rgb, a.npx, __float_as_uint(g1.z),
-                      shade_lights(a.lights, a.nl, make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y)));
-        }
+        reshade_tile(a, sl, B.entry[i]);
     }
     __syncthreads();
 }
 
-// The checked records of tile t: ranks hash(t, s) mod count, the same in every thread.
+// The checked records of tile t: ranks floor(hash(t, s) * count / 2^32), the same in every thread.
 __device__ __forceinline__ uint32_t sample_rank(uint32_t t, int s, uint32_t count) {
-    return hash32(t * 8u + (uint32_t)s + 0x9E3779B9u) % count;
+    return __umulhi(hash32(t * 8u + (uint32_t)s + 0x9E3779B9u), count);
 }
 
 // Issues the MMAs of one layer, A from TMEM columns a (K/16 steps of 8 columns) and B from shared
@@ -461,9 +488,11 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
     extern __shared__ __align__(1024) uint8_t sm[];
     const int row = threadIdx.x, warp = row >> 5;
     MlpMisc& M = *reinterpret_cast<MlpMisc*>(sm + kSmMisc);
+    const int n_samples = a.eval_out ? 0 : min(a.samples, (int)kMaxSamples);
+    float4* sl = mlp_lights_staged(a.nl, n_samples) ? reinterpret_cast<float4*>(sm + kSmLights) : nullptr;
 
-    // the weights and output scale arrive by one bulk copy (they do not depend on the grid this
-    // kernel may overlap with)
+    // the weights and output scale arrive by one bulk copy, the lights by plain loads (neither
+    // depends on the grid this kernel may overlap with)
     const uint32_t mbar = smem_addr(&M.mbar), mbar_w = smem_addr(&M.mbar_w);
     if (row == 0) {
         mbar_init(mbar, 1);
@@ -471,8 +500,8 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         mbar_expect_tx(mbar_w, sizeof(MlpImage));
         bulk_copy_g2s(smem_addr(sm + kSmW), a.mlp, sizeof(MlpImage), mbar_w);
     }
+    if (sl) stage_lights(a.lights, 0, a.nl, sl);
     if (warp == 0) tmem_alloc(smem_addr(&M.tmem), kTmemCols);
-    const int n_samples = a.eval_out ? 0 : min(a.samples, (int)kMaxSamples);
     // the records and the tile list are the previous kernel's output
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
@@ -492,19 +521,21 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    bool ok = __syncthreads_and(mbar_wait(mbar_w, 0));
-    const bool weights_pending = !ok;
+    bool failed = !__syncthreads_and(mbar_wait(mbar_w, 0));
+    const bool weights_pending = failed;
     const uint32_t tmem = M.tmem;
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lanes
     const float out_scale = reinterpret_cast<const MlpImage*>(sm + kSmW)->out_scale;
     const uint32_t sW1 = smem_addr(sm + kSmW1), sW2 = smem_addr(sm + kSmW2), sW3 = smem_addr(sm + kSmW3);
 
+    // Every barrier of the loop also ORs the threads' timeout flags, so all threads leave the loop
+    // at the same barrier (the loop condition itself is the same in every thread).
     uint32_t phase = 0;
-    unsigned long long n_tile = 0, n_fallback = 0, n_checked = 0;
+    unsigned long long n_tile = 0, n_fallback = 0;
     float max_err = 0.f;
     int nb = 0;  // tiles in the check batch
 
-    while (ok && t < n_tiles) {
+    while (!weights_pending && t < n_tiles) {
         const uint32_t t_next = t + stride;
         const uint32_t count_next = t_next < n_tiles ? tile_count(e_next) : 0u;
         float4 g0n = make_float4(0.f, 0.f, 0.f, 0.f), g1n = g0n;
@@ -516,40 +547,37 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         const bool valid = (uint32_t)row < count;
         const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
         const uint32_t pix = __float_as_uint(g1.z);
-        store_features(nv, alb, valid, lane_base + kColA);
+        // rows past the tile's records hold zeros: finite features whose results are not stored
+        store_features(nv, alb, lane_base + kColA);
         tc_fence_before();
-        __syncthreads();
+        if (__syncthreads_or(failed)) break;
 
         // layer 1: D = X (128 x 112) * W1^T
         if (row == 0)
             issue_layer(tmem + kColD, tmem + kColA, sW1, kMlpHid * 16, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-
-        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (!ok) break;
         tc_fence_after();
         hidden_epilogue(lane_base + kColD, lane_base + kColA);  // h1 over the consumed features
         tc_fence_before();
-        __syncthreads();
+        if (__syncthreads_or(failed)) break;
 
         // layer 2: D = H1 (128 x 64) * W2^T (layer 1's accumulators were read)
         if (row == 0)
             issue_layer(tmem + kColD, tmem + kColA, sW2, kMlpHid * 16, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (!ok) break;
         tc_fence_after();
         hidden_epilogue(lane_base + kColD, lane_base + kColA);  // h2 over the consumed h1
         tc_fence_before();
-        __syncthreads();
+        if (__syncthreads_or(failed)) break;
 
         // layer 3: D[0, 16) = H2 (128 x 64) * W3^T
         if (row == 0)
             issue_layer(tmem + kColD, tmem + kColA, sW3, kMlpOutPad * 16, kMlpHid / 16,
                         idesc_bf16(kMlpRows, kMlpOutPad), mbar);
-        ok = __syncthreads_and(mbar_wait(mbar, phase));
+        failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (!ok) break;
         tc_fence_after();
         uint32_t o[4];
         tmem_ld4(lane_base + kColD, o);
@@ -580,8 +608,7 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
                     }
                 if (row == 0) M.check.entry[nb] = e;
                 if (++nb == kCheckTiles) {
-                    run_checks(a, M.check, nb, n_samples, n_fallback, max_err);
-                    n_checked += (unsigned long long)nb * n_samples;
+                    run_checks(a, sl, M.check, nb, n_samples, n_fallback, max_err);
                     nb = 0;
                 }
             }
@@ -595,12 +622,10 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         g1 = g1n;
     }
 
-    if (ok && nb > 0) {
-        run_checks(a, M.check, nb, n_samples, n_fallback, max_err);
-        n_checked += (unsigned long long)nb * n_samples;
-    }
+    // the last batch (the loop ended at a barrier every thread passed, so `failed` is uniform)
+    if (!failed && nb > 0) run_checks(a, sl, M.check, nb, n_samples, n_fallback, max_err);
 
-    if (!ok) {
+    if (failed) {
         // the weights' copy or an MMA did not complete in time: record it, give the pending one
         // another bounded wait, then release the tensor memory
         if (row == 0) atomicOr(&a.counters[1], STATUS_SHADE_TIMEOUT);
@@ -617,28 +642,25 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         if (row == 0) {
             atomicAdd(a.stats + 0, n_tile);
             atomicAdd(a.stats + 1, n_fallback);
-            atomicAdd(a.stats + 2, n_checked);
+            atomicAdd(a.stats + 2, n_tile * (unsigned long long)n_samples);
         }
         if (max_err > 0.f) atomicMax(a.stats + 3, (unsigned long long)__float_as_uint(max_err));
     }
 }
 
 // The features of one row into its TMEM lane (declared above).
-__device__ __forceinline__ void store_features(float3 n, float3 alb, bool valid, uint32_t taddr) {
+__device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t taddr) {
     const float comp[3] = {n.x, n.y, n.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         uint32_t q[8];
         fourier16(comp[c], [&](int f, uint32_t p) {
-            q[f & 7] = valid ? p : 0u;
+            q[f & 7] = p;
             if ((f & 7) == 7) tmem_st8(taddr + (uint32_t)(c * kMlpFreq + f - 7), q);
         });
     }
     uint32_t t[8];
     tail_pairs(n, alb, t);
-    if (!valid)
-#pragma unroll
-        for (int i = 0; i < 8; ++i) t[i] = 0u;
     tmem_st8(taddr + 48, t);
     tmem_wait_st();
 }
@@ -929,7 +951,8 @@ static ShadeArgs shade_args(const FrameScratch& s, const DrawParams& p) {
 static int mlp_grid(int n_sm, int64_t blocks) {
     static bool attr_set = false;  // per process: the attribute is per function, all devices alike
     if (!attr_set) {
-        if (cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpSmem) !=
+        if (cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(kMlpSmem + 32 * kMlpSmemLights)) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
@@ -970,7 +993,7 @@ int launch_shade(const FrameScratch& s, const DrawParams& p, int64_t blocks, cud
     } else {
         const int grid = mlp_grid(p.n_sm, blocks);
         if (grid < 0) return -1;
-        err = launch_dependent(k_shade_mlp, grid, kMlpThreads, kMlpSmem, stream, a);
+        err = launch_dependent(k_shade_mlp, grid, kMlpThreads, mlp_smem_bytes(a.nl, a.samples), stream, a);
     }
     return err == cudaSuccess ? 1 : -1;
 }
@@ -1000,7 +1023,7 @@ int launch_mlp_eval(const float* src, int stride, int64_t n, bool exact, float4*
     } else {
         const int grid = mlp_grid(n_sm, blocks);
         if (grid < 0) return -1;
-        k_shade_mlp<<<grid, kMlpThreads, kMlpSmem, stream>>>(a);
+        k_shade_mlp<<<grid, kMlpThreads, mlp_smem_bytes(a.nl, a.samples), stream>>>(a);
     }
     return cudaGetLastError() == cudaSuccess ? 3 : -1;
 }
