@@ -40,6 +40,25 @@ using std::vector;
 
 static_assert(sizeof(Triangle) == 10 * sizeof(int), "Triangle must be 10 packed ints (face.h:6-13)");
 
+// Material keeps its texture private (material.h:11-16) and offers only sample(uv). The drop-in
+// uploads the texture itself, so it reads those two members through an explicit instantiation,
+// which may name private members (C++11 [temp.explicit] p12), without editing the reference's
+// header: member_of(Tag) returns the member pointer the instantiation was given.
+template <class Tag, typename Tag::type Member>
+struct PrivateMember {
+    friend typename Tag::type member_of(Tag) { return Member; }
+};
+struct MaterialHasTexture {
+    typedef bool Material::*type;
+    friend type member_of(MaterialHasTexture);
+};
+struct MaterialTexture {
+    typedef cimg_library::CImg<float> Material::*type;
+    friend type member_of(MaterialTexture);
+};
+template struct PrivateMember<MaterialHasTexture, &Material::has_texture>;
+template struct PrivateMember<MaterialTexture, &Material::diffuse_texture>;
+
 namespace {
 
 struct State {
@@ -238,9 +257,11 @@ void draw_frame(const vector<vec3>& model_vertices, const vector<Triangle>& face
     bool same = s.static_mesh && s.nmat == materials.size();
     for (int i = 0; i < 4; ++i) same = same && key[i] == s.key[i] && sizes[i] == s.sizes[i];
     if (!same) {
-        // Material::sample returns the constant albedo for an untextured material (material.cpp:24).
-        vector<float> kd(3 * materials.size());
+        // Material::sample returns the constant albedo for an untextured material (material.cpp:24);
+        // a textured one samples its texture (material.cpp:12-22), which librast does per fragment.
+        vector<float> kd(3 * materials.size(), 0.f);
         for (size_t i = 0; i < materials.size(); ++i) {
+            if (materials[i].*member_of(MaterialHasTexture())) continue;
             const vec3 c = materials[i].sample(vec2(0.f));
             kd[3 * i] = c.x;
             kd[3 * i + 1] = c.y;
@@ -252,6 +273,15 @@ void draw_frame(const vector<vec3>& model_vertices, const vector<Triangle>& face
                                (int64_t)vertuvs.size(), reinterpret_cast<const int32_t*>(faces.data()),
                                (int64_t)faces.size(), kd.data(), (int32_t)materials.size()),
               ctx, "rast_upload_mesh");
+        // the textures, already normalised to 0..1 by Material's constructor (material.h:21);
+        // librast's own normalisation leaves such an image as it is
+        for (size_t i = 0; i < materials.size(); ++i) {
+            if (!(materials[i].*member_of(MaterialHasTexture()))) continue;
+            const cimg_library::CImg<float>& tex = materials[i].*member_of(MaterialTexture());
+            check(rast_upload_texture(ctx, (int32_t)i, tex.data(), (uint32_t)tex.width(), (uint32_t)tex.height(),
+                                      (uint32_t)tex.spectrum()),
+                  ctx, "rast_upload_texture");
+        }
         for (int i = 0; i < 4; ++i) {
             s.key[i] = key[i];
             s.sizes[i] = sizes[i];

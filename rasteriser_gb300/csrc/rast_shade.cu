@@ -343,7 +343,7 @@ constexpr uint32_t kSmW2 = kSmW1 + kMlpHid * kMlpIn * 2;
 constexpr uint32_t kSmW3 = kSmW2 + kMlpHid * kMlpHid * 2;
 constexpr uint32_t kSmMisc = kSmW + sizeof(MlpImage);
 constexpr uint32_t kMaxSamples = 4;
-constexpr int kMlpSmemLights = 512;  // lights staged in shared memory (32 bytes each) for the checks
+constexpr int kMlpSmemLights = 512;  // lights staged in shared memory (24 bytes each) for the checks
 
 constexpr int kCheckTiles = 16;  // tiles whose checks a CTA batches before running them
 
@@ -360,23 +360,58 @@ struct MlpMisc {
     unsigned long long mbar_w;                   // the weights' bulk copy
     uint32_t tmem;
     uint32_t pad[3];
+    uint32_t rank[2][kMaxSamples];  // the checked rows of the tile, by tile parity
     CheckBatch check;
 };
 constexpr uint32_t kSmLights = kSmMisc + ((sizeof(MlpMisc) + 127) / 128) * 128;
 constexpr uint32_t kMlpSmem = kSmLights;  // without staged lights
 static_assert(kSmW1 % 16 == 0 && kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmMisc % 16 == 0, "operand alignment");
-static_assert(kMlpCtasPerSm * (kMlpSmem + 32 * kMlpSmemLights + 1024) <= 228 * 1024, "four CTAs per SM");
+static_assert(kMlpCtasPerSm * (kMlpSmem + 24 * kMlpSmemLights + 1024) <= 228 * 1024, "four CTAs per SM");
 static_assert(sizeof(MlpImage) % 16 == 0 && kSmW % 16 == 0, "bulk copy alignment");
 
 // Whether a launch stages its lights in shared memory, and its dynamic shared memory.
 RAST_HD inline bool mlp_lights_staged(int nl, int samples) { return samples > 0 && nl > 0 && nl <= kMlpSmemLights; }
 inline uint32_t mlp_smem_bytes(int nl, int samples) {
-    return kMlpSmem + (mlp_lights_staged(nl, samples) ? 32u * (uint32_t)nl : 0u);
+    return kMlpSmem + (mlp_lights_staged(nl, samples) ? 24u * (uint32_t)nl : 0u);
 }
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
     return x;
+}
+
+// The learned shader's light table in shared memory, one light per index in two arrays:
+// dirI[l] = (-dir xyz, I*r) and gb[l] = (I*g, I*b) (the products shading.cpp forms per light), so
+// the lanes of a warp read consecutive lights without bank conflicts.
+struct SmemLights {
+    float4* dirI;
+    float2* gb;
+};
+
+__device__ __forceinline__ void stage_lights_soa(const float* lights, int n, SmemLights L) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float* p = lights + 7 * (int64_t)i;
+        const float I = __ldg(p + 3);
+        L.dirI[i] = make_float4(-__ldg(p), -__ldg(p + 1), -__ldg(p + 2), mul(I, __ldg(p + 4)));
+        L.gb[i] = make_float2(mul(I, __ldg(p + 5)), mul(I, __ldg(p + 6)));
+    }
+}
+
+// The exact radiance (shading.cpp:20-34 in its order, as accumulate_lights) from the table.
+__device__ __forceinline__ float3 exact_radiance(SmemLights L, int nl, float3 nv, float3 alb) {
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+#pragma unroll 4
+    for (int l = 0; l < nl; ++l) {
+        const float4 A = L.dirI[l];
+        const float2 B = L.gb[l];
+        float cr = mul(A.w, alb.x), cg = mul(B.x, alb.y), cb = mul(B.y, alb.z);
+        const float d = add(add(mul(nv.x, A.x), mul(nv.y, A.y)), mul(nv.z, A.z));
+        const float m = gmax(0.f, d);
+        acc.x = add(acc.x, mul(mul(cr, m), kOneOverPi));
+        acc.y = add(acc.y, mul(mul(cg, m), kOneOverPi));
+        acc.z = add(acc.z, mul(mul(cb, m), kOneOverPi));
+    }
+    return acc;
 }
 
 // Epilogue of a hidden layer: this thread's 64 accumulators (TMEM columns from d) through ReLU,
@@ -408,48 +443,64 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a) {
 }
 
 // A tile whose check failed, shaded exactly (shading.cpp:20-34 in its order) by its rows.
-__device__ __forceinline__ void reshade_tile(const ShadeArgs& a, const float4* sl, uint32_t e) {
+__device__ __forceinline__ void reshade_tile(const ShadeArgs& a, const SmemLights* L, uint32_t e) {
     if (threadIdx.x >= tile_count(e)) return;
     const size_t slot = (size_t)tile_first(e) + threadIdx.x;
     const float4 g0 = a.gbuf[2 * slot], g1 = a.gbuf[2 * slot + 1];
     const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
-    uint32_t col;
-    if (sl) {
-        float3 acc = make_float3(0.f, 0.f, 0.f);
-        accumulate_lights(sl, a.nl, nv, alb, acc);
-        col = pack_rgb(acc);
-    } else {
-        col = shade_lights(a.lights, a.nl, nv, alb);
-    }
+    const uint32_t col =
+        L ? pack_rgb(exact_radiance(*L, a.nl, nv, alb)) : shade_lights(a.lights, a.nl, nv, alb);
     write_rgb(a.rgb, a.npx, __float_as_uint(g1.z), col);
 }
 
-// The checked records of a batch through the exact shader: warp w takes the pairs (tile, sample)
-// p = w, w + 4, ...; its lanes split the lights, read from shared memory when staged (sl), and add
-// their partial sums in a tree (the per-light terms of shading.cpp:24-31 summed in another order:
-// the check only estimates the error, it never produces a colour). Then each tile's largest channel
-// error decides whether it is shaded exactly, which the whole CTA does for the failing tiles. Ends
-// synchronised.
-__device__ void run_checks(const ShadeArgs& a, const float4* sl, CheckBatch& B, int nb, int n_samples,
+// The checked records of a batch against the exact shader: warp w takes the pairs (tile, sample)
+// p = w, w + 4, ...; its lanes split the lights. The check only estimates the error (it never
+// produces a colour), so it sums the per-light terms of shading.cpp:24-31 in another order and
+// with fused multiply-adds, albedo and 1/pi factored out: sum_l (I*c)_l * max(0, n . -dir_l),
+// then times albedo / pi. Then each tile's largest channel error decides whether it is shaded
+// exactly, which the whole CTA does for the failing tiles. Ends synchronised.
+__device__ void run_checks(const ShadeArgs& a, const SmemLights* L, CheckBatch& B, int nb, int n_samples,
                            unsigned long long& n_fallback, float& max_err) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __syncthreads();
-    for (int p = warp; p < nb * n_samples; p += kMlpThreads / 32) {
-        float* R = B.rec[p / n_samples][p % n_samples];
-        const float3 n = make_float3(R[0], R[1], R[2]), alb = make_float3(R[3], R[4], R[5]);
-        float x = 0.f, y = 0.f, z = 0.f;
-        for (int l = lane; l < a.nl; l += 32) {
-            const float3 c = sl ? light_term(sl, l, n, alb) : light_sum(a.lights + 7 * (int64_t)l, 1, n, alb);
-            x += c.x; y += c.y; z += c.z;
-        }
+    int p = 0;
+    for (int i = 0; i < nb; ++i)
+        for (int s = 0; s < n_samples; ++s, ++p) {
+            if ((p & 3) != warp) continue;
+            float* R = B.rec[i][s];
+            const float3 n = make_float3(R[0], R[1], R[2]);
+            float x = 0.f, y = 0.f, z = 0.f;
+            if (L) {
+                for (int l = lane; l < a.nl; l += 32) {
+                    const float4 A = L->dirI[l];
+                    const float2 G = L->gb[l];
+                    const float m = fmaxf(fmaf(n.z, A.z, fmaf(n.y, A.y, n.x * A.x)), 0.f);
+                    x = fmaf(A.w, m, x);
+                    y = fmaf(G.x, m, y);
+                    z = fmaf(G.y, m, z);
+                }
+            } else {
+                for (int l = lane; l < a.nl; l += 32) {
+                    const float* P = a.lights + 7 * (int64_t)l;
+                    const float I = __ldg(P + 3);
+                    const float m = fmaxf(-fmaf(n.z, __ldg(P + 2), fmaf(n.y, __ldg(P + 1), n.x * __ldg(P))), 0.f);
+                    x = fmaf(I * __ldg(P + 4), m, x);
+                    y = fmaf(I * __ldg(P + 5), m, y);
+                    z = fmaf(I * __ldg(P + 6), m, z);
+                }
+            }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            x += __shfl_xor_sync(kFull, x, o);
-            y += __shfl_xor_sync(kFull, y, o);
-            z += __shfl_xor_sync(kFull, z, o);
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_xor_sync(kFull, x, o);
+                y += __shfl_xor_sync(kFull, y, o);
+                z += __shfl_xor_sync(kFull, z, o);
+            }
+            if (lane == 0) {
+                R[9] = x * R[3] * kOneOverPi;
+                R[10] = y * R[4] * kOneOverPi;
+                R[11] = z * R[5] * kOneOverPi;
+            }
         }
-        if (lane == 0) { R[9] = x; R[10] = y; R[11] = z; }
-    }
     __syncthreads();
     if (threadIdx.x < (unsigned)nb) {
         float err = 0.f;
@@ -465,7 +516,7 @@ __device__ void run_checks(const ShadeArgs& a, const float4* sl, CheckBatch& B, 
     for (int i = 0; i < nb; ++i) {
         if (!B.fail[i]) continue;  // uniform: every thread reads the same flag
         if (threadIdx.x == 0) ++n_fallback;
-        reshade_tile(a, sl, B.entry[i]);
+        reshade_tile(a, L, B.entry[i]);
     }
     __syncthreads();
 }
@@ -489,7 +540,10 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
     const int row = threadIdx.x, warp = row >> 5;
     MlpMisc& M = *reinterpret_cast<MlpMisc*>(sm + kSmMisc);
     const int n_samples = a.eval_out ? 0 : min(a.samples, (int)kMaxSamples);
-    float4* sl = mlp_lights_staged(a.nl, n_samples) ? reinterpret_cast<float4*>(sm + kSmLights) : nullptr;
+    SmemLights lights_smem;
+    lights_smem.dirI = reinterpret_cast<float4*>(sm + kSmLights);
+    lights_smem.gb = reinterpret_cast<float2*>(sm + kSmLights + 16 * (size_t)max(a.nl, 0));
+    const SmemLights* sl = mlp_lights_staged(a.nl, n_samples) ? &lights_smem : nullptr;
 
     // the weights and output scale arrive by one bulk copy, the lights by plain loads (neither
     // depends on the grid this kernel may overlap with)
@@ -500,7 +554,7 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         mbar_expect_tx(mbar_w, sizeof(MlpImage));
         bulk_copy_g2s(smem_addr(sm + kSmW), a.mlp, sizeof(MlpImage), mbar_w);
     }
-    if (sl) stage_lights(a.lights, 0, a.nl, sl);
+    if (sl) stage_lights_soa(a.lights, a.nl, lights_smem);
     if (warp == 0) tmem_alloc(smem_addr(&M.tmem), kTmemCols);
     // the records and the tile list are the previous kernel's output
     asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -533,7 +587,8 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
     uint32_t phase = 0;
     unsigned long long n_tile = 0, n_fallback = 0;
     float max_err = 0.f;
-    int nb = 0;  // tiles in the check batch
+    int nb = 0;      // tiles in the check batch
+    uint32_t k = 0;  // tiles this CTA shaded
 
     while (!weights_pending && t < n_tiles) {
         const uint32_t t_next = t + stride;
@@ -544,11 +599,12 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
             g1n = a.gbuf[2 * ((size_t)tile_first(e_next) + row) + 1];
         }
         const uint32_t e_next2 = t_next + stride < n_tiles ? a.index[4 + t_next + stride] : 0u;
-        const bool valid = (uint32_t)row < count;
-        const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
-        const uint32_t pix = __float_as_uint(g1.z);
+        // the checked rows of this tile, for every thread after the barrier below (two slots by
+        // tile parity: a slot is rewritten only after every thread passed the next tile's barrier)
+        if (row == 0)
+            for (int s = 0; s < n_samples; ++s) M.rank[k & 1u][s] = sample_rank(t, s, count);
         // rows past the tile's records hold zeros: finite features whose results are not stored
-        store_features(nv, alb, lane_base + kColA);
+        store_features(make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y), lane_base + kColA);
         tc_fence_before();
         if (__syncthreads_or(failed)) break;
 
@@ -583,6 +639,9 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         tmem_ld4(lane_base + kColD, o);
         tmem_wait4(o);
         tc_fence_before();
+        const bool valid = (uint32_t)row < count;
+        const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
+        const uint32_t pix = __float_as_uint(g1.z);
         const float3 rad = make_float3(alb.x * (__uint_as_float(o[0]) * out_scale),
                                        alb.y * (__uint_as_float(o[1]) * out_scale),
                                        alb.z * (__uint_as_float(o[2]) * out_scale));
@@ -601,7 +660,7 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
             // the checked records join the batch; a failing tile is shaded again, exactly
             if (n_samples > 0) {
                 for (int s = 0; s < n_samples; ++s)
-                    if (sample_rank(t, s, count) == (uint32_t)row) {
+                    if (M.rank[k & 1u][s] == (uint32_t)row) {
                         float* R = M.check.rec[nb][s];
                         R[0] = nv.x; R[1] = nv.y; R[2] = nv.z; R[3] = alb.x; R[4] = alb.y; R[5] = alb.z;
                         R[6] = radc.x; R[7] = radc.y; R[8] = radc.z;
@@ -614,6 +673,7 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
             }
             ++n_tile;
         }
+        ++k;
         t = t_next;
         e = e_next;
         e_next = e_next2;
@@ -952,7 +1012,7 @@ static int mlp_grid(int n_sm, int64_t blocks) {
     static bool attr_set = false;  // per process: the attribute is per function, all devices alike
     if (!attr_set) {
         if (cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(kMlpSmem + 32 * kMlpSmemLights)) !=
+                                 (int)(kMlpSmem + 24 * kMlpSmemLights)) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)

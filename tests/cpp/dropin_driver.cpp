@@ -41,6 +41,22 @@ int main(int argc, char** argv) {
         !get(f, tris.data(), tris.size()) || !get(f, kd.data(), kd.size()) || !get(f, li.data(), li.size()) ||
         !get(f, frame_in.data(), frame_in.size()) || !get(f, depth_in.data(), depth_in.size()))
         return 5;
+    // optional: textures (int64 count; per texture int32 material, uint32 width, height, channels,
+    // then width*height*channels floats, planar)
+    std::vector<int32_t> tex_mat;
+    std::vector<cimg_library::CImg<float> > tex_img;
+    int64_t ntex = 0;
+    if (get(f, &ntex, 1)) {
+        for (int64_t i = 0; i < ntex; ++i) {
+            int32_t m;
+            uint32_t whc[3];
+            if (!get(f, &m, 1) || !get(f, whc, 3)) return 5;
+            cimg_library::CImg<float> img(whc[0], whc[1], 1, whc[2], 0.f);
+            if (!get(f, img.data(), (size_t)whc[0] * whc[1] * whc[2])) return 5;
+            tex_mat.push_back(m);
+            tex_img.push_back(img);
+        }
+    }
     std::fclose(f);
 
     std::vector<glm::vec3> mv, mn;
@@ -54,7 +70,12 @@ int main(int argc, char** argv) {
         faces.push_back(Triangle({t[0], t[1], t[2]}, {t[3], t[4], t[5]}, {t[6], t[7], t[8]}, t[9]));
     }
     std::vector<Material> mats;
-    for (int64_t i = 0; i < nmat; ++i) mats.push_back(Material(glm::vec3(kd[3 * i], kd[3 * i + 1], kd[3 * i + 2])));
+    for (int64_t i = 0; i < nmat; ++i) {
+        const glm::vec3 dc(kd[3 * i], kd[3 * i + 1], kd[3 * i + 2]);
+        size_t k = 0;
+        while (k < tex_mat.size() && tex_mat[k] != (int32_t)i) ++k;
+        mats.push_back(k < tex_mat.size() ? Material(dc, tex_img[k]) : Material(dc));
+    }
     std::vector<Light> lights;
     for (int64_t i = 0; i < nl; ++i) {
         const float* L = &li[7 * i];

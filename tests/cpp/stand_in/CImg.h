@@ -10,6 +10,7 @@ class CImg {
     std::vector<T> buf_;
     unsigned w_, h_, d_, s_;
 public:
+    CImg() : w_(0), h_(0), d_(0), s_(0) {}
     CImg(unsigned w, unsigned h, unsigned d, unsigned s, const T& value)
         : buf_((size_t)w * h * d * s, value), w_(w), h_(h), d_(d), s_(s) {}
     T* data() { return buf_.data(); }

@@ -56,7 +56,9 @@ def test_reference_renderer_links_against_the_drop_in():
     assert " T draw_frame(" in dyn
 
 
-def write_scene(path, sc, frame=None, depth=None, static_mesh=False):
+def write_scene(path, sc, frame=None, depth=None, static_mesh=False, textures=()):
+    """The driver's input; textures: (material, planar (channels, height, width) float32) pairs,
+    as CImg loads an image."""
     W, H = sc.width, sc.height
     frame = np.zeros((3, H, W), np.uint8) if frame is None else frame
     depth = np.ones((H, W), np.float32) if depth is None else depth
@@ -69,6 +71,11 @@ def write_scene(path, sc, frame=None, depth=None, static_mesh=False):
         for a, dt in ((sc.pos, np.float32), (sc.nrm, np.float32), (sc.uv, np.float32), (sc.tris, np.int32),
                       (sc.kd, np.float32), (sc.lights, np.float32), (frame, np.uint8), (depth, np.float32)):
             fh.write(np.ascontiguousarray(a, dt).tobytes())
+        fh.write(struct.pack("<q", len(textures)))
+        for m, img in textures:
+            c, h, w = img.shape
+            fh.write(struct.pack("<i3I", m, w, h, c))
+            fh.write(np.ascontiguousarray(img, np.float32).tobytes())
 
 
 def read_out(path, sc):
@@ -127,3 +134,25 @@ def test_dropin_keeps_untouched_pixels(tmp_path):
     fp, dpp, _, _ = oracle.Port().draw(sc, cam, nm, lights, frame, depth)
     assert np.array_equal(dp.view(np.uint32), dpp.view(np.uint32))
     assert np.abs(fr.astype(int) - fp.astype(int)).max() <= 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["square", "sphere_16bit", "textured_and_plain"])
+def test_dropin_textured_materials(tmp_path, case):
+    """Textured Materials (material.cpp:12-22) through the drop-in: the texture each Material
+    holds is uploaded and sampled per fragment, as the port samples it."""
+    from test_textures import textured_cases, normalised
+    from rasteriser_gb300 import abi
+    import oracle
+    drv = build_driver()
+    sc, _, raws = textured_cases(tmp_path)[case]
+    tex = [(m, np.moveaxis(r.astype(np.float32), 2, 0)) for m, r in enumerate(raws) if r is not None]
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    write_scene(inp, sc, textures=tex)
+    r = subprocess.run([drv, inp, out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    fr, dp, _ = read_out(out, sc)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    fp, dpp, _, _ = oracle.Port().draw(sc, cam, nm, lights, textures=[normalised(x) for x in raws])
+    assert np.array_equal(dp.view(np.uint32), dpp.view(np.uint32))
+    assert np.array_equal(fr, fp)
