@@ -454,7 +454,7 @@ __device__ __forceinline__ void reshade_tile(const ShadeArgs& a, const SmemLight
 }
 
 // The checked records of a batch against the exact shader: warp w takes the pairs (tile, sample)
-// p = w, w + 4, ...; its lanes split the lights. The check only estimates the error (it never
+// p = w, w + 4, ..., four at a time; its lanes split the lights. The check only estimates the error (it never
 // produces a colour), so it sums the per-light terms of shading.cpp:24-31 in another order and
 // with fused multiply-adds, albedo and 1/pi factored out: sum_l (I*c)_l * max(0, n . -dir_l),
 // then times albedo / pi. Then each tile's largest channel error decides whether it is shaded
@@ -463,44 +463,63 @@ __device__ void run_checks(const ShadeArgs& a, const SmemLights* L, CheckBatch& 
                            unsigned long long& n_fallback, float& max_err) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __syncthreads();
-    int p = 0;
-    for (int i = 0; i < nb; ++i)
-        for (int s = 0; s < n_samples; ++s, ++p) {
-            if ((p & 3) != warp) continue;
-            float* R = B.rec[i][s];
-            const float3 n = make_float3(R[0], R[1], R[2]);
-            float x = 0.f, y = 0.f, z = 0.f;
-            if (L) {
-                for (int l = lane; l < a.nl; l += 32) {
-                    const float4 A = L->dirI[l];
-                    const float2 G = L->gb[l];
-                    const float m = fmaxf(fmaf(n.z, A.z, fmaf(n.y, A.y, n.x * A.x)), 0.f);
-                    x = fmaf(A.w, m, x);
-                    y = fmaf(G.x, m, y);
-                    z = fmaf(G.y, m, z);
-                }
-            } else {
-                for (int l = lane; l < a.nl; l += 32) {
-                    const float* P = a.lights + 7 * (int64_t)l;
-                    const float I = __ldg(P + 3);
-                    const float m = fmaxf(-fmaf(n.z, __ldg(P + 2), fmaf(n.y, __ldg(P + 1), n.x * __ldg(P))), 0.f);
-                    x = fmaf(I * __ldg(P + 4), m, x);
-                    y = fmaf(I * __ldg(P + 5), m, y);
-                    z = fmaf(I * __ldg(P + 6), m, z);
-                }
-            }
+    // warp w takes the pairs p = w, w + 4, ... four at a time, so one pass over the lights serves
+    // four checked records (twelve independent sums)
+    constexpr int G = 4;
+    const int np = nb * n_samples;
+    for (int p0 = warp; p0 < np; p0 += G * (kMlpThreads / 32)) {
+        float* R[G];
+        float3 n[G];
+        float acc[G][3];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                x += __shfl_xor_sync(kFull, x, o);
-                y += __shfl_xor_sync(kFull, y, o);
-                z += __shfl_xor_sync(kFull, z, o);
+        for (int j = 0; j < G; ++j) {
+            const int p = min(p0 + j * (kMlpThreads / 32), np - 1);  // past the end: a repeat, not stored
+            R[j] = B.rec[p / n_samples][p % n_samples];
+            n[j] = make_float3(R[j][0], R[j][1], R[j][2]);
+            acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
+        }
+        if (L) {
+            for (int l = lane; l < a.nl; l += 32) {
+                const float4 A = L->dirI[l];
+                const float2 C = L->gb[l];
+#pragma unroll
+                for (int j = 0; j < G; ++j) {
+                    const float m = fmaxf(fmaf(n[j].z, A.z, fmaf(n[j].y, A.y, n[j].x * A.x)), 0.f);
+                    acc[j][0] = fmaf(A.w, m, acc[j][0]);
+                    acc[j][1] = fmaf(C.x, m, acc[j][1]);
+                    acc[j][2] = fmaf(C.y, m, acc[j][2]);
+                }
             }
-            if (lane == 0) {
-                R[9] = x * R[3] * kOneOverPi;
-                R[10] = y * R[4] * kOneOverPi;
-                R[11] = z * R[5] * kOneOverPi;
+        } else {
+            for (int l = lane; l < a.nl; l += 32) {
+                const float* P = a.lights + 7 * (int64_t)l;
+                const float I = __ldg(P + 3);
+                const float4 A = make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4));
+                const float2 C = make_float2(I * __ldg(P + 5), I * __ldg(P + 6));
+#pragma unroll
+                for (int j = 0; j < G; ++j) {
+                    const float m = fmaxf(fmaf(n[j].z, A.z, fmaf(n[j].y, A.y, n[j].x * A.x)), 0.f);
+                    acc[j][0] = fmaf(A.w, m, acc[j][0]);
+                    acc[j][1] = fmaf(C.x, m, acc[j][1]);
+                    acc[j][2] = fmaf(C.y, m, acc[j][2]);
+                }
             }
         }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int j = 0; j < G; ++j)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) acc[j][c] += __shfl_xor_sync(kFull, acc[j][c], o);
+        if (lane == 0)
+#pragma unroll
+            for (int j = 0; j < G; ++j)
+                if (p0 + j * (kMlpThreads / 32) < np) {
+                    R[j][9] = acc[j][0] * R[j][3] * kOneOverPi;
+                    R[j][10] = acc[j][1] * R[j][4] * kOneOverPi;
+                    R[j][11] = acc[j][2] * R[j][5] * kOneOverPi;
+                }
+    }
     __syncthreads();
     if (threadIdx.x < (unsigned)nb) {
         float err = 0.f;
