@@ -465,7 +465,8 @@ rast_status rast_set_option(rast_ctx* c, int option, int64_t value) {
             c->tile = (uint32_t)value;
             return RAST_OK;
         case RAST_OPT_ROW_CHUNK:
-            if (value != 4 && value != 8) return fail(c, RAST_ERR_INVALID_ARG, "row chunk must be 4 or 8");
+            if (value != 4 && value != 8 && value != 32)
+                return fail(c, RAST_ERR_INVALID_ARG, "row chunk must be 4, 8 or 32");
             c->row_chunk = (uint32_t)value;
             return RAST_OK;
         case RAST_OPT_STAGE_TIMING:

@@ -279,7 +279,7 @@ extern "C" rast_status rast_autotune(rast_ctx* c, const rast_frame_desc* frames,
     DeviceGuard g(c->device);
     const uint32_t tiles[3] = {8, 16, 32};
     const uint32_t smalls[3] = {256, 1024, 4096};
-    const uint32_t chunks[2] = {4, 8};
+    const uint32_t chunks[3] = {4, 8, 32};
     cudaEvent_t t0, t1;
     RAST_CUDA(c, cudaEventCreate(&t0));
     RAST_CUDA(c, cudaEventCreate(&t1));

@@ -104,7 +104,7 @@ struct DrawParams {
     uint32_t flags;
     uint32_t small_max;     // bounding boxes up to this many pixels take the per-triangle path
     uint32_t tile;          // tile edge: 8, 16, 32
-    uint32_t row_chunk;     // pixels per work item of the per-triangle path: 4 or 8
+    uint32_t row_chunk;     // pixels per work item of the per-triangle path: 4, 8 or 32 (whole rows)
     uint32_t tiles_x, tiles_y;
     int32_t n_sm;           // streaming multiprocessors of the device
     int32_t nl;

@@ -291,8 +291,8 @@ struct SetupStage {
     uint32_t incl[32];
     int slot[32];
     // Ring of work items with pixels the early reject could not rule out: first pixel
-    // (x | y << 16), and owning lane | candidate mask << 8.
-    uint32_t q_xy[64], q_om[64];
+    // (x | y << 16), owning lane, and the candidate mask (bit b: pixel x + b).
+    uint32_t q_xy[64], q_om[64], q_m[64];
 };
 
 struct SetupArgs {
@@ -406,8 +406,16 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
             S.rec[lane][0] = make_float4(T.x0, T.y0, T.x1, T.y1);
             S.rec[lane][1] = make_float4(T.x2, T.y2, mul(sg, T.area), T.nthr);
             S.rec[lane][2] = make_float4(mul(sg, T.d12x), mul(sg, T.d12y), mul(sg, T.d20x), mul(sg, T.d20y));
-            S.rec[lane][3] = make_float4(mul(sg, T.d01x), mul(sg, T.d01y), 0.f, 0.f);
-            S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, 0.f);
+            // Whole-row items (kRowChunk 32) also stage the reciprocals of the three edges' x
+            // coefficients, which bound the row's candidate span (see below).
+            float r0 = 0.f, r1 = 0.f, r2 = 0.f;
+            if (kRowChunk == 32u) {
+                r0 = __frcp_rn(mul(sg, T.d12y));
+                r1 = __frcp_rn(mul(sg, T.d20y));
+                r2 = __frcp_rn(mul(sg, T.d01y));
+            }
+            S.rec[lane][3] = make_float4(mul(sg, T.d01x), mul(sg, T.d01y), r0, r1);
+            S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, r2);
             S.tlx[lane] = tlx;
             S.tly[lane] = tly;
             S.brx[lane] = brx;
@@ -422,9 +430,9 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
             // Exact test, depth and atomic for the masked pixels of ring entry `e`
             // (drawing.cpp:108-121).
             auto finish = [&](uint32_t e) {
-                const uint32_t om = S.q_om[e], xy = S.q_xy[e];
-                const uint32_t j = om & 31u;
-                uint32_t mask = om >> 8;
+                const uint32_t xy = S.q_xy[e];
+                const uint32_t j = S.q_om[e] & 31u;
+                uint32_t mask = S.q_m[e];
                 const uint32_t x0 = xy & 0xFFFFu, y = xy >> 16;
                 const float4 q0 = S.rec[j][0], q1 = S.rec[j][1], q2 = S.rec[j][2], q3 = S.rec[j][3], q4 = S.rec[j][4];
                 const float py = (float)y;
@@ -467,7 +475,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                     const uint32_t ocpr = S.cpr[owner];
                     const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
                     x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
-                    const uint32_t x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
+                    uint32_t x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
                     y = S.tly[owner] + row;
                     bool live = true;
 #ifdef RAST_CHECKED
@@ -480,12 +488,54 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                     if (live) {
                         const float4 q0 = S.rec[owner][0], q1 = S.rec[owner][1], q2 = S.rec[owner][2],
                                      q3 = S.rec[owner][3];
-                        const float py = (float)y, px_lo = (float)x_lo;
+                        const float py = (float)y;
                         const float p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
                         const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
                         const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
-                        const uint32_t n_px = x_hi - x_lo + 1u;
-                        c_tested += n_px;
+                        c_tested += x_hi - x_lo + 1u;  // the reference tests every pixel of the row
+                        if (kRowChunk == 32u) {
+                            // Whole rows: only the pixels within one pixel of the row's span can
+                            // pass. Along the row each staged edge value is f = P - B*(px - X), so
+                            // f >= 0 bounds px by X + P/B (above when B > 0, below when B < 0).
+                            // The bound is computed to within 0.02 px when |X| and |P/B| are at most
+                            // 2^16, and where it is 0.98 px or more away the reference's rounded f
+                            // keeps its sign with |f| >= 0.9*|B|, so with |B| >= 2^-100 and a
+                            // finite area the barycentric f/|area| is negative and nonzero: the
+                            // pixel is outside. Edges that miss these conditions bound nothing; a
+                            // B of zero gives f = P for the whole row. Rows of triangles without
+                            // the early reject (nthr = -inf) keep every pixel.
+                            float lo = -INFINITY, hi = INFINITY;
+                            bool empty = false;
+                            if (q1.w > -INFINITY) {
+                                const float r2 = S.rec[owner][4].w;
+                                const float P[3] = {p0, p1, p2}, B[3] = {q2.y, q2.w, q3.y};
+                                const float X[3] = {q0.z, q1.x, q0.x}, R[3] = {q3.z, q3.w, r2};
+#pragma unroll
+                                for (int k = 0; k < 3; ++k) {
+                                    if (B[k] == 0.f) {
+                                        empty = empty || P[k] < q1.w;
+                                        continue;
+                                    }
+                                    const float off = P[k] * R[k];
+                                    if (!(fabsf(B[k]) >= 0x1p-100f && fabsf(X[k]) <= 0x1p16f && fabsf(off) <= 0x1p16f))
+                                        continue;
+                                    const float c = X[k] + off;
+                                    if (B[k] > 0.f) hi = fminf(hi, c);
+                                    else lo = fmaxf(lo, c);
+                                }
+                            }
+                            const float flo = fmaxf(lo - 1.f, (float)x_lo), fhi = fminf(hi + 1.f, (float)x_hi);
+                            if (empty || !(flo <= fhi)) {
+                                x_hi = x_lo;
+                                live = false;
+                            } else {
+                                x_lo = (uint32_t)ceilf(flo);
+                                x_hi = (uint32_t)floorf(fhi);
+                                live = x_lo <= x_hi;
+                            }
+                        }
+                        const float px_lo = (float)x_lo;
+                        const uint32_t n_px = live ? x_hi - x_lo + 1u : 0u;
                         // Two pixels per instruction: __fadd2_rn / __fmul2_rn round each component
                         // exactly as __fadd_rn / __fmul_rn, and a - b is a + (-b) bit for bit, so
                         //   e = p - d.y * (px - a.x)  ==  p + -(d.y * (px + -a.x)).
@@ -494,8 +544,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                                      NX0 = make_float2(-q0.x, -q0.x);
                         const float2 B0 = make_float2(q2.y, q2.y), B1 = make_float2(q2.w, q2.w),
                                      B2 = make_float2(q3.y, q3.y);
-#pragma unroll
-                        for (uint32_t sx = 0; sx < kRowChunk; sx += 2) {
+#pragma unroll(kRowChunk == 32u ? 1 : kRowChunk / 2)
+                        for (uint32_t sx = 0; sx < (kRowChunk == 32u ? n_px : kRowChunk); sx += 2) {
                             // pixel centres px_lo + sx, + sx + 1: exact, integers below 2^24
                             const float2 px = make_float2(add(px_lo, (float)sx), add(px_lo, (float)(sx + 1)));
                             const float2 t0 = __fmul2_rn(B0, __fadd2_rn(px, NX1));
@@ -516,7 +566,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_raster(SetupArgs a) {
                 if (has) {
                     const uint32_t e = (q_head + q_count + __popc(m & lt_mask)) & 63u;
                     S.q_xy[e] = x_lo | (y << 16);
-                    S.q_om[e] = (uint32_t)owner | (mask << 8);
+                    S.q_om[e] = (uint32_t)owner;
+                    S.q_m[e] = mask;
                 }
                 q_count += __popc(m);
                 if (q_count >= 32u) {
@@ -1175,7 +1226,8 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     sa.stats = s.stats;
     if (mesh.ntri > 0) {
         const unsigned blocks = (unsigned)((mesh.ntri + kSetupThreads - 1) / kSetupThreads);
-        if (p.row_chunk == 8) k_setup_raster<8><<<blocks, kSetupThreads, 0, stream>>>(sa);
+        if (p.row_chunk == 32) k_setup_raster<32><<<blocks, kSetupThreads, 0, stream>>>(sa);
+        else if (p.row_chunk == 8) k_setup_raster<8><<<blocks, kSetupThreads, 0, stream>>>(sa);
         else k_setup_raster<4><<<blocks, kSetupThreads, 0, stream>>>(sa);
         ++launches;
     }

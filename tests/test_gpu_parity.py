@@ -64,7 +64,8 @@ def random_scenes():
 
 
 @pytest.mark.parametrize("idx", range(len(random_scenes())))
-@pytest.mark.parametrize("tile,small_max,row_chunk", [(16, 4096, 4), (8, 1, 4), (32, 65536, 8), (16, 16, 8)])
+@pytest.mark.parametrize("tile,small_max,row_chunk", [(16, 4096, 4), (8, 1, 4), (32, 65536, 8), (16, 16, 8),
+                                                      (16, 4096, 32), (8, 65536, 32)])
 def test_against_port(renderer, port, idx, tile, small_max, row_chunk):
     sc = random_scenes()[idx]
     renderer.set_option(abi.OPT_TILE_SIZE, tile)
@@ -206,10 +207,12 @@ def test_invalid_arguments(renderer):
         renderer.set_lights(np.zeros((5000, 7), np.float32))
 
 
+@pytest.mark.parametrize("row_chunk", [8, 32])
 @pytest.mark.parametrize("key", sorted(golden_io.full_size()))
-def test_full_size_against_reference_digest(renderer, port, key):
+def test_full_size_against_reference_digest(renderer, port, key, row_chunk):
     """Full-size frames (1,046,528 triangles at 1920x1080; 4M at 3840x2160) against the digests of
-    the reference's own output, and against the port run here."""
+    the reference's own output, and against the port run here; per-triangle rows in chunks of 8
+    pixels and as whole rows clipped to the triangles' spans."""
     import hashlib
     e = golden_io.full_size()[key]
     sc = golden_io.full_size_scene(e)
@@ -218,7 +221,11 @@ def test_full_size_against_reference_digest(renderer, port, key):
     cam = np.array(e["camera"], np.float32)
     nm = np.array(e["normal"], np.float32)
     lights = np.array(e["lights7"], np.float32)
-    fg, dg, ig = gpu_draw(renderer, sc, cam, nm, lights)
+    renderer.set_option(abi.OPT_ROW_CHUNK, row_chunk)
+    try:
+        fg, dg, ig = gpu_draw(renderer, sc, cam, nm, lights)
+    finally:
+        renderer.set_option(abi.OPT_ROW_CHUNK, 8)
     assert hashlib.sha256(np.ascontiguousarray(dg).tobytes()).hexdigest() == e["depth"]
     assert hashlib.sha256(np.ascontiguousarray(fg).tobytes()).hexdigest() == e["frame_rgb"]
     fp, dp, ip, st = port.draw(sc, cam, nm, lights)
