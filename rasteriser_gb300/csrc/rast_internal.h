@@ -90,8 +90,14 @@ struct FrameScratch {
 // to finish lists the shading tiles (rast_tiles.cuh), up to 128 records of one block each.
 constexpr int kShadeTile = 128;
 constexpr int kShadeBlock = 1024;
-// shade_index layout: [0] fragments, [1] tiles, [2..3] unused, then up to 8 tile entries per block.
-inline int64_t kShadeIndexWords(int64_t blocks) { return 4 + 8 * blocks; }
+// shade_index layout: [0] fragments, [1] tiles, [2..3] unused, [4 .. 4 + blocks] the exclusive
+// prefix of the blocks' record counts (blocks + 1 words), then, from the next multiple of 4 words,
+// one 16-byte descriptor per tile (at most 8 tiles per block's worth of records).
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline int64_t kShadeTileDescWord(int64_t blocks) { return (5 + blocks + 3) / 4 * 4; }
+inline int64_t kShadeIndexWords(int64_t blocks) { return kShadeTileDescWord(blocks) + 4 * 8 * blocks; }
 // counters word counting the resolve blocks that finished (deferred shading)
 constexpr int kResolveTicket = 5;
 // shade_stats: [0] tiles shaded by the MLP, [1] tiles sent to the exact shader, [2] fragments

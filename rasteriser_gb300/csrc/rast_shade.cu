@@ -31,7 +31,8 @@ constexpr unsigned kFull = 0xFFFFFFFFu;
 
 struct ShadeArgs {
     const float4* gbuf;
-    const uint32_t* index;   // [0] fragments, [1] tiles, then the tile entries
+    const uint32_t* index;   // the tile list (rast_tiles.cuh)
+    uint32_t n_blocks;       // 1024-pixel blocks the list covers
     int64_t npx;
     const float* lights;
     int32_t nl;
@@ -45,9 +46,6 @@ struct ShadeArgs {
     float* eval_out;  // evaluation mode: radiance floats per record (pixel field = record index)
 };
 
-// First record of a tile and its record count.
-__device__ __forceinline__ uint32_t tile_first(uint32_t entry) { return (entry >> 8) * (uint32_t)kShadeTile; }
-__device__ __forceinline__ uint32_t tile_count(uint32_t entry) { return (entry & 0xFFu) + 1u; }
 
 __device__ __forceinline__ void write_rgb(uint8_t* rgb, int64_t npx, uint32_t p, uint32_t col) {
     rgb[p] = (uint8_t)(col & 0xFFu);
@@ -110,9 +108,9 @@ __global__ void __launch_bounds__(kExactThreads, kExactCtasPerSm) k_shade_exact(
     const uint32_t n_tiles = a.index[1];
     __syncthreads();
     for (uint32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-        const uint32_t e = a.index[4 + t];
-        const bool valid = r < tile_count(e);
-        const size_t slot = (size_t)tile_first(e) + r;
+        const bool valid = r < shade_tile_count(a.index, t);
+        const size_t slot =
+            valid ? shade_record_slot(a.index, a.n_blocks, shade_tile_desc(a.index, a.n_blocks, t), t, r) : 0;
         float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f), g1 = g0;
         if (valid) {
             g0 = a.gbuf[2 * slot];
@@ -350,7 +348,7 @@ constexpr int kCheckTiles = 16;  // tiles whose checks a CTA batches before runn
 // The checked records of the tiles a CTA shaded since its last check batch: the record, the MLP's
 // clamped radiance, then the exact radiance.
 struct CheckBatch {
-    uint32_t entry[kCheckTiles];
+    uint32_t tile[kCheckTiles];
     float rec[kCheckTiles][kMaxSamples][12];  // normal xyz, albedo rgb, MLP rgb, exact rgb
     uint32_t fail[kCheckTiles];
 };
@@ -443,9 +441,9 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a) {
 }
 
 // A tile whose check failed, shaded exactly (shading.cpp:20-34 in its order) by its rows.
-__device__ __forceinline__ void reshade_tile(const ShadeArgs& a, const SmemLights* L, uint32_t e) {
-    if (threadIdx.x >= tile_count(e)) return;
-    const size_t slot = (size_t)tile_first(e) + threadIdx.x;
+__device__ __forceinline__ void reshade_tile(const ShadeArgs& a, const SmemLights* L, uint32_t t) {
+    if (threadIdx.x >= shade_tile_count(a.index, t)) return;
+    const size_t slot = shade_record_slot(a.index, a.n_blocks, shade_tile_desc(a.index, a.n_blocks, t), t, threadIdx.x);
     const float4 g0 = a.gbuf[2 * slot], g1 = a.gbuf[2 * slot + 1];
     const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
     const uint32_t col =
@@ -535,7 +533,7 @@ __device__ void run_checks(const ShadeArgs& a, const SmemLights* L, CheckBatch& 
     for (int i = 0; i < nb; ++i) {
         if (!B.fail[i]) continue;  // uniform: every thread reads the same flag
         if (threadIdx.x == 0) ++n_fallback;
-        reshade_tile(a, L, B.entry[i]);
+        reshade_tile(a, L, B.tile[i]);
     }
     __syncthreads();
 }
@@ -580,16 +578,17 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
 
     const uint32_t n_tiles = a.index[1];
     // Tiles t = blockIdx.x + k * gridDim.x. This thread's record of the current tile is fetched
-    // one tile ahead and the tile list entry two tiles ahead, so neither load waits on the way.
+    // one tile ahead and the tile's descriptor two tiles ahead, so neither load waits on the way.
     const uint32_t stride = gridDim.x;
+    const uint4 d_none = make_uint4(0u, 0u, 0u, 0u);
     uint32_t t = blockIdx.x;
-    uint32_t e = t < n_tiles ? a.index[4 + t] : 0u;
-    uint32_t e_next = t + stride < n_tiles ? a.index[4 + t + stride] : 0u;
-    uint32_t count = t < n_tiles ? tile_count(e) : 0u;
+    uint32_t count = t < n_tiles ? shade_tile_count(a.index, t) : 0u;
+    uint4 d_next = t + stride < n_tiles ? shade_tile_desc(a.index, a.n_blocks, t + stride) : d_none;
     float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f), g1 = g0;
     if ((uint32_t)row < count) {
-        g0 = a.gbuf[2 * ((size_t)tile_first(e) + row)];
-        g1 = a.gbuf[2 * ((size_t)tile_first(e) + row) + 1];
+        const size_t slot = shade_record_slot(a.index, a.n_blocks, shade_tile_desc(a.index, a.n_blocks, t), t, row);
+        g0 = a.gbuf[2 * slot];
+        g1 = a.gbuf[2 * slot + 1];
     }
     tc_fence_before();
     __syncthreads();
@@ -611,13 +610,15 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
 
     while (!weights_pending && t < n_tiles) {
         const uint32_t t_next = t + stride;
-        const uint32_t count_next = t_next < n_tiles ? tile_count(e_next) : 0u;
+        const uint32_t count_next = t_next < n_tiles ? shade_tile_count(a.index, t_next) : 0u;
         float4 g0n = make_float4(0.f, 0.f, 0.f, 0.f), g1n = g0n;
         if ((uint32_t)row < count_next) {
-            g0n = a.gbuf[2 * ((size_t)tile_first(e_next) + row)];
-            g1n = a.gbuf[2 * ((size_t)tile_first(e_next) + row) + 1];
+            const size_t slot = shade_record_slot(a.index, a.n_blocks, d_next, t_next, row);
+            g0n = a.gbuf[2 * slot];
+            g1n = a.gbuf[2 * slot + 1];
         }
-        const uint32_t e_next2 = t_next + stride < n_tiles ? a.index[4 + t_next + stride] : 0u;
+        // the descriptor two tiles ahead
+        const uint4 d_next2 = t_next + stride < n_tiles ? shade_tile_desc(a.index, a.n_blocks, t_next + stride) : d_none;
         // the checked rows of this tile, for every thread after the barrier below (two slots by
         // tile parity: a slot is rewritten only after every thread passed the next tile's barrier)
         if (row == 0)
@@ -684,7 +685,7 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
                         R[0] = nv.x; R[1] = nv.y; R[2] = nv.z; R[3] = alb.x; R[4] = alb.y; R[5] = alb.z;
                         R[6] = radc.x; R[7] = radc.y; R[8] = radc.z;
                     }
-                if (row == 0) M.check.entry[nb] = e;
+                if (row == 0) M.check.tile[nb] = t;
                 if (++nb == kCheckTiles) {
                     run_checks(a, sl, M.check, nb, n_samples, n_fallback, max_err);
                     nb = 0;
@@ -694,9 +695,8 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         }
         ++k;
         t = t_next;
-        e = e_next;
-        e_next = e_next2;
         count = count_next;
+        d_next = d_next2;
         g0 = g0n;
         g1 = g1n;
     }
@@ -1013,6 +1013,7 @@ int grid_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads)
 static ShadeArgs shade_args(const FrameScratch& s, const DrawParams& p) {
     ShadeArgs a;
     a.gbuf = s.gbuf;
+    a.n_blocks = 0;
     a.index = s.shade_index;
     a.npx = (int64_t)p.width * p.height;
     a.lights = p.lights;
@@ -1066,6 +1067,7 @@ static cudaError_t launch_dependent(Kernel kernel, int grid, int threads, uint32
 
 int launch_shade(const FrameScratch& s, const DrawParams& p, int64_t blocks, cudaStream_t stream) {
     ShadeArgs a = shade_args(s, p);
+    a.n_blocks = (uint32_t)blocks;
     cudaError_t err;
     if (p.shader == 1) {
         err = launch_dependent(k_shade_exact, exact_grid(p.n_sm, blocks), kExactThreads, 0, stream, a);
@@ -1087,6 +1089,7 @@ int launch_mlp_eval(const float* src, int stride, int64_t n, bool exact, float4*
     ShadeArgs a;
     a.gbuf = gbuf;
     a.index = index;
+    a.n_blocks = (uint32_t)blocks;
     a.npx = 0;
     a.lights = lights;
     a.nl = nl;

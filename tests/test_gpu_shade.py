@@ -212,9 +212,8 @@ def test_learned_frame(rnd, port, trained):
     assert np.all(diff[:, ~cov] == 0)
     assert diff.max() <= RGB_TOL
     assert diff[:, cov].mean() <= MEAN_TOL
-    # tiles: up to 128 covered pixels of one 1024-pixel block (raster order) each
-    flat = np.concatenate([cov.ravel(), np.zeros(-cov.size % 1024, bool)]).reshape(-1, 1024)
-    assert st["tiles"] == int(((flat.sum(axis=1) + 127) // 128).sum())
+    # tiles: 128 consecutive covered pixels (in block order, which is raster order) each
+    assert st["tiles"] == (int(cov.sum()) + 127) // 128
 
 
 def test_learned_fallback_gives_exact_colour(rnd, port, trained):
