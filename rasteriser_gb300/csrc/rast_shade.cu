@@ -452,7 +452,7 @@ __device__ __forceinline__ void reshade_tile(const ShadeArgs& a, const SmemLight
 }
 
 // The checked records of a batch against the exact shader: warp w takes the pairs (tile, sample)
-// p = w, w + 4, ..., four at a time; its lanes split the lights. The check only estimates the error (it never
+// p = w, w + 4, ..., four at a time (two packed pairs); its lanes split the lights. The check only estimates the error (it never
 // produces a colour), so it sums the per-light terms of shading.cpp:24-31 in another order and
 // with fused multiply-adds, albedo and 1/pi factored out: sum_l (I*c)_l * max(0, n . -dir_l),
 // then times albedo / pi. Then each tile's largest channel error decides whether it is shaded
@@ -466,57 +466,63 @@ __device__ void run_checks(const ShadeArgs& a, const SmemLights* L, CheckBatch& 
     constexpr int G = 4;
     const int np = nb * n_samples;
     for (int p0 = warp; p0 < np; p0 += G * (kMlpThreads / 32)) {
-        float* R[G];
-        float3 n[G];
-        float acc[G][3];
+        // records j = 0, 1 and j = 2, 3 in the two halves of packed pairs
+        float2 nx[2], ny[2], nz[2], ar[2], ag[2], ab[2];
 #pragma unroll
-        for (int j = 0; j < G; ++j) {
-            const int p = min(p0 + j * (kMlpThreads / 32), np - 1);  // past the end: a repeat, not stored
-            R[j] = B.rec[p / n_samples][p % n_samples];
-            n[j] = make_float3(R[j][0], R[j][1], R[j][2]);
-            acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
+        for (int h = 0; h < 2; ++h) {
+            const int pa = min(p0 + (2 * h) * (kMlpThreads / 32), np - 1);  // past the end: a repeat, not stored
+            const int pb = min(p0 + (2 * h + 1) * (kMlpThreads / 32), np - 1);
+            const float* Ra = B.rec[pa / n_samples][pa % n_samples];
+            const float* Rb = B.rec[pb / n_samples][pb % n_samples];
+            nx[h] = make_float2(Ra[0], Rb[0]);
+            ny[h] = make_float2(Ra[1], Rb[1]);
+            nz[h] = make_float2(Ra[2], Rb[2]);
+            ar[h] = ag[h] = ab[h] = make_float2(0.f, 0.f);
         }
-        if (L) {
-            for (int l = lane; l < a.nl; l += 32) {
-                const float4 A = L->dirI[l];
-                const float2 C = L->gb[l];
+        auto light = [&](float4 A, float2 C) {
+            const float2 ax = make_float2(A.x, A.x), ay = make_float2(A.y, A.y), az = make_float2(A.z, A.z);
+            const float2 cr = make_float2(A.w, A.w), cg = make_float2(C.x, C.x), cb = make_float2(C.y, C.y);
 #pragma unroll
-                for (int j = 0; j < G; ++j) {
-                    const float m = fmaxf(fmaf(n[j].z, A.z, fmaf(n[j].y, A.y, n[j].x * A.x)), 0.f);
-                    acc[j][0] = fmaf(A.w, m, acc[j][0]);
-                    acc[j][1] = fmaf(C.x, m, acc[j][1]);
-                    acc[j][2] = fmaf(C.y, m, acc[j][2]);
-                }
+            for (int h = 0; h < 2; ++h) {
+                float2 d = __ffma2_rn(nz[h], az, __ffma2_rn(ny[h], ay, __fmul2_rn(nx[h], ax)));
+                d = make_float2(fmaxf(d.x, 0.f), fmaxf(d.y, 0.f));
+                ar[h] = __ffma2_rn(cr, d, ar[h]);
+                ag[h] = __ffma2_rn(cg, d, ag[h]);
+                ab[h] = __ffma2_rn(cb, d, ab[h]);
             }
+        };
+        if (L) {
+            for (int l = lane; l < a.nl; l += 32) light(L->dirI[l], L->gb[l]);
         } else {
             for (int l = lane; l < a.nl; l += 32) {
                 const float* P = a.lights + 7 * (int64_t)l;
                 const float I = __ldg(P + 3);
-                const float4 A = make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4));
-                const float2 C = make_float2(I * __ldg(P + 5), I * __ldg(P + 6));
-#pragma unroll
-                for (int j = 0; j < G; ++j) {
-                    const float m = fmaxf(fmaf(n[j].z, A.z, fmaf(n[j].y, A.y, n[j].x * A.x)), 0.f);
-                    acc[j][0] = fmaf(A.w, m, acc[j][0]);
-                    acc[j][1] = fmaf(C.x, m, acc[j][1]);
-                    acc[j][2] = fmaf(C.y, m, acc[j][2]);
-                }
+                light(make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4)),
+                      make_float2(I * __ldg(P + 5), I * __ldg(P + 6)));
             }
         }
+        // Sum the twelve values over the lanes by halving: at each level a lane keeps half of its
+        // values and adds its partner's copy of them, so lanes 2k and 2k + 1 end with value k
+        // (value 3j + c: record j, channel c).
+        float v[16] = {ar[0].x, ag[0].x, ab[0].x, ar[0].y, ag[0].y, ab[0].y,
+                       ar[1].x, ag[1].x, ab[1].x, ar[1].y, ag[1].y, ab[1].y, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
+        for (int lvl = 0; lvl < 4; ++lvl) {
+            const int half = 8 >> lvl, o = 16 >> lvl;
+            const bool up = (lane & o) != 0;
 #pragma unroll
-            for (int j = 0; j < G; ++j)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) acc[j][c] += __shfl_xor_sync(kFull, acc[j][c], o);
-        if (lane == 0)
-#pragma unroll
-            for (int j = 0; j < G; ++j)
-                if (p0 + j * (kMlpThreads / 32) < np) {
-                    R[j][9] = acc[j][0] * R[j][3] * kOneOverPi;
-                    R[j][10] = acc[j][1] * R[j][4] * kOneOverPi;
-                    R[j][11] = acc[j][2] * R[j][5] * kOneOverPi;
-                }
+            for (int i = 0; i < half; ++i) {
+                const float mine = up ? v[i + half] : v[i], other = up ? v[i] : v[i + half];
+                v[i] = mine + __shfl_xor_sync(kFull, other, o);
+            }
+        }
+        v[0] += __shfl_xor_sync(kFull, v[0], 1);
+        const int k = lane >> 1, j = k / 3, c = k - 3 * j;
+        const int p = p0 + j * (kMlpThreads / 32);
+        if ((lane & 1) == 0 && k < 3 * G && p < np) {
+            float* R = B.rec[p / n_samples][p % n_samples];
+            R[9 + c] = v[0] * R[3 + c] * kOneOverPi;
+        }
     }
     __syncthreads();
     if (threadIdx.x < (unsigned)nb) {
