@@ -26,6 +26,7 @@
 // whatever order the fragments arrive in.
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <utility>
 
 #include "rast_exact.cuh"
 #include "rast_internal.h"
@@ -158,6 +159,12 @@ __device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
     return v;
 }
 
+// Programmatic dependent launch: the kernels of a frame after the first are launched while their
+// predecessor runs; each lets its dependents launch as it starts, and waits for its predecessor
+// (and so for every earlier kernel of the frame) before anything else.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Records a failed internal check: sets STATUS_CHECK_FAILED and keeps the first failure's code
 // and detail in counters[2..3]. The caller skips the access that failed the check.
 __device__ __noinline__ void report(uint32_t* counters, uint32_t code, uint32_t detail) {
@@ -207,6 +214,7 @@ __device__ __forceinline__ uint32_t div_small(uint32_t n, uint32_t d, float rd) 
 // the y flip (geometry.cpp:44-74).
 __global__ void __launch_bounds__(256) k_vertex(const float* __restrict__ pos, int64_t nv, Mat4 cam, float wf,
                                                 float hf, float4* __restrict__ rv) {
+    pdl_launch_dependents();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
         const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
         const float cx = mrow(cam, 0, x, y, z, 1.f);
@@ -233,6 +241,7 @@ __device__ __forceinline__ float4 raster_vertex(const Mat4& cam, float x, float 
 // be 16-byte aligned); the last nv % 4 vertices are done one by one.
 __global__ void __launch_bounds__(256) k_vertex4(const float* __restrict__ pos, int64_t nv, Mat4 cam, float wf,
                                                  float hf, float4* __restrict__ rv) {
+    pdl_launch_dependents();
     const int64_t groups = nv / 4;
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups + (nv % 4); g += (int64_t)gridDim.x * blockDim.x) {
         if (g < groups) {
@@ -328,6 +337,8 @@ struct SetupArgs {
 // chains, and the extra warps hide them (6.0k vs 5.8k frames/s on the 1M-triangle 1080p frame).
 template <uint32_t kRowChunk>  // pixels of one bounding-box row per work item
 __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ SetupStage stage[kSetupWarps];
     __shared__ uint32_t s_large[kSetupWarps];
     __shared__ uint32_t s_large_base;
@@ -620,24 +631,33 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
 
 // Exclusive scans over the tiles: entry offsets (the tile counts) into offset[0..n_tiles] and
 // work-item offsets (ceil(count / kTileChunk)) into offset[n_tiles+1 .. 2*n_tiles+1]. One CTA of
-// 1024 threads walks the tiles 4096 at a time. Flags an overflow of the bin pool.
+// 1024 threads walks the tiles 8192 at a time, eight consecutive tiles a thread (two 16-byte loads
+// and stores). Flags an overflow of the bin pool.
 __global__ void __launch_bounds__(1024) k_bin_scan(const uint32_t* __restrict__ counters, uint32_t n_tiles,
                                                    uint32_t* __restrict__ offset, int64_t cap_entries,
                                                    uint32_t* __restrict__ status, unsigned long long* stats) {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ uint32_t warp_tot[2][32];
     __shared__ uint32_t carry_s[2];
-    const uint32_t* cnt = counters + kCounterHeader;
+    const uint32_t* cnt = counters + kCounterHeader;  // 16-byte aligned: the header is 8 words
     uint32_t* chunk_offset = offset + n_tiles + 1;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid < 2) carry_s[tid] = 0;
     __syncthreads();
-    for (uint32_t base = 0; base < n_tiles; base += 4096) {
-        uint32_t v[4], c[4];
+    for (uint32_t base = 0; base < n_tiles; base += 8192) {
+        const uint32_t i0 = base + tid * 8;
+        uint32_t v[8], c[8];
+        if (i0 + 8 <= n_tiles) {
+            const uint4 a = reinterpret_cast<const uint4*>(cnt + i0)[0], b = reinterpret_cast<const uint4*>(cnt + i0)[1];
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = i0 + k < n_tiles ? cnt[i0 + k] : 0u;
+        }
         uint32_t s = 0, sc = 0;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t i = base + tid * 4 + k;
-            v[k] = i < n_tiles ? cnt[i] : 0u;
+        for (int k = 0; k < 8; ++k) {
             c[k] = (v[k] + kTileChunk - 1) / kTileChunk;
             s += v[k];
             sc += c[k];
@@ -657,15 +677,21 @@ __global__ void __launch_bounds__(1024) k_bin_scan(const uint32_t* __restrict__ 
         __syncthreads();
         uint32_t run = carry_s[0] + warp_tot[0][warp] + incl - s;
         uint32_t run_c = carry_s[1] + warp_tot[1][warp] + incl_c - sc;
+        uint32_t o[8];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t i = base + tid * 4 + k;
-            if (i < n_tiles) {
-                offset[i] = run;
-                chunk_offset[i] = run_c;
-            }
+        for (int k = 0; k < 8; ++k) {
+            o[k] = run;
+            if (i0 + k < n_tiles) chunk_offset[i0 + k] = run_c;
             run += v[k];
             run_c += c[k];
+        }
+        if (i0 + 8 <= n_tiles) {
+            reinterpret_cast<uint4*>(offset + i0)[0] = make_uint4(o[0], o[1], o[2], o[3]);
+            reinterpret_cast<uint4*>(offset + i0)[1] = make_uint4(o[4], o[5], o[6], o[7]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (i0 + k < n_tiles) offset[i0 + k] = o[k];
         }
         __syncthreads();
         if (tid == 1023) {
@@ -697,6 +723,8 @@ struct ScatterArgs {
 // Writes every binned triangle's index into the lists of the tiles its box overlaps. Lanes of a
 // warp share the work of their 32 triangles' tiles, as in k_setup_raster.
 __global__ void __launch_bounds__(256) k_bin_scatter(ScatterArgs a) {
+    pdl_wait();
+    pdl_launch_dependents();
     __shared__ uint32_t s_tx0[8][32], s_ty0[8][32], s_tw[8][32], s_incl[8][32];
     __shared__ float s_rtw[8][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -762,6 +790,8 @@ struct TileArgs {
 // of one tile may run at once, and the per-triangle pass wrote its keys earlier on the stream).
 template <int TS>
 __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
+    pdl_wait();
+    pdl_launch_dependents();
     constexpr int kThreads = (TS * TS < 256) ? TS * TS : 256;
     constexpr int kPPT = (TS * TS) / kThreads;  // pixels per thread
     constexpr int kBlocksX = TS / 8;             // 8x4 blocks across a tile
@@ -996,9 +1026,10 @@ struct ResolveStage {
 __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
     __shared__ ResolveStage stage[kResolveWarps];
     __shared__ uint32_t s_count[kResolveWarps];
+    pdl_wait();
     // Deferred shading: the shading kernel may be launched once every block of this grid has
     // started (it waits for this grid's completion before it reads the records).
-    if (a.gbuf) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    pdl_launch_dependents();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     ResolveStage& S = stage[warp];
     const int64_t npx = (int64_t)a.width * a.height;
@@ -1162,11 +1193,29 @@ int grid_for(int64_t n, int threads, int max_blocks) {
     return (int)(b < max_blocks ? b : max_blocks);
 }
 
+// Launches a kernel of the frame after its first with programmatic stream serialization: it may
+// start while the kernel before it runs, and waits for it (pdl_wait) before anything else.
+template <typename... Params, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(Params...), unsigned grid, unsigned block, cudaStream_t stream,
+                       Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 template <int TS>
-void launch_tile(const TileArgs& ta, int n_sm, cudaStream_t stream) {
+cudaError_t launch_tile(const TileArgs& ta, int n_sm, cudaStream_t stream) {
     constexpr int kThreads = (TS * TS < 256) ? TS * TS : 256;
     const int per_sm = 2048 / kThreads < 8 ? 2048 / kThreads : 8;
-    k_tile_raster<TS><<<n_sm * per_sm, kThreads, 0, stream>>>(ta);
+    return launch_pdl(k_tile_raster<TS>, (unsigned)(n_sm * per_sm), (unsigned)kThreads, stream, ta);
 }
 
 }  // namespace
@@ -1228,14 +1277,18 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     sa.stats = s.stats;
     if (mesh.ntri > 0) {
         const unsigned blocks = (unsigned)((mesh.ntri + kSetupThreads - 1) / kSetupThreads);
-        if (p.row_chunk == 32) k_setup_raster<32><<<blocks, kSetupThreads, 0, stream>>>(sa);
-        else if (p.row_chunk == 8) k_setup_raster<8><<<blocks, kSetupThreads, 0, stream>>>(sa);
-        else k_setup_raster<4><<<blocks, kSetupThreads, 0, stream>>>(sa);
+        cudaError_t e;
+        if (p.row_chunk == 32) e = launch_pdl(k_setup_raster<32>, blocks, (unsigned)kSetupThreads, stream, sa);
+        else if (p.row_chunk == 8) e = launch_pdl(k_setup_raster<8>, blocks, (unsigned)kSetupThreads, stream, sa);
+        else e = launch_pdl(k_setup_raster<4>, blocks, (unsigned)kSetupThreads, stream, sa);
+        if (e != cudaSuccess) return -1;
         ++launches;
     }
     mark(3);
 
-    k_bin_scan<<<1, 1024, 0, stream>>>(s.counters, n_tiles, s.tile_offset, s.cap_entries, s.counters + 1, s.stats);
+    if (launch_pdl(k_bin_scan, 1u, 1024u, stream, (const uint32_t*)s.counters, n_tiles, s.tile_offset, s.cap_entries,
+                   s.counters + 1, s.stats) != cudaSuccess)
+        return -1;
     ++launches;
     mark(4);
 
@@ -1251,7 +1304,8 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     sc.tile_shift = shift;
     sc.tiles_x = p.tiles_x;
     sc.stats = s.stats;
-    k_bin_scatter<<<grid_for(s.cap_large, 256, 4 * p.n_sm), 256, 0, stream>>>(sc);
+    if (launch_pdl(k_bin_scatter, (unsigned)grid_for(s.cap_large, 256, p.n_sm), 256u, stream, sc) != cudaSuccess)
+        return -1;
     ++launches;
     mark(5);
 
@@ -1268,9 +1322,9 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ta.tiles_x = p.tiles_x;
     ta.n_tiles = n_tiles;
     ta.stats = s.stats;
-    if (p.tile == 8) launch_tile<8>(ta, p.n_sm, stream);
-    else if (p.tile == 16) launch_tile<16>(ta, p.n_sm, stream);
-    else launch_tile<32>(ta, p.n_sm, stream);
+    const cudaError_t et = p.tile == 8 ? launch_tile<8>(ta, p.n_sm, stream)
+                           : p.tile == 16 ? launch_tile<16>(ta, p.n_sm, stream) : launch_tile<32>(ta, p.n_sm, stream);
+    if (et != cudaSuccess) return -1;
     ++launches;
     mark(6);
 
@@ -1308,7 +1362,9 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.gbuf_count = deferred ? s.gbuf_count : nullptr;
     ra.shade_index = deferred ? s.shade_index : nullptr;
     const int64_t spans = (npx + kSpan - 1) / kSpan;
-    k_resolve<<<(unsigned)((spans + kResolveWarps - 1) / kResolveWarps), kResolveThreads, 0, stream>>>(ra);
+    if (launch_pdl(k_resolve, (unsigned)((spans + kResolveWarps - 1) / kResolveWarps), (unsigned)kResolveThreads, stream,
+                   ra) != cudaSuccess)
+        return -1;
     ++launches;
     mark(7);
     if (p.shader != 0) {
