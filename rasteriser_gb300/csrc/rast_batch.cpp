@@ -112,6 +112,7 @@ rast_status enqueue_batch(rast_ctx* c, const rast_frame_desc* frames, int32_t n,
         p.small_max = c->small_max;
         p.tile = c->tile;
         p.row_chunk = c->row_chunk;
+        p.chained = false;
         p.tiles_x = tiles_x;
         p.tiles_y = tiles_y;
         p.n_sm = c->n_sm;

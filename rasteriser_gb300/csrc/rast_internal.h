@@ -111,6 +111,8 @@ struct DrawParams {
     uint32_t small_max;     // bounding boxes up to this many pixels take the per-triangle path
     uint32_t tile;          // tile edge: 8, 16, 32
     uint32_t row_chunk;     // pixels per work item of the per-triangle path: 4, 8 or 32 (whole rows)
+    bool chained = true;    // launch the frame's kernels after the first as programmatic dependents
+                            // (off for batches, whose lanes fill the SMs with each other's work)
     uint32_t tiles_x, tiles_y;
     int32_t n_sm;           // streaming multiprocessors of the device
     int32_t nl;

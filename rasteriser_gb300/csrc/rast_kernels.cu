@@ -1196,7 +1196,7 @@ int grid_for(int64_t n, int threads, int max_blocks) {
 // Launches a kernel of the frame after its first with programmatic stream serialization: it may
 // start while the kernel before it runs, and waits for it (pdl_wait) before anything else.
 template <typename... Params, typename... Args>
-cudaError_t launch_pdl(void (*kernel)(Params...), unsigned grid, unsigned block, cudaStream_t stream,
+cudaError_t launch_pdl(bool chained, void (*kernel)(Params...), unsigned grid, unsigned block, cudaStream_t stream,
                        Args&&... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
@@ -1207,15 +1207,15 @@ cudaError_t launch_pdl(void (*kernel)(Params...), unsigned grid, unsigned block,
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = chained ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 template <int TS>
-cudaError_t launch_tile(const TileArgs& ta, int n_sm, cudaStream_t stream) {
+cudaError_t launch_tile(const TileArgs& ta, int n_sm, bool chained, cudaStream_t stream) {
     constexpr int kThreads = (TS * TS < 256) ? TS * TS : 256;
     const int per_sm = 2048 / kThreads < 8 ? 2048 / kThreads : 8;
-    return launch_pdl(k_tile_raster<TS>, (unsigned)(n_sm * per_sm), (unsigned)kThreads, stream, ta);
+    return launch_pdl(chained, k_tile_raster<TS>, (unsigned)(n_sm * per_sm), (unsigned)kThreads, stream, ta);
 }
 
 }  // namespace
@@ -1277,17 +1277,18 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     sa.stats = s.stats;
     if (mesh.ntri > 0) {
         const unsigned blocks = (unsigned)((mesh.ntri + kSetupThreads - 1) / kSetupThreads);
+        const unsigned th = (unsigned)kSetupThreads;
         cudaError_t e;
-        if (p.row_chunk == 32) e = launch_pdl(k_setup_raster<32>, blocks, (unsigned)kSetupThreads, stream, sa);
-        else if (p.row_chunk == 8) e = launch_pdl(k_setup_raster<8>, blocks, (unsigned)kSetupThreads, stream, sa);
-        else e = launch_pdl(k_setup_raster<4>, blocks, (unsigned)kSetupThreads, stream, sa);
+        if (p.row_chunk == 32) e = launch_pdl(p.chained, k_setup_raster<32>, blocks, th, stream, sa);
+        else if (p.row_chunk == 8) e = launch_pdl(p.chained, k_setup_raster<8>, blocks, th, stream, sa);
+        else e = launch_pdl(p.chained, k_setup_raster<4>, blocks, th, stream, sa);
         if (e != cudaSuccess) return -1;
         ++launches;
     }
     mark(3);
 
-    if (launch_pdl(k_bin_scan, 1u, 1024u, stream, (const uint32_t*)s.counters, n_tiles, s.tile_offset, s.cap_entries,
-                   s.counters + 1, s.stats) != cudaSuccess)
+    if (launch_pdl(p.chained, k_bin_scan, 1u, 1024u, stream, (const uint32_t*)s.counters, n_tiles, s.tile_offset,
+                   s.cap_entries, s.counters + 1, s.stats) != cudaSuccess)
         return -1;
     ++launches;
     mark(4);
@@ -1304,7 +1305,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     sc.tile_shift = shift;
     sc.tiles_x = p.tiles_x;
     sc.stats = s.stats;
-    if (launch_pdl(k_bin_scatter, (unsigned)grid_for(s.cap_large, 256, p.n_sm), 256u, stream, sc) != cudaSuccess)
+    if (launch_pdl(p.chained, k_bin_scatter, (unsigned)grid_for(s.cap_large, 256, p.n_sm), 256u, stream, sc) != cudaSuccess)
         return -1;
     ++launches;
     mark(5);
@@ -1322,8 +1323,9 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ta.tiles_x = p.tiles_x;
     ta.n_tiles = n_tiles;
     ta.stats = s.stats;
-    const cudaError_t et = p.tile == 8 ? launch_tile<8>(ta, p.n_sm, stream)
-                           : p.tile == 16 ? launch_tile<16>(ta, p.n_sm, stream) : launch_tile<32>(ta, p.n_sm, stream);
+    const cudaError_t et = p.tile == 8 ? launch_tile<8>(ta, p.n_sm, p.chained, stream)
+                           : p.tile == 16 ? launch_tile<16>(ta, p.n_sm, p.chained, stream)
+                                          : launch_tile<32>(ta, p.n_sm, p.chained, stream);
     if (et != cudaSuccess) return -1;
     ++launches;
     mark(6);
@@ -1362,8 +1364,8 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.gbuf_count = deferred ? s.gbuf_count : nullptr;
     ra.shade_index = deferred ? s.shade_index : nullptr;
     const int64_t spans = (npx + kSpan - 1) / kSpan;
-    if (launch_pdl(k_resolve, (unsigned)((spans + kResolveWarps - 1) / kResolveWarps), (unsigned)kResolveThreads, stream,
-                   ra) != cudaSuccess)
+    if (launch_pdl(p.chained, k_resolve, (unsigned)((spans + kResolveWarps - 1) / kResolveWarps),
+                   (unsigned)kResolveThreads, stream, ra) != cudaSuccess)
         return -1;
     ++launches;
     mark(7);
