@@ -146,7 +146,10 @@ rast_status rast_set_lights(rast_ctx* ctx, const float* lights7, int32_t n);
  *          incoming value is the depth every fragment must beat (drawing.cpp:119)
  *   tri_id (nullable): width*height uint32, the index of the triangle that wrote each pixel in
  *          this call, or 0xFFFFFFFF
- * Pixels no fragment wins keep their colour and depth. 1 <= width, height <= 32768. */
+ * Pixels no fragment wins keep their colour and depth. 1 <= width, height <= 32768. The colour
+ * input is uploaded while the first passes run, and the results and the device status are read
+ * back in one wait; after an error other than a bin overflow (which is redrawn from kept copies of
+ * the inputs) the buffers' contents are unspecified. */
 rast_status rast_draw(rast_ctx* ctx, const float camera[16], const float normal[16], uint32_t width,
                       uint32_t height, uint32_t flags, uint8_t* rgb_planar, float* depth, uint32_t* tri_id);
 

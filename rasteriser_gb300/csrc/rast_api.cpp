@@ -97,6 +97,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     p.small_max = c->small_max;
     p.tile = c->tile;
     p.row_chunk = c->row_chunk;
+    p.before_resolve = c->before_resolve;
     p.tiles_x = tiles_x;
     p.tiles_y = tiles_y;
     p.n_sm = c->n_sm;
@@ -228,6 +229,14 @@ void rast_destroy(rast_ctx* c) {
         for (DevBuf* b : {&m->pos, &m->tris10, &m->tri_v, &m->tri_nm, &m->nrm, &m->kd}) b->release();
     c->batch_stats.release();
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    for (DevBuf* b : {&c->d_rgb_in, &c->d_depth_in}) b->release();
+    if (c->ev_depth_in) cudaEventDestroy(c->ev_depth_in);
+    if (c->ev_rgb_in) cudaEventDestroy(c->ev_rgb_in);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    if (c->h_status) cudaFreeHost(c->h_status);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -406,26 +415,53 @@ rast_status rast_draw(rast_ctx* c, const float camera[16], const float normal[16
     if (w == 0 || h == 0 || w > kMaxDim || h > kMaxDim) return fail(c, RAST_ERR_INVALID_ARG, "frame size out of range");
     DeviceGuard g(c->device);
     const size_t npx = (size_t)w * h;
+    const bool rmw = !(flags & RAST_CLEAR);
     RAST_CUDA(c, c->d_rgb.reserve(3 * npx));
     RAST_CUDA(c, c->d_depth.reserve(sizeof(float) * npx));
     if (ids) RAST_CUDA(c, c->d_ids.reserve(sizeof(uint32_t) * npx));
+    if (rmw) {
+        RAST_CUDA(c, c->d_rgb_in.reserve(3 * npx));
+        RAST_CUDA(c, c->d_depth_in.reserve(sizeof(float) * npx));
+        if (!c->copy_stream) RAST_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        if (!c->ev_depth_in) RAST_CUDA(c, cudaEventCreateWithFlags(&c->ev_depth_in, cudaEventDisableTiming));
+        if (!c->ev_rgb_in) RAST_CUDA(c, cudaEventCreateWithFlags(&c->ev_rgb_in, cudaEventDisableTiming));
+    }
+    if (!c->h_status) RAST_CUDA(c, cudaMallocHost(&c->h_status, sizeof(uint32_t)));
     for (int attempt = 0; attempt < 3; ++attempt) {
-        if (!(flags & RAST_CLEAR)) {
-            RAST_CUDA(c, cudaMemcpyAsync(c->d_rgb.ptr, rgb, 3 * npx, cudaMemcpyHostToDevice, c->stream));
+        // The depth input is needed first (it arms the depth test); the colour input only by the
+        // resolve pass, so it is uploaded on the copy stream while the first passes run. Both are
+        // also kept on the device, so a redraw after a bin overflow starts from them again.
+        if (rmw && attempt == 0) {
             RAST_CUDA(c, cudaMemcpyAsync(c->d_depth.ptr, depth, sizeof(float) * npx, cudaMemcpyHostToDevice, c->stream));
+            RAST_CUDA(c, cudaEventRecord(c->ev_depth_in, c->stream));
+            RAST_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->ev_depth_in, 0));
+            RAST_CUDA(c, cudaMemcpyAsync(c->d_rgb.ptr, rgb, 3 * npx, cudaMemcpyHostToDevice, c->copy_stream));
+            RAST_CUDA(c, cudaMemcpyAsync(c->d_depth_in.ptr, c->d_depth.ptr, sizeof(float) * npx,
+                                         cudaMemcpyDeviceToDevice, c->copy_stream));
+            RAST_CUDA(c, cudaMemcpyAsync(c->d_rgb_in.ptr, c->d_rgb.ptr, 3 * npx, cudaMemcpyDeviceToDevice, c->copy_stream));
+            RAST_CUDA(c, cudaEventRecord(c->ev_rgb_in, c->copy_stream));
+        } else if (rmw) {
+            RAST_CUDA(c, cudaMemcpyAsync(c->d_depth.ptr, c->d_depth_in.ptr, sizeof(float) * npx,
+                                         cudaMemcpyDeviceToDevice, c->stream));
+            RAST_CUDA(c, cudaMemcpyAsync(c->d_rgb.ptr, c->d_rgb_in.ptr, 3 * npx, cudaMemcpyDeviceToDevice, c->stream));
+            RAST_CUDA(c, cudaEventRecord(c->ev_rgb_in, c->stream));
         }
+        c->before_resolve = rmw ? c->ev_rgb_in : nullptr;
         rast_status st = enqueue_draw(c, camera, normal, w, h, flags, c->d_rgb.as<uint8_t>(), c->d_depth.as<float>(),
                                       ids ? c->d_ids.as<uint32_t>() : nullptr);
+        c->before_resolve = nullptr;
         if (st != RAST_OK) return st;
-        RAST_CUDA(c, cudaStreamSynchronize(c->stream));
-        st = collect_status(c);
-        if (st == RAST_ERR_BIN_OVERFLOW) continue;  // pool grown; draw again from the same inputs
-        if (st != RAST_OK) return st;
+        // the outputs and the status word, read back in one wait
         RAST_CUDA(c, cudaMemcpyAsync(rgb, c->d_rgb.ptr, 3 * npx, cudaMemcpyDeviceToHost, c->stream));
         RAST_CUDA(c, cudaMemcpyAsync(depth, c->d_depth.ptr, sizeof(float) * npx, cudaMemcpyDeviceToHost, c->stream));
         if (ids) RAST_CUDA(c, cudaMemcpyAsync(ids, c->d_ids.ptr, sizeof(uint32_t) * npx, cudaMemcpyDeviceToHost, c->stream));
+        RAST_CUDA(c, cudaMemcpyAsync(c->h_status, c->counters.as<uint32_t>() + 1, sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, c->stream));
         RAST_CUDA(c, cudaStreamSynchronize(c->stream));
-        return RAST_OK;
+        if (*c->h_status == 0u) return RAST_OK;
+        st = collect_status(c);
+        if (st == RAST_ERR_BIN_OVERFLOW) continue;  // pool grown; draw again from the same inputs
+        return st;
     }
     return fail(c, RAST_ERR_BIN_OVERFLOW, "tile-bin pool still overflowing after regrowth");
 }

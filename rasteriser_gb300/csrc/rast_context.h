@@ -89,6 +89,13 @@ struct rast_ctx {
 
     // host-pointer draws stage through these
     DevBuf d_rgb, d_depth, d_ids;
+    // host draws: copies of the read-modify-write inputs (for a redraw after a bin overflow), the
+    // stream that uploads the colour input beside the first passes, and the status word's landing
+    DevBuf d_rgb_in, d_depth_in;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_depth_in = nullptr, ev_rgb_in = nullptr;
+    uint32_t* h_status = nullptr;
+    cudaEvent_t before_resolve = nullptr;  // set by rast_draw for the draw it enqueues
 
     // deferred shading
     int32_t shader = 0;           // RAST_SHADER_*

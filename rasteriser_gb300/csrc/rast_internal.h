@@ -113,6 +113,8 @@ struct DrawParams {
     uint32_t row_chunk;     // pixels per work item of the per-triangle path: 4, 8 or 32 (whole rows)
     bool chained = true;    // launch the frame's kernels after the first as programmatic dependents
                             // (off for batches, whose lanes fill the SMs with each other's work)
+    cudaEvent_t before_resolve = nullptr;  // when set, the resolve pass waits for it (the colour
+                                           // input of a host draw, copied beside the first passes)
     uint32_t tiles_x, tiles_y;
     int32_t n_sm;           // streaming multiprocessors of the device
     int32_t nl;

@@ -1329,6 +1329,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     if (et != cudaSuccess) return -1;
     ++launches;
     mark(6);
+    if (p.before_resolve && cudaStreamWaitEvent(stream, p.before_resolve, 0) != cudaSuccess) return -1;
 
     ResolveArgs ra;
     ra.counters = s.counters;
