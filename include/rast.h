@@ -177,8 +177,9 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 #define RAST_OPT_BIN_CAPACITY 3       /* initial tile-bin pool, entries */
 #define RAST_OPT_STAGE_TIMING 4       /* 1: record CUDA events between the kernels of each draw */
 #define RAST_OPT_ROW_CHUNK 5          /* pixels of a bounding-box row per work item of the
-                                         per-triangle path: 4, 8 (default), or 32: whole rows, each
-                                         clipped to the pixels near the triangle's span */
+                                         per-triangle path: 4 or 8, each pixel's edges evaluated,
+                                         or 32 (default): whole rows, the ends of the passing
+                                         interval found from the edges' crossings */
 #define RAST_OPT_SHADER 6             /* RAST_SHADER_* (default RAST_SHADER_EXACT) */
 #define RAST_OPT_MLP_SAMPLES 7        /* learned shader: fragments of each 128-fragment tile that
                                          are also shaded exactly to check it, 0..4 (default 2) */

@@ -116,7 +116,7 @@ struct rast_ctx {
     // options
     uint32_t small_max = 4096;
     uint32_t tile = 16;
-    uint32_t row_chunk = 8;
+    uint32_t row_chunk = 32;
     int64_t bin_capacity = 0;  // 0: sized from the mesh
 
     uint64_t last_launches = 0;

@@ -289,9 +289,10 @@ constexpr uint32_t kSmallMaxRow = 32;
 
 // Per-warp staging of 32 triangles. rec[j] holds lane j's triangle as five float4s so a lane
 // working on another lane's triangle loads it with five 16-byte shared loads:
-//   rec[j][0] = x0 y0 x1 y1      rec[j][1] = x2 y2 area nthr
-//   rec[j][2] = d12x d12y d20x d20y
-//   rec[j][3] = d01x d01y sgn -   rec[j][4] = z0 z1 z2 -
+//   rec[j][0] = x0 y0 x1 y1               rec[j][1] = x2 y2 |area| nthr
+//   rec[j][2] = sgn * (d12x d12y d20x d20y)
+//   rec[j][3] = sgn * (d01x d01y), r0 r1  rec[j][4] = z0 z1 z2 r2
+// (sgn = sign of the area; r0..r2 = reciprocals of the staged x coefficients, whole-row items only).
 // Its integer data (bounding box, items per row) is kept in integer arrays.
 struct SetupStage {
     float4 rec[32][5];
@@ -299,8 +300,8 @@ struct SetupStage {
     float rcpr[32];
     uint32_t incl[32];
     int slot[32];
-    // Ring of work items with pixels the early reject could not rule out: first pixel
-    // (x | y << 16), owning lane, and the candidate mask (bit b: pixel x + b).
+    // Ring of candidate runs (pixels of one row the early reject could not rule out): first pixel
+    // (x | y << 16), owning lane, and the run's length.
     uint32_t q_xy[64], q_om[64], q_m[64];
 };
 
@@ -402,12 +403,13 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
 
     unsigned long long c_tested = 0, c_inside = 0;
 
-    // Cooperative raster of the warp's small triangles. Each lane evaluates the three edge
-    // functions of the kRowChunk pixels of its item and keeps a mask of the pixels the early reject
-    // cannot rule out; items with a nonzero mask go to a per-warp ring, and whenever the ring holds
-    // 32 of them the whole warp takes one each for the exact test of its masked pixels (the
-    // reference's three divisions), the depth and the atomic. The tested pixels cost only the edge
-    // evaluations, and the divisions run on full warps.
+    // Cooperative raster of the warp's small triangles. Each lane finds the run of pixels of its
+    // item that the early reject cannot rule out: whole-row items (kRowChunk 32) from the two ends
+    // of the row's passing interval, verified exactly, shorter items by evaluating the edges at each
+    // of their pixels. Non-empty runs go to a per-warp ring, and whenever it holds 32 of them the
+    // warp shares out their pixels, one per lane, for the exact test (the reference's three
+    // divisions), the depth and the atomic. So the divisions and atomics run on full warps whatever
+    // the runs' lengths.
     {
         const uint32_t incl = warp_inclusive_scan(n_items, lane);
         const uint32_t total = __shfl_sync(kFull, incl, 31);
@@ -420,7 +422,7 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
             S.rec[lane][1] = make_float4(T.x2, T.y2, mul(sg, T.area), T.nthr);
             S.rec[lane][2] = make_float4(mul(sg, T.d12x), mul(sg, T.d12y), mul(sg, T.d20x), mul(sg, T.d20y));
             // Whole-row items (kRowChunk 32) also stage the reciprocals of the three edges' x
-            // coefficients, which bound the row's candidate span (see below).
+            // coefficients, from which each row's crossing of an edge is estimated (see below).
             float r0 = 0.f, r1 = 0.f, r2 = 0.f;
             if (kRowChunk == 32u) {
                 r0 = __frcp_rn(mul(sg, T.d12y));
@@ -440,30 +442,52 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
             const unsigned lt_mask = (1u << lane) - 1u;
             uint32_t q_head = 0, q_count = 0;  // warp-uniform
 
-            // Exact test, depth and atomic for the masked pixels of ring entry `e`
-            // (drawing.cpp:108-121).
-            auto finish = [&](uint32_t e) {
-                const uint32_t xy = S.q_xy[e];
-                const uint32_t j = S.q_om[e] & 31u;
-                uint32_t mask = S.q_m[e];
-                const uint32_t x0 = xy & 0xFFFFu, y = xy >> 16;
-                const float4 q0 = S.rec[j][0], q1 = S.rec[j][1], q2 = S.rec[j][2], q3 = S.rec[j][3], q4 = S.rec[j][4];
-                const float py = (float)y;
-                const float p0 = mul(q2.x, sub(py, q0.w)), p1 = mul(q2.z, sub(py, q1.y)), p2 = mul(q3.x, sub(py, q0.y));
-                while (mask) {
-                    const uint32_t b = __ffs(mask) - 1u;
-                    mask &= mask - 1u;
-                    const uint32_t x = x0 + b;
-                    const float px = (float)x;
-                    const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));
-                    const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));
-                    const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));
-                    const float b0 = dvd(e0, q1.z), b1 = dvd(e1, q1.z), b2 = dvd(e2, q1.z);
-                    if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
-                        ++c_inside;
-                        const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
-                        if (z == z && x < a.width && y < a.height)
-                            atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + j));
+            // Exact test, depth and atomic (drawing.cpp:108-121) for the pixels of the n ring entries
+            // from q_head (n <= 32, warp-uniform). Each entry is a run of candidate pixels of one
+            // row; the runs are laid end to end and their pixels taken 32 at a time, one per lane,
+            // the run of a pixel found as the owner of an item is below.
+            auto drain = [&](uint32_t n) {
+                uint32_t cnt = 0u, xy = 0u, own = 0u;
+                if ((uint32_t)lane < n) {
+                    const uint32_t e = (q_head + lane) & 63u;
+                    xy = S.q_xy[e];
+                    own = S.q_om[e];
+                    cnt = S.q_m[e];
+                }
+                const uint32_t incl_p = warp_inclusive_scan(cnt, lane);
+                const uint32_t total_p = __shfl_sync(kFull, incl_p, 31);
+                const uint32_t excl_p = incl_p - cnt;
+                int carry_p = 0;
+                for (uint32_t pb = 0; pb < total_p; pb += 32u) {
+                    const bool opens = cnt != 0u && excl_p >= pb && excl_p < pb + 32u;
+                    if (opens) S.slot[excl_p - pb] = lane;
+                    const unsigned starts = __reduce_or_sync(kFull, opens ? (1u << (excl_p - pb)) : 0u);
+                    __syncwarp();
+                    const unsigned upto = starts & (0xFFFFFFFFu >> (31 - lane));
+                    const int src = upto ? S.slot[31 - __clz(upto)] : carry_p;
+                    carry_p = __shfl_sync(kFull, src, 31);
+                    __syncwarp();
+                    const uint32_t sxy = __shfl_sync(kFull, xy, src);
+                    const uint32_t j = __shfl_sync(kFull, own, src) & 31u;
+                    const uint32_t sex = __shfl_sync(kFull, excl_p, src);
+                    const uint32_t k = pb + lane;
+                    if (k < total_p) {
+                        const uint32_t x = (sxy & 0xFFFFu) + (k - sex), y = sxy >> 16;
+                        const float4 q0 = S.rec[j][0], q1 = S.rec[j][1], q2 = S.rec[j][2], q3 = S.rec[j][3],
+                                     q4 = S.rec[j][4];
+                        const float py = (float)y, px = (float)x;
+                        const float p0 = mul(q2.x, sub(py, q0.w)), p1 = mul(q2.z, sub(py, q1.y)),
+                                    p2 = mul(q3.x, sub(py, q0.y));
+                        const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));
+                        const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));
+                        const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));
+                        const float b0 = dvd(e0, q1.z), b1 = dvd(e1, q1.z), b2 = dvd(e2, q1.z);
+                        if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
+                            ++c_inside;
+                            const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
+                            if (z == z && x < a.width && y < a.height)
+                                atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + j));
+                        }
                     }
                 }
             };
@@ -481,14 +505,16 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                 carry = __shfl_sync(kFull, owner, 31);
                 __syncwarp();
                 const uint32_t k = base + lane;
-                uint32_t x_lo = 0u, y = 0u, mask = 0u;
+                // The item's candidate run: pixels run_x .. run_x + run_n - 1 of row y. It holds every
+                // pixel of the item that the early reject cannot rule out (and possibly more).
+                uint32_t run_x = 0u, run_n = 0u, y = 0u;
                 if (k < total) {
                     const uint32_t ostart = owner ? S.incl[owner - 1] : 0u;
                     const uint32_t local = k - ostart;
                     const uint32_t ocpr = S.cpr[owner];
                     const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
-                    x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
-                    uint32_t x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
+                    const uint32_t x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
+                    const uint32_t x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
                     y = S.tly[owner] + row;
                     bool live = true;
 #ifdef RAST_CHECKED
@@ -506,93 +532,131 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                         const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
                         const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
                         c_tested += x_hi - x_lo + 1u;  // the reference tests every pixel of the row
-                        if (kRowChunk == 32u) {
-                            // Whole rows: only the pixels within one pixel of the row's span can
-                            // pass. Along the row each staged edge value is f = P - B*(px - X), so
-                            // f >= 0 bounds px by X + P/B (above when B > 0, below when B < 0).
-                            // The bound is computed to within 0.02 px when |X| and |P/B| are at most
-                            // 2^16, and where it is 0.98 px or more away the reference's rounded f
-                            // keeps its sign with |f| >= 0.9*|B|, so with |B| >= 2^-100 and a
-                            // finite area the barycentric f/|area| is negative and nonzero: the
-                            // pixel is outside. Edges that miss these conditions bound nothing; a
-                            // B of zero gives f = P for the whole row. Rows of triangles without
-                            // the early reject (nthr = -inf) keep every pixel.
-                            float lo = -INFINITY, hi = INFINITY;
-                            bool empty = false;
-                            if (q1.w > -INFINITY) {
-                                const float r2 = S.rec[owner][4].w;
-                                const float P[3] = {p0, p1, p2}, B[3] = {q2.y, q2.w, q3.y};
-                                const float X[3] = {q0.z, q1.x, q0.x}, R[3] = {q3.z, q3.w, r2};
-#pragma unroll
-                                for (int k = 0; k < 3; ++k) {
-                                    if (B[k] == 0.f) {
-                                        empty = empty || P[k] < q1.w;
-                                        continue;
-                                    }
-                                    const float off = P[k] * R[k];
-                                    if (!(fabsf(B[k]) >= 0x1p-100f && fabsf(X[k]) <= 0x1p16f && fabsf(off) <= 0x1p16f))
-                                        continue;
-                                    const float c = X[k] + off;
-                                    if (B[k] > 0.f) hi = fminf(hi, c);
-                                    else lo = fmaxf(lo, c);
-                                }
-                            }
-                            const float flo = fmaxf(lo - 1.f, (float)x_lo), fhi = fminf(hi + 1.f, (float)x_hi);
-                            if (empty || !(flo <= fhi)) {
-                                x_hi = x_lo;
-                                live = false;
-                            } else {
-                                x_lo = (uint32_t)ceilf(flo);
-                                x_hi = (uint32_t)floorf(fhi);
-                                live = x_lo <= x_hi;
-                            }
-                        }
-                        const float px_lo = (float)x_lo;
-                        const uint32_t n_px = live ? x_hi - x_lo + 1u : 0u;
-                        // Two pixels per instruction: __fadd2_rn / __fmul2_rn round each component
-                        // exactly as __fadd_rn / __fmul_rn, and a - b is a + (-b) bit for bit, so
-                        //   e = p - d.y * (px - a.x)  ==  p + -(d.y * (px + -a.x)).
+                        // Along the row each staged edge value is f(px) = P - B*(px - X), every step
+                        // rounded. Rounding is monotone, so for finite P, B, X the computed f is
+                        // monotone in px: non-increasing for B > 0, non-decreasing for B < 0, and P
+                        // itself for B = 0. The pixels passing the early reject (f >= thr on all three
+                        // edges) are then one interval of the row.
+                        const float thr = q1.w;
                         const float2 P0 = make_float2(p0, p0), P1 = make_float2(p1, p1), P2 = make_float2(p2, p2);
                         const float2 NX1 = make_float2(-q0.z, -q0.z), NX2 = make_float2(-q1.x, -q1.x),
                                      NX0 = make_float2(-q0.x, -q0.x);
                         const float2 B0 = make_float2(q2.y, q2.y), B1 = make_float2(q2.w, q2.w),
                                      B2 = make_float2(q3.y, q3.y);
-#pragma unroll(kRowChunk == 32u ? 1 : kRowChunk / 2)
-                        for (uint32_t sx = 0; sx < (kRowChunk == 32u ? n_px : kRowChunk); sx += 2) {
-                            // pixel centres px_lo + sx, + sx + 1: exact, integers below 2^24
-                            const float2 px = make_float2(add(px_lo, (float)sx), add(px_lo, (float)(sx + 1)));
+                        // Edge values at pixel centres (a, b): __fadd2_rn / __fmul2_rn round each
+                        // component exactly as __fadd_rn / __fmul_rn, and a - b is a + (-b) bit for
+                        // bit, so  e = p - d.y * (px - a.x)  ==  p + -(d.y * (px + -a.x)).
+                        auto edges2 = [&](float pa, float pb2, float2& e0, float2& e1, float2& e2) {
+                            const float2 px = make_float2(pa, pb2);
                             const float2 t0 = __fmul2_rn(B0, __fadd2_rn(px, NX1));
                             const float2 t1 = __fmul2_rn(B1, __fadd2_rn(px, NX2));
                             const float2 t2 = __fmul2_rn(B2, __fadd2_rn(px, NX0));
-                            const float2 e0 = __fadd2_rn(P0, make_float2(-t0.x, -t0.y));
-                            const float2 e1 = __fadd2_rn(P1, make_float2(-t1.x, -t1.y));
-                            const float2 e2 = __fadd2_rn(P2, make_float2(-t2.x, -t2.y));
-                            // Early reject on the smallest edge value; a NaN stays a candidate.
-                            const bool ca = sx < n_px && fminf(fminf(e0.x, e1.x), e2.x) >= q1.w;
-                            const bool cb = sx + 1 < n_px && fminf(fminf(e0.y, e1.y), e2.y) >= q1.w;
-                            mask |= ((uint32_t)ca | ((uint32_t)cb << 1)) << sx;
+                            e0 = __fadd2_rn(P0, make_float2(-t0.x, -t0.y));
+                            e1 = __fadd2_rn(P1, make_float2(-t1.x, -t1.y));
+                            e2 = __fadd2_rn(P2, make_float2(-t2.x, -t2.y));
+                        };
+                        bool scan_row = true;  // evaluate every pixel of the item
+                        if (kRowChunk == 32u) {
+                            // Whole rows: find the interval's ends from an estimate of each edge's
+                            // crossing, X + P/B, and verify each end exactly at the two pixels either
+                            // side of it. A row whose ends do not verify (or whose coefficients are
+                            // not finite) evaluates every pixel instead.
+                            const int lo = (int)x_lo, hi = (int)x_hi;
+                            int L = lo, U = hi;
+                            bool ok = thr > -INFINITY;  // without the early reject every pixel is a candidate
+                            if (ok) {
+                                const float r2 = S.rec[owner][4].w;
+                                const float P[3] = {p0, p1, p2}, B[3] = {q2.y, q2.w, q3.y};
+                                const float X[3] = {q0.z, q1.x, q0.x}, R[3] = {q3.z, q3.w, r2};
+#pragma unroll
+                                for (int ed = 0; ed < 3; ++ed) {
+                                    const bool finite = fabsf(P[ed]) < INFINITY && fabsf(X[ed]) < INFINITY &&
+                                                        fabsf(B[ed]) < INFINITY;
+                                    ok = ok && finite;
+                                    if (B[ed] == 0.f) {
+                                        if (!(P[ed] >= thr)) U = lo - 1;  // f = P along the whole row
+                                        continue;
+                                    }
+                                    const float est = X[ed] + P[ed] * R[ed];
+                                    float mf = B[ed] > 0.f ? floorf(est) : ceilf(est) - 1.f;
+                                    mf = fminf(fmaxf(mf, (float)(lo - 1)), (float)hi);  // a NaN estimate gives lo - 1
+                                    const int m = (int)mf;
+                                    // f at pixels m and m + 1 (exact integers)
+                                    const float2 px = make_float2((float)m, (float)(m + 1));
+                                    const float2 t = __fmul2_rn(make_float2(B[ed], B[ed]),
+                                                                __fadd2_rn(px, make_float2(-X[ed], -X[ed])));
+                                    const float2 f = __fadd2_rn(make_float2(P[ed], P[ed]), make_float2(-t.x, -t.y));
+                                    const bool in0 = m >= lo, in1 = m + 1 <= hi;
+                                    const bool pass0 = f.x >= thr, pass1 = f.y >= thr;
+                                    if (B[ed] > 0.f) {  // passing pixels end at m
+                                        ok = ok && (!in0 || pass0) && (!in1 || !pass1);
+                                        U = min(U, m);
+                                    } else {            // passing pixels start at m + 1
+                                        ok = ok && (!in0 || !pass0) && (!in1 || pass1);
+                                        L = max(L, m + 1);
+                                    }
+                                }
+                            }
+                            if (ok) {
+                                scan_row = false;
+                                if (L <= U) {
+                                    run_x = (uint32_t)L;
+                                    run_n = (uint32_t)(U - L + 1);
+                                }
+                            } else if (!(thr > -INFINITY)) {
+                                scan_row = false;
+                                run_x = x_lo;
+                                run_n = x_hi - x_lo + 1u;
+                            }
                         }
+                        if (scan_row) {
+                            // Early reject on the smallest edge value of each pixel; the run spans the
+                            // first to the last candidate.
+                            const float px_lo = (float)x_lo;
+                            const uint32_t n_px = x_hi - x_lo + 1u;
+                            uint32_t mask = 0u;
+#pragma unroll(kRowChunk == 32u ? 1 : kRowChunk / 2)
+                            for (uint32_t sx = 0; sx < (kRowChunk == 32u ? n_px : kRowChunk); sx += 2) {
+                                // pixel centres px_lo + sx, + sx + 1: exact, integers below 2^24
+                                float2 e0, e1, e2;
+                                edges2(add(px_lo, (float)sx), add(px_lo, (float)(sx + 1)), e0, e1, e2);
+                                const bool ca = sx < n_px && fminf(fminf(e0.x, e1.x), e2.x) >= thr;
+                                const bool cb = sx + 1 < n_px && fminf(fminf(e0.y, e1.y), e2.y) >= thr;
+                                mask |= ((uint32_t)ca | ((uint32_t)cb << 1)) << sx;
+                            }
+                            if (mask) {
+                                const uint32_t f0 = __ffs(mask) - 1u;
+                                run_x = x_lo + f0;
+                                run_n = (32u - __clz(mask)) - f0;
+                            }
+                        }
+#ifdef RAST_CHECKED
+                        if (run_n && (run_x < x_lo || run_x + run_n - 1u > x_hi)) {
+                            report(a.counters, 4u, run_x);
+                            run_n = 0u;
+                        }
+#endif
                     }
                 }
-                const bool has = mask != 0u;
+                const bool has = run_n != 0u;
                 const unsigned m = __ballot_sync(kFull, has);
                 if (has) {
                     const uint32_t e = (q_head + q_count + __popc(m & lt_mask)) & 63u;
-                    S.q_xy[e] = x_lo | (y << 16);
+                    S.q_xy[e] = run_x | (y << 16);
                     S.q_om[e] = (uint32_t)owner;
-                    S.q_m[e] = mask;
+                    S.q_m[e] = run_n;
                 }
                 q_count += __popc(m);
                 if (q_count >= 32u) {
                     __syncwarp();
-                    finish((q_head + lane) & 63u);
+                    drain(32u);
                     __syncwarp();
                     q_head = (q_head + 32u) & 63u;
                     q_count -= 32u;
                 }
             }
             __syncwarp();
-            if ((uint32_t)lane < q_count) finish((q_head + lane) & 63u);
+            if (q_count) drain(q_count);
             __syncwarp();
         }
     }

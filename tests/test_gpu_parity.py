@@ -82,7 +82,7 @@ def test_against_port(renderer, port, idx, tile, small_max, row_chunk):
     finally:
         renderer.set_option(abi.OPT_TILE_SIZE, 16)
         renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, 4096)
-        renderer.set_option(abi.OPT_ROW_CHUNK, 8)
+        renderer.set_option(abi.OPT_ROW_CHUNK, 32)
 
 
 def test_read_modify_write_buffers(renderer, port):
@@ -212,7 +212,7 @@ def test_invalid_arguments(renderer):
 def test_full_size_against_reference_digest(renderer, port, key, row_chunk):
     """Full-size frames (1,046,528 triangles at 1920x1080; 4M at 3840x2160) against the digests of
     the reference's own output, and against the port run here; per-triangle rows in chunks of 8
-    pixels and as whole rows clipped to the triangles' spans."""
+    pixels and as whole rows (the passing interval's ends found from the edges' crossings)."""
     import hashlib
     e = golden_io.full_size()[key]
     sc = golden_io.full_size_scene(e)
@@ -225,7 +225,7 @@ def test_full_size_against_reference_digest(renderer, port, key, row_chunk):
     try:
         fg, dg, ig = gpu_draw(renderer, sc, cam, nm, lights)
     finally:
-        renderer.set_option(abi.OPT_ROW_CHUNK, 8)
+        renderer.set_option(abi.OPT_ROW_CHUNK, 32)
     assert hashlib.sha256(np.ascontiguousarray(dg).tobytes()).hexdigest() == e["depth"]
     assert hashlib.sha256(np.ascontiguousarray(fg).tobytes()).hexdigest() == e["frame_rgb"]
     fp, dp, ip, st = port.draw(sc, cam, nm, lights)
