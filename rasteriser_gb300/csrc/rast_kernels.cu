@@ -285,7 +285,9 @@ __global__ void __launch_bounds__(256) k_split_triangles(const int32_t* __restri
 constexpr int kSetupThreads = 256;
 constexpr int kSetupWarps = kSetupThreads / 32;
 // Bounding boxes at most this many pixels wide take the per-triangle path; wider ones are binned.
-constexpr uint32_t kSmallMaxRow = 32;
+// A whole-row item costs the same whatever its length, so whole rows take wider boxes.
+template <uint32_t kRowChunk>
+__host__ __device__ constexpr uint32_t small_max_row() { return kRowChunk == 32u ? 64u : 32u; }
 
 // Per-warp staging of 32 triangles. rec[j] holds lane j's triangle as five float4s so a lane
 // working on another lane's triangle loads it with five 16-byte shared loads:
@@ -323,7 +325,7 @@ struct SetupArgs {
 };
 
 // One thread per triangle: load, cull and bound it. Front-facing triangles whose bounding box is
-// at most small_max pixels and kSmallMaxRow pixels wide are rasterised by their warp; the others
+// at most small_max pixels and small_max_row() pixels wide are rasterised by their warp; the others
 // are appended to the binned list (one atomic per block) and counted into the tiles their box
 // overlaps.
 //
@@ -361,8 +363,8 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
             const uint32_t bw = brx - tlx + 1u, bh = bry - tly + 1u;
             const unsigned long long npx = (unsigned long long)bw * bh;
             make_edge_tri(v0, v1, v2, T);
-            if (npx <= a.small_max && bw <= kSmallMaxRow) {
-                cpr = (bw + kRowChunk - 1u) / kRowChunk;
+            if (npx <= a.small_max && bw <= small_max_row<kRowChunk>()) {
+                cpr = kRowChunk == 32u ? 1u : (bw + kRowChunk - 1u) / kRowChunk;
                 n_items = bh * cpr;
             } else {
                 large = true;
@@ -440,56 +442,66 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
             __syncwarp();
             const uint32_t tri_base = (uint32_t)(blockIdx.x * (int64_t)kSetupThreads + warp * 32);
             const unsigned lt_mask = (1u << lane) - 1u;
-            uint32_t q_head = 0, q_count = 0;  // warp-uniform
+            // Ring state (warp-uniform): the oldest pending run, the runs pending, the pixels of the
+            // oldest run already done, and the pixels pending.
+            uint32_t q_head = 0, q_count = 0, q_skip = 0, q_pix = 0;
 
-            // Exact test, depth and atomic (drawing.cpp:108-121) for the pixels of the n ring entries
-            // from q_head (n <= 32, warp-uniform). Each entry is a run of candidate pixels of one
-            // row; the runs are laid end to end and their pixels taken 32 at a time, one per lane,
-            // the run of a pixel found as the owner of an item is below.
-            auto drain = [&](uint32_t n) {
+            // Exact test, depth and atomic (drawing.cpp:108-121) for the next min(q_pix, 32) pending
+            // pixels, one per lane. The pending runs are laid end to end from the ring's head; a
+            // lane's pixel belongs to the last run starting at or before it (an OR-reduction of the
+            // runs' start positions). The runs it completes leave the ring, and a run it ends inside
+            // stays at the head with its done pixels counted in q_skip.
+            auto drain_round = [&]() {
                 uint32_t cnt = 0u, xy = 0u, own = 0u;
-                if ((uint32_t)lane < n) {
+                if ((uint32_t)lane < q_count) {
                     const uint32_t e = (q_head + lane) & 63u;
                     xy = S.q_xy[e];
                     own = S.q_om[e];
                     cnt = S.q_m[e];
-                }
-                const uint32_t incl_p = warp_inclusive_scan(cnt, lane);
-                const uint32_t total_p = __shfl_sync(kFull, incl_p, 31);
-                const uint32_t excl_p = incl_p - cnt;
-                int carry_p = 0;
-                for (uint32_t pb = 0; pb < total_p; pb += 32u) {
-                    const bool opens = cnt != 0u && excl_p >= pb && excl_p < pb + 32u;
-                    if (opens) S.slot[excl_p - pb] = lane;
-                    const unsigned starts = __reduce_or_sync(kFull, opens ? (1u << (excl_p - pb)) : 0u);
-                    __syncwarp();
-                    const unsigned upto = starts & (0xFFFFFFFFu >> (31 - lane));
-                    const int src = upto ? S.slot[31 - __clz(upto)] : carry_p;
-                    carry_p = __shfl_sync(kFull, src, 31);
-                    __syncwarp();
-                    const uint32_t sxy = __shfl_sync(kFull, xy, src);
-                    const uint32_t j = __shfl_sync(kFull, own, src) & 31u;
-                    const uint32_t sex = __shfl_sync(kFull, excl_p, src);
-                    const uint32_t k = pb + lane;
-                    if (k < total_p) {
-                        const uint32_t x = (sxy & 0xFFFFu) + (k - sex), y = sxy >> 16;
-                        const float4 q0 = S.rec[j][0], q1 = S.rec[j][1], q2 = S.rec[j][2], q3 = S.rec[j][3],
-                                     q4 = S.rec[j][4];
-                        const float py = (float)y, px = (float)x;
-                        const float p0 = mul(q2.x, sub(py, q0.w)), p1 = mul(q2.z, sub(py, q1.y)),
-                                    p2 = mul(q3.x, sub(py, q0.y));
-                        const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));
-                        const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));
-                        const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));
-                        const float b0 = dvd(e0, q1.z), b1 = dvd(e1, q1.z), b2 = dvd(e2, q1.z);
-                        if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
-                            ++c_inside;
-                            const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
-                            if (z == z && x < a.width && y < a.height)
-                                atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + j));
-                        }
+                    if (lane == 0) {
+                        xy += q_skip;  // x in the low half-word, below 2^15
+                        cnt -= q_skip;
                     }
                 }
+                const uint32_t incl_p = warp_inclusive_scan(cnt, lane);
+                const uint32_t excl_p = incl_p - cnt;
+                // Every pending run has a pixel, so the first 32 pixels lie within the first 32 runs.
+                const bool opens = cnt != 0u && excl_p < 32u;
+                if (opens) S.slot[excl_p] = lane;
+                const unsigned starts = __reduce_or_sync(kFull, opens ? (1u << excl_p) : 0u);
+                __syncwarp();
+                const int src = S.slot[31 - __clz(starts & (0xFFFFFFFFu >> (31 - lane)))];
+                __syncwarp();
+                const uint32_t sxy = __shfl_sync(kFull, xy, src);
+                const uint32_t j = __shfl_sync(kFull, own, src) & 31u;
+                const uint32_t sex = __shfl_sync(kFull, excl_p, src);
+                const uint32_t avail = min(q_pix, 32u);
+                if ((uint32_t)lane < avail) {
+                    const uint32_t x = (sxy & 0xFFFFu) + ((uint32_t)lane - sex), y = sxy >> 16;
+                    const float4 q0 = S.rec[j][0], q1 = S.rec[j][1], q2 = S.rec[j][2], q3 = S.rec[j][3],
+                                 q4 = S.rec[j][4];
+                    const float py = (float)y, px = (float)x;
+                    const float p0 = mul(q2.x, sub(py, q0.w)), p1 = mul(q2.z, sub(py, q1.y)),
+                                p2 = mul(q3.x, sub(py, q0.y));
+                    const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));
+                    const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));
+                    const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));
+                    const float b0 = dvd(e0, q1.z), b1 = dvd(e1, q1.z), b2 = dvd(e2, q1.z);
+                    if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
+                        ++c_inside;
+                        const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
+                        if (z == z && x < a.width && y < a.height)
+                            atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + j));
+                    }
+                }
+                // runs completed by this round: a prefix of the ring
+                const uint32_t nd = __popc(__ballot_sync(kFull, (uint32_t)lane < q_count && incl_p <= avail));
+                const uint32_t sk = __shfl_sync(kFull, excl_p, nd & 31u);
+                // A run left partly done is the one at lane nd (when there is one within the first 32).
+                q_skip = nd == 0u ? q_skip + avail : (nd < q_count && nd < 32u ? avail - sk : 0u);
+                q_head = (q_head + nd) & 63u;
+                q_count -= nd;
+                q_pix -= avail;
             };
 
             int carry = 0;
@@ -514,7 +526,7 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                     const uint32_t ocpr = S.cpr[owner];
                     const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
                     const uint32_t x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
-                    const uint32_t x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
+                    const uint32_t x_hi = kRowChunk == 32u ? S.brx[owner] : min(S.brx[owner], x_lo + (kRowChunk - 1u));
                     y = S.tly[owner] + row;
                     bool live = true;
 #ifdef RAST_CHECKED
@@ -603,7 +615,9 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                                     run_x = (uint32_t)L;
                                     run_n = (uint32_t)(U - L + 1);
                                 }
-                            } else if (!(thr > -INFINITY)) {
+                            } else if (!(thr > -INFINITY) || x_hi - x_lo >= 32u) {
+                                // every pixel a candidate, or a row too long for the mask below:
+                                // the whole row is the run (the exact test sorts it out)
                                 scan_row = false;
                                 run_x = x_lo;
                                 run_n = x_hi - x_lo + 1u;
@@ -647,16 +661,11 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                     S.q_m[e] = run_n;
                 }
                 q_count += __popc(m);
-                if (q_count >= 32u) {
-                    __syncwarp();
-                    drain(32u);
-                    __syncwarp();
-                    q_head = (q_head + 32u) & 63u;
-                    q_count -= 32u;
-                }
+                q_pix += __reduce_add_sync(kFull, run_n);
+                __syncwarp();
+                while (q_pix >= 32u) drain_round();  // leaves fewer than 32 runs pending
             }
-            __syncwarp();
-            if (q_count) drain(q_count);
+            if (q_pix) drain_round();
             __syncwarp();
         }
     }
@@ -707,6 +716,16 @@ __global__ void __launch_bounds__(1024) k_bin_scan(const uint32_t* __restrict__ 
     const uint32_t* cnt = counters + kCounterHeader;  // 16-byte aligned: the header is 8 words
     uint32_t* chunk_offset = offset + n_tiles + 1;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (counters[0] == 0u) {
+        // Nothing binned: every tile count is zero (the counters are cleared before each frame), and
+        // the consumers read only the totals.
+        if (tid == 0) {
+            offset[n_tiles] = 0u;
+            chunk_offset[n_tiles] = 0u;
+            *stat_slot0(stats, STAT_BIN_ENTRIES) = 0ull;
+        }
+        return;
+    }
     if (tid < 2) carry_s[tid] = 0;
     __syncthreads();
     for (uint32_t base = 0; base < n_tiles; base += 8192) {
@@ -864,6 +883,7 @@ __global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t* chunk_offset = a.offset + a.n_tiles + 1;
     const uint32_t total_items = chunk_offset[a.n_tiles];
+    if (total_items == 0u) return;  // nothing binned
     const uint32_t n_large = a.counters[0];
     unsigned long long c_tested = 0, c_inside = 0;
 
