@@ -182,6 +182,15 @@ __device__ __forceinline__ void stat_add(unsigned long long* stats, int which, u
     }
 }
 
+// The same for a 32-bit count whose warp sum fits in 32 bits (one warp reduction instruction).
+__device__ __forceinline__ void stat_add32(unsigned long long* stats, int which, uint32_t v) {
+    v = __reduce_add_sync(kFull, v);
+    if ((threadIdx.x & 31) == 0 && v) {
+        const uint32_t warp_id = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) + blockIdx.y * 977u;
+        atomicAdd(stats + ((size_t)which * kStatSlots + (warp_id % kStatSlots)) * kSlotWords, (unsigned long long)v);
+    }
+}
+
 __device__ __forceinline__ unsigned long long* stat_slot0(unsigned long long* stats, int which) {
     return stats + (size_t)which * kStatSlots * kSlotWords;
 }
@@ -352,7 +361,7 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
     uint32_t n_items = 0, n_tiles = 0, cpr = 1;
     uint32_t tlx = 0, tly = 0, brx = 0, bry = 0;
     EdgeTri T;
-    unsigned long long c_front = 0;
+    uint32_t c_front = 0;
     bool large = false;
     if (t < a.ntri) {
         const int32_t i0 = a.tri_v[3 * t], i1 = a.tri_v[3 * t + 1], i2 = a.tri_v[3 * t + 2];
@@ -403,7 +412,9 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
         }
     }
 
-    unsigned long long c_tested = 0, c_inside = 0;
+    // Per-lane counts. A warp's small triangles have at most 32 * small_max (<= 2^21) tested pixels,
+    // so the warp sums fit in 32 bits.
+    uint32_t c_tested = 0, c_inside = 0;
 
     // Cooperative raster of the warp's small triangles. Each lane finds the run of pixels of its
     // item that the early reject cannot rule out: whole-row items (kRowChunk 32) from the two ends
@@ -422,22 +433,36 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
             const float sg = T.sgn;
             S.rec[lane][0] = make_float4(T.x0, T.y0, T.x1, T.y1);
             S.rec[lane][1] = make_float4(T.x2, T.y2, mul(sg, T.area), T.nthr);
-            S.rec[lane][2] = make_float4(mul(sg, T.d12x), mul(sg, T.d12y), mul(sg, T.d20x), mul(sg, T.d20y));
-            // Whole-row items (kRowChunk 32) also stage the reciprocals of the three edges' x
-            // coefficients, from which each row's crossing of an edge is estimated (see below).
+            const float A0 = mul(sg, T.d12x), B0 = mul(sg, T.d12y), A1 = mul(sg, T.d20x), B1 = mul(sg, T.d20y);
+            const float A2 = mul(sg, T.d01x), B2 = mul(sg, T.d01y);
+            S.rec[lane][2] = make_float4(A0, B0, A1, B1);
+            // Whole-row items (kRowChunk 32) also stage approximate reciprocals of the three edges'
+            // x coefficients, from which each row's crossing of an edge is estimated (see below),
+            // and flag (bit 31 of tly) the triangles whose rows may take that search: early reject
+            // on, every coefficient finite, and |A| * (|Y| + 2^16) < 2^126, so that each row's
+            // product A * (py - Y) is finite too.
             float r0 = 0.f, r1 = 0.f, r2 = 0.f;
+            uint32_t flag = 0u;
             if (kRowChunk == 32u) {
-                r0 = __frcp_rn(mul(sg, T.d12y));
-                r1 = __frcp_rn(mul(sg, T.d20y));
-                r2 = __frcp_rn(mul(sg, T.d01y));
+                r0 = __fdividef(1.0f, B0);
+                r1 = __fdividef(1.0f, B1);
+                r2 = __fdividef(1.0f, B2);
+                const bool searchable =
+                    T.nthr > -INFINITY &&
+                    fabsf(A0) * (fabsf(T.y1) + 65536.f) < 0x1p126f && fabsf(B0) < INFINITY && fabsf(T.x1) < INFINITY &&
+                    fabsf(A1) * (fabsf(T.y2) + 65536.f) < 0x1p126f && fabsf(B1) < INFINITY && fabsf(T.x2) < INFINITY &&
+                    fabsf(A2) * (fabsf(T.y0) + 65536.f) < 0x1p126f && fabsf(B2) < INFINITY && fabsf(T.x0) < INFINITY;
+                flag = searchable ? 0x80000000u : 0u;
             }
-            S.rec[lane][3] = make_float4(mul(sg, T.d01x), mul(sg, T.d01y), r0, r1);
+            S.rec[lane][3] = make_float4(A2, B2, r0, r1);
             S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, r2);
             S.tlx[lane] = tlx;
-            S.tly[lane] = tly;
+            S.tly[lane] = tly | flag;
             S.brx[lane] = brx;
-            S.cpr[lane] = cpr;
-            S.rcpr[lane] = __frcp_rn((float)cpr);
+            if (kRowChunk != 32u) {
+                S.cpr[lane] = cpr;
+                S.rcpr[lane] = __frcp_rn((float)cpr);
+            }
             S.incl[lane] = incl;
             __syncwarp();
             const uint32_t tri_base = (uint32_t)(blockIdx.x * (int64_t)kSetupThreads + warp * 32);
@@ -523,11 +548,21 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                 if (k < total) {
                     const uint32_t ostart = owner ? S.incl[owner - 1] : 0u;
                     const uint32_t local = k - ostart;
-                    const uint32_t ocpr = S.cpr[owner];
-                    const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
-                    const uint32_t x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
-                    const uint32_t x_hi = kRowChunk == 32u ? S.brx[owner] : min(S.brx[owner], x_lo + (kRowChunk - 1u));
-                    y = S.tly[owner] + row;
+                    uint32_t x_lo, x_hi;
+                    bool searchable = false;
+                    if constexpr (kRowChunk == 32u) {
+                        const uint32_t ty = S.tly[owner];
+                        searchable = (ty >> 31) != 0u;
+                        x_lo = S.tlx[owner];
+                        x_hi = S.brx[owner];
+                        y = (ty & 0x7FFFFFFFu) + local;
+                    } else {
+                        const uint32_t ocpr = S.cpr[owner];
+                        const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
+                        x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
+                        x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
+                        y = S.tly[owner] + row;
+                    }
                     bool live = true;
 #ifdef RAST_CHECKED
                     if (owner < 0 || owner > 31 || local >= S.incl[owner] - ostart || x_lo > x_hi ||
@@ -543,97 +578,107 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                         const float p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
                         const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
                         const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
-                        c_tested += x_hi - x_lo + 1u;  // the reference tests every pixel of the row
-                        // Along the row each staged edge value is f(px) = P - B*(px - X), every step
-                        // rounded. Rounding is monotone, so for finite P, B, X the computed f is
-                        // monotone in px: non-increasing for B > 0, non-decreasing for B < 0, and P
-                        // itself for B = 0. The pixels passing the early reject (f >= thr on all three
-                        // edges) are then one interval of the row.
                         const float thr = q1.w;
-                        const float2 P0 = make_float2(p0, p0), P1 = make_float2(p1, p1), P2 = make_float2(p2, p2);
-                        const float2 NX1 = make_float2(-q0.z, -q0.z), NX2 = make_float2(-q1.x, -q1.x),
-                                     NX0 = make_float2(-q0.x, -q0.x);
-                        const float2 B0 = make_float2(q2.y, q2.y), B1 = make_float2(q2.w, q2.w),
-                                     B2 = make_float2(q3.y, q3.y);
-                        // Edge values at pixel centres (a, b): __fadd2_rn / __fmul2_rn round each
-                        // component exactly as __fadd_rn / __fmul_rn, and a - b is a + (-b) bit for
-                        // bit, so  e = p - d.y * (px - a.x)  ==  p + -(d.y * (px + -a.x)).
-                        auto edges2 = [&](float pa, float pb2, float2& e0, float2& e1, float2& e2) {
-                            const float2 px = make_float2(pa, pb2);
-                            const float2 t0 = __fmul2_rn(B0, __fadd2_rn(px, NX1));
-                            const float2 t1 = __fmul2_rn(B1, __fadd2_rn(px, NX2));
-                            const float2 t2 = __fmul2_rn(B2, __fadd2_rn(px, NX0));
-                            e0 = __fadd2_rn(P0, make_float2(-t0.x, -t0.y));
-                            e1 = __fadd2_rn(P1, make_float2(-t1.x, -t1.y));
-                            e2 = __fadd2_rn(P2, make_float2(-t2.x, -t2.y));
-                        };
+                        c_tested += x_hi - x_lo + 1u;  // the reference tests every pixel of the row
                         bool scan_row = true;  // evaluate every pixel of the item
-                        if (kRowChunk == 32u) {
-                            // Whole rows: find the interval's ends from an estimate of each edge's
-                            // crossing, X + P/B, and verify each end exactly at the two pixels either
-                            // side of it. A row whose ends do not verify (or whose coefficients are
-                            // not finite) evaluates every pixel instead.
-                            const int lo = (int)x_lo, hi = (int)x_hi;
-                            int L = lo, U = hi;
-                            bool ok = thr > -INFINITY;  // without the early reject every pixel is a candidate
-                            if (ok) {
+                        if constexpr (kRowChunk == 32u) {
+                            // Along the row each staged edge value is f(px) = P - B*(px - X), every
+                            // step rounded. Rounding is monotone, so for finite P, B, X the computed f
+                            // is monotone in px: non-increasing for B > 0, non-decreasing for B < 0,
+                            // and P itself for B = 0. The pixels passing the early reject (f >= thr on
+                            // all three edges) are then one interval of the row. Its ends are found
+                            // from an estimate of each edge's crossing, X + P/B, and each end is
+                            // verified exactly at the two pixels either side of it. A row whose ends
+                            // do not verify evaluates every pixel instead.
+                            if (searchable) {
                                 const float r2 = S.rec[owner][4].w;
                                 const float P[3] = {p0, p1, p2}, B[3] = {q2.y, q2.w, q3.y};
                                 const float X[3] = {q0.z, q1.x, q0.x}, R[3] = {q3.z, q3.w, r2};
+                                const float lof = (float)x_lo, hif = (float)x_hi;
+                                float Lf = lof, Uf = hif;
+                                bool ok = true;
 #pragma unroll
                                 for (int ed = 0; ed < 3; ++ed) {
-                                    const bool finite = fabsf(P[ed]) < INFINITY && fabsf(X[ed]) < INFINITY &&
-                                                        fabsf(B[ed]) < INFINITY;
-                                    ok = ok && finite;
                                     if (B[ed] == 0.f) {
-                                        if (!(P[ed] >= thr)) U = lo - 1;  // f = P along the whole row
+                                        if (!(P[ed] >= thr)) Uf = lof - 1.f;  // f = P along the whole row
                                         continue;
                                     }
                                     const float est = X[ed] + P[ed] * R[ed];
-                                    float mf = B[ed] > 0.f ? floorf(est) : ceilf(est) - 1.f;
-                                    mf = fminf(fmaxf(mf, (float)(lo - 1)), (float)hi);  // a NaN estimate gives lo - 1
-                                    const int m = (int)mf;
-                                    // f at pixels m and m + 1 (exact integers)
-                                    const float2 px = make_float2((float)m, (float)(m + 1));
-                                    const float2 t = __fmul2_rn(make_float2(B[ed], B[ed]),
-                                                                __fadd2_rn(px, make_float2(-X[ed], -X[ed])));
-                                    const float2 f = __fadd2_rn(make_float2(P[ed], P[ed]), make_float2(-t.x, -t.y));
-                                    const bool in0 = m >= lo, in1 = m + 1 <= hi;
-                                    const bool pass0 = f.x >= thr, pass1 = f.y >= thr;
+                                    const float fl = floorf(est);
+                                    // B > 0: the last passing pixel is floor(est); B < 0: the first is
+                                    // ceil(est), and m is the pixel before it. A NaN estimate gives lo - 1.
+                                    float mf = (B[ed] < 0.f && fl == est) ? fl - 1.f : fl;
+                                    mf = fminf(fmaxf(mf, lof - 1.f), hif);
+                                    const float mf1 = mf + 1.f;  // exact: integers below 2^16
+                                    const float f0 = sub(P[ed], mul(B[ed], sub(mf, X[ed])));
+                                    const float f1 = sub(P[ed], mul(B[ed], sub(mf1, X[ed])));
+                                    const bool in0 = mf >= lof, in1 = mf1 <= hif;
+                                    const bool pass0 = f0 >= thr, pass1 = f1 >= thr;
                                     if (B[ed] > 0.f) {  // passing pixels end at m
                                         ok = ok && (!in0 || pass0) && (!in1 || !pass1);
-                                        U = min(U, m);
+                                        Uf = fminf(Uf, mf);
                                     } else {            // passing pixels start at m + 1
                                         ok = ok && (!in0 || !pass0) && (!in1 || pass1);
-                                        L = max(L, m + 1);
+                                        Lf = fmaxf(Lf, mf1);
                                     }
                                 }
-                            }
-                            if (ok) {
-                                scan_row = false;
-                                if (L <= U) {
-                                    run_x = (uint32_t)L;
-                                    run_n = (uint32_t)(U - L + 1);
+                                if (ok) {
+                                    scan_row = false;
+                                    if (Lf <= Uf) {
+                                        run_x = (uint32_t)Lf;
+                                        run_n = (uint32_t)(Uf - Lf) + 1u;
+                                    }
                                 }
-                            } else if (!(thr > -INFINITY) || x_hi - x_lo >= 32u) {
-                                // every pixel a candidate, or a row too long for the mask below:
-                                // the whole row is the run (the exact test sorts it out)
-                                scan_row = false;
+                            } else if (!(thr > -INFINITY)) {
+                                scan_row = false;  // no early reject: every pixel is a candidate
                                 run_x = x_lo;
                                 run_n = x_hi - x_lo + 1u;
                             }
-                        }
-                        if (scan_row) {
+                            if (scan_row && x_hi - x_lo >= 32u) {
+                                scan_row = false;  // too long for the mask below: the whole row
+                                run_x = x_lo;
+                                run_n = x_hi - x_lo + 1u;
+                            }
+                            if (scan_row) {
+                                const uint32_t n_px = x_hi - x_lo + 1u;
+                                uint32_t mask = 0u;
+                                for (uint32_t sx = 0; sx < n_px; ++sx) {
+                                    const float px = (float)(x_lo + sx);
+                                    const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));
+                                    const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));
+                                    const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));
+                                    if (fminf(fminf(e0, e1), e2) >= thr) mask |= 1u << sx;
+                                }
+                                if (mask) {
+                                    const uint32_t f0 = __ffs(mask) - 1u;
+                                    run_x = x_lo + f0;
+                                    run_n = (32u - __clz(mask)) - f0;
+                                }
+                            }
+                        } else {
                             // Early reject on the smallest edge value of each pixel; the run spans the
-                            // first to the last candidate.
+                            // first to the last candidate. Two pixels per instruction: __fadd2_rn /
+                            // __fmul2_rn round each component exactly as __fadd_rn / __fmul_rn, and
+                            // a - b is a + (-b) bit for bit, so
+                            //   e = p - d.y * (px - a.x)  ==  p + -(d.y * (px + -a.x)).
+                            const float2 P0 = make_float2(p0, p0), P1 = make_float2(p1, p1), P2 = make_float2(p2, p2);
+                            const float2 NX1 = make_float2(-q0.z, -q0.z), NX2 = make_float2(-q1.x, -q1.x),
+                                         NX0 = make_float2(-q0.x, -q0.x);
+                            const float2 B0 = make_float2(q2.y, q2.y), B1 = make_float2(q2.w, q2.w),
+                                         B2 = make_float2(q3.y, q3.y);
                             const float px_lo = (float)x_lo;
                             const uint32_t n_px = x_hi - x_lo + 1u;
                             uint32_t mask = 0u;
-#pragma unroll(kRowChunk == 32u ? 1 : kRowChunk / 2)
-                            for (uint32_t sx = 0; sx < (kRowChunk == 32u ? n_px : kRowChunk); sx += 2) {
+#pragma unroll
+                            for (uint32_t sx = 0; sx < kRowChunk; sx += 2) {
                                 // pixel centres px_lo + sx, + sx + 1: exact, integers below 2^24
-                                float2 e0, e1, e2;
-                                edges2(add(px_lo, (float)sx), add(px_lo, (float)(sx + 1)), e0, e1, e2);
+                                const float2 px = make_float2(add(px_lo, (float)sx), add(px_lo, (float)(sx + 1)));
+                                const float2 t0 = __fmul2_rn(B0, __fadd2_rn(px, NX1));
+                                const float2 t1 = __fmul2_rn(B1, __fadd2_rn(px, NX2));
+                                const float2 t2 = __fmul2_rn(B2, __fadd2_rn(px, NX0));
+                                const float2 e0 = __fadd2_rn(P0, make_float2(-t0.x, -t0.y));
+                                const float2 e1 = __fadd2_rn(P1, make_float2(-t1.x, -t1.y));
+                                const float2 e2 = __fadd2_rn(P2, make_float2(-t2.x, -t2.y));
                                 const bool ca = sx < n_px && fminf(fminf(e0.x, e1.x), e2.x) >= thr;
                                 const bool cb = sx + 1 < n_px && fminf(fminf(e0.y, e1.y), e2.y) >= thr;
                                 mask |= ((uint32_t)ca | ((uint32_t)cb << 1)) << sx;
@@ -697,9 +742,9 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
         }
     }
 
-    stat_add(a.stats, STAT_FRONT, c_front);
-    stat_add(a.stats, STAT_TESTED, c_tested);
-    stat_add(a.stats, STAT_INSIDE, c_inside);
+    stat_add32(a.stats, STAT_FRONT, c_front);
+    stat_add32(a.stats, STAT_TESTED, c_tested);
+    stat_add32(a.stats, STAT_INSIDE, c_inside);
 }
 
 // Exclusive scans over the tiles: entry offsets (the tile counts) into offset[0..n_tiles] and
