@@ -599,28 +599,27 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                                 bool ok = true;
 #pragma unroll
                                 for (int ed = 0; ed < 3; ++ed) {
-                                    if (B[ed] == 0.f) {
-                                        if (!(P[ed] >= thr)) Uf = lof - 1.f;  // f = P along the whole row
-                                        continue;
-                                    }
+                                    // Branch-free. B >= 0 edges (B = 0 included) pass a prefix of
+                                    // the row, B < 0 edges a suffix. For B = 0, f = P along the row,
+                                    // so the prefix is the whole row or nothing.
+                                    const bool pos = B[ed] >= 0.f;
                                     const float est = X[ed] + P[ed] * R[ed];
                                     const float fl = floorf(est);
                                     // B > 0: the last passing pixel is floor(est); B < 0: the first is
-                                    // ceil(est), and m is the pixel before it. A NaN estimate gives lo - 1.
-                                    float mf = (B[ed] < 0.f && fl == est) ? fl - 1.f : fl;
-                                    mf = fminf(fmaxf(mf, lof - 1.f), hif);
+                                    // ceil(est), and m is the pixel before it.
+                                    float mf = (!pos && fl == est) ? fl - 1.f : fl;
+                                    if (B[ed] == 0.f) mf = P[ed] >= thr ? hif : lof - 1.f;
+                                    mf = fminf(fmaxf(mf, lof - 1.f), hif);  // a NaN estimate gives lo - 1
                                     const float mf1 = mf + 1.f;  // exact: integers below 2^16
                                     const float f0 = sub(P[ed], mul(B[ed], sub(mf, X[ed])));
                                     const float f1 = sub(P[ed], mul(B[ed], sub(mf1, X[ed])));
                                     const bool in0 = mf >= lof, in1 = mf1 <= hif;
                                     const bool pass0 = f0 >= thr, pass1 = f1 >= thr;
-                                    if (B[ed] > 0.f) {  // passing pixels end at m
-                                        ok = ok && (!in0 || pass0) && (!in1 || !pass1);
-                                        Uf = fminf(Uf, mf);
-                                    } else {            // passing pixels start at m + 1
-                                        ok = ok && (!in0 || !pass0) && (!in1 || pass1);
-                                        Lf = fmaxf(Lf, mf1);
-                                    }
+                                    // the prefix ends at m (pixel m passes, m + 1 does not), or the
+                                    // suffix starts at m + 1 (m does not pass, m + 1 does)
+                                    ok = ok && (!in0 || pass0 == pos) && (!in1 || pass1 != pos);
+                                    Uf = pos ? fminf(Uf, mf) : Uf;
+                                    Lf = pos ? Lf : fmaxf(Lf, mf1);
                                 }
                                 if (ok) {
                                     scan_row = false;
