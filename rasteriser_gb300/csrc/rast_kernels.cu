@@ -294,25 +294,32 @@ __global__ void __launch_bounds__(256) k_split_triangles(const int32_t* __restri
 constexpr int kSetupThreads = 256;
 constexpr int kSetupWarps = kSetupThreads / 32;
 // Bounding boxes at most this many pixels wide take the per-triangle path; wider ones are binned.
-// A whole-row item costs the same whatever its length, so whole rows take wider boxes.
+// Whole-row items cost the same whatever their length and run along the box's longer side, so for
+// them the limit is on the shorter side.
 template <uint32_t kRowChunk>
 __host__ __device__ constexpr uint32_t small_max_row() { return kRowChunk == 32u ? 64u : 32u; }
 
 // Per-warp staging of 32 triangles. rec[j] holds lane j's triangle as five float4s so a lane
-// working on another lane's triangle loads it with five 16-byte shared loads:
-//   rec[j][0] = x0 y0 x1 y1               rec[j][1] = x2 y2 |area| nthr
-//   rec[j][2] = sgn * (d12x d12y d20x d20y)
-//   rec[j][3] = sgn * (d01x d01y), r0 r1  rec[j][4] = z0 z1 z2 r2
-// (sgn = sign of the area; r0..r2 = reciprocals of the staged x coefficients, whole-row items only).
-// Its integer data (bounding box, items per row) is kept in integer arrays.
+// working on another lane's triangle loads it with 16-byte shared loads:
+//   rec[j][k] = U_k V_k W_k Z_k  (k = 0, 1, 2: edge k)   rec[j][3] = R_0 R_1 R_2 nthr
+//   rec[j][4] = z0 z1 z2 |area|
+// Edge k's value at the pixel with coordinate t along the item and `fixed` across it is
+//   f_k = U_k * (fixed - V_k) - W_k * (t - Z_k),
+// which is sgn(area) times the reference's edge function (drawing.cpp:36-39) bit for bit: for items
+// along rows (t = px, fixed = py) U, V, W, Z = A, Y, B, X; along columns (t = py, fixed = px)
+// U, V, W, Z = -B, X, -A, Y, where A = sgn * (b.x - a.x), B = sgn * (b.y - a.y) and (X, Y) is the
+// edge's first vertex. Negating a product's factor negates the rounded product, and
+// -p - (-q) = q - p exactly, so both give the same rounded f. R_k ~ 1/W_k (whole-row items only).
+// The integer data (item range along, first item across and flags, items per row) is kept in
+// integer arrays.
 struct SetupStage {
     float4 rec[32][5];
     uint32_t tlx[32], tly[32], brx[32], cpr[32];
     float rcpr[32];
     uint32_t incl[32];
     int slot[32];
-    // Ring of candidate runs (pixels of one row the early reject could not rule out): first pixel
-    // (x | y << 16), owning lane, and the run's length.
+    // Ring of candidate runs (pixels of one item the early reject could not rule out): first pixel
+    // (t | fixed << 16), owning lane with the column flag in bit 5, and the run's length.
     uint32_t q_xy[64], q_om[64], q_m[64];
 };
 
@@ -362,7 +369,7 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
     uint32_t tlx = 0, tly = 0, brx = 0, bry = 0;
     EdgeTri T;
     uint32_t c_front = 0;
-    bool large = false;
+    bool large = false, col = false;
     if (t < a.ntri) {
         const int32_t i0 = a.tri_v[3 * t], i1 = a.tri_v[3 * t + 1], i2 = a.tri_v[3 * t + 2];
         const float4 v0 = a.rv[i0], v1 = a.rv[i1], v2 = a.rv[i2];
@@ -372,9 +379,14 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
             const uint32_t bw = brx - tlx + 1u, bh = bry - tly + 1u;
             const unsigned long long npx = (unsigned long long)bw * bh;
             make_edge_tri(v0, v1, v2, T);
-            if (npx <= a.small_max && bw <= small_max_row<kRowChunk>()) {
-                cpr = kRowChunk == 32u ? 1u : (bw + kRowChunk - 1u) / kRowChunk;
-                n_items = bh * cpr;
+            if (npx <= a.small_max && (kRowChunk == 32u ? min(bw, bh) : bw) <= small_max_row<kRowChunk>()) {
+                if (kRowChunk == 32u) {
+                    col = bw < bh;  // whole items along the longer side: fewer of them
+                    n_items = col ? bw : bh;
+                } else {
+                    cpr = (bw + kRowChunk - 1u) / kRowChunk;
+                    n_items = bh * cpr;
+                }
             } else {
                 large = true;
             }
@@ -417,48 +429,45 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
     uint32_t c_tested = 0, c_inside = 0;
 
     // Cooperative raster of the warp's small triangles. Each lane finds the run of pixels of its
-    // item that the early reject cannot rule out: whole-row items (kRowChunk 32) from the two ends
-    // of the row's passing interval, verified exactly, shorter items by evaluating the edges at each
-    // of their pixels. Non-empty runs go to a per-warp ring, and whenever it holds 32 of them the
-    // warp shares out their pixels, one per lane, for the exact test (the reference's three
-    // divisions), the depth and the atomic. So the divisions and atomics run on full warps whatever
-    // the runs' lengths.
+    // item that the early reject cannot rule out: whole items (kRowChunk 32: a row or a column of
+    // the box) from the two ends of their passing interval, verified exactly, shorter items (row
+    // chunks) by evaluating the edges at each of their pixels. Non-empty runs go to a per-warp ring,
+    // and whenever 32 pixels are pending the warp shares them out, one per lane, for the exact test
+    // (the reference's three divisions), the depth and the atomic. So the divisions and atomics run
+    // on full warps whatever the runs' lengths.
     {
         const uint32_t incl = warp_inclusive_scan(n_items, lane);
         const uint32_t total = __shfl_sync(kFull, incl, 31);
         if (total) {
             const uint32_t start = incl - n_items;
-            // The edge coefficients are staged multiplied by sgn (+-1, exact), so the staged edge
-            // values are f = sgn*e bit for bit, and f / (sgn*area) is e / area exactly.
+            // The coefficients are staged multiplied by sgn (+-1, exact), so the staged edge values
+            // are f = sgn*e bit for bit, and f / (sgn*area) is e / area exactly.
             const float sg = T.sgn;
-            S.rec[lane][0] = make_float4(T.x0, T.y0, T.x1, T.y1);
-            S.rec[lane][1] = make_float4(T.x2, T.y2, mul(sg, T.area), T.nthr);
-            const float A0 = mul(sg, T.d12x), B0 = mul(sg, T.d12y), A1 = mul(sg, T.d20x), B1 = mul(sg, T.d20y);
-            const float A2 = mul(sg, T.d01x), B2 = mul(sg, T.d01y);
-            S.rec[lane][2] = make_float4(A0, B0, A1, B1);
-            // Whole-row items (kRowChunk 32) also stage approximate reciprocals of the three edges'
-            // x coefficients, from which each row's crossing of an edge is estimated (see below),
-            // and flag (bit 31 of tly) the triangles whose rows may take that search: early reject
-            // on, every coefficient finite, and |A| * (|Y| + 2^16) < 2^126, so that each row's
-            // product A * (py - Y) is finite too.
-            float r0 = 0.f, r1 = 0.f, r2 = 0.f;
-            uint32_t flag = 0u;
-            if (kRowChunk == 32u) {
-                r0 = __fdividef(1.0f, B0);
-                r1 = __fdividef(1.0f, B1);
-                r2 = __fdividef(1.0f, B2);
-                const bool searchable =
-                    T.nthr > -INFINITY &&
-                    fabsf(A0) * (fabsf(T.y1) + 65536.f) < 0x1p126f && fabsf(B0) < INFINITY && fabsf(T.x1) < INFINITY &&
-                    fabsf(A1) * (fabsf(T.y2) + 65536.f) < 0x1p126f && fabsf(B1) < INFINITY && fabsf(T.x2) < INFINITY &&
-                    fabsf(A2) * (fabsf(T.y0) + 65536.f) < 0x1p126f && fabsf(B2) < INFINITY && fabsf(T.x0) < INFINITY;
-                flag = searchable ? 0x80000000u : 0u;
+            const float A[3] = {mul(sg, T.d12x), mul(sg, T.d20x), mul(sg, T.d01x)};
+            const float B[3] = {mul(sg, T.d12y), mul(sg, T.d20y), mul(sg, T.d01y)};
+            const float X[3] = {T.x1, T.x2, T.x0}, Y[3] = {T.y1, T.y2, T.y0};
+            float R[3] = {0.f, 0.f, 0.f};
+            // Whole items also flag (bit 31 of the `fixed` word) the triangles whose items may take
+            // the crossing search: early reject on, every coefficient finite, and
+            // |U| * (|V| + 2^16) < 2^126, so that each item's product U * (fixed - V) is finite too.
+            bool searchable = T.nthr > -INFINITY;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float U = col ? -B[k] : A[k], V = col ? X[k] : Y[k];
+                const float W = col ? -A[k] : B[k], Z = col ? Y[k] : X[k];
+                S.rec[lane][k] = make_float4(U, V, W, Z);
+                if (kRowChunk == 32u) {
+                    R[k] = __fdividef(1.0f, W);  // an estimate: the search verifies what it gives
+                    searchable = searchable && fabsf(U) * (fabsf(V) + 65536.f) < 0x1p126f && fabsf(W) < INFINITY &&
+                                 fabsf(Z) < INFINITY;
+                }
             }
-            S.rec[lane][3] = make_float4(A2, B2, r0, r1);
-            S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, r2);
-            S.tlx[lane] = tlx;
-            S.tly[lane] = tly | flag;
-            S.brx[lane] = brx;
+            S.rec[lane][3] = make_float4(R[0], R[1], R[2], T.nthr);
+            S.rec[lane][4] = make_float4(T.z0, T.z1, T.z2, mul(sg, T.area));
+            S.tlx[lane] = col ? tly : tlx;  // the items' range along
+            S.brx[lane] = col ? bry : brx;
+            S.tly[lane] = (col ? tlx : tly) | (kRowChunk == 32u && searchable ? 0x80000000u : 0u) |
+                          (col ? 0x40000000u : 0u);  // the first item across, flags
             if (kRowChunk != 32u) {
                 S.cpr[lane] = cpr;
                 S.rcpr[lane] = __frcp_rn((float)cpr);
@@ -477,14 +486,14 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
             // runs' start positions). The runs it completes leave the ring, and a run it ends inside
             // stays at the head with its done pixels counted in q_skip.
             auto drain_round = [&]() {
-                uint32_t cnt = 0u, xy = 0u, own = 0u;
+                uint32_t cnt = 0u, tf = 0u, own = 0u;
                 if ((uint32_t)lane < q_count) {
                     const uint32_t e = (q_head + lane) & 63u;
-                    xy = S.q_xy[e];
+                    tf = S.q_xy[e];
                     own = S.q_om[e];
                     cnt = S.q_m[e];
                     if (lane == 0) {
-                        xy += q_skip;  // x in the low half-word, below 2^15
+                        tf += q_skip;  // t in the low half-word, below 2^15
                         cnt -= q_skip;
                     }
                 }
@@ -497,24 +506,24 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                 __syncwarp();
                 const int src = S.slot[31 - __clz(starts & (0xFFFFFFFFu >> (31 - lane)))];
                 __syncwarp();
-                const uint32_t sxy = __shfl_sync(kFull, xy, src);
-                const uint32_t j = __shfl_sync(kFull, own, src) & 31u;
+                const uint32_t stf = __shfl_sync(kFull, tf, src);
+                const uint32_t som = __shfl_sync(kFull, own, src);
                 const uint32_t sex = __shfl_sync(kFull, excl_p, src);
                 const uint32_t avail = min(q_pix, 32u);
                 if ((uint32_t)lane < avail) {
-                    const uint32_t x = (sxy & 0xFFFFu) + ((uint32_t)lane - sex), y = sxy >> 16;
-                    const float4 q0 = S.rec[j][0], q1 = S.rec[j][1], q2 = S.rec[j][2], q3 = S.rec[j][3],
-                                 q4 = S.rec[j][4];
-                    const float py = (float)y, px = (float)x;
-                    const float p0 = mul(q2.x, sub(py, q0.w)), p1 = mul(q2.z, sub(py, q1.y)),
-                                p2 = mul(q3.x, sub(py, q0.y));
-                    const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));
-                    const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));
-                    const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));
-                    const float b0 = dvd(e0, q1.z), b1 = dvd(e1, q1.z), b2 = dvd(e2, q1.z);
+                    const uint32_t j = som & 31u;
+                    const uint32_t tt = (stf & 0xFFFFu) + ((uint32_t)lane - sex), fx = stf >> 16;
+                    const float4 q0 = S.rec[j][0], q1 = S.rec[j][1], q2 = S.rec[j][2], q4 = S.rec[j][4];
+                    const float ff = (float)fx, tv = (float)tt;
+                    const float e0 = sub(mul(q0.x, sub(ff, q0.y)), mul(q0.z, sub(tv, q0.w)));
+                    const float e1 = sub(mul(q1.x, sub(ff, q1.y)), mul(q1.z, sub(tv, q1.w)));
+                    const float e2 = sub(mul(q2.x, sub(ff, q2.y)), mul(q2.z, sub(tv, q2.w)));
+                    const float b0 = dvd(e0, q4.w), b1 = dvd(e1, q4.w), b2 = dvd(e2, q4.w);
                     if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
                         ++c_inside;
                         const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
+                        const bool cl = (som & 32u) != 0u;
+                        const uint32_t x = cl ? fx : tt, y = cl ? tt : fx;
                         if (z == z && x < a.width && y < a.height)
                             atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + j));
                     }
@@ -542,31 +551,33 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                 carry = __shfl_sync(kFull, owner, 31);
                 __syncwarp();
                 const uint32_t k = base + lane;
-                // The item's candidate run: pixels run_x .. run_x + run_n - 1 of row y. It holds every
-                // pixel of the item that the early reject cannot rule out (and possibly more).
-                uint32_t run_x = 0u, run_n = 0u, y = 0u;
+                // The item's candidate run: pixels run_t .. run_t + run_n - 1 along the item at
+                // `fixed` across it. It holds every pixel of the item that the early reject cannot
+                // rule out (and possibly more).
+                uint32_t run_t = 0u, run_n = 0u, fixed = 0u, cflag = 0u;
                 if (k < total) {
                     const uint32_t ostart = owner ? S.incl[owner - 1] : 0u;
                     const uint32_t local = k - ostart;
-                    uint32_t x_lo, x_hi;
+                    uint32_t lo, hi;
                     bool searchable = false;
                     if constexpr (kRowChunk == 32u) {
-                        const uint32_t ty = S.tly[owner];
-                        searchable = (ty >> 31) != 0u;
-                        x_lo = S.tlx[owner];
-                        x_hi = S.brx[owner];
-                        y = (ty & 0x7FFFFFFFu) + local;
+                        const uint32_t fw = S.tly[owner];
+                        searchable = (fw >> 31) != 0u;
+                        cflag = (fw >> 25) & 32u;  // the column flag, as ring bit 5
+                        lo = S.tlx[owner];
+                        hi = S.brx[owner];
+                        fixed = (fw & 0x3FFFFFFFu) + local;
                     } else {
                         const uint32_t ocpr = S.cpr[owner];
                         const uint32_t row = ocpr == 1u ? local : div_small(local, ocpr, S.rcpr[owner]);
-                        x_lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
-                        x_hi = min(S.brx[owner], x_lo + (kRowChunk - 1u));
-                        y = S.tly[owner] + row;
+                        lo = S.tlx[owner] + (local - row * ocpr) * kRowChunk;
+                        hi = min(S.brx[owner], lo + (kRowChunk - 1u));
+                        fixed = S.tly[owner] + row;
                     }
                     bool live = true;
 #ifdef RAST_CHECKED
-                    if (owner < 0 || owner > 31 || local >= S.incl[owner] - ostart || x_lo > x_hi ||
-                        x_hi >= a.width || y >= a.height) {
+                    if (owner < 0 || owner > 31 || local >= S.incl[owner] - ostart || lo > hi ||
+                        hi >= (cflag ? a.height : a.width) || fixed >= (cflag ? a.width : a.height)) {
                         report(a.counters, 1u, (uint32_t)owner);
                         live = false;
                     }
@@ -574,45 +585,44 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                     if (live) {
                         const float4 q0 = S.rec[owner][0], q1 = S.rec[owner][1], q2 = S.rec[owner][2],
                                      q3 = S.rec[owner][3];
-                        const float py = (float)y;
-                        const float p0 = mul(q2.x, sub(py, q0.w));  // d12x * (py - y1)
-                        const float p1 = mul(q2.z, sub(py, q1.y));  // d20x * (py - y2)
-                        const float p2 = mul(q3.x, sub(py, q0.y));  // d01x * (py - y0)
-                        const float thr = q1.w;
-                        c_tested += x_hi - x_lo + 1u;  // the reference tests every pixel of the row
+                        const float ff = (float)fixed;
+                        const float K0 = mul(q0.x, sub(ff, q0.y));  // U * (fixed - V), edge 0
+                        const float K1 = mul(q1.x, sub(ff, q1.y));
+                        const float K2 = mul(q2.x, sub(ff, q2.y));
+                        const float thr = q3.w;
+                        c_tested += hi - lo + 1u;  // the reference tests every pixel of the box
                         bool scan_row = true;  // evaluate every pixel of the item
                         if constexpr (kRowChunk == 32u) {
-                            // Along the row each staged edge value is f(px) = P - B*(px - X), every
-                            // step rounded. Rounding is monotone, so for finite P, B, X the computed f
-                            // is monotone in px: non-increasing for B > 0, non-decreasing for B < 0,
-                            // and P itself for B = 0. The pixels passing the early reject (f >= thr on
-                            // all three edges) are then one interval of the row. Its ends are found
-                            // from an estimate of each edge's crossing, X + P/B, and each end is
-                            // verified exactly at the two pixels either side of it. A row whose ends
-                            // do not verify evaluates every pixel instead.
+                            // Along the item each staged edge value is f(t) = K - W*(t - Z), every
+                            // step rounded. Rounding is monotone, so for finite K, W, Z the computed
+                            // f is monotone in t: non-increasing for W > 0, non-decreasing for W < 0,
+                            // and K itself for W = 0. The pixels passing the early reject (f >= thr
+                            // on all three edges) are then one interval of the item. Its ends are
+                            // found from an estimate of each edge's crossing, Z + K/W, and each end
+                            // is verified exactly at the two pixels either side of it. An item whose
+                            // ends do not verify evaluates every pixel instead.
                             if (searchable) {
-                                const float r2 = S.rec[owner][4].w;
-                                const float P[3] = {p0, p1, p2}, B[3] = {q2.y, q2.w, q3.y};
-                                const float X[3] = {q0.z, q1.x, q0.x}, R[3] = {q3.z, q3.w, r2};
-                                const float lof = (float)x_lo, hif = (float)x_hi;
+                                const float P[3] = {K0, K1, K2}, Wc[3] = {q0.z, q1.z, q2.z};
+                                const float Zc[3] = {q0.w, q1.w, q2.w}, Rc[3] = {q3.x, q3.y, q3.z};
+                                const float lof = (float)lo, hif = (float)hi;
                                 float Lf = lof, Uf = hif;
                                 bool ok = true;
 #pragma unroll
                                 for (int ed = 0; ed < 3; ++ed) {
-                                    // Branch-free. B >= 0 edges (B = 0 included) pass a prefix of
-                                    // the row, B < 0 edges a suffix. For B = 0, f = P along the row,
-                                    // so the prefix is the whole row or nothing.
-                                    const bool pos = B[ed] >= 0.f;
-                                    const float est = X[ed] + P[ed] * R[ed];
+                                    // Branch-free. W >= 0 edges (W = 0 included) pass a prefix of
+                                    // the item, W < 0 edges a suffix. For W = 0, f = K along the item,
+                                    // so the prefix is the whole item or nothing.
+                                    const bool pos = Wc[ed] >= 0.f;
+                                    const float est = Zc[ed] + P[ed] * Rc[ed];
                                     const float fl = floorf(est);
-                                    // B > 0: the last passing pixel is floor(est); B < 0: the first is
+                                    // W > 0: the last passing pixel is floor(est); W < 0: the first is
                                     // ceil(est), and m is the pixel before it.
                                     float mf = (!pos && fl == est) ? fl - 1.f : fl;
-                                    if (B[ed] == 0.f) mf = P[ed] >= thr ? hif : lof - 1.f;
+                                    if (Wc[ed] == 0.f) mf = P[ed] >= thr ? hif : lof - 1.f;
                                     mf = fminf(fmaxf(mf, lof - 1.f), hif);  // a NaN estimate gives lo - 1
                                     const float mf1 = mf + 1.f;  // exact: integers below 2^16
-                                    const float f0 = sub(P[ed], mul(B[ed], sub(mf, X[ed])));
-                                    const float f1 = sub(P[ed], mul(B[ed], sub(mf1, X[ed])));
+                                    const float f0 = sub(P[ed], mul(Wc[ed], sub(mf, Zc[ed])));
+                                    const float f1 = sub(P[ed], mul(Wc[ed], sub(mf1, Zc[ed])));
                                     const bool in0 = mf >= lof, in1 = mf1 <= hif;
                                     const bool pass0 = f0 >= thr, pass1 = f1 >= thr;
                                     // the prefix ends at m (pixel m passes, m + 1 does not), or the
@@ -624,33 +634,33 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                                 if (ok) {
                                     scan_row = false;
                                     if (Lf <= Uf) {
-                                        run_x = (uint32_t)Lf;
+                                        run_t = (uint32_t)Lf;
                                         run_n = (uint32_t)(Uf - Lf) + 1u;
                                     }
                                 }
                             } else if (!(thr > -INFINITY)) {
                                 scan_row = false;  // no early reject: every pixel is a candidate
-                                run_x = x_lo;
-                                run_n = x_hi - x_lo + 1u;
+                                run_t = lo;
+                                run_n = hi - lo + 1u;
                             }
-                            if (scan_row && x_hi - x_lo >= 32u) {
-                                scan_row = false;  // too long for the mask below: the whole row
-                                run_x = x_lo;
-                                run_n = x_hi - x_lo + 1u;
+                            if (scan_row && hi - lo >= 32u) {
+                                scan_row = false;  // too long for the mask below: the whole item
+                                run_t = lo;
+                                run_n = hi - lo + 1u;
                             }
                             if (scan_row) {
-                                const uint32_t n_px = x_hi - x_lo + 1u;
+                                const uint32_t n_px = hi - lo + 1u;
                                 uint32_t mask = 0u;
                                 for (uint32_t sx = 0; sx < n_px; ++sx) {
-                                    const float px = (float)(x_lo + sx);
-                                    const float e0 = sub(p0, mul(q2.y, sub(px, q0.z)));
-                                    const float e1 = sub(p1, mul(q2.w, sub(px, q1.x)));
-                                    const float e2 = sub(p2, mul(q3.y, sub(px, q0.x)));
+                                    const float tv = (float)(lo + sx);
+                                    const float e0 = sub(K0, mul(q0.z, sub(tv, q0.w)));
+                                    const float e1 = sub(K1, mul(q1.z, sub(tv, q1.w)));
+                                    const float e2 = sub(K2, mul(q2.z, sub(tv, q2.w)));
                                     if (fminf(fminf(e0, e1), e2) >= thr) mask |= 1u << sx;
                                 }
                                 if (mask) {
                                     const uint32_t f0 = __ffs(mask) - 1u;
-                                    run_x = x_lo + f0;
+                                    run_t = lo + f0;
                                     run_n = (32u - __clz(mask)) - f0;
                                 }
                             }
@@ -659,22 +669,22 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                             // first to the last candidate. Two pixels per instruction: __fadd2_rn /
                             // __fmul2_rn round each component exactly as __fadd_rn / __fmul_rn, and
                             // a - b is a + (-b) bit for bit, so
-                            //   e = p - d.y * (px - a.x)  ==  p + -(d.y * (px + -a.x)).
-                            const float2 P0 = make_float2(p0, p0), P1 = make_float2(p1, p1), P2 = make_float2(p2, p2);
-                            const float2 NX1 = make_float2(-q0.z, -q0.z), NX2 = make_float2(-q1.x, -q1.x),
-                                         NX0 = make_float2(-q0.x, -q0.x);
-                            const float2 B0 = make_float2(q2.y, q2.y), B1 = make_float2(q2.w, q2.w),
-                                         B2 = make_float2(q3.y, q3.y);
-                            const float px_lo = (float)x_lo;
-                            const uint32_t n_px = x_hi - x_lo + 1u;
+                            //   f = K - W * (t - Z)  ==  K + -(W * (t + -Z)).
+                            const float2 P0 = make_float2(K0, K0), P1 = make_float2(K1, K1), P2 = make_float2(K2, K2);
+                            const float2 NZ0 = make_float2(-q0.w, -q0.w), NZ1 = make_float2(-q1.w, -q1.w),
+                                         NZ2 = make_float2(-q2.w, -q2.w);
+                            const float2 W0 = make_float2(q0.z, q0.z), W1 = make_float2(q1.z, q1.z),
+                                         W2 = make_float2(q2.z, q2.z);
+                            const float t_lo = (float)lo;
+                            const uint32_t n_px = hi - lo + 1u;
                             uint32_t mask = 0u;
 #pragma unroll
                             for (uint32_t sx = 0; sx < kRowChunk; sx += 2) {
-                                // pixel centres px_lo + sx, + sx + 1: exact, integers below 2^24
-                                const float2 px = make_float2(add(px_lo, (float)sx), add(px_lo, (float)(sx + 1)));
-                                const float2 t0 = __fmul2_rn(B0, __fadd2_rn(px, NX1));
-                                const float2 t1 = __fmul2_rn(B1, __fadd2_rn(px, NX2));
-                                const float2 t2 = __fmul2_rn(B2, __fadd2_rn(px, NX0));
+                                // pixel centres t_lo + sx, + sx + 1: exact, integers below 2^24
+                                const float2 tv = make_float2(add(t_lo, (float)sx), add(t_lo, (float)(sx + 1)));
+                                const float2 t0 = __fmul2_rn(W0, __fadd2_rn(tv, NZ0));
+                                const float2 t1 = __fmul2_rn(W1, __fadd2_rn(tv, NZ1));
+                                const float2 t2 = __fmul2_rn(W2, __fadd2_rn(tv, NZ2));
                                 const float2 e0 = __fadd2_rn(P0, make_float2(-t0.x, -t0.y));
                                 const float2 e1 = __fadd2_rn(P1, make_float2(-t1.x, -t1.y));
                                 const float2 e2 = __fadd2_rn(P2, make_float2(-t2.x, -t2.y));
@@ -684,13 +694,13 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                             }
                             if (mask) {
                                 const uint32_t f0 = __ffs(mask) - 1u;
-                                run_x = x_lo + f0;
+                                run_t = lo + f0;
                                 run_n = (32u - __clz(mask)) - f0;
                             }
                         }
 #ifdef RAST_CHECKED
-                        if (run_n && (run_x < x_lo || run_x + run_n - 1u > x_hi)) {
-                            report(a.counters, 4u, run_x);
+                        if (run_n && (run_t < lo || run_t + run_n - 1u > hi)) {
+                            report(a.counters, 4u, run_t);
                             run_n = 0u;
                         }
 #endif
@@ -700,8 +710,8 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                 const unsigned m = __ballot_sync(kFull, has);
                 if (has) {
                     const uint32_t e = (q_head + q_count + __popc(m & lt_mask)) & 63u;
-                    S.q_xy[e] = run_x | (y << 16);
-                    S.q_om[e] = (uint32_t)owner;
+                    S.q_xy[e] = run_t | (fixed << 16);
+                    S.q_om[e] = (uint32_t)owner | cflag;
                     S.q_m[e] = run_n;
                 }
                 q_count += __popc(m);
