@@ -65,9 +65,6 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
         if (rast::launch_arm_keys_clear(c->keys.as<unsigned long long>(), npx, c->stream) < 0)
             return cuda_fail(c, cudaGetLastError(), "arm keys");
     }
-    RAST_CUDA(c, cudaMemsetAsync(c->counters.ptr, 0, sizeof(uint32_t) * (rast::kCounterHeader + 2 * (size_t)n_tiles),
-                                 c->stream));
-    RAST_CUDA(c, cudaMemsetAsync(c->stats.ptr, 0, sizeof(unsigned long long) * rast::kStatWords, c->stream));
     if (c->shader != RAST_SHADER_EXACT)
         RAST_CUDA(c, cudaMemsetAsync(c->shade_stats.ptr, 0, sizeof(unsigned long long) * rast::kShadeStats, c->stream));
 
@@ -81,6 +78,10 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     s.stats = c->stats.as<unsigned long long>();
     s.cap_large = c->cap_large;
     s.cap_entries = c->cap_entries;
+    // the counters (header, tile counts and cursors) and statistics start at zero: the frame's
+    // first kernel clears them
+    s.clear_counter_words = (uint32_t)(rast::kCounterHeader + 2 * (size_t)n_tiles);
+    s.clear_stats = true;
     if (c->shader != RAST_SHADER_EXACT) {
         s.gbuf = c->gbuf.as<float4>();
         s.gbuf_count = c->gbuf_count.as<uint32_t>();

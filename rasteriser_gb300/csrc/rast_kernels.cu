@@ -219,11 +219,26 @@ __device__ __forceinline__ uint32_t div_small(uint32_t n, uint32_t d, float rd) 
 // kernels
 // ---------------------------------------------------------------------------------------------
 
+// The frame's per-draw clears, done by its first kernel: counters (bins, status) and statistics.
+struct FrameClear {
+    uint32_t* words;
+    uint32_t n_words;
+    unsigned long long* stats;
+    uint32_t n_stats;
+};
+
+__device__ __forceinline__ void frame_clear(const FrameClear& c) {
+    const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x, step = gridDim.x * blockDim.x;
+    for (uint32_t i = i0; i < c.n_words; i += step) c.words[i] = 0u;
+    for (uint32_t i = i0; i < c.n_stats; i += step) c.stats[i] = 0ull;
+}
+
 // Vertex stage: clip = camera * (x, y, z, 1); (x/w, y/w, z/w, 1/w); x, y to raster pixels with
 // the y flip (geometry.cpp:44-74).
 __global__ void __launch_bounds__(256) k_vertex(const float* __restrict__ pos, int64_t nv, Mat4 cam, float wf,
-                                                float hf, float4* __restrict__ rv) {
+                                                float hf, float4* __restrict__ rv, FrameClear clr) {
     pdl_launch_dependents();
+    frame_clear(clr);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
         const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
         const float cx = mrow(cam, 0, x, y, z, 1.f);
@@ -249,8 +264,9 @@ __device__ __forceinline__ float4 raster_vertex(const Mat4& cam, float x, float 
 // The same for four consecutive vertices per thread, read as three 16-byte loads (positions must
 // be 16-byte aligned); the last nv % 4 vertices are done one by one.
 __global__ void __launch_bounds__(256) k_vertex4(const float* __restrict__ pos, int64_t nv, Mat4 cam, float wf,
-                                                 float hf, float4* __restrict__ rv) {
+                                                 float hf, float4* __restrict__ rv, FrameClear clr) {
     pdl_launch_dependents();
+    frame_clear(clr);
     const int64_t groups = nv / 4;
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups + (nv % 4); g += (int64_t)gridDim.x * blockDim.x) {
         if (g < groups) {
@@ -1386,12 +1402,13 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
         ++launches;
     }
     mark(1);
+    const FrameClear clr{s.counters, s.clear_counter_words, s.stats, s.clear_stats ? (uint32_t)kStatWords : 0u};
     if ((reinterpret_cast<uintptr_t>(mesh.pos) % 16u) == 0)
         k_vertex4<<<grid_for(mesh.nv / 4 + mesh.nv % 4, 256, 1 << 16), 256, 0, stream>>>(
-            mesh.pos, mesh.nv, p.camera, (float)(int)p.width, (float)(int)p.height, s.rv);
+            mesh.pos, mesh.nv, p.camera, (float)(int)p.width, (float)(int)p.height, s.rv, clr);
     else
         k_vertex<<<grid_for(mesh.nv, 256, 1 << 16), 256, 0, stream>>>(mesh.pos, mesh.nv, p.camera, (float)(int)p.width,
-                                                                       (float)(int)p.height, s.rv);
+                                                                       (float)(int)p.height, s.rv, clr);
     ++launches;
     mark(2);
 
