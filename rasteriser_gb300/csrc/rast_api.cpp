@@ -65,9 +65,6 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
         if (rast::launch_arm_keys_clear(c->keys.as<unsigned long long>(), npx, c->stream) < 0)
             return cuda_fail(c, cudaGetLastError(), "arm keys");
     }
-    if (c->shader != RAST_SHADER_EXACT)
-        RAST_CUDA(c, cudaMemsetAsync(c->shade_stats.ptr, 0, sizeof(unsigned long long) * rast::kShadeStats, c->stream));
-
     rast::FrameScratch s;
     s.rv = c->rv.as<float4>();
     s.keys = c->keys.as<unsigned long long>();
@@ -87,6 +84,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
         s.gbuf_count = c->gbuf_count.as<uint32_t>();
         s.shade_index = c->shade_index.as<uint32_t>();
         s.shade_stats = c->shade_stats.as<unsigned long long>();
+        s.clear_shade_stats = true;
     }
 
     rast::DrawParams p;

@@ -79,9 +79,10 @@ struct FrameScratch {
     unsigned long long* stats = nullptr;  // kStatWords
     int64_t cap_large = 0, cap_entries = 0;
     // Cleared by the frame's first kernel when nonzero / set (the caller then skips its own
-    // clears): the first clear_counter_words words of counters, and stats.
+    // clears): the first clear_counter_words words of counters, stats, and shade_stats.
     uint32_t clear_counter_words = 0;
     bool clear_stats = false;
+    bool clear_shade_stats = false;
     // deferred shading (DrawParams::shader != 0)
     float4* gbuf = nullptr;             // 2 float4 per record: (normal xyz, albedo r), (albedo gb, pixel, 0)
     uint32_t* gbuf_count = nullptr;     // records per block of 1024 pixels

@@ -225,12 +225,15 @@ struct FrameClear {
     uint32_t n_words;
     unsigned long long* stats;
     uint32_t n_stats;
+    unsigned long long* shade_stats;
+    uint32_t n_shade_stats;
 };
 
 __device__ __forceinline__ void frame_clear(const FrameClear& c) {
     const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x, step = gridDim.x * blockDim.x;
     for (uint32_t i = i0; i < c.n_words; i += step) c.words[i] = 0u;
     for (uint32_t i = i0; i < c.n_stats; i += step) c.stats[i] = 0ull;
+    for (uint32_t i = i0; i < c.n_shade_stats; i += step) c.shade_stats[i] = 0ull;
 }
 
 // Vertex stage: clip = camera * (x, y, z, 1); (x/w, y/w, z/w, 1/w); x, y to raster pixels with
@@ -1402,7 +1405,9 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
         ++launches;
     }
     mark(1);
-    const FrameClear clr{s.counters, s.clear_counter_words, s.stats, s.clear_stats ? (uint32_t)kStatWords : 0u};
+    const FrameClear clr{s.counters,    s.clear_counter_words,
+                         s.stats,       s.clear_stats ? (uint32_t)kStatWords : 0u,
+                         s.shade_stats, s.clear_shade_stats && s.shade_stats ? (uint32_t)kShadeStats : 0u};
     if ((reinterpret_cast<uintptr_t>(mesh.pos) % 16u) == 0)
         k_vertex4<<<grid_for(mesh.nv / 4 + mesh.nv % 4, 256, 1 << 16), 256, 0, stream>>>(
             mesh.pos, mesh.nv, p.camera, (float)(int)p.width, (float)(int)p.height, s.rv, clr);
