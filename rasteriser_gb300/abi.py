@@ -320,13 +320,17 @@ class Renderer:
         self._check(self.lib.rast_set_stream(self.h, _P(stream_handle) if stream_handle else None), "rast_set_stream")
 
     # drawing --------------------------------------------------------------------------------
-    def draw(self, camera, normal, width, height, flags=0, frame=None, depth=None, want_ids=False):
-        """Host-buffer draw. frame: (3, H, W) uint8, depth: (H, W) float32, both read and written."""
+    def draw(self, camera, normal, width, height, flags=0, frame=None, depth=None, want_ids=False, ids=None):
+        """Host-buffer draw. frame: (3, H, W) uint8, depth: (H, W) float32, both read and written;
+        ids: an optional (H, W) uint32 output (made here when want_ids and none is given)."""
         frame = np.zeros((3, height, width), np.uint8) if frame is None else frame
         depth = np.ones((height, width), np.float32) if depth is None else depth
         assert frame.dtype == np.uint8 and frame.flags.c_contiguous and frame.size == 3 * width * height
         assert depth.dtype == np.float32 and depth.flags.c_contiguous and depth.size == width * height
-        ids = np.empty((height, width), np.uint32) if want_ids else None
+        if ids is None and want_ids:
+            ids = np.empty((height, width), np.uint32)
+        if ids is not None:
+            assert ids.dtype == np.uint32 and ids.flags.c_contiguous and ids.size == width * height
         st = self.lib.rast_draw(self.h, _fp(_f32(camera)), _fp(_f32(normal)), width, height, flags,
                                 frame.ctypes.data_as(C.POINTER(C.c_uint8)), _fp(depth),
                                 ids.ctypes.data_as(C.POINTER(C.c_uint32)) if ids is not None else None)

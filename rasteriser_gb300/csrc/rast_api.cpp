@@ -1,5 +1,6 @@
 // Host side of librast's C ABI (include/rast.h): contexts, validation, device buffers and the
 // orchestration of one draw. The kernels are in rast_kernels.cu.
+#include <cuda.h>  // pointer attribute names; the driver function is reached through cudart
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -23,11 +24,41 @@ namespace {
 
 uint32_t tile_shift(uint32_t tile) { return tile == 8 ? 3u : (tile == 16 ? 4u : 5u); }
 
+// The device address of [p, p + bytes) when the whole range lies in one page-locked host
+// allocation that the device maps (cudaHostAlloc, cudaHostRegister, torch's pinned memory), else
+// nullptr. Both ends must be host memory of the same CUDA allocation (one buffer id), mapped
+// contiguously for the device.
+void* mapped_host_range(const void* p, size_t bytes) {
+    using GetAttr = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+    static const GetAttr get = [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+        return reinterpret_cast<GetAttr>(fn);
+    }();
+    if (!get || !p || bytes == 0) return nullptr;
+    const CUdeviceptr a = (CUdeviceptr)(uintptr_t)p, b = a + (CUdeviceptr)(bytes - 1);
+    unsigned int ta = 0, tb = 0;
+    unsigned long long ia = 0, ib = 0;
+    void* da = nullptr;
+    void* db = nullptr;
+    if (get(&ta, CU_POINTER_ATTRIBUTE_MEMORY_TYPE, a) != CUDA_SUCCESS || ta != CU_MEMORYTYPE_HOST) return nullptr;
+    if (get(&tb, CU_POINTER_ATTRIBUTE_MEMORY_TYPE, b) != CUDA_SUCCESS || tb != CU_MEMORYTYPE_HOST) return nullptr;
+    if (get(&ia, CU_POINTER_ATTRIBUTE_BUFFER_ID, a) != CUDA_SUCCESS) return nullptr;
+    if (get(&ib, CU_POINTER_ATTRIBUTE_BUFFER_ID, b) != CUDA_SUCCESS || ia != ib) return nullptr;
+    if (get(&da, CU_POINTER_ATTRIBUTE_DEVICE_POINTER, a) != CUDA_SUCCESS || !da) return nullptr;
+    if (get(&db, CU_POINTER_ATTRIBUTE_DEVICE_POINTER, b) != CUDA_SUCCESS || !db) return nullptr;
+    if ((uintptr_t)db - (uintptr_t)da != bytes - 1) return nullptr;
+    return da;
+}
+
 // Sizes the per-draw scratch for a width x height frame.
 rast_status ensure_scratch(rast_ctx* c, uint32_t w, uint32_t h, uint32_t tiles) {
     const int64_t npx = (int64_t)w * h;
     RAST_CUDA(c, c->rv.reserve(sizeof(float4) * (size_t)std::max<int64_t>(c->mesh.nv, 1)));
-    if (c->keys.bytes < sizeof(unsigned long long) * (size_t)npx) c->keys_armed_clear = false;
+    if (c->keys.bytes < sizeof(unsigned long long) * (size_t)npx) c->keys_armed = false;
     RAST_CUDA(c, c->keys.reserve(sizeof(unsigned long long) * (size_t)npx));
     c->cap_large = std::max<int64_t>(c->mesh.ntri, 1);
     RAST_CUDA(c, c->large.reserve(sizeof(rast::BinnedTri) * (size_t)c->cap_large));
@@ -59,10 +90,10 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     const uint32_t n_tiles = tiles_x * tiles_y;
     rast_status st = ensure_scratch(c, w, h, n_tiles);
     if (st != RAST_OK) return st;
-    const bool clear = (flags & RAST_CLEAR) != 0;
     const int64_t npx = (int64_t)w * h;
-    if (clear && (!c->keys_armed_clear || c->keys_px != npx)) {
-        if (rast::launch_arm_keys_clear(c->keys.as<unsigned long long>(), npx, c->stream) < 0)
+    const bool clear = (flags & RAST_CLEAR) != 0;
+    if (!c->keys_armed || c->keys_px != npx || c->keys_clear != clear) {
+        if (rast::launch_arm_keys(c->keys.as<unsigned long long>(), npx, clear, c->stream) < 0)
             return cuda_fail(c, cudaGetLastError(), "arm keys");
     }
     rast::FrameScratch s;
@@ -97,6 +128,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     p.tile = c->tile;
     p.row_chunk = c->row_chunk;
     p.before_resolve = c->before_resolve;
+    p.keep_outputs_on_overflow = c->keep_outputs;
     p.tiles_x = tiles_x;
     p.tiles_y = tiles_y;
     p.n_sm = c->n_sm;
@@ -117,7 +149,8 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     c->ev_recorded = c->timing;
     if (n < 0) return cuda_fail(c, cudaGetLastError(), "launch draw");
     c->last_launches = (uint64_t)n;
-    c->keys_armed_clear = clear;
+    c->keys_armed = true;  // the resolve pass re-arms every key it reads
+    c->keys_clear = clear;
     c->keys_px = npx;
     return RAST_OK;
 }
@@ -137,7 +170,7 @@ rast_status collect_status(rast_ctx* c) {
         RAST_CUDA(c, c->entries.reserve(sizeof(uint32_t) * (size_t)c->cap_entries));
         uint32_t zero = 0;
         RAST_CUDA(c, cudaMemcpy(c->counters.as<uint32_t>() + 1, &zero, sizeof zero, cudaMemcpyHostToDevice));
-        c->keys_armed_clear = false;
+        c->keys_armed = false;
         return fail(c, RAST_ERR_BIN_OVERFLOW, "tile-bin pool overflowed; it was grown to " +
                                                   std::to_string(c->cap_entries) + " entries, draw again");
     }
@@ -426,14 +459,42 @@ rast_status rast_draw(rast_ctx* c, const float camera[16], const float normal[16
         if (!c->ev_rgb_in) RAST_CUDA(c, cudaEventCreateWithFlags(&c->ev_rgb_in, cudaEventDisableTiming));
     }
     if (!c->h_status) RAST_CUDA(c, cudaMallocHost(&c->h_status, sizeof(uint32_t)));
+    // Page-locked host buffers that the device maps are used in place by the exact shader: the
+    // resolve pass reads the incoming depth where a fragment landed and writes the frame's pixels
+    // (read-modify-write: only the winners) straight into the host buffers, so no frame-sized
+    // copy crosses the link. After a bin-pool overflow the resolve pass writes nothing, and the
+    // redraw starts from the same buffers.
+    if (c->shader == RAST_SHADER_EXACT) {
+        uint8_t* hr = static_cast<uint8_t*>(mapped_host_range(rgb, 3 * npx));
+        float* hd = static_cast<float*>(mapped_host_range(depth, sizeof(float) * npx));
+        uint32_t* hi = ids ? static_cast<uint32_t*>(mapped_host_range(ids, sizeof(uint32_t) * npx)) : nullptr;
+        if (hr && hd && (!ids || hi)) {
+            for (int attempt = 0; attempt < 3; ++attempt) {
+                c->keep_outputs = true;
+                rast_status st = enqueue_draw(c, camera, normal, w, h, flags, hr, hd, hi);
+                c->keep_outputs = false;
+                if (st != RAST_OK) return st;
+                RAST_CUDA(c, cudaMemcpyAsync(c->h_status, c->counters.as<uint32_t>() + 1, sizeof(uint32_t),
+                                             cudaMemcpyDeviceToHost, c->stream));
+                RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+                if (*c->h_status == 0u) return RAST_OK;
+                st = collect_status(c);
+                if (st == RAST_ERR_BIN_OVERFLOW) continue;  // pool grown; the buffers are untouched
+                return st;
+            }
+            return fail(c, RAST_ERR_BIN_OVERFLOW, "tile-bin pool still overflowing after regrowth");
+        }
+    }
     for (int attempt = 0; attempt < 3; ++attempt) {
-        // The depth input is needed first (it arms the depth test); the colour input only by the
-        // resolve pass, so it is uploaded on the copy stream while the first passes run. Both are
-        // also kept on the device, so a redraw after a bin overflow starts from them again.
+        // The inputs are needed only by the resolve pass (the incoming depth each winner must beat,
+        // the colour of the pixels nothing wins), so they are uploaded on the copy stream while the
+        // first passes run. Both are also kept on the device, so a redraw after a bin overflow
+        // starts from them again.
         if (rmw && attempt == 0) {
-            RAST_CUDA(c, cudaMemcpyAsync(c->d_depth.ptr, depth, sizeof(float) * npx, cudaMemcpyHostToDevice, c->stream));
-            RAST_CUDA(c, cudaEventRecord(c->ev_depth_in, c->stream));
+            RAST_CUDA(c, cudaEventRecord(c->ev_depth_in, c->stream));  // after earlier work on the stream
             RAST_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->ev_depth_in, 0));
+            RAST_CUDA(c, cudaMemcpyAsync(c->d_depth.ptr, depth, sizeof(float) * npx, cudaMemcpyHostToDevice,
+                                         c->copy_stream));
             RAST_CUDA(c, cudaMemcpyAsync(c->d_rgb.ptr, rgb, 3 * npx, cudaMemcpyHostToDevice, c->copy_stream));
             RAST_CUDA(c, cudaMemcpyAsync(c->d_depth_in.ptr, c->d_depth.ptr, sizeof(float) * npx,
                                          cudaMemcpyDeviceToDevice, c->copy_stream));

@@ -91,7 +91,7 @@ rast_status enqueue_batch(rast_ctx* c, const rast_frame_desc* frames, int32_t n,
             RAST_CUDA(c, cudaMemsetAsync(counters + 4, 0, sizeof(uint32_t) * (words - 4), L.stream));
         }
         const int64_t npx = (int64_t)f.width * f.height;
-        if ((f.flags & RAST_CLEAR) && rast::launch_arm_keys_clear(L.keys.as<unsigned long long>(), npx, L.stream) < 0)
+        if (rast::launch_arm_keys(L.keys.as<unsigned long long>(), npx, (f.flags & RAST_CLEAR) != 0, L.stream) < 0)
             return cuda_fail(c, cudaGetLastError(), "arm keys");
         FrameScratch s;
         s.rv = L.rv.as<float4>();

@@ -84,7 +84,8 @@ struct rast_ctx {
     // per-draw scratch
     DevBuf rv, keys, large, counters, tile_offset, entries, stats;
     int64_t cap_large = 0, cap_entries = 0;
-    bool keys_armed_clear = false;
+    bool keys_armed = false;  // keys[0, keys_px) hold the armed value of keys_clear's mode
+    bool keys_clear = false;
     int64_t keys_px = 0;
 
     // host-pointer draws stage through these
@@ -96,6 +97,7 @@ struct rast_ctx {
     cudaEvent_t ev_depth_in = nullptr, ev_rgb_in = nullptr;
     uint32_t* h_status = nullptr;
     cudaEvent_t before_resolve = nullptr;  // set by rast_draw for the draw it enqueues
+    bool keep_outputs = false;             // set by rast_draw when the kernels use its host buffers
 
     // deferred shading
     int32_t shader = 0;           // RAST_SHADER_*

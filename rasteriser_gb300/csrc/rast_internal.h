@@ -120,6 +120,8 @@ struct DrawParams {
                             // (off for batches, whose lanes fill the SMs with each other's work)
     cudaEvent_t before_resolve = nullptr;  // when set, the resolve pass waits for it (the colour
                                            // input of a host draw, copied beside the first passes)
+    bool keep_outputs_on_overflow = false;  // the resolve pass writes nothing after a bin-pool
+                                            // overflow, so a redraw starts from the same buffers
     uint32_t tiles_x, tiles_y;
     int32_t n_sm;           // streaming multiprocessors of the device
     int32_t nl;
@@ -149,8 +151,10 @@ int launch_shade(const FrameScratch& s, const DrawParams& p, int64_t blocks, cud
 int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams& p, cudaStream_t stream,
                 cudaEvent_t* events = nullptr);
 
-// Fills keys[0, n) with the value a cleared depth buffer (1.0) arms them with.
-int launch_arm_keys_clear(unsigned long long* keys, int64_t n, cudaStream_t stream);
+// Fills keys[0, n) with the key of a pixel no fragment has reached: for clear mode the key that
+// only fragments nearer than 1.0 beat, else a key above every fragment's. The resolve pass re-arms
+// every key it reads for its own mode, so this is needed only for fresh keys or a change of mode.
+int launch_arm_keys(unsigned long long* keys, int64_t n, bool clear, cudaStream_t stream);
 
 // Sets the text rast_last_error(NULL) returns on this thread.
 void set_thread_error(const std::string& msg);

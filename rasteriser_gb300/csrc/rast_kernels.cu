@@ -21,9 +21,13 @@
 //
 // Depth test: the reference keeps a fragment when `ndcdepth < depth(x,y)` while walking the
 // triangles in order (drawing.cpp:119), so a pixel ends with the smallest depth and, among equal
-// depths, the earliest triangle. Here every fragment proposes the 64-bit key
-// (order(depth) << 32 | triangle) and the pixel keeps the minimum, which is the same winner
-// whatever order the fragments arrive in.
+// depths, the earliest triangle, provided that depth beats the incoming one. Here every fragment
+// proposes the 64-bit key (order(depth) << 32 | triangle) and the pixel keeps the minimum, which
+// is the same fragment whatever order the fragments arrive in. In clear mode the keys start at the
+// key of the cleared depth 1.0, so only nearer fragments can land. In read-modify-write mode they
+// start above every fragment, and the resolve pass keeps the nearest fragment when its depth is
+// below the incoming one: it passes the reference's sequence of tests exactly when any fragment
+// does.
 #include <cstdint>
 #include <cuda_runtime.h>
 #include <utility>
@@ -37,6 +41,7 @@ namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr unsigned long long kNoWinner = 0xFFFFFFFFull;  // low word of a key with no fragment
+constexpr unsigned long long kArmed = ~0ull;             // read-modify-write: a key before any fragment
 
 // Row r of mat4 * vec4, summed (c0*x + c1*y) + (c2*z + c3*w).
 __device__ __forceinline__ float mrow(const Mat4& M, int r, float x, float y, float z, float w) {
@@ -52,11 +57,9 @@ __device__ __forceinline__ uint32_t depth_order(float z) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
-// Initial key of a pixel whose depth buffer holds d: a fragment (z, t) beats it exactly when
-// z < d. For NaN d nothing may pass, and the key sits below every fragment key.
-__device__ __forceinline__ unsigned long long arm_key(float d) {
-    if (d != d) return kNoWinner;
-    return (static_cast<unsigned long long>(depth_order(d)) << 32) - 1ull;
+// Clear mode: the key a fragment (z, t) beats exactly when z < 1.0 (the cleared depth).
+__device__ __forceinline__ unsigned long long clear_key() {
+    return (static_cast<unsigned long long>(depth_order(1.0f)) << 32) - 1ull;
 }
 
 __device__ __forceinline__ unsigned long long frag_key(float z, uint32_t tri) {
@@ -287,14 +290,8 @@ __global__ void __launch_bounds__(256) k_vertex4(const float* __restrict__ pos, 
     }
 }
 
-__global__ void __launch_bounds__(256) k_arm_from_depth(const float* __restrict__ depth, int64_t n,
-                                                        unsigned long long* __restrict__ keys) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        keys[i] = arm_key(depth[i]);
-}
-
-__global__ void __launch_bounds__(256) k_arm_clear(unsigned long long* __restrict__ keys, int64_t n) {
-    const unsigned long long v = arm_key(1.0f);
+__global__ void __launch_bounds__(256) k_arm_keys(unsigned long long* __restrict__ keys, int64_t n, bool clear) {
+    const unsigned long long v = clear ? clear_key() : kArmed;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         keys[i] = v;
 }
@@ -1058,7 +1055,7 @@ struct ResolveArgs {
     uint32_t* counters;
     int64_t ntri;
     const unsigned long long* keys;
-    unsigned long long* keys_rearm;  // non-null in clear mode: keys are re-armed for the next frame
+    unsigned long long* keys_rearm;  // non-null: keys are re-armed for the next frame as they are read
     const int32_t* tri_v;
     const int4* tri_nm;
     const float4* rv;
@@ -1068,7 +1065,7 @@ struct ResolveArgs {
     int32_t nl;
     Mat4 normal;
     uint32_t width, height;
-    bool cw, clear;
+    bool cw;
     bool vec_ok;  // npx % 4 == 0 (planes stay 4-byte aligned), rgb 4-byte and depth 16-byte aligned
     uint8_t* rgb;
     float* depth;
@@ -1083,6 +1080,7 @@ struct ResolveArgs {
     float4* gbuf;         // deferred shading: 2 float4 per fragment record, or null to shade here
     uint32_t* gbuf_count; // deferred shading: records per block (1024 pixels)
     uint32_t* shade_index;  // deferred shading: the tile list build_shade_tiles writes
+    bool keep_on_overflow;  // write nothing when the frame's bin pools overflowed
 };
 
 constexpr int kResolveThreads = 256;
@@ -1177,9 +1175,11 @@ struct ResolveStage {
 };
 
 // Each warp takes kSpan consecutive pixels (4 per lane) of the flattened frame: it loads their keys
-// (16-byte loads), re-arms them in clear mode, compacts the pixels that have a winner, shades the
+// (16-byte loads), re-arms them, compacts the pixels that have a winner, shades the
 // winners one per lane so the gathers of 32 fragments are in flight together, and writes the
 // frame and depth buffers 4 pixels per lane.
+// kClear: RAST_CLEAR (every pixel written, the incoming depth 1.0); else read-modify-write.
+template <bool kClear>
 __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
     __shared__ ResolveStage stage[kResolveWarps];
     __shared__ uint32_t s_count[kResolveWarps];
@@ -1187,6 +1187,8 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
     // Deferred shading: the shading kernel may be launched once every block of this grid has
     // started (it waits for this grid's completion before it reads the records).
     pdl_launch_dependents();
+    // Every earlier pass of the frame is complete here, so the status word is final.
+    if (a.keep_on_overflow && (a.counters[1] & (STATUS_BIN_OVERFLOW | STATUS_LARGE_OVERFLOW))) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     ResolveStage& S = stage[warp];
     const int64_t npx = (int64_t)a.width * a.height;
@@ -1207,7 +1209,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             for (int k = 0; k < 4; ++k) key[k] = in_range && p0 + k < npx ? a.keys[p0 + k] : kNoWinner;
         }
         if (a.keys_rearm && in_range) {
-            const unsigned long long r = arm_key(1.0f);
+            const unsigned long long r = kClear ? clear_key() : kArmed;
             if (full) {
                 *reinterpret_cast<ulonglong2*>(a.keys_rearm + p0) = make_ulonglong2(r, r);
                 *reinterpret_cast<ulonglong2*>(a.keys_rearm + p0 + 2) = make_ulonglong2(r, r);
@@ -1216,6 +1218,14 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
                     if (p0 + k < npx) a.keys_rearm[p0 + k] = r;
             }
         }
+        // Read-modify-write: the nearest fragment wins when it beats the incoming depth
+        // (drawing.cpp:119), the depth buffer's value, read only where a fragment landed (the keys
+        // of pixels outside the frame hold no fragment). For a NaN incoming depth nothing passes.
+        // Clear mode: every fragment that landed beat 1.0 already.
+        float din[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            din[k] = (!kClear && (uint32_t)key[k] != 0xFFFFFFFFu) ? a.depth[p0 + k] : 0.f;
         // compact the winners of the span
         bool win[4];
         uint32_t n_win = 0;
@@ -1224,6 +1234,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
         for (int k = 0; k < 4; ++k) {
             const uint32_t t = (uint32_t)(key[k] & 0xFFFFFFFFull);
             win[k] = t != 0xFFFFFFFFu;
+            if (!kClear) win[k] = win[k] && din[k] == din[k] && (uint32_t)(key[k] >> 32) < depth_order(din[k]);
             if (win[k] && (int64_t)t >= a.ntri) {
                 report(a.counters, 3u, t);
                 win[k] = false;
@@ -1295,7 +1306,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             col[k] = win[k] ? S.rgb[4 * lane + k] : 0u;
         }
         const int64_t plane = npx;
-        if (a.clear && vec) {
+        if (kClear && vec) {
             // every pixel is written: background 0 / 1.0 where nothing won
             *reinterpret_cast<float4*>(a.depth + p0) = make_float4(dep[0], dep[1], dep[2], dep[3]);
             uint32_t pr = 0, pg = 0, pb = 0;
@@ -1311,7 +1322,7 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
         } else {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                if (p0 + k < npx && (win[k] || a.clear)) {
+                if (p0 + k < npx && (win[k] || kClear)) {
                     a.depth[p0 + k] = dep[k];
                     a.rgb[p0 + k] = (uint8_t)(col[k] & 0xFFu);
                     a.rgb[plane + p0 + k] = (uint8_t)((col[k] >> 8) & 0xFFu);
@@ -1382,8 +1393,8 @@ int launch_split_triangles(const int32_t* tris10, int64_t ntri, int32_t* tri_v, 
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
-int launch_arm_keys_clear(unsigned long long* keys, int64_t n, cudaStream_t stream) {
-    k_arm_clear<<<grid_for(n, 256, 1 << 16), 256, 0, stream>>>(keys, n);
+int launch_arm_keys(unsigned long long* keys, int64_t n, bool clear, cudaStream_t stream) {
+    k_arm_keys<<<grid_for(n, 256, 1 << 16), 256, 0, stream>>>(keys, n, clear);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -1400,10 +1411,6 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     int launches = 0;
 
     mark(0);
-    if (!clear) {
-        k_arm_from_depth<<<grid_for(npx, 256, 1 << 16), 256, 0, stream>>>(p.depth, npx, s.keys);
-        ++launches;
-    }
     mark(1);
     const FrameClear clr{s.counters,    s.clear_counter_words,
                          s.stats,       s.clear_stats ? (uint32_t)kStatWords : 0u,
@@ -1495,7 +1502,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.counters = s.counters;
     ra.ntri = mesh.ntri;
     ra.keys = s.keys;
-    ra.keys_rearm = clear ? s.keys : nullptr;
+    ra.keys_rearm = s.keys;
     ra.tri_v = mesh.tri_v;
     ra.tri_nm = mesh.tri_nm;
     ra.rv = s.rv;
@@ -1507,7 +1514,6 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.width = p.width;
     ra.height = p.height;
     ra.cw = cw;
-    ra.clear = clear;
     ra.vec_ok = (reinterpret_cast<uintptr_t>(p.rgb) % 4u) == 0 && (npx % 4) == 0 &&
                 (reinterpret_cast<uintptr_t>(p.depth) % 16u) == 0;
     ra.rgb = p.rgb;
@@ -1522,10 +1528,11 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.tris10 = mesh.tris10;
     const bool deferred = p.shader != 0;
     ra.gbuf = deferred ? s.gbuf : nullptr;
+    ra.keep_on_overflow = p.keep_outputs_on_overflow;
     ra.gbuf_count = deferred ? s.gbuf_count : nullptr;
     ra.shade_index = deferred ? s.shade_index : nullptr;
     const int64_t spans = (npx + kSpan - 1) / kSpan;
-    if (launch_pdl(p.chained, k_resolve, (unsigned)((spans + kResolveWarps - 1) / kResolveWarps),
+    if (launch_pdl(p.chained, clear ? k_resolve<true> : k_resolve<false>, (unsigned)((spans + kResolveWarps - 1) / kResolveWarps),
                    (unsigned)kResolveThreads, stream, ra) != cudaSuccess)
         return -1;
     ++launches;

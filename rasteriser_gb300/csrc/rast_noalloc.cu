@@ -145,7 +145,7 @@ extern "C" rast_status rast_draw_noalloc(const float* d_pos, int64_t nv, const f
         if (rast::launch_split_triangles(d_tris, ntri, tri_v, tri_nm, st) < 0)
             return fail(RAST_ERR_CUDA, "split triangles launch failed");
     }
-    if ((flags & RAST_CLEAR) && rast::launch_arm_keys_clear(s.keys, npx, st) < 0)
+    if (rast::launch_arm_keys(s.keys, npx, (flags & RAST_CLEAR) != 0, st) < 0)
         return fail(RAST_ERR_CUDA, "arm keys launch failed");
 
     rast::DeviceMesh mesh;

@@ -232,3 +232,82 @@ def test_full_size_against_reference_digest(renderer, port, key, row_chunk):
     assert np.array_equal(ig, ip)
     s = renderer.stats()
     assert (s["front"], s["tested"], s["inside"]) == (int(st[0]), int(st[1]), int(st[2]))
+
+
+def _pinned(torch, shape, dtype):
+    """A numpy view of page-locked host memory (the device maps it)."""
+    tdt = {np.uint8: torch.uint8, np.float32: torch.float32, np.uint32: torch.int32}[dtype]
+    a = torch.zeros(shape, dtype=tdt).pin_memory().numpy()
+    return a.view(np.uint32) if dtype is np.uint32 else a
+
+
+@pytest.mark.parametrize("clear", [False, True])
+def test_pinned_host_buffers_used_in_place(renderer, port, clear):
+    """Page-locked buffers are read and written by the kernels in place: read-modify-write keeps
+    the pixels nothing wins, clear mode writes them all; both equal the port and the copy path."""
+    torch = pytest.importorskip("torch")
+    sc = S.soup(8000, 300, 200, seed=23, area_range=(0.5, 4000.0))
+    rng = np.random.default_rng(9)
+    depth0 = rng.uniform(-1.5, 1.5, (sc.height, sc.width)).astype(np.float32)
+    depth0[::7, ::5] = -0.0
+    depth0[3::11, ::3] = np.nan
+    frame0 = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    renderer.upload_scene_mesh(sc)
+    renderer.set_lights(lights)
+    f = _pinned(torch, (3, sc.height, sc.width), np.uint8)
+    d = _pinned(torch, (sc.height, sc.width), np.float32)
+    i = _pinned(torch, (sc.height, sc.width), np.uint32)
+    f[...] = frame0
+    d[...] = depth0
+    renderer.draw(cam, nm, sc.width, sc.height, flags_of(sc, clear), f, d, ids=i)
+    fp, dp, ip, _ = port.draw(sc, cam, nm, lights, None if clear else frame0, None if clear else depth0)
+    assert_parity((f, d, i), fp, dp, ip)
+    pageable = gpu_draw(renderer, sc, cam, nm, lights, frame0, depth0, clear=clear)
+    assert np.array_equal(pageable[0], f) and np.array_equal(bits(pageable[1]), bits(d))
+    assert np.array_equal(pageable[2], i)
+
+
+def test_pinned_host_buffers_overflow_recovers(renderer, port):
+    """After a bin-pool overflow the in-place draw has written nothing; the redraw is exact."""
+    torch = pytest.importorskip("torch")
+    sc = S.soup(5000, 400, 300, seed=41, area_range=(200.0, 5000.0))
+    rng = np.random.default_rng(3)
+    depth0 = rng.uniform(-1.0, 1.5, (sc.height, sc.width)).astype(np.float32)
+    frame0 = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    renderer.upload_scene_mesh(sc)
+    renderer.set_lights(lights)
+    f = _pinned(torch, (3, sc.height, sc.width), np.uint8)
+    d = _pinned(torch, (sc.height, sc.width), np.float32)
+    f[...] = frame0
+    d[...] = depth0
+    renderer.set_option(abi.OPT_BIN_CAPACITY, 16)
+    try:
+        renderer.draw(cam, nm, sc.width, sc.height, flags_of(sc), f, d)
+        assert renderer.get_option(abi.OPT_BIN_CAPACITY) > 16
+    finally:
+        renderer.set_option(abi.OPT_BIN_CAPACITY, 0)
+    fp, dp, _, _ = port.draw(sc, cam, nm, lights, frame0, depth0)
+    assert np.array_equal(bits(d), bits(dp))
+    assert np.abs(f.astype(int) - fp).max() <= RGB_TOL
+
+
+def test_pinned_slice_of_larger_allocation(renderer, port):
+    """A frame that is a slice of a bigger page-locked buffer is used in place too."""
+    torch = pytest.importorskip("torch")
+    sc = S.config_icosphere_small()
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    renderer.upload_scene_mesh(sc)
+    renderer.set_lights(lights)
+    n = sc.width * sc.height
+    big = torch.zeros(3 * n + 4096, dtype=torch.uint8).pin_memory().numpy()
+    f = big[1000:1000 + 3 * n].reshape(3, sc.height, sc.width)
+    dbig = torch.ones(n + 64, dtype=torch.float32).pin_memory().numpy()
+    d = dbig[16:16 + n].reshape(sc.height, sc.width)
+    renderer.draw(cam, nm, sc.width, sc.height, flags_of(sc, True), f, d)
+    fp, dp, _, _ = port.draw(sc, cam, nm, lights)
+    assert np.array_equal(bits(d), bits(dp))
+    assert np.abs(f.astype(int) - fp).max() <= RGB_TOL
+    assert np.all(big[:1000] == 0) and np.all(big[1000 + 3 * n:] == 0)
+    assert np.all(dbig[:16] == 1.0) and np.all(dbig[16 + n:] == 1.0)
