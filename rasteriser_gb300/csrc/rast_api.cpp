@@ -29,29 +29,31 @@ uint32_t tile_shift(uint32_t tile) { return tile == 8 ? 3u : (tile == 16 ? 4u : 
 // nullptr. Both ends must be host memory of the same CUDA allocation (one buffer id), mapped
 // contiguously for the device.
 void* mapped_host_range(const void* p, size_t bytes) {
-    using GetAttr = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
-    static const GetAttr get = [] {
+    using GetAttrs = CUresult (*)(unsigned int, CUpointer_attribute*, void**, CUdeviceptr);
+    static const GetAttrs get = [] {
         void* fn = nullptr;
         cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttributes", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
             q != cudaDriverEntryPointSuccess)
             fn = nullptr;
-        return reinterpret_cast<GetAttr>(fn);
+        return reinterpret_cast<GetAttrs>(fn);
     }();
     if (!get || !p || bytes == 0) return nullptr;
-    const CUdeviceptr a = (CUdeviceptr)(uintptr_t)p, b = a + (CUdeviceptr)(bytes - 1);
-    unsigned int ta = 0, tb = 0;
-    unsigned long long ia = 0, ib = 0;
-    void* da = nullptr;
-    void* db = nullptr;
-    if (get(&ta, CU_POINTER_ATTRIBUTE_MEMORY_TYPE, a) != CUDA_SUCCESS || ta != CU_MEMORYTYPE_HOST) return nullptr;
-    if (get(&tb, CU_POINTER_ATTRIBUTE_MEMORY_TYPE, b) != CUDA_SUCCESS || tb != CU_MEMORYTYPE_HOST) return nullptr;
-    if (get(&ia, CU_POINTER_ATTRIBUTE_BUFFER_ID, a) != CUDA_SUCCESS) return nullptr;
-    if (get(&ib, CU_POINTER_ATTRIBUTE_BUFFER_ID, b) != CUDA_SUCCESS || ia != ib) return nullptr;
-    if (get(&da, CU_POINTER_ATTRIBUTE_DEVICE_POINTER, a) != CUDA_SUCCESS || !da) return nullptr;
-    if (get(&db, CU_POINTER_ATTRIBUTE_DEVICE_POINTER, b) != CUDA_SUCCESS || !db) return nullptr;
-    if ((uintptr_t)db - (uintptr_t)da != bytes - 1) return nullptr;
-    return da;
+    struct Ends {
+        unsigned int type = 0;
+        unsigned long long id = 0;
+        void* dev = nullptr;
+    } e[2];
+    const CUdeviceptr at[2] = {(CUdeviceptr)(uintptr_t)p, (CUdeviceptr)(uintptr_t)p + (CUdeviceptr)(bytes - 1)};
+    for (int i = 0; i < 2; ++i) {
+        // A pointer of no CUDA allocation (pageable memory) reads back type 0 and buffer id 0.
+        CUpointer_attribute attrs[3] = {CU_POINTER_ATTRIBUTE_MEMORY_TYPE, CU_POINTER_ATTRIBUTE_BUFFER_ID,
+                                        CU_POINTER_ATTRIBUTE_DEVICE_POINTER};
+        void* data[3] = {&e[i].type, &e[i].id, &e[i].dev};
+        if (get(3, attrs, data, at[i]) != CUDA_SUCCESS || e[i].type != CU_MEMORYTYPE_HOST || !e[i].dev) return nullptr;
+    }
+    if (e[0].id == 0 || e[0].id != e[1].id || (uintptr_t)e[1].dev - (uintptr_t)e[0].dev != bytes - 1) return nullptr;
+    return e[0].dev;
 }
 
 // Sizes the per-draw scratch for a width x height frame.
