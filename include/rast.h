@@ -137,8 +137,11 @@ rast_status rast_set_lights(rast_ctx* ctx, const float* lights7, int32_t n);
 /* drawing                                                                                     */
 /* ------------------------------------------------------------------------------------------ */
 
-/* One frame of draw_frame with HOST buffers (the reference's calling convention): copies the
- * frame and depth buffers in (unless RAST_CLEAR), renders, copies them back; returns when done.
+/* One frame of draw_frame with HOST buffers (the reference's calling convention); returns when
+ * done. Buffers in page-locked memory that the device maps (cudaHostAlloc, cudaHostRegister),
+ * each within one allocation, are used in place with RAST_SHADER_EXACT: the kernels read the
+ * incoming depth where a fragment landed and write the pixels they draw over the link. Other
+ * buffers are copied in (unless RAST_CLEAR), rendered on the device and copied back.
  *   camera, normal: the frame's camera and normal matrices (rast_frame_matrices)
  *   rgb_planar: width*height*3 bytes, planar (x + y*width + c*width*height) as CImg stores
  *               CImg<unsigned char>(W,H,1,3) (renderer.cpp:85); read and written
@@ -146,10 +149,10 @@ rast_status rast_set_lights(rast_ctx* ctx, const float* lights7, int32_t n);
  *          incoming value is the depth every fragment must beat (drawing.cpp:119)
  *   tri_id (nullable): width*height uint32, the index of the triangle that wrote each pixel in
  *          this call, or 0xFFFFFFFF
- * Pixels no fragment wins keep their colour and depth. 1 <= width, height <= 32768. The colour
- * input is uploaded while the first passes run, and the results and the device status are read
- * back in one wait; after an error other than a bin overflow (which is redrawn from kept copies of
- * the inputs) the buffers' contents are unspecified. */
+ * Pixels no fragment wins keep their colour and depth. 1 <= width, height <= 32768. Copied inputs
+ * are uploaded while the first passes run, and the results and the device status are read back in
+ * one wait. A bin overflow is redrawn from the same inputs (kept copies, or in place buffers the
+ * overflowed pass left untouched); after any other error the buffers' contents are unspecified. */
 rast_status rast_draw(rast_ctx* ctx, const float camera[16], const float normal[16], uint32_t width,
                       uint32_t height, uint32_t flags, uint8_t* rgb_planar, float* depth, uint32_t* tri_id);
 
