@@ -358,7 +358,7 @@ struct SetupArgs {
 
 // One thread per triangle: load, cull and bound it. Front-facing triangles whose bounding box is
 // at most small_max pixels and small_max_row() pixels wide are rasterised by their warp; the others
-// are appended to the binned list (one atomic per block) and counted into the tiles their box
+// are appended to the binned list (one atomic per warp) and counted into the tiles their box
 // overlaps.
 //
 // The warp's raster work is split into items of up to kRowChunk pixels of one bounding-box row.
@@ -375,8 +375,6 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
     pdl_wait();
     pdl_launch_dependents();
     __shared__ SetupStage stage[kSetupWarps];
-    __shared__ uint32_t s_large[kSetupWarps];
-    __shared__ uint32_t s_large_base;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     SetupStage& S = stage[warp];
     const int64_t t = blockIdx.x * (int64_t)kSetupThreads + threadIdx.x;
@@ -409,22 +407,17 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
         }
     }
 
-    // Binned path: append (one atomic per block), and count the tiles the box overlaps.
+    // Binned path: append (one atomic per warp that has any, so no warp waits for the others of its
+    // block), and count the tiles the box overlaps. The list's order does not matter: the depth
+    // test is a minimum over keys.
     const unsigned lmask = __ballot_sync(kFull, large);
-    if (lane == 0) s_large[warp] = __popc(lmask);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t tot = 0;
-        for (int w = 0; w < kSetupWarps; ++w) {
-            const uint32_t c = s_large[w];
-            s_large[w] = tot;
-            tot += c;
-        }
-        s_large_base = tot ? atomicAdd(&a.counters[0], tot) : 0u;
+    uint32_t lbase = 0u;
+    if (lmask) {
+        if (lane == 0) lbase = atomicAdd(&a.counters[0], (uint32_t)__popc(lmask));
+        lbase = __shfl_sync(kFull, lbase, 0);
     }
-    __syncthreads();
     if (large) {
-        const uint32_t slot = s_large_base + s_large[warp] + __popc(lmask & ((1u << lane) - 1u));
+        const uint32_t slot = lbase + __popc(lmask & ((1u << lane) - 1u));
         if (slot < a.cap_large) {
             BinnedTri r;
             r.x0 = T.x0; r.y0 = T.y0; r.x1 = T.x1; r.y1 = T.y1;
