@@ -459,19 +459,16 @@ def extra_batch(torch, abi, stream, steps=10):
 
 
 def e2e_line(value, shader, W, H, stats):
-    """The e2e entry for page-locked host buffers. The exact shader uses them in place: its resolve
-    pass reads the incoming depth of each pixel a fragment landed on and writes the winners' colour
-    (3 B) and depth (4 B), plus the 4-byte status word; the other shaders copy both buffers."""
-    if shader == "exact":
-        covered = int(stats["written"])
-        return {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 4 * covered,
-                "d2h_bytes_per_step": 7 * covered + 4,
-                "path": "rast_draw with page-locked host frame (planar RGB8) and depth buffers used in place "
-                        "(read-modify-write; the kernels read the incoming depth of covered pixels and write "
-                        "their colour and depth over the link); mesh resident"}
-    return {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 7 * W * H, "d2h_bytes_per_step": 7 * W * H + 4,
-            "path": "rast_draw with page-locked host frame (planar RGB8) and depth buffers, copied both ways "
-                    "(read-modify-write); mesh resident"}
+    """The e2e entry for page-locked host buffers, which the kernels use in place: the resolve pass
+    reads the incoming depth of each pixel a fragment landed on and writes the winners' colour (3 B)
+    and depth (4 B), plus the 4-byte status word; deferred shading writes the colour once more."""
+    covered = int(stats["written"])
+    colour = 3 * covered if shader != "exact" else 0
+    return {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 4 * covered,
+            "d2h_bytes_per_step": 7 * covered + colour + 4,
+            "path": "rast_draw with page-locked host frame (planar RGB8) and depth buffers used in place "
+                    "(read-modify-write; the kernels read the incoming depth of covered pixels and write "
+                    "their colour and depth over the link); mesh resident"}
 
 
 def run_ours(args):

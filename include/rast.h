@@ -139,8 +139,8 @@ rast_status rast_set_lights(rast_ctx* ctx, const float* lights7, int32_t n);
 
 /* One frame of draw_frame with HOST buffers (the reference's calling convention); returns when
  * done. Buffers in page-locked memory that the device maps (cudaHostAlloc, cudaHostRegister),
- * each within one allocation, are used in place with RAST_SHADER_EXACT: the kernels read the
- * incoming depth where a fragment landed and write the pixels they draw over the link. Other
+ * each within one allocation, are used in place: the kernels read the incoming depth where a
+ * fragment landed and write the pixels they draw over the link. Other
  * buffers are copied in (unless RAST_CLEAR), rendered on the device and copied back.
  *   camera, normal: the frame's camera and normal matrices (rast_frame_matrices)
  *   rgb_planar: width*height*3 bytes, planar (x + y*width + c*width*height) as CImg stores

@@ -461,12 +461,12 @@ rast_status rast_draw(rast_ctx* c, const float camera[16], const float normal[16
         if (!c->ev_rgb_in) RAST_CUDA(c, cudaEventCreateWithFlags(&c->ev_rgb_in, cudaEventDisableTiming));
     }
     if (!c->h_status) RAST_CUDA(c, cudaMallocHost(&c->h_status, sizeof(uint32_t)));
-    // Page-locked host buffers that the device maps are used in place by the exact shader: the
-    // resolve pass reads the incoming depth where a fragment landed and writes the frame's pixels
-    // (read-modify-write: only the winners) straight into the host buffers, so no frame-sized
-    // copy crosses the link. After a bin-pool overflow the resolve pass writes nothing, and the
-    // redraw starts from the same buffers.
-    if (c->shader == RAST_SHADER_EXACT) {
+    // Page-locked host buffers that the device maps are used in place: the resolve pass reads the
+    // incoming depth where a fragment landed and writes the frame's pixels (read-modify-write:
+    // only the winners; deferred shading then writes their colour) straight into the host
+    // buffers, so no frame-sized copy crosses the link. After a bin-pool overflow nothing is
+    // written, and the redraw starts from the same buffers.
+    {
         uint8_t* hr = static_cast<uint8_t*>(mapped_host_range(rgb, 3 * npx));
         float* hd = static_cast<float*>(mapped_host_range(depth, sizeof(float) * npx));
         uint32_t* hi = ids ? static_cast<uint32_t*>(mapped_host_range(ids, sizeof(uint32_t) * npx)) : nullptr;

@@ -1180,8 +1180,15 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
     // Deferred shading: the shading kernel may be launched once every block of this grid has
     // started (it waits for this grid's completion before it reads the records).
     pdl_launch_dependents();
-    // Every earlier pass of the frame is complete here, so the status word is final.
-    if (a.keep_on_overflow && (a.counters[1] & (STATUS_BIN_OVERFLOW | STATUS_LARGE_OVERFLOW))) return;
+    // Every earlier pass of the frame is complete here, so the status word is final. A deferred
+    // frame's shading pass then finds an empty tile list and writes nothing either.
+    if (a.keep_on_overflow && (a.counters[1] & (STATUS_BIN_OVERFLOW | STATUS_LARGE_OVERFLOW))) {
+        if (a.shade_index && blockIdx.x == 0 && threadIdx.x == 0) {
+            a.shade_index[0] = 0u;
+            a.shade_index[1] = 0u;
+        }
+        return;
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     ResolveStage& S = stage[warp];
     const int64_t npx = (int64_t)a.width * a.height;

@@ -254,3 +254,61 @@ def test_learned_needs_matching_rig(rnd, trained):
         rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
     hdr = mlp_ref.parse_blob(blob)
     assert hdr["lights_hash"] == mlp_ref.lights_hash(lights)
+
+
+def _pinned(torch, shape, dtype):
+    tdt = {np.uint8: torch.uint8, np.float32: torch.float32, np.uint32: torch.int32}[dtype]
+    a = torch.zeros(shape, dtype=tdt).pin_memory().numpy()
+    return a.view(np.uint32) if dtype is np.uint32 else a
+
+
+@pytest.mark.parametrize("clear", [False, True])
+def test_deferred_in_place_pinned(rnd, port, clear):
+    """Page-locked buffers with the deferred shader: drawn in place, bit for bit the oracle's, and
+    after a bin-pool overflow the redraw starts from untouched buffers."""
+    torch = pytest.importorskip("torch")
+    sc = S.soup(5000, 320, 240, seed=43, area_range=(100.0, 4000.0))
+    rng = np.random.default_rng(7)
+    frame0 = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
+    depth0 = rng.uniform(-1.0, 1.5, (sc.height, sc.width)).astype(np.float32)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    rnd.upload_scene_mesh(sc)
+    rnd.set_lights(lights)
+    f = _pinned(torch, (3, sc.height, sc.width), np.uint8)
+    d = _pinned(torch, (sc.height, sc.width), np.float32)
+    i = _pinned(torch, (sc.height, sc.width), np.uint32)
+    f[...] = frame0
+    d[...] = depth0
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT_DEFERRED)
+    rnd.set_option(abi.OPT_BIN_CAPACITY, 16)
+    try:
+        rnd.draw(cam, nm, sc.width, sc.height, abi.CLEAR if clear else 0, f, d, ids=i)
+        assert rnd.get_option(abi.OPT_BIN_CAPACITY) > 16
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+        rnd.set_option(abi.OPT_BIN_CAPACITY, 0)
+    of, od, oids, _ = port.draw(sc, cam, nm, lights, None if clear else frame0, None if clear else depth0)
+    assert np.array_equal(bits(d), bits(od))
+    assert np.array_equal(i, oids)
+    assert np.array_equal(f, of)
+
+
+def test_learned_in_place_pinned(rnd, trained):
+    """The learned shader writes page-locked buffers in place: the same frame as the copy path."""
+    torch = pytest.importorskip("torch")
+    sc, lights, _, blob = trained
+    rnd.mlp_load(blob)
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
+    try:
+        f0, d0, i0 = rnd.draw_scene(sc, clear=True)
+        cam, nm, l7, _ = abi.scene_frame_inputs(sc)
+        f = _pinned(torch, (3, sc.height, sc.width), np.uint8)
+        d = _pinned(torch, (sc.height, sc.width), np.float32)
+        i = _pinned(torch, (sc.height, sc.width), np.uint32)
+        rnd.draw(cam, nm, sc.width, sc.height, abi.CLEAR | (abi.WIND_CLOCKWISE if sc.wind_clockwise else 0),
+                 f, d, ids=i)
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+    assert np.array_equal(bits(d), bits(d0))
+    assert np.array_equal(i, i0)
+    assert np.array_equal(f, f0)
