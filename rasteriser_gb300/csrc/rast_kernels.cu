@@ -6,7 +6,8 @@
 // intrinsics (never contracted into FMA), and the file is built with -fmad=false besides.
 //
 // Pipeline of one frame:
-//   k_vertex        transform_vertices + z_divide_all + ndc_to_raster_all (geometry.cpp:85-142)
+//   k_vertex        transform_vertices + z_divide_all + ndc_to_raster_all (geometry.cpp:85-142);
+//                   also clears the frame's counters and statistics
 //   k_setup_raster  per triangle: de-index, signed_area_2d cull, bounding_box (drawing.cpp:77-93,
 //                   160-188); triangles with small boxes are rasterised here by their warp, the
 //                   rest are appended to the binned list and counted into 16x16 (8/32) tiles
@@ -15,9 +16,10 @@
 //   k_tile_raster   persistent CTAs take (tile, up to 64 binned triangles) work items; each thread
 //                   owns pixels of the tile and keeps their minimum keys in registers; warp
 //                   ballots give the coverage masks and skip triangles that miss a warp's block
-//   k_resolve       per pixel: decode the winner, recompute its barycentrics, perspective-correct
-//                   normal, Lambert shading over the lights (shading.cpp:20-34), planar RGB8 +
-//                   depth writes
+//   k_resolve       per pixel: decode the winner (read-modify-write: test it against the incoming
+//                   depth), recompute its barycentrics, perspective-correct normal, Lambert
+//                   shading over the lights (shading.cpp:20-34), planar RGB8 + depth writes; re-arms
+//                   the keys for the next frame
 //
 // Depth test: the reference keeps a fragment when `ndcdepth < depth(x,y)` while walking the
 // triangles in order (drawing.cpp:119), so a pixel ends with the smallest depth and, among equal
@@ -357,20 +359,20 @@ struct SetupArgs {
 };
 
 // One thread per triangle: load, cull and bound it. Front-facing triangles whose bounding box is
-// at most small_max pixels and small_max_row() pixels wide are rasterised by their warp; the others
-// are appended to the binned list (one atomic per warp) and counted into the tiles their box
-// overlaps.
+// at most small_max pixels, and at most small_max_row() pixels on its shorter side (whole items) or
+// wide (row chunks), are rasterised by their warp; the others are appended to the binned list (one
+// atomic per warp) and counted into the tiles their box overlaps.
 //
-// The warp's raster work is split into items of up to kRowChunk pixels of one bounding-box row.
-// The items of its 32 triangles are laid end to end and taken 32 at a time, so every lane has at
-// most kRowChunk pixels whatever the box sizes. The owner of an item is the last triangle whose
-// items start at or before it in the current window (an OR-reduction of start positions), else
-// the owner of the window's first item, carried over from the previous window. Each edge function
+// The warp's raster work is split into items: whole rows or columns of a box (kRowChunk 32, along
+// the box's longer side), or chunks of kRowChunk pixels of one row. The items of its 32 triangles
+// are laid end to end and taken 32 at a time. The owner of an item is the last triangle whose items
+// start at or before it in the current window (an OR-reduction of start positions), else the owner
+// of the window's first item, carried over from the previous window. Each edge function
 //   e = (b.x - a.x)*(py - a.y) - (b.y - a.y)*(px - a.x)     (drawing.cpp:36-39)
-// is evaluated as the reference does, its first product taken once per item.
+// is evaluated in the reference's operation order, its first product taken once per item.
 // At most 48 registers, so 5 CTAs (40 warps) fit an SM: the kernel is issue-bound on dependent
-// chains, and the extra warps hide them (6.0k vs 5.8k frames/s on the 1M-triangle 1080p frame).
-template <uint32_t kRowChunk>  // pixels of one bounding-box row per work item
+// chains, and the extra warps hide them (6 CTAs, at 40 registers, spill and measured slower).
+template <uint32_t kRowChunk>  // pixels of one bounding-box row per work item; 32: whole rows or columns
 __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) {
     pdl_wait();
     pdl_launch_dependents();
