@@ -374,12 +374,20 @@ struct SetupArgs {
 // chains, and the extra warps hide them (6 CTAs, at 40 registers, spill and measured slower).
 template <uint32_t kRowChunk>  // pixels of one bounding-box row per work item; 32: whole rows or columns
 __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) {
-    pdl_wait();
-    pdl_launch_dependents();
     __shared__ SetupStage stage[kSetupWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     SetupStage& S = stage[warp];
     const int64_t t = blockIdx.x * (int64_t)kSetupThreads + threadIdx.x;
+    // The mesh's vertex indices were uploaded before the frame: they are fetched while the vertex
+    // pass finishes. Everything after the wait depends on that pass or the frame's clears.
+    int32_t i0 = 0, i1 = 0, i2 = 0;
+    if (t < a.ntri) {
+        i0 = a.tri_v[3 * t];
+        i1 = a.tri_v[3 * t + 1];
+        i2 = a.tri_v[3 * t + 2];
+    }
+    pdl_wait();
+    pdl_launch_dependents();
 
     uint32_t n_items = 0, n_tiles = 0, cpr = 1;
     uint32_t tlx = 0, tly = 0, brx = 0, bry = 0;
@@ -387,7 +395,6 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
     uint32_t c_front = 0;
     bool large = false, col = false;
     if (t < a.ntri) {
-        const int32_t i0 = a.tri_v[3 * t], i1 = a.tri_v[3 * t + 1], i2 = a.tri_v[3 * t + 2];
         const float4 v0 = a.rv[i0], v1 = a.rv[i1], v2 = a.rv[i2];
         if (front_facing(v0, v1, v2, a.cw)) {
             c_front = 1;
