@@ -338,7 +338,7 @@ struct SetupStage {
     int slot[32];
     // Ring of candidate runs (pixels of one item the early reject could not rule out): first pixel
     // (t | fixed << 16), owning lane with the column flag in bit 5, and the run's length.
-    uint32_t q_xy[64], q_om[64], q_m[64];
+    uint32_t q_tf[64], q_om[64], q_m[64];
 };
 
 struct SetupArgs {
@@ -507,7 +507,7 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                 uint32_t cnt = 0u, tf = 0u, own = 0u;
                 if ((uint32_t)lane < q_count) {
                     const uint32_t e = (q_head + lane) & 63u;
-                    tf = S.q_xy[e];
+                    tf = S.q_tf[e];
                     own = S.q_om[e];
                     cnt = S.q_m[e];
                     if (lane == 0) {
@@ -524,13 +524,14 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                 __syncwarp();
                 const int src = S.slot[31 - __clz(starts & (0xFFFFFFFFu >> (31 - lane)))];
                 __syncwarp();
-                const uint32_t stf = __shfl_sync(kFull, tf, src);
-                const uint32_t som = __shfl_sync(kFull, own, src);
-                const uint32_t sex = __shfl_sync(kFull, excl_p, src);
+                // the lane's run, from the lane that loaded it
+                const uint32_t r_tf = __shfl_sync(kFull, tf, src);
+                const uint32_t r_om = __shfl_sync(kFull, own, src);
+                const uint32_t r_excl = __shfl_sync(kFull, excl_p, src);
                 const uint32_t avail = min(q_pix, 32u);
                 if ((uint32_t)lane < avail) {
-                    const uint32_t j = som & 31u;
-                    const uint32_t tt = (stf & 0xFFFFu) + ((uint32_t)lane - sex), fx = stf >> 16;
+                    const uint32_t j = r_om & 31u;
+                    const uint32_t tt = (r_tf & 0xFFFFu) + ((uint32_t)lane - r_excl), fx = r_tf >> 16;
                     const float4 q0 = S.rec[j][0], q1 = S.rec[j][1], q2 = S.rec[j][2], q4 = S.rec[j][4];
                     const float ff = (float)fx, tv = (float)tt;
                     const float e0 = sub(mul(q0.x, sub(ff, q0.y)), mul(q0.z, sub(tv, q0.w)));
@@ -540,7 +541,7 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                     if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
                         ++c_inside;
                         const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
-                        const bool cl = (som & 32u) != 0u;
+                        const bool cl = (r_om & 32u) != 0u;
                         const uint32_t x = cl ? fx : tt, y = cl ? tt : fx;
                         if (z == z && x < a.width && y < a.height)
                             atomicMin(&a.keys[(size_t)y * a.width + x], frag_key(z, tri_base + j));
@@ -728,7 +729,7 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                 const unsigned m = __ballot_sync(kFull, has);
                 if (has) {
                     const uint32_t e = (q_head + q_count + __popc(m & lt_mask)) & 63u;
-                    S.q_xy[e] = run_t | (fixed << 16);
+                    S.q_tf[e] = run_t | (fixed << 16);
                     S.q_om[e] = (uint32_t)owner | cflag;
                     S.q_m[e] = run_n;
                 }
