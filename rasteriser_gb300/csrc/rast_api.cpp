@@ -450,16 +450,6 @@ rast_status rast_draw(rast_ctx* c, const float camera[16], const float normal[16
     DeviceGuard g(c->device);
     const size_t npx = (size_t)w * h;
     const bool rmw = !(flags & RAST_CLEAR);
-    RAST_CUDA(c, c->d_rgb.reserve(3 * npx));
-    RAST_CUDA(c, c->d_depth.reserve(sizeof(float) * npx));
-    if (ids) RAST_CUDA(c, c->d_ids.reserve(sizeof(uint32_t) * npx));
-    if (rmw) {
-        RAST_CUDA(c, c->d_rgb_in.reserve(3 * npx));
-        RAST_CUDA(c, c->d_depth_in.reserve(sizeof(float) * npx));
-        if (!c->copy_stream) RAST_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-        if (!c->ev_depth_in) RAST_CUDA(c, cudaEventCreateWithFlags(&c->ev_depth_in, cudaEventDisableTiming));
-        if (!c->ev_rgb_in) RAST_CUDA(c, cudaEventCreateWithFlags(&c->ev_rgb_in, cudaEventDisableTiming));
-    }
     if (!c->h_status) RAST_CUDA(c, cudaMallocHost(&c->h_status, sizeof(uint32_t)));
     // Page-locked host buffers that the device maps are used in place: the resolve pass reads the
     // incoming depth where a fragment landed and writes the frame's pixels (read-modify-write:
@@ -486,6 +476,17 @@ rast_status rast_draw(rast_ctx* c, const float camera[16], const float normal[16
             }
             return fail(c, RAST_ERR_BIN_OVERFLOW, "tile-bin pool still overflowing after regrowth");
         }
+    }
+    // Otherwise the buffers are copied through device memory.
+    RAST_CUDA(c, c->d_rgb.reserve(3 * npx));
+    RAST_CUDA(c, c->d_depth.reserve(sizeof(float) * npx));
+    if (ids) RAST_CUDA(c, c->d_ids.reserve(sizeof(uint32_t) * npx));
+    if (rmw) {
+        RAST_CUDA(c, c->d_rgb_in.reserve(3 * npx));
+        RAST_CUDA(c, c->d_depth_in.reserve(sizeof(float) * npx));
+        if (!c->copy_stream) RAST_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        if (!c->ev_depth_in) RAST_CUDA(c, cudaEventCreateWithFlags(&c->ev_depth_in, cudaEventDisableTiming));
+        if (!c->ev_rgb_in) RAST_CUDA(c, cudaEventCreateWithFlags(&c->ev_rgb_in, cudaEventDisableTiming));
     }
     for (int attempt = 0; attempt < 3; ++attempt) {
         // The inputs are needed only by the resolve pass (the incoming depth each winner must beat,
