@@ -311,3 +311,30 @@ def test_pinned_slice_of_larger_allocation(renderer, port):
     assert np.abs(f.astype(int) - fp).max() <= RGB_TOL
     assert np.all(big[:1000] == 0) and np.all(big[1000 + 3 * n:] == 0)
     assert np.all(dbig[:16] == 1.0) and np.all(dbig[16 + n:] == 1.0)
+
+
+def test_registered_host_buffers_used_in_place(renderer, port):
+    """Ordinary arrays registered with cudaHostRegister are page-locked and mapped too: drawn in
+    place, equal to the port."""
+    torch = pytest.importorskip("torch")
+    sc = S.soup(6000, 300, 200, seed=29, area_range=(0.5, 3000.0))
+    rng = np.random.default_rng(13)
+    depth0 = rng.uniform(-1.0, 1.5, (sc.height, sc.width)).astype(np.float32)
+    frame0 = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    renderer.upload_scene_mesh(sc)
+    renderer.set_lights(lights)
+    f, d = frame0.copy(), depth0.copy()
+    rt = torch.cuda.cudart()
+    assert int(rt.cudaHostRegister(f.ctypes.data, f.nbytes, 0)) == 0
+    try:
+        assert int(rt.cudaHostRegister(d.ctypes.data, d.nbytes, 0)) == 0
+        try:
+            renderer.draw(cam, nm, sc.width, sc.height, flags_of(sc), f, d)
+        finally:
+            rt.cudaHostUnregister(d.ctypes.data)
+    finally:
+        rt.cudaHostUnregister(f.ctypes.data)
+    fp, dp, _, _ = port.draw(sc, cam, nm, lights, frame0, depth0)
+    assert np.array_equal(bits(d), bits(dp))
+    assert np.abs(f.astype(int) - fp).max() <= RGB_TOL
