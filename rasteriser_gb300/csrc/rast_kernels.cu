@@ -211,6 +211,21 @@ __device__ __forceinline__ int owner_of(const uint32_t* incl, uint32_t k) {
     return lo;
 }
 
+// RN(a / b) from y = RN(1/b), the correctly rounded reciprocal: q0 = RN(a*y), then one fused
+// correction q = RN(q0 + RN(a - b*q0)*y) (Markstein's correction step). Checked bit for bit
+// against __fdiv_rn on every pair of significands (2^46 pairs, a and b in [1, 2)); scaling a and
+// b by powers of two scales every step exactly while all values stay normal, which holds for
+// |a| and |b| in [2^-60, 2^60], and every step is symmetric in the signs. Outside that range, for
+// zeros, and when y is 0 (b outside it), the quotient is __fdiv_rn's.
+__device__ __forceinline__ float div_by(float a, float b, float y) {
+    const float aa = fabsf(a);
+    if (y != 0.f && aa >= 0x1p-60f && aa <= 0x1p60f) {
+        const float q0 = __fmul_rn(a, y);
+        return __fmaf_rn(__fmaf_rn(-b, q0, a), y, q0);
+    }
+    return dvd(a, b);
+}
+
 // q = n / d for n <= 2^24, d >= 1: a float-reciprocal estimate (within 2 of the quotient at
 // that range) corrected to the exact quotient.
 __device__ __forceinline__ uint32_t div_small(uint32_t n, uint32_t d, float rd) {
@@ -489,6 +504,12 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
             if (kRowChunk != 32u) {
                 S.cpr[lane] = cpr;
                 S.rcpr[lane] = __frcp_rn((float)cpr);
+            } else {
+                // The correctly rounded reciprocal of the staged area (rec[4].w) for div_by, or 0
+                // (use __fdiv_rn) when its magnitude is outside [2^-60, 2^60]. The correction step
+                // is symmetric in the divisor's sign.
+                const float ba = mul(sg, T.area), aa = fabsf(ba);
+                S.rcpr[lane] = aa >= 0x1p-60f && aa <= 0x1p60f ? __frcp_rn(ba) : 0.f;
             }
             S.incl[lane] = incl;
             __syncwarp();
@@ -537,7 +558,8 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                     const float e0 = sub(mul(q0.x, sub(ff, q0.y)), mul(q0.z, sub(tv, q0.w)));
                     const float e1 = sub(mul(q1.x, sub(ff, q1.y)), mul(q1.z, sub(tv, q1.w)));
                     const float e2 = sub(mul(q2.x, sub(ff, q2.y)), mul(q2.z, sub(tv, q2.w)));
-                    const float b0 = dvd(e0, q4.w), b1 = dvd(e1, q4.w), b2 = dvd(e2, q4.w);
+                    const float ra = kRowChunk == 32u ? S.rcpr[j] : 0.f;
+                    const float b0 = div_by(e0, q4.w, ra), b1 = div_by(e1, q4.w, ra), b2 = div_by(e2, q4.w, ra);
                     if (b0 >= 0.f && b1 >= 0.f && b2 >= 0.f) {
                         ++c_inside;
                         const float z = add(add(mul(q4.x, b0), mul(q4.y, b1)), mul(q4.z, b2));
