@@ -86,15 +86,31 @@ def max_over_ranks(dist, seconds, device):
     return float(t.item())
 
 
-def frame_inputs(scene, n_frames):
-    from rasteriser_gb300 import abi
+def frame_inputs(scene, n_frames, source=None):
+    """(scene, camera, normal matrix, transformed lights) of each spin frame. The matrices and
+    lights come from librast's host code, or from `source.frame_inputs` (the oracle port, for the
+    reference arm, which loads nothing of this package's native code)."""
     from rasteriser_gb300 import scenes as S
+    if source is None:
+        from rasteriser_gb300 import abi
+        source_fn = abi.scene_frame_inputs
+    else:
+        source_fn = source.frame_inputs
     out = []
     for f in range(n_frames):
         sc = scene.with_view(angles=S.spin_angles(f))
-        cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+        cam, nm, lights, _ = source_fn(sc)
         out.append((sc, cam, nm, lights))
     return out
+
+
+def workload_config(scene, workload, n_frames, n_lights, world, shader):
+    """The `config` object of both arms' lines: the workload, its sizes and the draw mode."""
+    return {"workload": workload, "width": scene.width, "height": scene.height, "triangles": scene.ntri,
+            "vertices": int(scene.pos.shape[0]), "lights": int(n_lights), "frames_cycled": n_frames,
+            "l2": "GPU arm: flushed between steps (256 MiB write, outside the timed events)",
+            "parallelism": f"replicas x{world}", "mode": "RAST_CLEAR (spin-loop clear + draw_frame)",
+            "shader": shader}
 
 
 class ClockSampler:
@@ -186,11 +202,15 @@ def load_traffic(kernel, workload):
     return None if e is None else float(e["dram_bytes_per_launch"])
 
 
-def cpu_baseline(frames, seconds, threads=1):
-    """The oracle port (C restatement of the reference's draw_frame) on the host cores."""
+def oracle_port():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    port = oracle.Port()
+    return oracle.Port()
+
+
+def cpu_baseline(frames, seconds, threads=1):
+    """The oracle port (C restatement of the reference's draw_frame) on the host cores."""
+    port = oracle_port()
     done = []
     lock = threading.Lock()
     t0 = time.perf_counter()
@@ -217,9 +237,7 @@ def cpu_baseline(frames, seconds, threads=1):
 def parallel_steps(frames, steps, threads, first=0):
     """`steps` rounds; in each, `threads` threads render one frame each of the spin (the port
     releases the GIL inside its C call). Returns the wall seconds of all rounds."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    port = oracle.Port()
+    port = oracle_port()
 
     def render(i):
         sc, cam, nm, lights = frames[i % len(frames)]
@@ -240,7 +258,10 @@ def run_reference(args):
     if rank != 0:
         return
     scene, workload = make_scene(args.workload)
-    frames = frame_inputs(scene, SPIN_FRAMES)
+    n_frames = SPIN_FRAMES if args.workload == "displaced_sphere" else 1
+    # matrices and lights from the oracle port's restatement of drawing.cpp:221-238
+    frames = frame_inputs(scene, n_frames, source=oracle_port())
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     threads = os.cpu_count() or 1
     warm = parallel_steps(frames, max(1, min(args.warmup, 2)), threads)
     per_step = warm / max(1, min(args.warmup, 2))
@@ -252,7 +273,7 @@ def run_reference(args):
             "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": workload, "width": scene.width, "height": scene.height, "triangles": scene.ntri},
+            "config": workload_config(scene, workload, n_frames, frames[0][3].shape[0], world, args.shader),
             "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
                              "sample": f"{steps} steps x {threads} threads, one full frame of the 60-frame spin per "
                                        f"thread per step, {dt:.1f} s"},
@@ -634,11 +655,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload, "width": W, "height": H, "triangles": scene.ntri,
-                   "vertices": int(scene.pos.shape[0]), "lights": int(frames[0][3].shape[0]),
-                   "frames_cycled": n_frames, "l2": "flushed between steps (256 MiB write, outside the timed events)",
-                   "parallelism": f"replicas x{world}", "mode": "RAST_CLEAR (spin-loop clear + draw_frame)",
-                   "shader": args.shader},
+        "config": workload_config(scene, workload, n_frames, frames[0][3].shape[0], world, args.shader),
         "e2e": e2e_line(e2e_value, args.shader, W, H, stats),
         "e2e_pageable": {"value": e2e_pageable, "unit": "frames/s", "h2d_bytes_per_step": 7 * W * H,
                          "d2h_bytes_per_step": 7 * W * H,

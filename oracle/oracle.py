@@ -19,16 +19,23 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
-REFERENCE_TREE = "/root/reference"
+# The canmom/rasteriser source tree the reference oracle compiles from: RAST_REFERENCE, else the
+# place this build's container mounts it. Absent on hosts without the reference sources.
+REFERENCE_TREE = os.environ.get("RAST_REFERENCE") or "/root/reference"
+
+
+def reference_tree():
+    """The reference source tree, or None where it is not present."""
+    return REFERENCE_TREE if os.path.isdir(os.path.join(REFERENCE_TREE, "headers")) else None
 
 
 def build(with_reference=None, quiet=True):
     """Compile the port, and the reference when its sources are present."""
     if with_reference is None:
-        with_reference = os.path.isdir(REFERENCE_TREE)
+        with_reference = reference_tree() is not None
     targets = ["port"] + (["ref"] if with_reference else [])
     out = None if not quiet else subprocess.DEVNULL
-    subprocess.run(["make", "-C", HERE, "-j8"] + targets, check=True, stdout=out)
+    subprocess.run(["make", "-C", HERE, "-j8", f"REF={REFERENCE_TREE}"] + targets, check=True, stdout=out)
 
 
 def _f32(a):
@@ -83,6 +90,13 @@ class Port:
                                                     C.c_uint32, C.c_uint32, C.POINTER(C.c_float)]
         self.lib.oracle_shade.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                           C.c_int32, C.POINTER(C.c_uint32)]
+        self.lib.oracle_frame_matrices.restype = C.c_int
+        self.lib.oracle_frame_matrices.argtypes = [C.c_uint32, C.c_uint32, C.c_float, C.POINTER(C.c_float),
+                                                   C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float] + \
+            [C.POINTER(C.c_float)] * 5
+        self.lib.oracle_transform_lights.restype = C.c_int
+        self.lib.oracle_transform_lights.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
+                                                     C.POINTER(C.c_float)]
 
     def draw(self, scene, camera, normal_matrix, lights7, frame=None, depth=None, want_ids=True, textures=None):
         """Returns (frame (3,H,W) uint8, depth (H,W) float32, ids (H,W) uint32 or None, stats).
@@ -117,6 +131,31 @@ class Port:
         if rc != 0:
             raise RuntimeError("oracle_draw_frame failed")
         return frame, depth, ids, stats
+
+    def matrices(self, width, height, scale, disp, angles, fovy_deg, z_near, z_far):
+        """dict of model, view, modelview, camera, normal (each (16,) float32, column major):
+        drawing.cpp:221-229 with the given projection (the C restatement)."""
+        out = {k: np.zeros(16, np.float32) for k in ("model", "view", "modelview", "camera", "normal")}
+        rc = self.lib.oracle_frame_matrices(width, height, scale, _p(_f32(disp)), _p(_f32(angles)), fovy_deg,
+                                            z_near, z_far, *[_p(out[k]) for k in out])
+        if rc != 0:
+            raise RuntimeError("oracle_frame_matrices: bad argument")
+        return out
+
+    def transform_lights(self, view, lights7):
+        """Light::transform of every (direction, intensity, rgb) record (geometry.cpp:124-133)."""
+        li = _f32(lights7).reshape(-1, 7)
+        out = np.empty_like(li)
+        if self.lib.oracle_transform_lights(_p(_f32(view)), _p(li), li.shape[0], _p(out)) != 0:
+            raise RuntimeError("oracle_transform_lights: bad argument")
+        return out
+
+    def frame_inputs(self, scene):
+        """(camera, normal matrix, transformed lights, matrices) of a scene's frame, all from the
+        C restatement."""
+        m = self.matrices(scene.width, scene.height, scene.scale, scene.disp, scene.angles, scene.fovy_deg,
+                          scene.z_near, scene.z_far)
+        return m["camera"], m["normal"], self.transform_lights(m["view"], scene.lights), m
 
     def raster_vertices(self, camera, pos, width, height):
         pos = _f32(pos)

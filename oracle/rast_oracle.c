@@ -96,6 +96,143 @@ void oracle_shade(const float* normal3, const float* albedo3, const float* light
     shade(n, a, lights7, nl, out3);
 }
 
+/* ---- per-frame matrices and lights (drawing.cpp:221-238) -------------------------------------
+ * 4x4 matrices are 16 floats, column major (m[4*c + r] is row r of column c), in the operation
+ * order of the project's glm subset: mat4*mat4 sums each column left to right, translate and
+ * rotate post-multiply, normalize is v * (1 / sqrt(dot(v, v))). */
+static void m4_identity(float* m, float d) {
+    for (int i = 0; i < 16; ++i) m[i] = 0.f;
+    m[0] = m[5] = m[10] = m[15] = d;
+}
+
+static void m4_mul(const float* a, const float* b, float* out) {
+    float r[16];
+    for (int c = 0; c < 4; ++c)
+        for (int k = 0; k < 4; ++k)
+            r[4 * c + k] = ((a[k] * b[4 * c] + a[4 + k] * b[4 * c + 1]) + a[8 + k] * b[4 * c + 2]) +
+                           a[12 + k] * b[4 * c + 3];
+    memcpy(out, r, sizeof r);
+}
+
+/* glm::rotate(mat4(1), angle, axis): Rodrigues' rotation, columns R[j]. */
+static void m4_rotation(float angle, float ax, float ay, float az, float* out) {
+    const float c = cosf(angle), s = sinf(angle);
+    const float inv = 1.0f / sqrtf((ax * ax + ay * ay) + az * az);
+    const float kx = ax * inv, ky = ay * inv, kz = az * inv;
+    const float omc = 1.0f - c;
+    const float tx = omc * kx, ty = omc * ky, tz = omc * kz;
+    const float R[3][3] = {{c + tx * kx, tx * ky + s * kz, tx * kz - s * ky},
+                           {ty * kx - s * kz, c + ty * ky, ty * kz + s * kx},
+                           {tz * kx + s * ky, tz * ky - s * kx, c + tz * kz}};
+    /* identity columns times R: (m0*R.x + m1*R.y) + m2*R.z with m = I */
+    float id[16];
+    m4_identity(id, 1.f);
+    for (int j = 0; j < 3; ++j)
+        for (int r = 0; r < 4; ++r)
+            out[4 * j + r] = (id[r] * R[j][0] + id[4 + r] * R[j][1]) + id[8 + r] * R[j][2];
+    for (int r = 0; r < 4; ++r) out[12 + r] = id[12 + r];
+}
+
+/* geometry.cpp:22-25: translate(I, d) * rotate(ry) * rotate(rx) * rotate(rz) * scale(f). */
+static void transformation_matrix(float factor, const float* d, const float* tb, float* out) {
+    float T[16], Ry[16], Rx[16], Rz[16], S[16], acc[16];
+    m4_identity(T, 1.f);
+    for (int r = 0; r < 4; ++r) /* glm::translate: ((m0*dx + m1*dy) + m2*dz) + m3 */
+        T[12 + r] = ((T[r] * d[0] + T[4 + r] * d[1]) + T[8 + r] * d[2]) + T[12 + r];
+    m4_rotation(tb[1], 0.f, 1.f, 0.f, Ry);
+    m4_rotation(tb[0], 1.f, 0.f, 0.f, Rx);
+    m4_rotation(tb[2], 0.f, 0.f, 1.f, Rz);
+    m4_identity(S, 1.f);
+    for (int r = 0; r < 4; ++r) { S[r] = S[r] * factor; S[4 + r] = S[4 + r] * factor; S[8 + r] = S[8 + r] * factor; }
+    m4_mul(T, Ry, acc);
+    m4_mul(acc, Rx, acc);
+    m4_mul(acc, Rz, acc);
+    m4_mul(acc, S, out);
+}
+
+/* glm::inverse through the adjugate (the 2x2 minors of the top and bottom row pairs). */
+static void m4_inverse(const float* m, float* out) {
+#define A(r, c) m[4 * (c) + (r)]
+    const float a00 = A(0, 0), a01 = A(0, 1), a02 = A(0, 2), a03 = A(0, 3);
+    const float a10 = A(1, 0), a11 = A(1, 1), a12 = A(1, 2), a13 = A(1, 3);
+    const float a20 = A(2, 0), a21 = A(2, 1), a22 = A(2, 2), a23 = A(2, 3);
+    const float a30 = A(3, 0), a31 = A(3, 1), a32 = A(3, 2), a33 = A(3, 3);
+#undef A
+    const float s0 = a00 * a11 - a10 * a01, s1 = a00 * a12 - a10 * a02, s2 = a00 * a13 - a10 * a03;
+    const float s3 = a01 * a12 - a11 * a02, s4 = a01 * a13 - a11 * a03, s5 = a02 * a13 - a12 * a03;
+    const float c5 = a22 * a33 - a32 * a23, c4 = a21 * a33 - a31 * a23, c3 = a21 * a32 - a31 * a22;
+    const float c2 = a20 * a33 - a30 * a23, c1 = a20 * a32 - a30 * a22, c0 = a20 * a31 - a30 * a21;
+    const float det = (s0 * c5 - s1 * c4 + s2 * c3) + (s3 * c2 - s4 * c1 + s5 * c0);
+    const float inv = 1.0f / det;
+#define B(r, c) out[4 * (c) + (r)]
+    B(0, 0) = ( a11 * c5 - a12 * c4 + a13 * c3) * inv;
+    B(0, 1) = (-a01 * c5 + a02 * c4 - a03 * c3) * inv;
+    B(0, 2) = ( a31 * s5 - a32 * s4 + a33 * s3) * inv;
+    B(0, 3) = (-a21 * s5 + a22 * s4 - a23 * s3) * inv;
+    B(1, 0) = (-a10 * c5 + a12 * c2 - a13 * c1) * inv;
+    B(1, 1) = ( a00 * c5 - a02 * c2 + a03 * c1) * inv;
+    B(1, 2) = (-a30 * s5 + a32 * s2 - a33 * s1) * inv;
+    B(1, 3) = ( a20 * s5 - a22 * s2 + a23 * s1) * inv;
+    B(2, 0) = ( a10 * c4 - a11 * c2 + a13 * c0) * inv;
+    B(2, 1) = (-a00 * c4 + a01 * c2 - a03 * c0) * inv;
+    B(2, 2) = ( a30 * s4 - a31 * s2 + a33 * s0) * inv;
+    B(2, 3) = (-a20 * s4 + a21 * s2 - a23 * s0) * inv;
+    B(3, 0) = (-a10 * c3 + a11 * c1 - a12 * c0) * inv;
+    B(3, 1) = ( a00 * c3 - a01 * c1 + a02 * c0) * inv;
+    B(3, 2) = (-a30 * s3 + a31 * s1 - a32 * s0) * inv;
+    B(3, 3) = ( a20 * s3 - a21 * s1 + a22 * s0) * inv;
+#undef B
+}
+
+int oracle_frame_matrices(uint32_t width, uint32_t height, float scale, const float* disp, const float* angles,
+                          float fovy_deg, float z_near, float z_far, float* model, float* view,
+                          float* modelview, float* camera, float* normal) {
+    if (width == 0 || height == 0 || !disp || !angles || !model || !view || !modelview || !camera || !normal)
+        return -1;
+    /* arguments.cpp:39 */
+    const float aspect = (float)width / (float)height;
+    const float zero[3] = {0.f, 0.f, 0.f}, eye[3] = {0.f, 0.f, -3.f};
+    transformation_matrix(scale, disp, angles, model);   /* drawing.cpp:222 */
+    transformation_matrix(1.f, eye, zero, view);          /* drawing.cpp:224 */
+    m4_mul(view, model, modelview);                       /* drawing.cpp:226 */
+    /* geometry.cpp:27-33 with the caller's projection: glm::perspective(radians(fovy), ...) */
+    const float fovy = fovy_deg * (float)0.01745329251994329576923690768489;
+    const float th = tanf(fovy / 2.0f);
+    float P[16];
+    m4_identity(P, 0.f);
+    P[0] = 1.0f / (aspect * th);
+    P[5] = 1.0f / th;
+    P[10] = -(z_far + z_near) / (z_far - z_near);
+    P[11] = -1.0f;
+    P[14] = -(2.0f * z_far * z_near) / (z_far - z_near);
+    m4_mul(P, modelview, camera);
+    /* geometry.cpp:101: transpose(inverse(modelview)) */
+    float inv[16];
+    m4_inverse(modelview, inv);
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) normal[4 * c + r] = inv[4 * r + c];
+    return 0;
+}
+
+int oracle_transform_lights(const float* view, const float* lights_in, int32_t n, float* lights_out) {
+    if (n < 0 || (n > 0 && (!view || !lights_in || !lights_out))) return -1;
+    for (int32_t i = 0; i < n; ++i) {
+        const float* L = lights_in + 7 * i;
+        float rec[7];
+        memcpy(rec, L, sizeof rec);
+        /* geometry.cpp:35-42 transform_direction (w = 0), then normalize (geometry.cpp:124-127) */
+        const float tx = mrow(view, 0, rec[0], rec[1], rec[2], 0.f);
+        const float ty = mrow(view, 1, rec[0], rec[1], rec[2], 0.f);
+        const float tz = mrow(view, 2, rec[0], rec[1], rec[2], 0.f);
+        const float inv = 1.0f / sqrtf((tx * tx + ty * ty) + tz * tz);
+        rec[0] = tx * inv;
+        rec[1] = ty * inv;
+        rec[2] = tz * inv;
+        memcpy(lights_out + 7 * i, rec, sizeof rec);
+    }
+    return 0;
+}
+
 /* CImg's linear_atXY(fx, fy, 0, c) with Neumann boundaries: the coordinates clamped to the image
  * (cimg::cut), the integer corner, and the bilinear blend in CImg's order of operations. */
 static float cimg_linear_xy(const float* img, int w, int h, int c, float fx, float fy) {

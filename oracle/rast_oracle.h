@@ -58,6 +58,17 @@ void oracle_raster_vertices(const float* camera, const float* pos, int64_t nv, u
 void oracle_shade(const float* normal3, const float* albedo3, const float* lights7, int32_t nl,
                   uint32_t* out3);
 
+/* The per-frame matrices of draw_frame (drawing.cpp:221-229; geometry.cpp:22-33, 101): model,
+ * view, modelview, camera = perspective(fovy_deg, width/height, z_near, z_far) * modelview, and the
+ * normal matrix transpose(inverse(modelview)); each 16 floats, column major. Returns 0 or -1. */
+int oracle_frame_matrices(uint32_t width, uint32_t height, float scale, const float* disp, const float* angles,
+                          float fovy_deg, float z_near, float z_far, float* model, float* view,
+                          float* modelview, float* camera, float* normal);
+
+/* Light::transform over n (direction xyz, intensity, rgb) records (geometry.cpp:124-133):
+ * trans_dir = normalize(xyz(view * (direction, 0))). Returns 0 or -1. */
+int oracle_transform_lights(const float* view, const float* lights_in, int32_t n, float* lights_out);
+
 #ifdef __cplusplus
 }
 #endif

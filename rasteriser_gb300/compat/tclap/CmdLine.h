@@ -1,7 +1,7 @@
-// Oracle test infrastructure: a minimal stand-in for the TCLAP command-line parser, covering only
-// the calls canmom/rasteriser's arguments.cpp makes (CmdLine, ValueArg<T>, SwitchArg, parse,
-// getValue, ArgException). TCLAP is not installed here; this lets the reference's own
-// arguments.cpp compile unmodified for the oracle and drop-in link builds.
+// A minimal stand-in for the TCLAP command-line parser, covering only the calls
+// canmom/rasteriser's arguments.cpp makes (CmdLine, ValueArg<T>, SwitchArg, parse, getValue,
+// ArgException). Where TCLAP is not installed, this lets the reference's own arguments.cpp compile
+// unmodified, both for the drop-in link build and for the oracle.
 #ifndef RAST_ORACLE_TCLAP_SHIM_H
 #define RAST_ORACLE_TCLAP_SHIM_H
 

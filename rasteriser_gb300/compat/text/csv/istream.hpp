@@ -1,7 +1,8 @@
-// Oracle test infrastructure: a minimal stand-in for the text-csv reader, covering only what
-// canmom/rasteriser's fileloader.cpp uses (`csv_istream(std::istream&)`, `operator>>(float&)` and
-// the stream's truth value). Fields are separated by commas and records by newlines. text-csv is
-// not installed here; this lets the reference's own fileloader.cpp compile unmodified.
+// A minimal stand-in for the text-csv reader, covering only what canmom/rasteriser's
+// fileloader.cpp uses (`csv_istream(std::istream&)`, `operator>>(float&)` and the stream's truth
+// value). Fields are separated by commas and records by newlines. Where text-csv is not installed,
+// this lets the reference's own fileloader.cpp compile unmodified, for the drop-in link build and
+// for the oracle.
 #ifndef RAST_ORACLE_TEXT_CSV_SHIM_HPP
 #define RAST_ORACLE_TEXT_CSV_SHIM_HPP
 

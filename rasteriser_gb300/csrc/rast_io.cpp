@@ -40,6 +40,23 @@ inline bool is_digit(char c) { return (unsigned)(c - '0') < 10u; }
 inline bool is_eol(char c) { return c == '\r' || c == '\n' || c == '\0'; }
 
 // The decimal parser described above, on [s, e). False when no number starts at s.
+//
+// Attribution: this function follows the steps of tinyobjloader's tryParseDouble
+// (tiny_obj_loader.h 1.0.5, which canmom/rasteriser vendors), because those steps decide the
+// float bits of every vertex an OBJ file loads to. tinyobjloader is under the MIT License:
+//   Copyright (c) 2012-2016 Syoyo Fujita and many contributors.
+//   Permission is hereby granted, free of charge, to any person obtaining a copy of this software
+//   and associated documentation files (the "Software"), to deal in the Software without
+//   restriction, including without limitation the rights to use, copy, modify, merge, publish,
+//   distribute, sublicense, and/or sell copies of the Software, and to permit persons to whom the
+//   Software is furnished to do so, subject to the following conditions: The above copyright
+//   notice and this permission notice shall be included in all copies or substantial portions of
+//   the Software. THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS OR
+//   IMPLIED, INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF MERCHANTABILITY, FITNESS FOR A
+//   PARTICULAR PURPOSE AND NONINFRINGEMENT. IN NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE
+//   LIABLE FOR ANY CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT, TORT OR
+//   OTHERWISE, ARISING FROM, OUT OF OR IN CONNECTION WITH THE SOFTWARE OR THE USE OR OTHER
+//   DEALINGS IN THE SOFTWARE.
 bool parse_real(const char* s, const char* e, double* out) {
     if (s >= e) return false;
     double mantissa = 0.0;

@@ -23,10 +23,10 @@ def port():
 def reference():
     import oracle
     if not os.path.exists(oracle.REF_SO):
-        if os.path.isdir(oracle.REFERENCE_TREE):
+        if oracle.reference_tree() is not None:
             oracle.build(with_reference=True)
         else:
-            pytest.skip("the reference sources are not present on this machine")
+            pytest.skip("the reference sources are not present on this machine (set RAST_REFERENCE)")
     return oracle.Reference()
 
 

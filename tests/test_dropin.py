@@ -16,7 +16,6 @@ import pytest
 import golden_io
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
 DRIVER = os.path.join(ROOT, "tests", "cpp", "_build", "dropin_driver")
 
 REFERENCE_ENTRY_POINTS = [
@@ -44,8 +43,10 @@ def test_driver_builds_and_defines_the_reference_entry_points():
 
 
 def test_reference_renderer_links_against_the_drop_in():
-    if not os.path.isdir(REF):
-        pytest.skip("the reference sources are not present on this machine")
+    import oracle
+    REF = oracle.reference_tree()
+    if REF is None:
+        pytest.skip("the reference sources are not present on this machine (set RAST_REFERENCE)")
     from rasteriser_gb300 import _build
     _build.build()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "rasteriser_gb300", "cpp"), "-j8", f"REF={REF}"], check=True)

@@ -12,7 +12,10 @@ import pytest
 
 from rasteriser_gb300 import abi
 
-REF_DATA = "/root/reference/sampledata"
+import oracle
+
+# the reference's sample data, where its source tree is present (RAST_REFERENCE)
+REF_DATA = os.path.join(oracle.REFERENCE_TREE, "sampledata")
 
 
 def write(path, text, newline="\n"):

@@ -88,3 +88,37 @@ def test_port_shade_matches_reference(reference, port):
         li = np.concatenate([rng.normal(size=(nl, 3)), rng.uniform(0, 300, (nl, 1)), rng.uniform(0, 1, (nl, 3))],
                             axis=1).astype(np.float32)
         assert np.array_equal(port.shade(n, alb, li), reference.shade(n, alb, li))
+
+
+def _random_views(n, seed):
+    rng = np.random.default_rng(seed)
+    for _ in range(n):
+        yield (int(rng.integers(1, 4000)), int(rng.integers(1, 3000)), float(rng.uniform(0.1, 3.0)),
+               rng.uniform(-2, 2, 3).astype(np.float32), rng.uniform(-7, 7, 3).astype(np.float32),
+               float(rng.uniform(10, 120)), float(rng.uniform(0.01, 1.0)), float(rng.uniform(2.0, 200.0)))
+
+
+def test_port_frame_inputs_match_reference(reference, port):
+    """The port's restatement of drawing.cpp:221-238 (matrices and Light::transform) gives the
+    reference's matrices and transformed lights bit for bit."""
+    for sc in _live_scenes()[:8]:
+        m = reference.matrices(sc)
+        cam, nm, l7, mp = port.frame_inputs(sc)
+        for k in ("model", "view", "modelview", "camera", "normal"):
+            assert np.array_equal(bits(mp[k]), bits(m[k])), k
+        _, _, td = reference.draw(S.square_scene().with_view(lights=sc.lights, width=sc.width, height=sc.height))
+        assert np.array_equal(bits(l7[:, :3]), bits(td))
+
+
+def test_port_frame_inputs_match_librast_host_code(port):
+    """librast's host matrices (rast_frame_matrices, rast_transform_lights) and the port's agree
+    bit for bit on random views and projections (no GPU is needed for these two calls)."""
+    from rasteriser_gb300 import abi
+    rng = np.random.default_rng(7)
+    for W, H, scale, d, a, fov, zn, zf in _random_views(300, 5):
+        mp = port.matrices(W, H, scale, d, a, fov, zn, zf)
+        ml = abi.frame_matrices(W, H, scale, d, a, fov, zn, zf)
+        for k in mp:
+            assert np.array_equal(bits(mp[k]), bits(ml[k])), k
+        li = rng.normal(size=(4, 7)).astype(np.float32)
+        assert np.array_equal(bits(port.transform_lights(mp["view"], li)), bits(abi.transform_lights(ml["view"], li)))
