@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["displaced_sphere", "soup", "icosphere", "many_lights"],
+    ap.add_argument("--workload", choices=["displaced_sphere", "soup", "soup_1m", "icosphere", "many_lights"],
                     default="displaced_sphere")
     ap.add_argument("--shader", choices=["exact", "deferred", "learned"], default="exact",
                     help="shading mode (learned: the MLP is trained on 4M samples first)")
@@ -65,6 +65,8 @@ def make_scene(name):
         return S.config_displaced_sphere(), "displaced_sphere_1024x512_1080p_spin60"
     if name == "soup":
         return S.config_soup(), "triangle_soup_4M_2160p"
+    if name == "soup_1m":  # a cropped soup for profiling: 1M triangles at 1920x1080
+        return S.config_soup(1_000_000, 1920, 1080), "triangle_soup_1M_1080p"
     if name == "many_lights":
         return S.config_many_lights(), "displaced_sphere_1M_1080p_256_lights"
     return S.config_icosphere_small(), "icosphere_l4_480p"
@@ -332,8 +334,20 @@ def extra_soup(torch, abi, stream, flush, steps=30):
         fps, st, stage = time_scene_device(torch, abi, r, stream, fr, steps, 3, flush)
     finally:
         r.close()
+    # the dominant pass (setup, which also performs the depth test's 64-bit atomicMins): HBM
+    # roofline of its algorithmic bytes, its DRAM traffic scaled from the 1M-triangle 1080p capture
+    # (a quarter of the triangles and of the pixels), and the atomic rate
+    peak, peak_kind = peaks()
+    alg = algorithmic_bytes("setup_raster", sc, st)
+    achieved = alg / (stage["setup_raster"] / 1000.0) / 1e9
+    small = load_traffic("k_setup_raster", "triangle_soup_1M_1080p")
     return {"workload": "triangle_soup_4M_2160p", "frames_per_s": fps, "fragments_per_s": st["inside"] * fps,
             "ms_per_frame": 1000.0 / fps, "stage_ms": stage,
+            "roofline": {"kernel": "k_setup_raster", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg,
+                         "traffic": None if small is None else 4.0 * small,
+                         "traffic_note": "4 x the DRAM bytes of the 1M-triangle 1920x1080 capture"},
+            "depth_atomics_per_s": st["inside"] / (stage["setup_raster"] / 1000.0),
             "frame_stats": {k: st[k] for k in ("front", "tested", "inside", "written", "binned_tris", "bin_entries")}}
 
 
@@ -394,9 +408,10 @@ def extra_many_lights(torch, abi, stream, flush, steps=30):
             if name.startswith("learned"):
                 ck = m["checks"]
                 m["fallback_tile_fraction"] = ck["fallback_tiles"] / max(ck["tiles"], 1)
-                # algorithmic tensor work: 2 * (103*64 + 64*64 + 64*3) FLOP per shaded pixel
-                alg = covered * 2.0 * (103 * 64 + 64 * 64 + 64 * 3)
-                executed = ck["tiles"] * 128 * 2.0 * (112 * 64 + 64 * 64 + 64 * 16)
+                # algorithmic tensor work: 2 * (55*64 + 64*64 + 64*3) FLOP per shaded pixel (55
+                # features in use, two hidden layers of 64, 3 outputs); executed: padded K 64, N 16
+                alg = covered * 2.0 * (55 * 64 + 64 * 64 + 64 * 3)
+                executed = ck["tiles"] * 128 * 2.0 * (64 * 64 + 64 * 64 + 64 * 16)
                 tflops = alg / (m["shade_ms"] * 1e-3) / 1e12
                 m["tensor"] = {"algorithmic_flop": alg, "executed_flop": executed, "achieved_tflops": tflops,
                                "peak_tflops": peak, "frac": tflops / peak, "peak_source": peak_kind}
@@ -410,40 +425,20 @@ def extra_many_lights(torch, abi, stream, flush, steps=30):
     return out
 
 
-def batch_workload(seed=3, n_frames=256, n_soups=16):
-    """The uneven batch: icospheres L2-L7 and seeded soups of 1k-500k triangles (log-uniform sizes); each
-    frame picks a mesh uniformly, a resolution from {256x256, 640x480, 1280x720, 1920x1080}, random
-    rx/ry and a 1-8 light rig."""
-    from rasteriser_gb300 import scenes as S
-    rng = np.random.default_rng(seed)
-    meshes = [S.icosphere(l) for l in range(2, 8)]
-    for k in range(n_soups):
-        n = int(round(float(S.det_exp(np.log(1000.0) + (np.log(500000.0) - np.log(1000.0)) * rng.random()))))
-        meshes.append(S.soup(n, 1280, 720, seed=1000 + k))
-    sizes = [(256, 256), (640, 480), (1280, 720), (1920, 1080)]
-    frames = []
-    for i in range(n_frames):
-        mi = int(rng.integers(len(meshes)))
-        W, H = sizes[int(rng.integers(4))]
-        nl = int(rng.integers(1, 9))
-        angles = (float(rng.uniform(-np.pi, np.pi)), float(rng.uniform(-np.pi, np.pi)), 0.0)
-        frames.append((mi, W, H, angles, S.rig_random(nl, seed=10_000 + i)))
-    return meshes, frames
-
-
 def extra_batch(torch, abi, stream, steps=10):
     """The 256-frame batch as one CUDA graph over 8 lanes after autotuning, against the
     same frames drawn one after another on one stream."""
-    meshes, frames = batch_workload()
+    from rasteriser_gb300 import scenes as S
+    meshes, frames = S.batch_workload()
     r = abi.Renderer(0)
     r.set_stream(stream.cuda_stream)
     keep = []
     try:
         ids = [r.add_mesh(m.pos, m.nrm, m.uv, m.tris, m.kd) for m in meshes]
         descs = []
-        for mi, W, H, angles, lights in frames:
-            sc = meshes[mi].with_view(width=W, height=H, angles=angles, lights=lights, fovy_deg=60.0, z_near=0.1,
-                                      z_far=100.0)
+        for fr in frames:
+            mi, W, H = fr[0], fr[1], fr[2]
+            sc = S.batch_frame_scene(meshes, fr)
             cam, nm, l7, _ = abi.scene_frame_inputs(sc)
             d = (torch.from_numpy(l7).cuda(), torch.empty(3 * W * H, dtype=torch.uint8, device="cuda"),
                  torch.empty(W * H, dtype=torch.float32, device="cuda"))
@@ -466,16 +461,44 @@ def extra_batch(torch, abi, stream, steps=10):
         t_graph = timed(8, True)
         st = r.batch_stats(len(descs))
         t_serial = timed(1, False)
+        # where the time goes: each frame alone on the stream (tuned options), by mesh kind and size
+        per_frame = []
+        for d in descs:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r.draw_batch([d], lanes=1, graph=False)
+            b.record(stream)
+            per_frame.append((a, b))
+        r.sync()
+        frame_ms = [a.elapsed_time(b) for a, b in per_frame]
+        # the same two forms with the untuned defaults (tile 16, small-box limit 4096, whole rows,
+        # 256 threads per tile): how much of the gain is the lanes' overlap and how much the tuning
+        for opt, v in ((abi.OPT_TILE_SIZE, 16), (abi.OPT_SMALL_MAX_PIXELS, 4096), (abi.OPT_ROW_CHUNK, 32),
+                       (abi.OPT_TILE_THREADS, 0)):
+            r.set_option(opt, v)
+        t_graph_default = timed(8, True)
+        t_serial_default = timed(1, False)
     finally:
         r.close()
     n = len(descs)
     frags = int(st[:, 2].sum())
+    classes = {}
+    for fr, ms, row in zip(frames, frame_ms, st):
+        kind = f"icosphere_L{fr[0] + 2}" if fr[0] < 6 else "soup"
+        key = f"{kind} {fr[1]}x{fr[2]}"
+        c = classes.setdefault(key, {"frames": 0, "ms": 0.0, "fragments": 0})
+        c["frames"] += 1
+        c["ms"] += ms
+        c["fragments"] += int(row[2])
     return {"workload": "batch_256_frames_uneven", "frames": n, "meshes": len(meshes),
             "triangles_per_batch": int(sum(meshes[f[0]].ntri for f in frames)),
             "autotuned": tuned, "lanes": 8,
             "graph_frames_per_s": n / t_graph, "graph_fragments_per_s": frags / t_graph,
             "serial_frames_per_s": n / t_serial, "speedup_vs_frame_by_frame": t_serial / t_graph,
             "ms_per_batch_graph": 1000 * t_graph, "ms_per_batch_serial": 1000 * t_serial,
+            "untuned": {"ms_per_batch_graph": 1000 * t_graph_default, "ms_per_batch_serial": 1000 * t_serial_default},
+            "sum_of_frames_alone_ms": sum(frame_ms),
+            "by_class": dict(sorted(classes.items(), key=lambda kv: -kv[1]["ms"])),
             "l2": "not flushed (the batch's working set exceeds L2)"}
 
 

@@ -47,8 +47,13 @@ typedef struct rast_ctx rast_ctx;
 #define RAST_CLEAR 2u          /* treat the frame as cleared to 0 and the depth buffer to 1.0
                                   before drawing, as the reference's spin loop does
                                   (renderer.cpp:107-108); the incoming buffers are not read */
-#define RAST_FLAT 4u           /* Args::flat (arguments.h:12). Accepted and ignored, as in the
-                                  reference, which parses the flag but never reads it */
+#define RAST_FLAT 4u           /* Args::flat (arguments.h:12, readme.md:46): flat shading with
+                                  face normals computed in the path. Each triangle's three vertex
+                                  normals are replaced by cross(p1 - p0, p2 - p0) of its model-space
+                                  positions, which then go through the normal matrix, perspective
+                                  interpolation, normalisation and the clockwise flip as vertex
+                                  normals do. The mesh's normals are still uploaded and checked but
+                                  not read. (The reference parses the flag and never reads it.) */
 
 /* ------------------------------------------------------------------------------------------ */
 /* host-side geometry (no device work)                                                         */
@@ -189,6 +194,15 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 #define RAST_OPT_MLP_BOUND_MILLI 8    /* learned shader: a tile whose checked fragments differ from
                                          the exact shader by more than this many thousandths of
                                          1/255 in a channel is shaded exactly (default 500) */
+#define RAST_OPT_TILE_THREADS 10      /* threads per tile of the tile raster (binned triangles):
+                                         64, 128, 256 or, with tile 32, 512; 0 (default):
+                                         min(tile * tile, 256) */
+#define RAST_OPT_TEST_SHADE_STALL 9   /* test only (default 0). 1: the learned shader's first wait
+                                         for a tensor-core MMA polls an mbarrier nothing arrives
+                                         on, 1024 times, so it gives up as a lost MMA would: the
+                                         kernel waits for the MMA in flight with the full bound,
+                                         frees its tensor memory and returns, and the draw
+                                         reports RAST_ERR_TIMEOUT */
 /* Shading (RAST_OPT_SHADER). Coverage, depth and triangle ids are the same in every mode.
  *   EXACT: shading.cpp's per-light sum inside the resolve pass (the reference's colour, bit for bit)
  *   EXACT_DEFERRED: the resolve pass stores the winning fragments (normal, albedo, pixel); a
@@ -244,11 +258,12 @@ rast_status rast_draw_batch(rast_ctx* ctx, const rast_frame_desc* frames, int32_
 rast_status rast_get_batch_stats(rast_ctx* ctx, uint64_t* out);
 
 /* Autotuner: draws the batch (as a CUDA graph) `repeats` times for each tile size (8, 16, 32),
- * per-triangle-path limit (256, 1024, 4096 pixels) and row chunk (4, 8), keeps the fastest as the
- * context's options, and sizes the bin pools to what the batch needed. out: tile, small_max,
- * row_chunk, bin capacity (entries). */
+ * per-triangle-path limit (256, 1024, 4096 pixels) and row chunk (4, 8, 32); then, for the fastest
+ * of those, for each number of threads per tile of the tile raster (64, 128, 256, and 512 with
+ * tile 32). It keeps the fastest as the context's options and sizes the bin pools to what the
+ * batch needed. out: tile, small_max, row_chunk, bin capacity (entries), threads per tile. */
 rast_status rast_autotune(rast_ctx* ctx, const rast_frame_desc* frames, int32_t n, int32_t lanes,
-                          int32_t repeats, int64_t out[4]);
+                          int32_t repeats, int64_t out[5]);
 
 /* Device status words of the last draw (waits for the stream): [0] triangles on the binned path,
  * [1] status bits (1 bin-pool overflow, 2 binned-list overflow, 4 failed consistency check,
@@ -275,7 +290,7 @@ rast_status rast_get_stage_times(rast_ctx* ctx, float out_ms[9]);
 typedef struct rast_mlp_train_desc {
     int64_t samples;   /* training samples (default 4194304) */
     int64_t holdout;   /* held-out samples for the error report (default 65536) */
-    int32_t epochs;    /* passes over the samples (default 12) */
+    int32_t epochs;    /* passes over the samples (default 24) */
     int32_t ctas;      /* CTAs per step, 64 samples each (default: the SM count) */
     float lr;          /* peak learning rate (default 0.003), cosine decay to lr/100 */
     uint64_t seed;     /* samples and initial weights (default 1) */
@@ -319,8 +334,12 @@ rast_status rast_get_shade_stats(rast_ctx* ctx, uint64_t out[4]);
  * the lights (as for rast_set_lights) and the outputs are the caller's device buffers, and every
  * intermediate buffer lives in one fixed 64 MiB array inside the library, which each GPU that
  * loads the library holds until the process exits. A frame whose buffers do not fit is refused
- * with RAST_ERR_INVALID_ARG: about 100 bytes per triangle, 16 per vertex and 8 per pixel must
- * fit, e.g. a closed mesh of about 590 k triangles at 640x480 or 460 k at 1920x1080. Indices are checked on the device (RAST_ERR_BAD_INDEX); uv indices are not read. The
+ * with RAST_ERR_INVALID_ARG: 92 bytes per triangle, 16 per vertex, 8 per pixel and 256 KiB of
+ * tile-bin entries must fit, e.g. a closed mesh of about 640 k triangles at 640x480 or 500 k at
+ * 1920x1080. The tile-bin entries (one per large triangle and 16x16 tile it covers) take the rest
+ * of the array; a frame that needs more returns RAST_ERR_BIN_OVERFLOW and leaves the frame, depth
+ * and id buffers as they were. Indices are checked on the device (RAST_ERR_BAD_INDEX); uv indices
+ * are not read. The draw uses the context's default options (tile 16, whole-row items). The
  * first call on a device looks up the array's device address (with that device current); make
  * that first call before any stream capture. All calls share the array and it keeps the last
  * call's contents; each call clears what it needs. Calls that overlap on the GPU race on the
@@ -390,7 +409,7 @@ rast_status rast_depth_to_u8_host(rast_ctx* ctx, const float* depth, uint32_t wi
  * enqueued without waiting in between. */
 typedef struct rast_spin_desc {
     uint32_t width, height;   /* 1..32768 */
-    uint32_t flags;           /* RAST_WIND_CLOCKWISE */
+    uint32_t flags;           /* RAST_WIND_CLOCKWISE, RAST_FLAT */
     int32_t frames;           /* >= 1 */
     float scale, disp[3], angles[3];
     float step;               /* ry increment per frame, radians */

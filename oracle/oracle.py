@@ -60,7 +60,7 @@ class _OracleFrame(C.Structure):
                 ("lights", C.POINTER(C.c_float)), ("nl", C.c_int32),
                 ("width", C.c_uint32), ("height", C.c_uint32), ("wind_clockwise", C.c_int32),
                 ("vcol", C.POINTER(C.c_float)), ("tex", C.POINTER(C.c_float)), ("tex_off", C.POINTER(C.c_int64)),
-                ("tex_wh", C.POINTER(C.c_int32))]
+                ("tex_wh", C.POINTER(C.c_int32)), ("flat", C.c_int32)]
 
 
 def cimg_normalize01(texels):
@@ -98,9 +98,11 @@ class Port:
         self.lib.oracle_transform_lights.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
                                                      C.POINTER(C.c_float)]
 
-    def draw(self, scene, camera, normal_matrix, lights7, frame=None, depth=None, want_ids=True, textures=None):
+    def draw(self, scene, camera, normal_matrix, lights7, frame=None, depth=None, want_ids=True, textures=None,
+             flat=False):
         """Returns (frame (3,H,W) uint8, depth (H,W) float32, ids (H,W) uint32 or None, stats).
-        textures: per material a normalised (c>=3, h, w) float32 texture or None."""
+        textures: per material a normalised (c>=3, h, w) float32 texture or None. flat: face
+        normals in place of the vertex normals (Args::flat)."""
         W, H = scene.width, scene.height
         frame = np.zeros((3, H, W), np.uint8) if frame is None else np.ascontiguousarray(frame, np.uint8).copy()
         depth = np.ones((H, W), np.float32) if depth is None else _f32(depth).copy()
@@ -124,7 +126,7 @@ class Port:
                          _p(keep[2]), scene.nrm.shape[0], _p(keep[3]), scene.uv.shape[0],
                          _p(keep[4]), scene.kd.shape[0], _p(keep[5]), _p(keep[6]), _p(keep[7]),
                          keep[7].shape[0], W, H, int(scene.wind_clockwise), _p(vcol), _p(tex),
-                         _p(off, C.c_int64), _p(wh, C.c_int32))
+                         _p(off, C.c_int64), _p(wh, C.c_int32), int(bool(flat)))
         stats = np.zeros(4, np.uint64)
         rc = self.lib.oracle_draw_frame(C.byref(f), _p(frame, C.c_uint8), _p(depth),
                                         _p(ids, C.c_uint32), _p(stats, C.c_uint64))

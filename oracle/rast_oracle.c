@@ -271,7 +271,21 @@ int oracle_draw_frame(const oracle_frame* f, uint8_t* frame, float* depth, uint3
         const int32_t* tri = f->tris + 10 * t;
         /* drawing.cpp:165-173: de-index */
         v4 v0 = rv[tri[0]], v1 = rv[tri[1]], v2 = rv[tri[2]];
-        v3 n0 = cn[tri[3]], n1 = cn[tri[4]], n2 = cn[tri[5]];
+        v3 n0, n1, n2;
+        if (f->flat) {
+            const float* p0 = f->pos + 3 * tri[0];
+            const float* p1 = f->pos + 3 * tri[1];
+            const float* p2 = f->pos + 3 * tri[2];
+            const float a[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+            const float b[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+            /* glm::cross(a, b) */
+            const float fn[3] = {a[1] * b[2] - b[1] * a[2], a[2] * b[0] - b[2] * a[0], a[0] * b[1] - b[0] * a[1]};
+            n0 = n1 = n2 = camera_normal(f->normal_matrix, fn);
+        } else {
+            n0 = cn[tri[3]];
+            n1 = cn[tri[4]];
+            n2 = cn[tri[5]];
+        }
         const float* kd = f->kd + 3 * tri[9];
         v3 albedo = {kd[0], kd[1], kd[2]};
         v3 c0 = {0, 0, 0}, c1 = {0, 0, 0}, c2 = {0, 0, 0};

@@ -43,6 +43,10 @@ typedef struct oracle_frame {
     const float* tex;
     const int64_t* tex_off;
     const int32_t* tex_wh;
+    /* Flat shading (Args::flat, readme.md:46; the reference parses it but never reads it): each
+     * triangle's three normals are its face normal cross(p1 - p0, p2 - p0) in model space, which
+     * then goes through the path as vertex normals do. */
+    int32_t flat;
 } oracle_frame;
 
 /* stats (nullable) receives: [0] front-facing triangles, [1] bounding-box pixels tested,

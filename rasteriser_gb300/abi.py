@@ -21,7 +21,7 @@ STATUS_NAMES = {0: "RAST_OK", 1: "RAST_ERR_INVALID_ARG", 2: "RAST_ERR_BAD_INDEX"
                 7: "RAST_ERR_TIMEOUT", 8: "RAST_ERR_NO_DEVICE", 9: "RAST_ERR_INTERNAL"}
 WIND_CLOCKWISE, CLEAR, FLAT = 1, 2, 4
 OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY, OPT_STAGE_TIMING, OPT_ROW_CHUNK = 1, 2, 3, 4, 5
-OPT_SHADER, OPT_MLP_SAMPLES, OPT_MLP_BOUND_MILLI = 6, 7, 8
+OPT_SHADER, OPT_MLP_SAMPLES, OPT_MLP_BOUND_MILLI, OPT_TEST_SHADE_STALL, OPT_TILE_THREADS = 6, 7, 8, 9, 10
 SHADER_EXACT, SHADER_EXACT_DEFERRED, SHADER_LEARNED = 0, 1, 2
 STAGES = ["arm", "vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve", "shade", "total"]
 NO_TRIANGLE = 0xFFFFFFFF
@@ -73,8 +73,9 @@ SIGNATURES = {
     "rast_get_stream": (_P, [_P]),
     "rast_upload_mesh": (C.c_int, [_P, _F, _I64, _F, _I64, _F, _I64, C.POINTER(C.c_int32), _I64, _F, _I32]),
     "rast_set_lights": (C.c_int, [_P, _F, _I32]),
-    "rast_draw": (C.c_int, [_P, _F, _F, _U32, _U32, _U32, C.POINTER(C.c_uint8), _F, C.POINTER(C.c_uint32)]),
-    "rast_draw_device": (C.c_int, [_P, _F, _F, _U32, _U32, _U32, _P, _P, _P]),
+    # the per-frame calls take plain addresses (cheaper to pass than typed pointers)
+    "rast_draw": (C.c_int, [_P, _P, _P, _U32, _U32, _U32, _P, _P, _P]),
+    "rast_draw_device": (C.c_int, [_P, _P, _P, _U32, _U32, _U32, _P, _P, _P]),
     "rast_sync": (C.c_int, [_P]),
     "rast_get_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "rast_set_option": (C.c_int, [_P, C.c_int, _I64]),
@@ -331,16 +332,17 @@ class Renderer:
             ids = np.empty((height, width), np.uint32)
         if ids is not None:
             assert ids.dtype == np.uint32 and ids.flags.c_contiguous and ids.size == width * height
-        st = self.lib.rast_draw(self.h, _fp(_f32(camera)), _fp(_f32(normal)), width, height, flags,
-                                frame.ctypes.data_as(C.POINTER(C.c_uint8)), _fp(depth),
-                                ids.ctypes.data_as(C.POINTER(C.c_uint32)) if ids is not None else None)
+        cam, nrm = _f32(camera), _f32(normal)  # kept alive across the call
+        st = self.lib.rast_draw(self.h, cam.ctypes.data, nrm.ctypes.data, width, height, flags, frame.ctypes.data,
+                                depth.ctypes.data, ids.ctypes.data if ids is not None else None)
         self._check(st, "rast_draw")
         return frame, depth, ids
 
     def draw_device(self, camera, normal, width, height, flags, d_rgb, d_depth, d_ids=0):
         """Device-buffer draw on the context's stream; pointers are integers (e.g. tensor.data_ptr())."""
-        st = self.lib.rast_draw_device(self.h, _fp(_f32(camera)), _fp(_f32(normal)), width, height, flags,
-                                       _P(d_rgb), _P(d_depth), _P(d_ids) if d_ids else None)
+        cam, nrm = _f32(camera), _f32(normal)  # kept alive across the call
+        st = self.lib.rast_draw_device(self.h, cam.ctypes.data, nrm.ctypes.data, width, height, flags, d_rgb,
+                                       d_depth, d_ids or None)
         self._check(st, "rast_draw_device")
 
     def sync(self):
@@ -381,9 +383,9 @@ class Renderer:
 
     def autotune(self, frames, lanes=8, repeats=3):
         arr = (FrameDesc * len(frames))(*frames)
-        out = (C.c_int64 * 4)()
+        out = (C.c_int64 * 5)()
         self._check(self.lib.rast_autotune(self.h, arr, len(frames), lanes, repeats, out), "rast_autotune")
-        return dict(zip(["tile", "small_max", "row_chunk", "bin_capacity"], list(out)))
+        return dict(zip(["tile", "small_max", "row_chunk", "bin_capacity", "tile_threads"], list(out)))
 
     def stats(self):
         out = (C.c_uint64 * 8)()

@@ -9,8 +9,11 @@
 //     the device one after another (clear, draw), ry advancing by --step radians per frame (the
 //     reference advances it by each frame's wall-clock duration); prints the frame rate and, with
 //     --dump, writes frame_NNNN.ppm for every frame.
-// Extra options: --frames N (60), --step S (1/60), --out DIR (.), --dump, --device D,
-// --deferred (per-light shading in a separate pass).
+// -f/--flat shades with face normals computed in the path (readme.md:46; the reference parses the
+// flag but never reads it). Extra options: --frames N (60), --step S (1/60), --out DIR (.), --dump,
+// --device D, --deferred (per-light shading in a separate pass), and the projection and light units
+// the reference hard-codes: --fovy DEG (45), --near Z (0.1), --far Z (6) (geometry.cpp:30) and
+// --light-scale K (1: every light's intensity is multiplied by K as it is loaded).
 #include <chrono>
 #include <cstdint>
 #include <cstdio>
@@ -30,13 +33,15 @@ struct Options {
     float rx = 0.f, ry = 0.f, rz = 0.f, scale = 1.f, dx = 0.f, dy = 0.f, dz = 0.f;
     int frames = 60, device = 0;
     float step = 1.f / 60.f;
+    float fovy = 45.f, z_near = 0.1f, z_far = 6.f, light_scale = 1.f;
 };
 
 [[noreturn]] void usage(const char* msg) {
     std::fprintf(stderr,
                  "Error: %s\nusage: rast_render -l lights.csv [-o model.obj] [--mats-dir dir/] [-x width] "
                  "[-y height]\n  [-s] [-f] [--wind-clockwise] [--rx a] [--ry a] [--rz a] [--scale s] [--dx d] [--dy d] "
-                 "[--dz d]\n  [--frames n] [--step rad] [--out dir] [--dump] [--device d] [--deferred]\n",
+                 "[--dz d]\n  [--frames n] [--step rad] [--out dir] [--dump] [--device d] [--deferred]\n"
+                 "  [--fovy deg] [--near z] [--far z] [--light-scale k]\n",
                  msg);
     std::exit(1);
 }
@@ -85,9 +90,15 @@ Options parse(int argc, char** argv) {
         else if (a == "--dump") o.dump = true;
         else if (a == "--device") o.device = (int)num();
         else if (a == "--deferred") o.deferred = true;
+        else if (a == "--fovy") o.fovy = num();
+        else if (a == "--near") o.z_near = num();
+        else if (a == "--far") o.z_far = num();
+        else if (a == "--light-scale") o.light_scale = num();
         else usage(("unknown option " + a).c_str());
     }
     if (!have_lights) usage("-l/--lights is required");
+    if (!(o.fovy > 0.f && o.fovy < 180.f)) usage("--fovy must be in (0, 180) degrees");
+    if (!(o.z_near > 0.f && o.z_far > o.z_near)) usage("--near must be > 0 and --far > --near");
     return o;
 }
 
@@ -137,6 +148,8 @@ int main(int argc, char** argv) {
     check(rast_lights_load(o.lights.c_str(), nullptr, 0, &nl), nullptr, "lights");
     std::vector<float> lights(7 * (size_t)(nl > 0 ? nl : 1));
     check(rast_lights_load(o.lights.c_str(), lights.data(), nl, &nl), nullptr, "lights");
+    if (o.light_scale != 1.f)
+        for (int32_t i = 0; i < nl; ++i) lights[7 * (size_t)i + 3] *= o.light_scale;
 
     // model: the OBJ, or renderer.cpp's add_square
     std::vector<float> pos, nrm, uv, kd;
@@ -187,13 +200,14 @@ int main(int argc, char** argv) {
     const unsigned W = o.width, H = o.height;
     const size_t npx = (size_t)W * H;
     const float disp[3] = {o.dx, o.dy, o.dz};
-    const uint32_t flags = (o.wind_clockwise ? RAST_WIND_CLOCKWISE : 0u) | RAST_CLEAR;
+    const uint32_t shading = (o.wind_clockwise ? RAST_WIND_CLOCKWISE : 0u) | (o.flat ? RAST_FLAT : 0u);
+    const uint32_t flags = shading | RAST_CLEAR;
     float model[16], view[16], mv[16], cam[16], nm[16];
     std::vector<float> lt(lights.size());
     auto frame_inputs = [&](float ry) {
         const float angles[3] = {o.rx, ry, o.rz};
-        check(rast_frame_matrices(W, H, o.scale, disp, angles, 45.f, 0.1f, 6.f, model, view, mv, cam, nm), ctx,
-              "matrices");
+        check(rast_frame_matrices(W, H, o.scale, disp, angles, o.fovy, o.z_near, o.z_far, model, view, mv, cam, nm),
+              ctx, "matrices");
         check(rast_transform_lights(view, lights.data(), nl, lt.data()), ctx, "lights");
         check(rast_set_lights(ctx, lt.data(), nl), ctx, "lights");
     };
@@ -217,14 +231,14 @@ int main(int argc, char** argv) {
         rast_spin_desc sd = {};
         sd.width = W;
         sd.height = H;
-        sd.flags = o.wind_clockwise ? RAST_WIND_CLOCKWISE : 0u;
+        sd.flags = shading;
         sd.scale = o.scale;
         sd.disp[0] = o.dx; sd.disp[1] = o.dy; sd.disp[2] = o.dz;
         sd.angles[0] = o.rx; sd.angles[1] = o.ry; sd.angles[2] = o.rz;
         sd.step = o.step;
-        sd.fovy_deg = 45.f;
-        sd.z_near = 0.1f;
-        sd.z_far = 6.f;
+        sd.fovy_deg = o.fovy;
+        sd.z_near = o.z_near;
+        sd.z_far = o.z_far;
         sd.lights7 = lights.data();
         sd.nl = nl;
         double seconds = 0.0;

@@ -129,6 +129,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     p.small_max = c->small_max;
     p.tile = c->tile;
     p.row_chunk = c->row_chunk;
+    p.tile_threads = c->tile_threads;
     p.before_resolve = c->before_resolve;
     p.keep_outputs_on_overflow = c->keep_outputs;
     p.tiles_x = tiles_x;
@@ -143,6 +144,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     p.mlp = c->mlp_image.ptr;
     p.mlp_samples = c->mlp_samples;
     p.mlp_bound = (float)c->mlp_bound_milli * 1e-3f;
+    p.mlp_stall_test = c->test_shade_stall;
     if (c->timing && !c->ev_made) {
         for (auto& e : c->ev) RAST_CUDA(c, cudaEventCreate(&e));
         c->ev_made = true;
@@ -179,7 +181,7 @@ rast_status collect_status(rast_ctx* c) {
     if (status & rast::STATUS_SHADE_TIMEOUT) {
         uint32_t zero = 0;
         RAST_CUDA(c, cudaMemcpy(c->counters.as<uint32_t>() + 1, &zero, sizeof zero, cudaMemcpyHostToDevice));
-        return fail(c, RAST_ERR_INTERNAL, "learned shader: a tensor-core MMA did not complete in time");
+        return fail(c, RAST_ERR_TIMEOUT, "learned shader: a tensor-core MMA did not complete in time");
     }
     if (status & rast::STATUS_CHECK_FAILED) {
         uint32_t w[2] = {0, 0};
@@ -590,6 +592,15 @@ rast_status rast_set_option(rast_ctx* c, int option, int64_t value) {
             if (value < 0 || value > 255000) return fail(c, RAST_ERR_INVALID_ARG, "MLP bound out of range");
             c->mlp_bound_milli = (int32_t)value;
             return RAST_OK;
+        case RAST_OPT_TILE_THREADS:
+            if (value != 0 && value != 64 && value != 128 && value != 256 && value != 512)
+                return fail(c, RAST_ERR_INVALID_ARG, "threads per tile must be 0, 64, 128, 256 or 512");
+            c->tile_threads = (uint32_t)value;
+            return RAST_OK;
+        case RAST_OPT_TEST_SHADE_STALL:
+            if (value != 0 && value != 1) return fail(c, RAST_ERR_INVALID_ARG, "shade stall test is 0 or 1");
+            c->test_shade_stall = value == 1;
+            return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
 }
@@ -605,6 +616,8 @@ rast_status rast_get_option(rast_ctx* c, int option, int64_t* value) {
         case RAST_OPT_SHADER: *value = c->shader; return RAST_OK;
         case RAST_OPT_MLP_SAMPLES: *value = c->mlp_samples; return RAST_OK;
         case RAST_OPT_MLP_BOUND_MILLI: *value = c->mlp_bound_milli; return RAST_OK;
+        case RAST_OPT_TEST_SHADE_STALL: *value = c->test_shade_stall ? 1 : 0; return RAST_OK;
+        case RAST_OPT_TILE_THREADS: *value = c->tile_threads; return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
 }
@@ -679,7 +692,7 @@ rast_status rast_spin(rast_ctx* c, const rast_spin_desc* d, uint8_t* last_rgb, f
     if (st != RAST_OK) return st;
     RAST_CUDA(c, c->d_rgb.reserve(3 * npx));
     RAST_CUDA(c, c->d_depth.reserve(sizeof(float) * npx));
-    const uint32_t flags = (d->flags & RAST_WIND_CLOCKWISE) | RAST_CLEAR;
+    const uint32_t flags = (d->flags & (RAST_WIND_CLOCKWISE | RAST_FLAT)) | RAST_CLEAR;
     const auto t0 = std::chrono::steady_clock::now();
     for (int32_t k = 0; k < d->frames; ++k) {
         angles[1] = d->angles[1] + (float)k * d->step;

@@ -112,6 +112,7 @@ rast_status enqueue_batch(rast_ctx* c, const rast_frame_desc* frames, int32_t n,
         p.small_max = c->small_max;
         p.tile = c->tile;
         p.row_chunk = c->row_chunk;
+        p.tile_threads = c->tile_threads;
         p.chained = false;
         p.tiles_x = tiles_x;
         p.tiles_y = tiles_y;
@@ -133,9 +134,9 @@ rast_status enqueue_batch(rast_ctx* c, const rast_frame_desc* frames, int32_t n,
 
 std::vector<unsigned char> batch_key(const rast_ctx* c, const rast_frame_desc* frames, int32_t n, int32_t lanes) {
     std::vector<unsigned char> k((const unsigned char*)frames, (const unsigned char*)(frames + n));
-    const int64_t extra[7] = {n, lanes, c->tile, c->small_max, c->row_chunk, (int64_t)(uintptr_t)c->stream,
-                              (int64_t)(uintptr_t)c->batch_stats.ptr};
-    k.insert(k.end(), (const unsigned char*)extra, (const unsigned char*)(extra + 7));
+    const int64_t extra[8] = {n, lanes, c->tile, c->small_max, c->row_chunk, c->tile_threads,
+                              (int64_t)(uintptr_t)c->stream, (int64_t)(uintptr_t)c->batch_stats.ptr};
+    k.insert(k.end(), (const unsigned char*)extra, (const unsigned char*)(extra + 8));
     return k;
 }
 
@@ -275,55 +276,81 @@ rast_status rast::collect_batch_status(rast_ctx* c) {
 }
 
 extern "C" rast_status rast_autotune(rast_ctx* c, const rast_frame_desc* frames, int32_t n, int32_t lanes,
-                                     int32_t repeats, int64_t out[4]) {
+                                     int32_t repeats, int64_t out[5]) {
     if (!c || !out || repeats < 1) return RAST_ERR_INVALID_ARG;
     DeviceGuard g(c->device);
     const uint32_t tiles[3] = {8, 16, 32};
     const uint32_t smalls[3] = {256, 1024, 4096};
     const uint32_t chunks[3] = {4, 8, 32};
+    const uint32_t threads[4] = {64, 128, 256, 512};
     cudaEvent_t t0, t1;
     RAST_CUDA(c, cudaEventCreate(&t0));
     RAST_CUDA(c, cudaEventCreate(&t1));
     float best = 1e30f;
-    uint32_t bt = c->tile, bs = c->small_max, bc = c->row_chunk;
+    uint32_t bt = c->tile, bs = c->small_max, bc = c->row_chunk, bth = c->tile_threads;
     rast_status st = RAST_OK;
+    // the batch's time with the context's current options (they are the ones being tried)
+    auto time_batch = [&](float& ms) -> rast_status {
+        rast_status s = RAST_OK;
+        // the first run records the graph and settles the bin pools
+        for (int attempt = 0; attempt < 4; ++attempt) {
+            s = rast_draw_batch(c, frames, n, lanes, RAST_BATCH_GRAPH);
+            if (s != RAST_OK) return s;
+            RAST_CUDA(c, cudaStreamSynchronize(c->stream));
+            s = collect_batch_status(c);
+            if (s != RAST_ERR_BIN_OVERFLOW) break;
+        }
+        if (s != RAST_OK) return s;
+        RAST_CUDA(c, cudaEventRecord(t0, c->stream));
+        for (int r = 0; r < repeats; ++r) {
+            s = rast_draw_batch(c, frames, n, lanes, RAST_BATCH_GRAPH);
+            if (s != RAST_OK) return s;
+        }
+        RAST_CUDA(c, cudaEventRecord(t1, c->stream));
+        RAST_CUDA(c, cudaEventSynchronize(t1));
+        RAST_CUDA(c, cudaEventElapsedTime(&ms, t0, t1));
+        return RAST_OK;
+    };
+    // stage 1: tile size, per-triangle limit and row chunk, with the default threads per tile
+    c->tile_threads = 0;
     for (uint32_t t : tiles)
         for (uint32_t sm : smalls)
             for (uint32_t ch : chunks) {
                 c->tile = t;
                 c->small_max = sm;
                 c->row_chunk = ch;
-                // first run records the graph and settles the bin pools
-                for (int attempt = 0; attempt < 4; ++attempt) {
-                    st = rast_draw_batch(c, frames, n, lanes, RAST_BATCH_GRAPH);
-                    if (st != RAST_OK) break;
-                    RAST_CUDA(c, cudaStreamSynchronize(c->stream));
-                    st = collect_batch_status(c);
-                    if (st != RAST_ERR_BIN_OVERFLOW) break;
-                }
-                if (st != RAST_OK) goto done;
-                RAST_CUDA(c, cudaEventRecord(t0, c->stream));
-                for (int r = 0; r < repeats; ++r) {
-                    st = rast_draw_batch(c, frames, n, lanes, RAST_BATCH_GRAPH);
-                    if (st != RAST_OK) goto done;
-                }
-                RAST_CUDA(c, cudaEventRecord(t1, c->stream));
-                RAST_CUDA(c, cudaEventSynchronize(t1));
                 float ms = 0.f;
-                RAST_CUDA(c, cudaEventElapsedTime(&ms, t0, t1));
+                if ((st = time_batch(ms)) != RAST_OK) goto done;
                 if (ms < best) {
                     best = ms;
                     bt = t;
                     bs = sm;
                     bc = ch;
+                    bth = 0;
                 }
             }
+    // stage 2: threads per tile for the fastest of those (tile 8 has one choice)
+    c->tile = bt;
+    c->small_max = bs;
+    c->row_chunk = bc;
+    if (bt != 8)
+        for (uint32_t th : threads) {
+            if (th == 512 && bt != 32) continue;
+            c->tile_threads = th;
+            float ms = 0.f;
+            if ((st = time_batch(ms)) != RAST_OK) goto done;
+            if (ms < best) {
+                best = ms;
+                bth = th;
+            }
+        }
 done:
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     c->tile = bt;
     c->small_max = bs;
     c->row_chunk = bc;
+    c->tile_threads = bth;
     drop_graph(c);
     if (st != RAST_OK) return st;
     int64_t cap = 0;
@@ -332,5 +359,6 @@ done:
     out[1] = bs;
     out[2] = bc;
     out[3] = cap;
+    out[4] = bth ? bth : std::min<uint32_t>(bt * bt, 256u);
     return RAST_OK;
 }

@@ -103,6 +103,7 @@ struct rast_ctx {
     int32_t shader = 0;           // RAST_SHADER_*
     int32_t mlp_samples = 2;      // RAST_OPT_MLP_SAMPLES
     int32_t mlp_bound_milli = 500;  // RAST_OPT_MLP_BOUND_MILLI
+    bool test_shade_stall = false;  // RAST_OPT_TEST_SHADE_STALL
     DevBuf gbuf, gbuf_count, shade_index, shade_stats;
     DevBuf view_mm;  // rast_depth_to_u8: the depth range
 
@@ -119,6 +120,7 @@ struct rast_ctx {
     uint32_t small_max = 4096;
     uint32_t tile = 16;
     uint32_t row_chunk = 32;
+    uint32_t tile_threads = 0;  // RAST_OPT_TILE_THREADS
     int64_t bin_capacity = 0;  // 0: sized from the mesh
 
     uint64_t last_launches = 0;

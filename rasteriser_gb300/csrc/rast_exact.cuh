@@ -19,6 +19,27 @@ __device__ __forceinline__ float dvd(float a, float b) { return __fdiv_rn(a, b);
 __device__ __forceinline__ float gmin(float x, float y) { return x < y ? x : y; }
 __device__ __forceinline__ float gmax(float x, float y) { return x > y ? x : y; }
 
+// RN(a / b) from y = RN(1/b), the correctly rounded reciprocal: q0 = RN(a*y), then one fused
+// correction q = RN(q0 + RN(a - b*q0)*y) (Markstein's correction step). Checked bit for bit
+// against __fdiv_rn on every pair of significands (2^46 pairs, a and b in [1, 2)); scaling a and
+// b by powers of two scales every step exactly while all values stay normal, which holds for
+// |a| and |b| in [2^-60, 2^60], and every step is symmetric in the signs. Outside that range, for
+// zeros, and when y is 0 (b outside it), the quotient is __fdiv_rn's. Several divisions by one b
+// share y = div_by_recip(b).
+__device__ __forceinline__ float div_by_recip(float b) {
+    const float ab = fabsf(b);
+    return ab >= 0x1p-60f && ab <= 0x1p60f ? __frcp_rn(b) : 0.f;
+}
+
+__device__ __forceinline__ float div_by(float a, float b, float y) {
+    const float aa = fabsf(a);
+    if (y != 0.f && aa >= 0x1p-60f && aa <= 0x1p60f) {
+        const float q0 = __fmul_rn(a, y);
+        return __fmaf_rn(__fmaf_rn(-b, q0, a), y, q0);
+    }
+    return dvd(a, b);
+}
+
 // 1/pi as the reference's glm::one_over_pi<float>() rounds it.
 constexpr float kOneOverPi = 0.318309886183790671537767526745028724f;
 

@@ -116,6 +116,8 @@ struct DrawParams {
     uint32_t small_max;     // bounding boxes up to this many pixels take the per-triangle path
     uint32_t tile;          // tile edge: 8, 16, 32
     uint32_t row_chunk;     // pixels per work item of the per-triangle path: 4, 8 or 32 (whole rows)
+    uint32_t tile_threads = 0;  // threads per tile of the tile raster: 64, 128, 256, 512 (tile 32 only);
+                                // 0 or a value the tile edge does not take: min(tile^2, 256)
     bool chained = true;    // launch the frame's kernels after the first as programmatic dependents
                             // (off for batches, whose lanes fill the SMs with each other's work)
     cudaEvent_t before_resolve = nullptr;  // when set, the resolve pass waits for it (the colour
@@ -133,6 +135,7 @@ struct DrawParams {
     const void* mlp = nullptr;  // shader 2: the device MlpImage
     int32_t mlp_samples = 2;    // shader 2: fragments per tile checked against the exact shader
     float mlp_bound = 0.5f;     // shader 2: largest checked channel error (1/255 units) a tile may have
+    bool mlp_stall_test = false;  // shader 2, test only: the first MMA wait gives up (RAST_OPT_TEST_SHADE_STALL)
 };
 
 // The depth view (rast_view.cu): min / max of n depths into mm[0..1] (order keys), then the bytes.

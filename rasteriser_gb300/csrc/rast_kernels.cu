@@ -146,6 +146,18 @@ __device__ __forceinline__ float3 camera_normal(const Mat4& M, float x, float y,
     return make_float3(mrow(M, 0, x, y, z, 0.f), mrow(M, 1, x, y, z, 0.f), mrow(M, 2, x, y, z, 0.f));
 }
 
+// The face normal of flat shading (the reference's --flat, readme.md:46): cross(p1 - p0, p2 - p0)
+// of the model-space positions, not normalised (the path normalises after interpolation), with
+// cross(a, b) = (a.y*b.z - b.y*a.z, a.z*b.x - b.z*a.x, a.x*b.y - b.x*a.y).
+__device__ __forceinline__ float3 face_normal(const float* pos, int32_t i0, int32_t i1, int32_t i2) {
+    const float* P0 = pos + 3 * (int64_t)i0;
+    const float* P1 = pos + 3 * (int64_t)i1;
+    const float* P2 = pos + 3 * (int64_t)i2;
+    const float ax = sub(__ldg(P1), __ldg(P0)), ay = sub(__ldg(P1 + 1), __ldg(P0 + 1)), az = sub(__ldg(P1 + 2), __ldg(P0 + 2));
+    const float bx = sub(__ldg(P2), __ldg(P0)), by = sub(__ldg(P2 + 1), __ldg(P0 + 1)), bz = sub(__ldg(P2 + 2), __ldg(P0 + 2));
+    return make_float3(sub(mul(ay, bz), mul(by, az)), sub(mul(az, bx), mul(bz, ax)), sub(mul(ax, by), mul(bx, ay)));
+}
+
 // ---------------------------------------------------------------------------------------------
 // warp and bookkeeping helpers
 // ---------------------------------------------------------------------------------------------
@@ -209,21 +221,6 @@ __device__ __forceinline__ int owner_of(const uint32_t* incl, uint32_t k) {
         if (incl[mid] > k) hi = mid; else lo = mid + 1;
     }
     return lo;
-}
-
-// RN(a / b) from y = RN(1/b), the correctly rounded reciprocal: q0 = RN(a*y), then one fused
-// correction q = RN(q0 + RN(a - b*q0)*y) (Markstein's correction step). Checked bit for bit
-// against __fdiv_rn on every pair of significands (2^46 pairs, a and b in [1, 2)); scaling a and
-// b by powers of two scales every step exactly while all values stay normal, which holds for
-// |a| and |b| in [2^-60, 2^60], and every step is symmetric in the signs. Outside that range, for
-// zeros, and when y is 0 (b outside it), the quotient is __fdiv_rn's.
-__device__ __forceinline__ float div_by(float a, float b, float y) {
-    const float aa = fabsf(a);
-    if (y != 0.f && aa >= 0x1p-60f && aa <= 0x1p60f) {
-        const float q0 = __fmul_rn(a, y);
-        return __fmaf_rn(__fmaf_rn(-b, q0, a), y, q0);
-    }
-    return dvd(a, b);
 }
 
 // q = n / d for n <= 2^24, d >= 1: a float-reciprocal estimate (within 2 of the quotient at
@@ -508,8 +505,7 @@ __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) 
                 // The correctly rounded reciprocal of the staged area (rec[4].w) for div_by, or 0
                 // (use __fdiv_rn) when its magnitude is outside [2^-60, 2^60]. The correction step
                 // is symmetric in the divisor's sign.
-                const float ba = mul(sg, T.area), aa = fabsf(ba);
-                S.rcpr[lane] = aa >= 0x1p-60f && aa <= 0x1p60f ? __frcp_rn(ba) : 0.f;
+                S.rcpr[lane] = div_by_recip(mul(sg, T.area));
             }
             S.incl[lane] = incl;
             __syncwarp();
@@ -962,15 +958,17 @@ struct TileArgs {
 };
 
 // Persistent CTAs take work items (a tile and up to kTileChunk of its binned triangles) from a
-// counter until none are left, so a tile crowded with triangles is shared out among CTAs. Each
-// thread owns kPPT pixels of the tile (a warp covers an 8x4 block per pixel slot) and keeps their
-// minimum keys in registers; the item ends with one 64-bit atomicMin per pixel it improved (items
-// of one tile may run at once, and the per-triangle pass wrote its keys earlier on the stream).
-template <int TS>
-__global__ void __launch_bounds__(256) k_tile_raster(TileArgs a) {
+// counter until none are left, so a tile crowded with triangles is shared out among CTAs. Each of
+// the TPT threads of a CTA (threads per tile) owns kPPT pixels of the tile (a warp covers an 8x4
+// block per pixel slot) and keeps their minimum keys in registers; the item ends with one 64-bit
+// atomicMin per pixel it improved (items of one tile may run at once, and the per-triangle pass
+// wrote its keys earlier on the stream).
+template <int TS, int TPT>
+__global__ void __launch_bounds__(TPT) k_tile_raster(TileArgs a) {
     pdl_wait();
     pdl_launch_dependents();
-    constexpr int kThreads = (TS * TS < 256) ? TS * TS : 256;
+    constexpr int kThreads = TPT;
+    static_assert(TPT % 32 == 0 && (TS * TS) % TPT == 0, "whole warps, whole pixels per thread");
     constexpr int kPPT = (TS * TS) / kThreads;  // pixels per thread
     constexpr int kBlocksX = TS / 8;             // 8x4 blocks across a tile
     __shared__ TileStage S;
@@ -1085,12 +1083,14 @@ struct ResolveArgs {
     const int4* tri_nm;
     const float4* rv;
     const float* nrm;
+    const float* pos;     // model-space positions (flat shading's face normals)
     const float* kd;
     const float* lights;
     int32_t nl;
     Mat4 normal;
     uint32_t width, height;
     bool cw;
+    bool flat;            // RAST_FLAT: face normals in place of the vertex normals
     bool vec_ok;  // npx % 4 == 0 (planes stay 4-byte aligned), rgb 4-byte and depth 16-byte aligned
     uint8_t* rgb;
     float* depth;
@@ -1304,15 +1304,20 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             const int32_t i0 = __ldg(a.tri_v + 3 * tt), i1 = __ldg(a.tri_v + 3 * tt + 1), i2 = __ldg(a.tri_v + 3 * tt + 2);
             const int4 nm = __ldg(a.tri_nm + tt);
             const float4 v0 = __ldg(a.rv + i0), v1 = __ldg(a.rv + i1), v2 = __ldg(a.rv + i2);
-            const float* q0 = a.nrm + 3 * (int64_t)nm.x;
-            const float* q1 = a.nrm + 3 * (int64_t)nm.y;
-            const float* q2 = a.nrm + 3 * (int64_t)nm.z;
-            const float3 m0 = make_float3(__ldg(q0), __ldg(q0 + 1), __ldg(q0 + 2));
-            const float3 m1 = make_float3(__ldg(q1), __ldg(q1 + 1), __ldg(q1 + 2));
-            const float3 m2 = make_float3(__ldg(q2), __ldg(q2 + 1), __ldg(q2 + 2));
-            const float3 n0 = camera_normal(a.normal, m0.x, m0.y, m0.z);
-            const float3 n1 = camera_normal(a.normal, m1.x, m1.y, m1.z);
-            const float3 n2 = camera_normal(a.normal, m2.x, m2.y, m2.z);
+            float3 n0, n1, n2;
+            if (a.flat) {
+                // flat shading: every vertex takes the face normal (model space), then the path is
+                // unchanged
+                const float3 f = face_normal(a.pos, i0, i1, i2);
+                n0 = n1 = n2 = camera_normal(a.normal, f.x, f.y, f.z);
+            } else {
+                const float* q0 = a.nrm + 3 * (int64_t)nm.x;
+                const float* q1 = a.nrm + 3 * (int64_t)nm.y;
+                const float* q2 = a.nrm + 3 * (int64_t)nm.z;
+                n0 = camera_normal(a.normal, __ldg(q0), __ldg(q0 + 1), __ldg(q0 + 2));
+                n1 = camera_normal(a.normal, __ldg(q1), __ldg(q1 + 1), __ldg(q1 + 2));
+                n2 = camera_normal(a.normal, __ldg(q2), __ldg(q2 + 1), __ldg(q2 + 2));
+            }
             float dep;
             float3 nrm, alb;
             fragment_attributes(a, x, y, v0, v1, v2, n0, n1, n2, nm.w, i0, i1, i2, tt, dep, nrm, alb);
@@ -1411,11 +1416,25 @@ cudaError_t launch_pdl(bool chained, void (*kernel)(Params...), unsigned grid, u
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
-template <int TS>
+template <int TS, int TPT>
 cudaError_t launch_tile(const TileArgs& ta, int n_sm, bool chained, cudaStream_t stream) {
-    constexpr int kThreads = (TS * TS < 256) ? TS * TS : 256;
-    const int per_sm = 2048 / kThreads < 8 ? 2048 / kThreads : 8;
-    return launch_pdl(chained, k_tile_raster<TS>, (unsigned)(n_sm * per_sm), (unsigned)kThreads, stream, ta);
+    const int per_sm = 2048 / TPT < 8 ? 2048 / TPT : 8;
+    return launch_pdl(chained, k_tile_raster<TS, TPT>, (unsigned)(n_sm * per_sm), (unsigned)TPT, stream, ta);
+}
+
+// The tile raster for tile edge TS with `threads` threads per tile (0: min(TS*TS, 256)); values
+// the kernel does not take fall back to the default.
+template <int TS>
+cudaError_t launch_tile_threads(const TileArgs& ta, uint32_t threads, int n_sm, bool chained, cudaStream_t stream) {
+    if constexpr (TS == 8) {
+        return launch_tile<8, 64>(ta, n_sm, chained, stream);
+    } else {
+        if (threads == 64u) return launch_tile<TS, 64>(ta, n_sm, chained, stream);
+        if (threads == 128u) return launch_tile<TS, 128>(ta, n_sm, chained, stream);
+        if constexpr (TS == 32)
+            if (threads == 512u) return launch_tile<TS, 512>(ta, n_sm, chained, stream);
+        return launch_tile<TS, 256>(ta, n_sm, chained, stream);
+    }
 }
 
 }  // namespace
@@ -1437,6 +1456,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     };
     const bool clear = (p.flags & 2u) != 0;  // RAST_CLEAR
     const bool cw = (p.flags & 1u) != 0;     // RAST_WIND_CLOCKWISE
+    const bool flat = (p.flags & 4u) != 0;   // RAST_FLAT
     const int64_t npx = (int64_t)p.width * p.height;
     const uint32_t n_tiles = p.tiles_x * p.tiles_y;
     const uint32_t shift = p.tile == 8 ? 3u : (p.tile == 16 ? 4u : 5u);
@@ -1522,9 +1542,9 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ta.tiles_x = p.tiles_x;
     ta.n_tiles = n_tiles;
     ta.stats = s.stats;
-    const cudaError_t et = p.tile == 8 ? launch_tile<8>(ta, p.n_sm, p.chained, stream)
-                           : p.tile == 16 ? launch_tile<16>(ta, p.n_sm, p.chained, stream)
-                                          : launch_tile<32>(ta, p.n_sm, p.chained, stream);
+    const cudaError_t et = p.tile == 8 ? launch_tile_threads<8>(ta, p.tile_threads, p.n_sm, p.chained, stream)
+                           : p.tile == 16 ? launch_tile_threads<16>(ta, p.tile_threads, p.n_sm, p.chained, stream)
+                                          : launch_tile_threads<32>(ta, p.tile_threads, p.n_sm, p.chained, stream);
     if (et != cudaSuccess) return -1;
     ++launches;
     mark(6);
@@ -1539,6 +1559,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.tri_nm = mesh.tri_nm;
     ra.rv = s.rv;
     ra.nrm = mesh.nrm;
+    ra.pos = mesh.pos;
     ra.kd = mesh.kd;
     ra.lights = p.lights;
     ra.nl = p.nl;
@@ -1546,6 +1567,7 @@ int launch_draw(const DeviceMesh& mesh, const FrameScratch& s, const DrawParams&
     ra.width = p.width;
     ra.height = p.height;
     ra.cw = cw;
+    ra.flat = flat;
     ra.vec_ok = (reinterpret_cast<uintptr_t>(p.rgb) % 4u) == 0 && (npx % 4) == 0 &&
                 (reinterpret_cast<uintptr_t>(p.depth) % 16u) == 0;
     ra.rgb = p.rgb;

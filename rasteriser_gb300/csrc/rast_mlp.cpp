@@ -143,7 +143,7 @@ rast_status rast_mlp_train(rast_ctx* c, const rast_mlp_train_desc* desc, float o
     if (desc) d = *desc;
     if (d.samples == 0) d.samples = 4194304;
     if (d.holdout == 0) d.holdout = 65536;
-    if (d.epochs == 0) d.epochs = 12;
+    if (d.epochs == 0) d.epochs = 24;
     if (d.ctas == 0) d.ctas = c->n_sm;
     if (d.lr == 0.f) d.lr = 3e-3f;
     if (d.seed == 0) d.seed = 1;
@@ -237,7 +237,7 @@ rast_status rast_mlp_save(rast_ctx* c, void* buf, size_t cap, size_t* size) {
     MlpBlobHeader h;
     std::memset(&h, 0, sizeof h);
     std::memcpy(h.magic, "RMLP", 4);
-    h.version = 1;
+    h.version = 2;
     h.n_in = kMlpFeat;
     h.n_hidden = kMlpHid;
     h.n_out = kMlpOut;
@@ -267,8 +267,8 @@ rast_status rast_mlp_load(rast_ctx* c, const void* buf, size_t size) {
     if (size != kMlpBlobBytes) return fail(c, RAST_ERR_INVALID_ARG, "weight blob has the wrong size");
     MlpBlobHeader h;
     std::memcpy(&h, buf, sizeof h);
-    if (std::memcmp(h.magic, "RMLP", 4) != 0 || h.version != 1)
-        return fail(c, RAST_ERR_INVALID_ARG, "not an RMLP version 1 blob");
+    if (std::memcmp(h.magic, "RMLP", 4) != 0 || h.version != 2)
+        return fail(c, RAST_ERR_INVALID_ARG, "not an RMLP version 2 blob");
     if (h.n_in != (uint32_t)kMlpFeat || h.n_hidden != (uint32_t)kMlpHid || h.n_out != (uint32_t)kMlpOut ||
         h.n_freq != (uint32_t)kMlpFreq || !(h.out_scale > 0.f))
         return fail(c, RAST_ERR_INVALID_ARG, "weight blob has other dimensions");

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -96,22 +97,27 @@ extern "C" rast_status rast_draw_noalloc(const float* d_pos, int64_t nv, const f
         base = g_scratch_ptr[dev];
     }
 
-    // Lay out the frame's buffers in the array, as the context path sizes them.
+    // Lay out the frame's fixed-size buffers first; the tile-bin entries then take every byte of
+    // the array that is left, since their need depends on how much screen the triangles cover (a
+    // screen-sized triangle is one entry per tile) and this entry point cannot grow them.
     const uint32_t tile = 16;
     const uint32_t tiles_x = (width + tile - 1) / tile, tiles_y = (height + tile - 1) / tile;
     const uint32_t n_tiles = tiles_x * tiles_y;
     const int64_t npx = (int64_t)width * height;
     const int64_t cap_large = ntri > 0 ? ntri : 1;
-    const int64_t cap_entries = 2 * ntri > 65536 ? 2 * ntri : 65536;
     const size_t counter_words = rast::kCounterHeader + 2 * (size_t)n_tiles;
-    size_t need = 0;
+    size_t fixed = 0;
     for (size_t b : {(size_t)12 * cap_large, (size_t)16 * cap_large, (size_t)16 * (nv > 0 ? nv : 1), (size_t)8 * npx,
                      sizeof(rast::BinnedTri) * (size_t)cap_large, 4 * counter_words, 4 * 2 * ((size_t)n_tiles + 1),
-                     (size_t)4 * cap_entries, sizeof(unsigned long long) * rast::kStatWords, (size_t)256})
-        need += (b + 255) & ~size_t(255);
-    if (need > kNoAllocScratchBytes)
-        return fail(RAST_ERR_INVALID_ARG, "frame needs " + std::to_string(need) + " bytes of scratch; the fixed array holds " +
+                     sizeof(unsigned long long) * rast::kStatWords, (size_t)256})
+        fixed += (b + 255) & ~size_t(255);
+    const size_t min_entries = 65536;
+    if (fixed + 4 * min_entries > kNoAllocScratchBytes)
+        return fail(RAST_ERR_INVALID_ARG, "frame needs " + std::to_string(fixed + 4 * min_entries) +
+                                              " bytes of scratch; the fixed array holds " +
                                               std::to_string(kNoAllocScratchBytes));
+    // the entry count travels in 32-bit counters
+    const int64_t cap_entries = (int64_t)std::min<size_t>((kNoAllocScratchBytes - fixed) / 4 / 64 * 64, 0x7FFFFFFFu);
 
     Carver c{static_cast<unsigned char*>(base)};
     int32_t* tri_v = c.take<int32_t>((size_t)12 * cap_large);
@@ -122,9 +128,9 @@ extern "C" rast_status rast_draw_noalloc(const float* d_pos, int64_t nv, const f
     s.large = c.take<rast::BinnedTri>(sizeof(rast::BinnedTri) * (size_t)cap_large);
     s.counters = c.take<uint32_t>(4 * counter_words);
     s.tile_offset = c.take<uint32_t>(4 * 2 * ((size_t)n_tiles + 1));
-    s.entries = c.take<uint32_t>((size_t)4 * cap_entries);
     s.stats = c.take<unsigned long long>(sizeof(unsigned long long) * rast::kStatWords);
     uint32_t* check = c.take<uint32_t>(256);
+    s.entries = c.take<uint32_t>((size_t)4 * cap_entries);
     s.cap_large = cap_large;
     s.cap_entries = cap_entries;
 
@@ -165,9 +171,12 @@ extern "C" rast_status rast_draw_noalloc(const float* d_pos, int64_t nv, const f
     p.width = width;
     p.height = height;
     p.flags = flags;
+    // the context path's defaults (rast_create): whole-row items on the per-triangle path
     p.small_max = 4096;
     p.tile = tile;
-    p.row_chunk = 8;
+    p.row_chunk = 32;
+    // after a bin overflow the resolve pass writes nothing: the caller's buffers stay as they were
+    p.keep_outputs_on_overflow = true;
     p.tiles_x = tiles_x;
     p.tiles_y = tiles_y;
     int n_sm = 1;
@@ -186,8 +195,10 @@ extern "C" rast_status rast_draw_noalloc(const float* d_pos, int64_t nv, const f
     if ((e = cudaMemcpyAsync(&status, s.counters + 1, sizeof status, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (e = cudaStreamSynchronize(st)) != cudaSuccess)
         return fail(RAST_ERR_CUDA, std::string("draw: ") + cudaGetErrorString(e));
-    if (status & rast::STATUS_BIN_OVERFLOW)
-        return fail(RAST_ERR_BIN_OVERFLOW, "the frame needs more tile-bin entries than the fixed array provides");
+    if (status & (rast::STATUS_BIN_OVERFLOW | rast::STATUS_LARGE_OVERFLOW))
+        return fail(RAST_ERR_BIN_OVERFLOW,
+                    "the frame needs more tile-bin entries than the fixed array provides; the frame, depth and "
+                    "triangle-id buffers were left unchanged");
     if (status) return fail(RAST_ERR_INTERNAL, "device status " + std::to_string(status));
     return RAST_OK;
 }

@@ -44,6 +44,7 @@ struct ShadeArgs {
     float bound;
     unsigned long long* stats;
     float* eval_out;  // evaluation mode: radiance floats per record (pixel field = record index)
+    uint32_t stall_test;  // test only: the first MMA wait polls an mbarrier nothing arrives on
 };
 
 
@@ -160,12 +161,12 @@ __device__ __forceinline__ float bf16_round(float v) { return __bfloat162float(_
 
 constexpr float kPi = 3.14159265358979323846f;
 
-// sin and cos of f*pi*v for f = 1..16 come from the base pair (the hardware sine and cosine of
+// sin and cos of f*pi*v for f = 1..kMlpFreq come from the base pair (the hardware sine and cosine of
 // pi*v, |pi*v| <= pi) by the three-term recurrence x_{f+1} = 2 cos(pi v) x_f - x_{f-1}, which both
 // sequences satisfy; one packed FMA advances the pair. Its error stays far below BF16's step.
 // emit(f, pair) receives the BF16 pair (sin, cos) of frequency f + 1 (sin in the low half).
 template <class Emit>
-__device__ __forceinline__ void fourier16(float v, Emit&& emit) {
+__device__ __forceinline__ void fourier_pairs(float v, Emit&& emit) {
     float s1, c1;
     __sincosf(kPi * v, &s1, &c1);
     const float2 k2 = make_float2(2.f * c1, 2.f * c1);
@@ -180,8 +181,8 @@ __device__ __forceinline__ void fourier16(float v, Emit&& emit) {
     }
 }
 
-// Pairs 48..55 of the features: n, albedo, the constant 1 that carries layer 1's bias (feature
-// 102), zeros.
+// The last 8 pairs of the features: n, albedo, the constant 1 that carries layer 1's bias
+// (feature kMlpConst), zeros.
 __device__ __forceinline__ void tail_pairs(float3 n, float3 alb, uint32_t (&t)[8]) {
     t[0] = pack_bf16x2(n.x, n.y);
     t[1] = pack_bf16x2(n.z, alb.x);
@@ -190,20 +191,17 @@ __device__ __forceinline__ void tail_pairs(float3 n, float3 alb, uint32_t (&t)[8
     t[4] = t[5] = t[6] = t[7] = 0u;
 }
 
-// The 112 input features, each rounded to BF16, as 56 packed pairs (feature 2i in the low half).
+// The kMlpIn input features, each rounded to BF16, as packed pairs (feature 2i in the low half).
+static_assert(kMlpIn / 2 == 3 * kMlpFreq + 8 && kMlpConst == 6 * kMlpFreq + 6, "feature layout");
 __device__ __forceinline__ void mlp_feature_pairs(float3 n, float3 alb, uint32_t (&pairs)[kMlpIn / 2]) {
     const float comp[3] = {n.x, n.y, n.z};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) fourier16(comp[c], [&](int f, uint32_t p) { pairs[c * kMlpFreq + f] = p; });
+    for (int c = 0; c < 3; ++c) fourier_pairs(comp[c], [&](int f, uint32_t p) { pairs[c * kMlpFreq + f] = p; });
     uint32_t t[8];
     tail_pairs(n, alb, t);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) pairs[48 + i] = t[i];
+    for (int i = 0; i < 8; ++i) pairs[3 * kMlpFreq + i] = t[i];
 }
-
-// The same features, written as they are made into this thread's TMEM lane from column taddr on
-// (56 columns, two BF16 features each): the A operand of the first layer.
-__device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t taddr);
 
 // ---------------------------------------------------------------------------------------------
 // learned shader: tcgen05 helpers
@@ -246,10 +244,11 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Waits for the phase with the given parity to complete; false after kWaitTries polls.
+// Waits for the phase with the given parity to complete; false after `tries` polls.
 constexpr uint32_t kWaitTries = 1u << 22;
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitTries; ++i) {
+constexpr uint32_t kStallTestTries = 1024;  // RAST_OPT_TEST_SHADE_STALL: polls of the idle mbarrier
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32_t tries = kWaitTries) {
+    for (uint32_t i = 0; i < tries; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -328,220 +327,73 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 // ---------------------------------------------------------------------------------------------
 // learned shader: the kernel
 // ---------------------------------------------------------------------------------------------
-constexpr int kMlpThreads = 128;  // one thread per tile row; warps 0..3 own TMEM lanes 0..127
-constexpr uint32_t kTmemCols = 128;
-constexpr int kMlpCtasPerSm = 4;  // 4 x 128 TMEM columns: the whole tensor memory of an SM
-// Tensor memory of a CTA: columns [0, 56) the A operand (features, then h1, then h2, each written
-// after the MMA that read the previous content completed), [64, 128) the FP32 accumulators.
-constexpr uint32_t kColA = 0, kColD = 64;
-// Shared memory (bytes): the weights (B operands) and a small block.
-constexpr uint32_t kSmW = 0;
-constexpr uint32_t kSmW1 = kSmW;
-constexpr uint32_t kSmW2 = kSmW1 + kMlpHid * kMlpIn * 2;
-constexpr uint32_t kSmW3 = kSmW2 + kMlpHid * kMlpHid * 2;
-constexpr uint32_t kSmMisc = kSmW + sizeof(MlpImage);
+// One CTA per SM with kSlots independent tile slots. A slot is four warps, one thread per row of a
+// 128-record tile; it walks its tiles through the three layers on its own (named barriers), so
+// while one slot waits for its MMAs the others compute features and epilogues. The slots share
+// the weights (B operands, one copy in shared memory) and the light table of the checks. A slot's
+// FP32 accumulators are 64 columns of tensor memory; its A operand (features, then h1, then h2) is
+// either 32 further columns of tensor memory (kATmem) or a [128][K] BF16 matrix in shared memory.
+//
+// The layout can be changed at build time (RAST_MLP_SLOTS, RAST_MLP_LD, RAST_MLP_A_TMEM) to
+// measure the alternatives; the defaults are the fastest measured.
+#ifndef RAST_MLP_SLOTS
+#define RAST_MLP_SLOTS 5
+#endif
+#ifndef RAST_MLP_LD
+#define RAST_MLP_LD 4
+#endif
+#ifndef RAST_MLP_A_TMEM
+#define RAST_MLP_A_TMEM 1
+#endif
+constexpr int kSlots = RAST_MLP_SLOTS;
+constexpr int kLdBatch = RAST_MLP_LD;  // 16-column accumulator loads in flight per wait (1, 2 or 4)
+constexpr bool kATmem = RAST_MLP_A_TMEM != 0;
+constexpr int kSlotThreads = 128;  // warp w of a slot reads TMEM lanes 32w..32w+31 (w = warp id mod 4)
+constexpr int kMlpThreads = kSlots * kSlotThreads;
+constexpr uint32_t kSlotCols = 64;                       // a slot's accumulators
+constexpr uint32_t kACols = kMlpIn / 2;                  // a slot's A operand in tensor memory
+constexpr uint32_t kTmemCols = 512;
+static_assert(kMlpIn == kMlpHid, "one A operand per slot serves every layer");
+static_assert(kSlots * kSlotCols + (kATmem ? kSlots * kACols : 0u) <= kTmemCols, "tensor memory of one SM");
+static_assert(kLdBatch == 1 || kLdBatch == 2 || kLdBatch == 4, "accumulator loads per wait");
+constexpr uint32_t kABytes = kATmem ? 0u : kMlpRows * kMlpIn * 2;  // a slot's A operand in shared memory
+constexpr uint32_t kALbo = kMlpRows * 16;                            // its K-direction core-matrix step
 constexpr uint32_t kMaxSamples = 4;
 constexpr int kMlpSmemLights = 512;  // lights staged in shared memory (24 bytes each) for the checks
 
-constexpr int kCheckTiles = 16;  // tiles whose checks a CTA batches before running them
+// Shared memory (bytes): the weights and output scale, the slots' A operands, the light table,
+// then the small block.
+constexpr uint32_t kSmW1 = 0;
+constexpr uint32_t kSmW2 = kSmW1 + kMlpHid * kMlpIn * 2;
+constexpr uint32_t kSmW3 = kSmW2 + kMlpHid * kMlpHid * 2;
+constexpr uint32_t kSmA = (sizeof(MlpImage) + 1023) / 1024 * 1024;
+constexpr uint32_t kSmLights = kSmA + kSlots * kABytes;
+constexpr uint32_t kSmMisc = kSmLights + 24u * kMlpSmemLights;
 
-// The checked records of the tiles a CTA shaded since its last check batch: the record, the MLP's
-// clamped radiance, then the exact radiance.
-struct CheckBatch {
-    uint32_t tile[kCheckTiles];
-    float rec[kCheckTiles][kMaxSamples][12];  // normal xyz, albedo rgb, MLP rgb, exact rgb
-    uint32_t fail[kCheckTiles];
+struct SlotMisc {
+    unsigned long long mbar;          // MMA completion
+    uint32_t fail[2];                 // by tile parity: a checked row exceeded the bound
+    float rec[kMaxSamples][4];        // the checked rows' normals (xyz), written by their threads
+    float sum[kMaxSamples][4];        // their light sums sum_l (I c)_l max(0, n . -dir_l) (warp s)
 };
-
 struct MlpMisc {
-    unsigned long long mbar;                     // MMA completion
-    unsigned long long mbar_w;                   // the weights' bulk copy
+    unsigned long long mbar_w;        // the weights' bulk copy
+    unsigned long long mbar_idle;     // nothing arrives on it (the stall test's first wait)
     uint32_t tmem;
     uint32_t pad[3];
-    uint32_t rank[2][kMaxSamples];  // the checked rows of the tile, by tile parity
-    CheckBatch check;
+    SlotMisc slot[kSlots];
 };
-constexpr uint32_t kSmLights = kSmMisc + ((sizeof(MlpMisc) + 127) / 128) * 128;
-constexpr uint32_t kMlpSmem = kSmLights;  // without staged lights
-static_assert(kSmW1 % 16 == 0 && kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmMisc % 16 == 0, "operand alignment");
-static_assert(kMlpCtasPerSm * (kMlpSmem + 24 * kMlpSmemLights + 1024) <= 228 * 1024, "four CTAs per SM");
-static_assert(sizeof(MlpImage) % 16 == 0 && kSmW % 16 == 0, "bulk copy alignment");
+constexpr uint32_t kMlpSmem = kSmMisc + sizeof(MlpMisc);
+static_assert(kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmA % 1024 == 0 && kSmLights % 16 == 0 && kSmMisc % 16 == 0,
+              "operand alignment");
+static_assert(kMlpSmem <= 227 * 1024, "shared memory of one CTA");
+static_assert(sizeof(MlpImage) % 16 == 0, "bulk copy alignment");
 
-// Whether a launch stages its lights in shared memory, and its dynamic shared memory.
-RAST_HD inline bool mlp_lights_staged(int nl, int samples) { return samples > 0 && nl > 0 && nl <= kMlpSmemLights; }
-inline uint32_t mlp_smem_bytes(int nl, int samples) {
-    return kMlpSmem + (mlp_lights_staged(nl, samples) ? 24u * (uint32_t)nl : 0u);
-}
+inline uint32_t mlp_smem_bytes() { return kMlpSmem; }
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
     return x;
-}
-
-// The learned shader's light table in shared memory, one light per index in two arrays:
-// dirI[l] = (-dir xyz, I*r) and gb[l] = (I*g, I*b) (the products shading.cpp forms per light), so
-// the lanes of a warp read consecutive lights without bank conflicts.
-struct SmemLights {
-    float4* dirI;
-    float2* gb;
-};
-
-__device__ __forceinline__ void stage_lights_soa(const float* lights, int n, SmemLights L) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float* p = lights + 7 * (int64_t)i;
-        const float I = __ldg(p + 3);
-        L.dirI[i] = make_float4(-__ldg(p), -__ldg(p + 1), -__ldg(p + 2), mul(I, __ldg(p + 4)));
-        L.gb[i] = make_float2(mul(I, __ldg(p + 5)), mul(I, __ldg(p + 6)));
-    }
-}
-
-// The exact radiance (shading.cpp:20-34 in its order, as accumulate_lights) from the table.
-__device__ __forceinline__ float3 exact_radiance(SmemLights L, int nl, float3 nv, float3 alb) {
-    float3 acc = make_float3(0.f, 0.f, 0.f);
-#pragma unroll 4
-    for (int l = 0; l < nl; ++l) {
-        const float4 A = L.dirI[l];
-        const float2 B = L.gb[l];
-        float cr = mul(A.w, alb.x), cg = mul(B.x, alb.y), cb = mul(B.y, alb.z);
-        const float d = add(add(mul(nv.x, A.x), mul(nv.y, A.y)), mul(nv.z, A.z));
-        const float m = gmax(0.f, d);
-        acc.x = add(acc.x, mul(mul(cr, m), kOneOverPi));
-        acc.y = add(acc.y, mul(mul(cg, m), kOneOverPi));
-        acc.z = add(acc.z, mul(mul(cb, m), kOneOverPi));
-    }
-    return acc;
-}
-
-// Epilogue of a hidden layer: this thread's 64 accumulators (TMEM columns from d) through ReLU,
-// rounded to BF16, into 32 columns of its lane from column a: the next layer's A operand.
-__device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a) {
-    uint32_t v0[16], v1[16], v2[16], v3[16];
-    tmem_ld16(d, v0);
-    tmem_ld16(d + 16, v1);
-    tmem_ld16(d + 32, v2);
-    tmem_ld16(d + 48, v3);
-    tmem_wait16(v0);
-    reg_fence16(v1);
-    reg_fence16(v2);
-    reg_fence16(v3);
-    uint32_t p[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) p[j] = relu_bf16x2(__uint_as_float(v0[2 * j]), __uint_as_float(v0[2 * j + 1]));
-    tmem_st8(a, p);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) p[j] = relu_bf16x2(__uint_as_float(v1[2 * j]), __uint_as_float(v1[2 * j + 1]));
-    tmem_st8(a + 8, p);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) p[j] = relu_bf16x2(__uint_as_float(v2[2 * j]), __uint_as_float(v2[2 * j + 1]));
-    tmem_st8(a + 16, p);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) p[j] = relu_bf16x2(__uint_as_float(v3[2 * j]), __uint_as_float(v3[2 * j + 1]));
-    tmem_st8(a + 24, p);
-    tmem_wait_st();
-}
-
-// A tile whose check failed, shaded exactly (shading.cpp:20-34 in its order) by its rows.
-__device__ __forceinline__ void reshade_tile(const ShadeArgs& a, const SmemLights* L, uint32_t t) {
-    if (threadIdx.x >= shade_tile_count(a.index, t)) return;
-    const size_t slot = shade_record_slot(a.index, a.n_blocks, shade_tile_desc(a.index, a.n_blocks, t), t, threadIdx.x);
-    const float4 g0 = a.gbuf[2 * slot], g1 = a.gbuf[2 * slot + 1];
-    const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
-    const uint32_t col =
-        L ? pack_rgb(exact_radiance(*L, a.nl, nv, alb)) : shade_lights(a.lights, a.nl, nv, alb);
-    write_rgb(a.rgb, a.npx, __float_as_uint(g1.z), col);
-}
-
-// The checked records of a batch against the exact shader: warp w takes the pairs (tile, sample)
-// p = w, w + 4, ..., four at a time (two packed pairs); its lanes split the lights. The check only estimates the error (it never
-// produces a colour), so it sums the per-light terms of shading.cpp:24-31 in another order and
-// with fused multiply-adds, albedo and 1/pi factored out: sum_l (I*c)_l * max(0, n . -dir_l),
-// then times albedo / pi. Then each tile's largest channel error decides whether it is shaded
-// exactly, which the whole CTA does for the failing tiles. Ends synchronised.
-__device__ void run_checks(const ShadeArgs& a, const SmemLights* L, CheckBatch& B, int nb, int n_samples,
-                           unsigned long long& n_fallback, float& max_err) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    // warp w takes the pairs p = w, w + 4, ... four at a time, so one pass over the lights serves
-    // four checked records (twelve independent sums)
-    constexpr int G = 4;
-    const int np = nb * n_samples;
-    for (int p0 = warp; p0 < np; p0 += G * (kMlpThreads / 32)) {
-        // records j = 0, 1 and j = 2, 3 in the two halves of packed pairs
-        float2 nx[2], ny[2], nz[2], ar[2], ag[2], ab[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int pa = min(p0 + (2 * h) * (kMlpThreads / 32), np - 1);  // past the end: a repeat, not stored
-            const int pb = min(p0 + (2 * h + 1) * (kMlpThreads / 32), np - 1);
-            const float* Ra = B.rec[pa / n_samples][pa % n_samples];
-            const float* Rb = B.rec[pb / n_samples][pb % n_samples];
-            nx[h] = make_float2(Ra[0], Rb[0]);
-            ny[h] = make_float2(Ra[1], Rb[1]);
-            nz[h] = make_float2(Ra[2], Rb[2]);
-            ar[h] = ag[h] = ab[h] = make_float2(0.f, 0.f);
-        }
-        auto light = [&](float4 A, float2 C) {
-            const float2 ax = make_float2(A.x, A.x), ay = make_float2(A.y, A.y), az = make_float2(A.z, A.z);
-            const float2 cr = make_float2(A.w, A.w), cg = make_float2(C.x, C.x), cb = make_float2(C.y, C.y);
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                float2 d = __ffma2_rn(nz[h], az, __ffma2_rn(ny[h], ay, __fmul2_rn(nx[h], ax)));
-                d = make_float2(fmaxf(d.x, 0.f), fmaxf(d.y, 0.f));
-                ar[h] = __ffma2_rn(cr, d, ar[h]);
-                ag[h] = __ffma2_rn(cg, d, ag[h]);
-                ab[h] = __ffma2_rn(cb, d, ab[h]);
-            }
-        };
-        if (L) {
-            for (int l = lane; l < a.nl; l += 32) light(L->dirI[l], L->gb[l]);
-        } else {
-            for (int l = lane; l < a.nl; l += 32) {
-                const float* P = a.lights + 7 * (int64_t)l;
-                const float I = __ldg(P + 3);
-                light(make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4)),
-                      make_float2(I * __ldg(P + 5), I * __ldg(P + 6)));
-            }
-        }
-        // Sum the twelve values over the lanes by halving: at each level a lane keeps half of its
-        // values and adds its partner's copy of them, so lanes 2k and 2k + 1 end with value k
-        // (value 3j + c: record j, channel c).
-        float v[16] = {ar[0].x, ag[0].x, ab[0].x, ar[0].y, ag[0].y, ab[0].y,
-                       ar[1].x, ag[1].x, ab[1].x, ar[1].y, ag[1].y, ab[1].y, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int lvl = 0; lvl < 4; ++lvl) {
-            const int half = 8 >> lvl, o = 16 >> lvl;
-            const bool up = (lane & o) != 0;
-#pragma unroll
-            for (int i = 0; i < half; ++i) {
-                const float mine = up ? v[i + half] : v[i], other = up ? v[i] : v[i + half];
-                v[i] = mine + __shfl_xor_sync(kFull, other, o);
-            }
-        }
-        v[0] += __shfl_xor_sync(kFull, v[0], 1);
-        const int k = lane >> 1, j = k / 3, c = k - 3 * j;
-        const int p = p0 + j * (kMlpThreads / 32);
-        if ((lane & 1) == 0 && k < 3 * G && p < np) {
-            float* R = B.rec[p / n_samples][p % n_samples];
-            R[9 + c] = v[0] * R[3 + c] * kOneOverPi;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < (unsigned)nb) {
-        float err = 0.f;
-        for (int s = 0; s < n_samples; ++s) {
-            const float* R = B.rec[threadIdx.x][s];
-            err = fmaxf(err, fmaxf(fmaxf(fabsf(R[6] - fminf(R[9], 255.f)), fabsf(R[7] - fminf(R[10], 255.f))),
-                                   fabsf(R[8] - fminf(R[11], 255.f))));
-        }
-        B.fail[threadIdx.x] = err > a.bound;
-        max_err = fmaxf(max_err, err);  // per thread; reduced by the caller's atomics
-    }
-    __syncthreads();
-    for (int i = 0; i < nb; ++i) {
-        if (!B.fail[i]) continue;  // uniform: every thread reads the same flag
-        if (threadIdx.x == 0) ++n_fallback;
-        reshade_tile(a, L, B.tile[i]);
-    }
-    __syncthreads();
 }
 
 // The checked records of tile t: ranks floor(hash(t, s) * count / 2^32), the same in every thread.
@@ -549,52 +401,212 @@ __device__ __forceinline__ uint32_t sample_rank(uint32_t t, int s, uint32_t coun
     return __umulhi(hash32(t * 8u + (uint32_t)s + 0x9E3779B9u), count);
 }
 
-// Issues the MMAs of one layer, A from TMEM columns a (K/16 steps of 8 columns) and B from shared
-// memory, into TMEM at d, and commits them to mbar.
-__device__ __forceinline__ void issue_layer(uint32_t d, uint32_t a, uint32_t b, uint32_t lbo_b, int k_steps,
+// Named barrier of slot s (ids 1..kSlots; 0 is __syncthreads), with an OR of `v` over its threads.
+__device__ __forceinline__ bool slot_sync_or(int s, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(s + 1), "r"(kSlotThreads)
+        : "memory");
+    return r != 0u;
+}
+__device__ __forceinline__ void slot_sync(int s) {
+    asm volatile("bar.sync %0, %1;" ::"r"(s + 1), "r"(kSlotThreads) : "memory");
+}
+
+// Makes this thread's shared-memory stores visible to the tensor cores' reads (async proxy).
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t x, uint32_t y, uint32_t z, uint32_t w) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(x), "r"(y), "r"(z), "r"(w) : "memory");
+}
+
+// Row r's 16-byte chunk j (K elements 8j..8j+7) of a slot's A operand at `base`: the K-major,
+// unswizzled core layout of core_offset().
+__device__ __forceinline__ uint32_t a_chunk(uint32_t base, uint32_t r, uint32_t j) {
+    return base + j * kALbo + (r >> 3) * 128u + (r & 7u) * 16u;
+}
+
+// tcgen05.mma kind::f16, A and B from shared memory (descriptors), D in tensor memory.
+__device__ __forceinline__ void mma_bf16_ss(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// One layer's MMAs into the slot's accumulators, A (128 x K) from its operand (tensor memory
+// columns or shared memory) and B (b_rows x K) from the weights; committed to mbar.
+__device__ __forceinline__ void issue_layer(uint32_t d, uint32_t a, uint32_t b_smem, uint32_t b_rows, int k_steps,
                                             uint32_t idesc, uint32_t mbar) {
     tc_fence_after();
-    for (int s = 0; s < k_steps; ++s) mma_bf16_ta(d, a + 8 * s, mma_desc(b + 2 * s * lbo_b, lbo_b, 128), idesc, s > 0);
+    const uint32_t lbo_b = b_rows * 16u;
+    for (int s = 0; s < k_steps; ++s) {
+        const uint64_t b = mma_desc(b_smem + 2u * s * lbo_b, lbo_b, 128);
+        if constexpr (kATmem) mma_bf16_ta(d, a + 8u * s, b, idesc, s > 0);
+        else mma_bf16_ss(d, mma_desc(a + 2u * s * kALbo, kALbo, 128), b, idesc, s > 0);
+    }
     mma_commit(mbar);
 }
 
-__global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeArgs a) {
-    extern __shared__ __align__(1024) uint8_t sm[];
-    const int row = threadIdx.x, warp = row >> 5;
-    MlpMisc& M = *reinterpret_cast<MlpMisc*>(sm + kSmMisc);
-    const int n_samples = a.eval_out ? 0 : min(a.samples, (int)kMaxSamples);
-    SmemLights lights_smem;
-    lights_smem.dirI = reinterpret_cast<float4*>(sm + kSmLights);
-    lights_smem.gb = reinterpret_cast<float2*>(sm + kSmLights + 16 * (size_t)max(a.nl, 0));
-    const SmemLights* sl = mlp_lights_staged(a.nl, n_samples) ? &lights_smem : nullptr;
-
-    // the weights and output scale arrive by one bulk copy, the lights by plain loads (neither
-    // depends on the grid this kernel may overlap with)
-    const uint32_t mbar = smem_addr(&M.mbar), mbar_w = smem_addr(&M.mbar_w);
-    if (row == 0) {
-        mbar_init(mbar, 1);
-        mbar_init(mbar_w, 1);
-        mbar_expect_tx(mbar_w, sizeof(MlpImage));
-        bulk_copy_g2s(smem_addr(sm + kSmW), a.mlp, sizeof(MlpImage), mbar_w);
+// Eight packed pairs (16 K elements) of row r into the slot's A operand at chunk pair j2 (K
+// elements 16 j2 .. 16 j2 + 15): 8 tensor-memory columns of this thread's lane, or two 16-byte
+// shared-memory chunks.
+__device__ __forceinline__ void put_a8(uint32_t a, uint32_t r, uint32_t j2, const uint32_t (&q)[8]) {
+    if constexpr (kATmem) {
+        tmem_st8(a + 8u * j2, q);
+    } else {
+        st_shared_v4(a_chunk(a, r, 2u * j2), q[0], q[1], q[2], q[3]);
+        st_shared_v4(a_chunk(a, r, 2u * j2 + 1u), q[4], q[5], q[6], q[7]);
     }
-    if (sl) stage_lights_soa(a.lights, a.nl, lights_smem);
-    if (warp == 0) tmem_alloc(smem_addr(&M.tmem), kTmemCols);
+}
+
+// Makes the A operand written by this thread visible to the MMA the slot issues next (before the
+// slot barrier).
+__device__ __forceinline__ void a_written() {
+    if constexpr (kATmem) tmem_wait_st();
+    else fence_async_smem();
+    tc_fence_before();
+}
+
+// The features of one row (mlp_feature_pairs' order) into its A operand, 8 pairs at a time.
+__device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t a, uint32_t r) {
+    static_assert(kMlpFreq == 8, "one 8-pair store per normal component");
+    const float comp[3] = {n.x, n.y, n.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        uint32_t q[8];
+        fourier_pairs(comp[c], [&](int f, uint32_t p) { q[f] = p; });
+        put_a8(a, r, (uint32_t)c, q);
+    }
+    uint32_t t[8];
+    tail_pairs(n, alb, t);
+    put_a8(a, r, 3u, t);
+}
+
+// Epilogue of a hidden layer: row r's 64 accumulators (TMEM columns from d) through ReLU, rounded
+// to BF16, into its A operand (over the consumed features or h1): the next layer's A.
+// kLdBatch 16-column loads are in flight per wait.
+__device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a, uint32_t r) {
+#pragma unroll
+    for (int g = 0; g < kMlpHid / 16; g += kLdBatch) {
+        uint32_t v[kLdBatch][16];
+#pragma unroll
+        for (int i = 0; i < kLdBatch; ++i) tmem_ld16(d + 16u * (g + i), v[i]);
+        tmem_wait16(v[0]);
+#pragma unroll
+        for (int i = 1; i < kLdBatch; ++i) reg_fence16(v[i]);
+#pragma unroll
+        for (int i = 0; i < kLdBatch; ++i) {
+            uint32_t p[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) p[j] = relu_bf16x2(__uint_as_float(v[i][2 * j]), __uint_as_float(v[i][2 * j + 1]));
+            put_a8(a, r, (uint32_t)(g + i), p);
+        }
+    }
+}
+
+// The light table of the checks: dirI[l] = (-dir xyz, I*r), gb[l] = (I*g, I*b).
+struct SmemLights {
+    const float4* dirI;
+    const float2* gb;
+};
+
+__device__ __forceinline__ void stage_lights_soa(const float* lights, int n, float4* dirI, float2* gb) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float* p = lights + 7 * (int64_t)i;
+        const float I = __ldg(p + 3);
+        dirI[i] = make_float4(-__ldg(p), -__ldg(p + 1), -__ldg(p + 2), I * __ldg(p + 4));
+        gb[i] = make_float2(I * __ldg(p + 5), I * __ldg(p + 6));
+    }
+}
+
+// The light sum of checked row s of a tile, by one warp: lanes split the lights, then a butterfly
+// over the lanes. The check only estimates the error (it never produces a colour), so it sums
+// sum_l (I c)_l * max(0, n . -dir_l) with fused multiply-adds; albedo and 1/pi are applied by the
+// checked row itself. Lights from the shared table when it holds them, else from global memory.
+__device__ __forceinline__ void check_sum(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int s, int lane) {
+    const float nx = S.rec[s][0], ny = S.rec[s][1], nz = S.rec[s][2];
+    float sr = 0.f, sg = 0.f, sb = 0.f;
+    if (L) {
+#pragma unroll 4
+        for (int l = lane; l < a.nl; l += 32) {
+            const float4 A = L->dirI[l];
+            const float2 B = L->gb[l];
+            const float m = fmaxf(fmaf(nz, A.z, fmaf(ny, A.y, nx * A.x)), 0.f);
+            sr = fmaf(A.w, m, sr);
+            sg = fmaf(B.x, m, sg);
+            sb = fmaf(B.y, m, sb);
+        }
+    } else {
+        for (int l = lane; l < a.nl; l += 32) {
+            const float* P = a.lights + 7 * (int64_t)l;
+            const float I = __ldg(P + 3);
+            const float m = fmaxf(fmaf(nz, -__ldg(P + 2), fmaf(ny, -__ldg(P + 1), nx * -__ldg(P))), 0.f);
+            sr = fmaf(I * __ldg(P + 4), m, sr);
+            sg = fmaf(I * __ldg(P + 5), m, sg);
+            sb = fmaf(I * __ldg(P + 6), m, sb);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(kFull, sr, o);
+        sg += __shfl_xor_sync(kFull, sg, o);
+        sb += __shfl_xor_sync(kFull, sb, o);
+    }
+    if (lane == 0) {
+        S.sum[s][0] = sr;
+        S.sum[s][1] = sg;
+        S.sum[s][2] = sb;
+    }
+}
+
+__global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    MlpMisc& M = *reinterpret_cast<MlpMisc*>(sm + kSmMisc);
+    const int slot = threadIdx.x / kSlotThreads, row = threadIdx.x % kSlotThreads;
+    const int wq = row >> 5, lane = threadIdx.x & 31;  // warp within the slot = its TMEM lane quarter
+    SlotMisc& S = M.slot[slot];
+    const int n_samples = a.eval_out ? 0 : min(a.samples, (int)kMaxSamples);
+    float4* lights_dirI = reinterpret_cast<float4*>(sm + kSmLights);
+    float2* lights_gb = reinterpret_cast<float2*>(sm + kSmLights + 16u * kMlpSmemLights);
+    SmemLights table{lights_dirI, lights_gb};
+    const SmemLights* L = (n_samples > 0 && a.nl <= kMlpSmemLights) ? &table : nullptr;
+
+    const uint32_t mbar_w = smem_addr(&M.mbar_w), mbar = smem_addr(&S.mbar);
+    // The stall test's first MMA wait polls an mbarrier that nothing arrives on, briefly, and so
+    // gives up as a wait for a lost MMA would; the MMA itself runs and completes.
+    const uint32_t mbar_first = a.stall_test ? smem_addr(&M.mbar_idle) : mbar;
+    const uint32_t tries_first = a.stall_test ? kStallTestTries : kWaitTries;
+    if (threadIdx.x == 0) {
+        mbar_init(mbar_w, 1);
+        mbar_init(smem_addr(&M.mbar_idle), 1);
+        for (int s = 0; s < kSlots; ++s) mbar_init(smem_addr(&M.slot[s].mbar), 1);
+        // the weights and output scale arrive by one bulk copy (independent of the grid this
+        // kernel may overlap with)
+        mbar_expect_tx(mbar_w, sizeof(MlpImage));
+        bulk_copy_g2s(smem_addr(sm), a.mlp, sizeof(MlpImage), mbar_w);
+    }
+    if (row == 0) S.fail[0] = S.fail[1] = 0u;
+    if (L) stage_lights_soa(a.lights, a.nl, lights_dirI, lights_gb);
+    if (threadIdx.x < 32) tmem_alloc(smem_addr(&M.tmem), kTmemCols);
     // the records and the tile list are the previous kernel's output
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
     const uint32_t n_tiles = a.index[1];
-    // Tiles t = blockIdx.x + k * gridDim.x. This thread's record of the current tile is fetched
-    // one tile ahead and the tile's descriptor two tiles ahead, so neither load waits on the way.
-    const uint32_t stride = gridDim.x;
-    const uint4 d_none = make_uint4(0u, 0u, 0u, 0u);
-    uint32_t t = blockIdx.x;
+    // Slot g = blockIdx.x * kSlots + slot takes tiles g, g + stride, ...
+    const uint32_t stride = gridDim.x * kSlots;
+    uint32_t t = blockIdx.x * kSlots + slot;
     uint32_t count = t < n_tiles ? shade_tile_count(a.index, t) : 0u;
-    uint4 d_next = t + stride < n_tiles ? shade_tile_desc(a.index, a.n_blocks, t + stride) : d_none;
     float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f), g1 = g0;
     if ((uint32_t)row < count) {
-        const size_t slot = shade_record_slot(a.index, a.n_blocks, shade_tile_desc(a.index, a.n_blocks, t), t, row);
-        g0 = a.gbuf[2 * slot];
-        g1 = a.gbuf[2 * slot + 1];
+        const size_t rs = shade_record_slot(a.index, a.n_blocks, shade_tile_desc(a.index, a.n_blocks, t), t, row);
+        g0 = a.gbuf[2 * rs];
+        g1 = a.gbuf[2 * rs + 1];
     }
     tc_fence_before();
     __syncthreads();
@@ -602,71 +614,86 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
     bool failed = !__syncthreads_and(mbar_wait(mbar_w, 0));
     const bool weights_pending = failed;
     const uint32_t tmem = M.tmem;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's lanes
-    const float out_scale = reinterpret_cast<const MlpImage*>(sm + kSmW)->out_scale;
+    const uint32_t d_cols = tmem + (uint32_t)slot * kSlotCols;                // lane 0, this slot's accumulators
+    const uint32_t lane_off = (uint32_t)(wq * 32) << 16;                      // this warp's lanes
+    const uint32_t d_lane = d_cols + lane_off;
+    const float out_scale = reinterpret_cast<const MlpImage*>(sm)->out_scale;
     const uint32_t sW1 = smem_addr(sm + kSmW1), sW2 = smem_addr(sm + kSmW2), sW3 = smem_addr(sm + kSmW3);
+    // the slot's A operand: for the MMA (lane 0) and for this thread's writes
+    const uint32_t a_mma = kATmem ? tmem + kSlots * kSlotCols + (uint32_t)slot * kACols
+                                  : smem_addr(sm + kSmA + (size_t)slot * kABytes);
+    const uint32_t a_mine = kATmem ? a_mma + lane_off : a_mma;
 
-    // Every barrier of the loop also ORs the threads' timeout flags, so all threads leave the loop
-    // at the same barrier (the loop condition itself is the same in every thread).
+    // Every slot barrier of the loop also ORs the threads' timeout flags, so a slot's threads leave
+    // the loop at the same barrier (the loop condition itself is the same in all of them).
     uint32_t phase = 0;
-    unsigned long long n_tile = 0, n_fallback = 0;
+    uint32_t n_tile = 0, n_fallback = 0;
     float max_err = 0.f;
-    int nb = 0;      // tiles in the check batch
-    uint32_t k = 0;  // tiles this CTA shaded
+    uint32_t k = 0;  // tiles this slot shaded
 
     while (!weights_pending && t < n_tiles) {
+        const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
+        // which checked sample this row is, if any
+        int my_sample = -1;
+        for (int s = 0; s < n_samples; ++s)
+            if (sample_rank(t, s, count) == (uint32_t)row) my_sample = s;
+        if (my_sample >= 0) {
+            S.rec[my_sample][0] = nv.x;
+            S.rec[my_sample][1] = nv.y;
+            S.rec[my_sample][2] = nv.z;
+        }
+        // Rows past the tile's records hold zeros: finite features whose results are not stored.
+        // The previous tile's MMAs completed (its last wait), so the operand is free, unless that
+        // wait gave up. After a wait gave up (`failed`), a warp touches tensor memory and the A
+        // operand no more: an MMA may still be using them. The test is warp-uniform, as the
+        // .sync.aligned tcgen05 instructions need.
+        if (!__any_sync(kFull, failed)) store_features(nv, alb, a_mine, (uint32_t)row);
+        a_written();
+        if (slot_sync_or(slot, failed)) break;
+        if (row == 0) S.fail[(k + 1u) & 1u] = 0u;  // every thread read it before this barrier
+
+        // layer 1: D = X (128 x K) * W1^T
+        if (row == 0) issue_layer(d_cols, a_mma, sW1, kMlpHid, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
+        // the checked rows' light sums (warp w takes row w), while the MMAs run
+        if (wq < n_samples) check_sum(a, L, S, wq, lane);
+        failed |= !mbar_wait(mbar_first, phase, tries_first);
+        phase ^= 1u;
+        tc_fence_after();
+        if (!__any_sync(kFull, failed)) hidden_epilogue(d_lane, a_mine, (uint32_t)row);  // h1 over the features
+        a_written();
+        if (slot_sync_or(slot, failed)) break;
+
+        // layer 2: D = H1 (128 x 64) * W2^T (layer 1's accumulators were read)
+        if (row == 0) issue_layer(d_cols, a_mma, sW2, kMlpHid, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
+        // this thread's record of the slot's next tile, fetched during the last two MMAs
         const uint32_t t_next = t + stride;
         const uint32_t count_next = t_next < n_tiles ? shade_tile_count(a.index, t_next) : 0u;
         float4 g0n = make_float4(0.f, 0.f, 0.f, 0.f), g1n = g0n;
         if ((uint32_t)row < count_next) {
-            const size_t slot = shade_record_slot(a.index, a.n_blocks, d_next, t_next, row);
-            g0n = a.gbuf[2 * slot];
-            g1n = a.gbuf[2 * slot + 1];
+            const size_t rs =
+                shade_record_slot(a.index, a.n_blocks, shade_tile_desc(a.index, a.n_blocks, t_next), t_next, row);
+            g0n = a.gbuf[2 * rs];
+            g1n = a.gbuf[2 * rs + 1];
         }
-        // the descriptor two tiles ahead
-        const uint4 d_next2 = t_next + stride < n_tiles ? shade_tile_desc(a.index, a.n_blocks, t_next + stride) : d_none;
-        // the checked rows of this tile, for every thread after the barrier below (two slots by
-        // tile parity: a slot is rewritten only after every thread passed the next tile's barrier)
-        if (row == 0)
-            for (int s = 0; s < n_samples; ++s) M.rank[k & 1u][s] = sample_rank(t, s, count);
-        // rows past the tile's records hold zeros: finite features whose results are not stored
-        store_features(make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y), lane_base + kColA);
-        tc_fence_before();
-        if (__syncthreads_or(failed)) break;
-
-        // layer 1: D = X (128 x 112) * W1^T
-        if (row == 0)
-            issue_layer(tmem + kColD, tmem + kColA, sW1, kMlpHid * 16, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
         failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
         tc_fence_after();
-        hidden_epilogue(lane_base + kColD, lane_base + kColA);  // h1 over the consumed features
-        tc_fence_before();
-        if (__syncthreads_or(failed)) break;
-
-        // layer 2: D = H1 (128 x 64) * W2^T (layer 1's accumulators were read)
-        if (row == 0)
-            issue_layer(tmem + kColD, tmem + kColA, sW2, kMlpHid * 16, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-        failed |= !mbar_wait(mbar, phase);
-        phase ^= 1u;
-        tc_fence_after();
-        hidden_epilogue(lane_base + kColD, lane_base + kColA);  // h2 over the consumed h1
-        tc_fence_before();
-        if (__syncthreads_or(failed)) break;
+        if (!__any_sync(kFull, failed)) hidden_epilogue(d_lane, a_mine, (uint32_t)row);  // h2 over h1
+        a_written();
+        if (slot_sync_or(slot, failed)) break;
 
         // layer 3: D[0, 16) = H2 (128 x 64) * W3^T
-        if (row == 0)
-            issue_layer(tmem + kColD, tmem + kColA, sW3, kMlpOutPad * 16, kMlpHid / 16,
-                        idesc_bf16(kMlpRows, kMlpOutPad), mbar);
+        if (row == 0) issue_layer(d_cols, a_mma, sW3, kMlpOutPad, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpOutPad), mbar);
         failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
         tc_fence_after();
-        uint32_t o[4];
-        tmem_ld4(lane_base + kColD, o);
-        tmem_wait4(o);
+        uint32_t o[4] = {0u, 0u, 0u, 0u};
+        if (!__any_sync(kFull, failed)) {
+            tmem_ld4(d_lane, o);
+            tmem_wait4(o);
+        }
         tc_fence_before();
-        const bool valid = (uint32_t)row < count;
-        const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
+        const bool valid = (uint32_t)row < count && !failed;
         const uint32_t pix = __float_as_uint(g1.z);
         const float3 rad = make_float3(alb.x * (__uint_as_float(o[0]) * out_scale),
                                        alb.y * (__uint_as_float(o[1]) * out_scale),
@@ -683,18 +710,21 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
             if (valid)
                 write_rgb(a.rgb, a.npx, pix,
                           __float2uint_rz(radc.x) | (__float2uint_rz(radc.y) << 8) | (__float2uint_rz(radc.z) << 16));
-            // the checked records join the batch; a failing tile is shaded again, exactly
             if (n_samples > 0) {
-                for (int s = 0; s < n_samples; ++s)
-                    if (M.rank[k & 1u][s] == (uint32_t)row) {
-                        float* R = M.check.rec[nb][s];
-                        R[0] = nv.x; R[1] = nv.y; R[2] = nv.z; R[3] = alb.x; R[4] = alb.y; R[5] = alb.z;
-                        R[6] = radc.x; R[7] = radc.y; R[8] = radc.z;
-                    }
-                if (row == 0) M.check.tile[nb] = t;
-                if (++nb == kCheckTiles) {
-                    run_checks(a, sl, M.check, nb, n_samples, n_fallback, max_err);
-                    nb = 0;
+                // the checked rows against their light sums (written before two slot barriers); a
+                // failing tile is shaded again, exactly, by all its rows
+                if (my_sample >= 0 && valid) {
+                    const float er = fabsf(radc.x - fminf(S.sum[my_sample][0] * alb.x * kOneOverPi, 255.f));
+                    const float eg = fabsf(radc.y - fminf(S.sum[my_sample][1] * alb.y * kOneOverPi, 255.f));
+                    const float eb = fabsf(radc.z - fminf(S.sum[my_sample][2] * alb.z * kOneOverPi, 255.f));
+                    const float err = fmaxf(er, fmaxf(eg, eb));
+                    max_err = fmaxf(max_err, err);
+                    if (err > a.bound) S.fail[k & 1u] = 1u;
+                }
+                slot_sync(slot);
+                if (S.fail[k & 1u]) {  // the same in every thread of the slot
+                    if (row == 0) ++n_fallback;
+                    if ((uint32_t)row < count) write_rgb(a.rgb, a.npx, pix, shade_lights(a.lights, a.nl, nv, alb));
                 }
             }
             ++n_tile;
@@ -702,13 +732,9 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
         ++k;
         t = t_next;
         count = count_next;
-        d_next = d_next2;
         g0 = g0n;
         g1 = g1n;
     }
-
-    // the last batch (the loop ended at a barrier every thread passed, so `failed` is uniform)
-    if (!failed && nb > 0) run_checks(a, sl, M.check, nb, n_samples, n_fallback, max_err);
 
     if (failed) {
         // the weights' copy or an MMA did not complete in time: record it, give the pending one
@@ -719,35 +745,18 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpCtasPerSm) k_shade_mlp(ShadeA
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) {
+    if (threadIdx.x < 32) {
         tc_fence_after();
         tmem_dealloc(tmem, kTmemCols);
     }
     if (a.stats && !a.eval_out) {
-        if (row == 0) {
-            atomicAdd(a.stats + 0, n_tile);
-            atomicAdd(a.stats + 1, n_fallback);
-            atomicAdd(a.stats + 2, n_tile * (unsigned long long)n_samples);
+        if (row == 0 && n_tile) {
+            atomicAdd(a.stats + 0, (unsigned long long)n_tile);
+            if (n_fallback) atomicAdd(a.stats + 1, (unsigned long long)n_fallback);
+            atomicAdd(a.stats + 2, (unsigned long long)n_tile * (unsigned long long)n_samples);
         }
         if (max_err > 0.f) atomicMax(a.stats + 3, (unsigned long long)__float_as_uint(max_err));
     }
-}
-
-// The features of one row into its TMEM lane (declared above).
-__device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t taddr) {
-    const float comp[3] = {n.x, n.y, n.z};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        uint32_t q[8];
-        fourier16(comp[c], [&](int f, uint32_t p) {
-            q[f & 7] = p;
-            if ((f & 7) == 7) tmem_st8(taddr + (uint32_t)(c * kMlpFreq + f - 7), q);
-        });
-    }
-    uint32_t t[8];
-    tail_pairs(n, alb, t);
-    tmem_st8(taddr + 48, t);
-    tmem_wait_st();
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -797,7 +806,7 @@ __global__ void k_mlp_stage(const float* __restrict__ src, int stride, int64_t n
 
 constexpr int kTrainB = 64;          // samples per CTA and step
 constexpr int kTrainThreads = 256;
-constexpr int kSX = 116;             // shared row stride (floats) of X and W1: rows stay 16-byte
+constexpr int kSX = kMlpIn + 4;      // shared row stride (floats) of X and W1: rows stay 16-byte
 constexpr int kSH = 68;              // aligned and eight rows cover all banks; of H, D and W2
 
 struct TrainSmem {
@@ -949,16 +958,18 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train(TrainArgs a) {
         }
     }
     __syncthreads();
-    // layer 1 gradients: unit j, inputs 28*q4 .. 28*q4+27
+    // layer 1 gradients: unit j, inputs kQ*q4 .. kQ*q4 + kQ - 1
     {
-        float acc[28];
+        constexpr int kQ = kMlpIn / 4;
+        static_assert(kQ % 4 == 0, "a quarter of the inputs is whole float4s");
+        float acc[kQ];
 #pragma unroll
-        for (int kk = 0; kk < 28; ++kk) acc[kk] = 0.f;
+        for (int kk = 0; kk < kQ; ++kk) acc[kk] = 0.f;
         for (int b = 0; b < kTrainB; ++b) {
             const float d = S.d1[b * kSH + j];
 #pragma unroll
-            for (int kk = 0; kk < 28; kk += 4) {
-                const float4 x = *reinterpret_cast<const float4*>(S.x + b * kSX + 28 * q4 + kk);
+            for (int kk = 0; kk < kQ; kk += 4) {
+                const float4 x = *reinterpret_cast<const float4*>(S.x + b * kSX + kQ * q4 + kk);
                 acc[kk] = fmaf(d, x.x, acc[kk]);
                 acc[kk + 1] = fmaf(d, x.y, acc[kk + 1]);
                 acc[kk + 2] = fmaf(d, x.z, acc[kk + 2]);
@@ -966,7 +977,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train(TrainArgs a) {
             }
         }
 #pragma unroll
-        for (int kk = 0; kk < 28; ++kk) g[kPW1 + j * kMlpIn + 28 * q4 + kk] = acc[kk];
+        for (int kk = 0; kk < kQ; ++kk) g[kPW1 + j * kMlpIn + kQ * q4 + kk] = acc[kk];
     }
     // loss
     S.red[tid] = sq;
@@ -1031,21 +1042,24 @@ static ShadeArgs shade_args(const FrameScratch& s, const DrawParams& p) {
     a.bound = p.mlp_bound;
     a.stats = s.shade_stats;
     a.eval_out = nullptr;
+    a.stall_test = p.mlp_stall_test ? 1u : 0u;
     return a;
 }
 
 static int mlp_grid(int n_sm, int64_t blocks) {
     static bool attr_set = false;  // per process: the attribute is per function, all devices alike
     if (!attr_set) {
-        if (cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(kMlpSmem + 24 * kMlpSmemLights)) !=
+        if (cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpSmem) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return -1;
         attr_set = true;
     }
-    return (int)std::min<int64_t>((int64_t)kMlpCtasPerSm * n_sm, std::max<int64_t>(8 * blocks, 1));
+    // one CTA per SM at most, and no more CTAs than the tiles need (a block of 1024 records makes
+    // at most 8 tiles)
+    const int64_t max_tiles = (int64_t)(kShadeBlock / kShadeTile) * blocks;
+    return (int)std::min<int64_t>((int64_t)n_sm, std::max<int64_t>((max_tiles + kSlots - 1) / kSlots, 1));
 }
 
 static int exact_grid(int n_sm, int64_t blocks) {
@@ -1080,7 +1094,7 @@ int launch_shade(const FrameScratch& s, const DrawParams& p, int64_t blocks, cud
     } else {
         const int grid = mlp_grid(p.n_sm, blocks);
         if (grid < 0) return -1;
-        err = launch_dependent(k_shade_mlp, grid, kMlpThreads, mlp_smem_bytes(a.nl, a.samples), stream, a);
+        err = launch_dependent(k_shade_mlp, grid, kMlpThreads, mlp_smem_bytes(), stream, a);
     }
     return err == cudaSuccess ? 1 : -1;
 }
@@ -1106,12 +1120,13 @@ int launch_mlp_eval(const float* src, int stride, int64_t n, bool exact, float4*
     a.bound = 0.f;
     a.stats = nullptr;
     a.eval_out = out;
+    a.stall_test = 0u;
     if (exact) {
         k_shade_exact<<<exact_grid(n_sm, blocks), kExactThreads, 0, stream>>>(a);
     } else {
         const int grid = mlp_grid(n_sm, blocks);
         if (grid < 0) return -1;
-        k_shade_mlp<<<grid, kMlpThreads, mlp_smem_bytes(a.nl, a.samples), stream>>>(a);
+        k_shade_mlp<<<grid, kMlpThreads, mlp_smem_bytes(), stream>>>(a);
     }
     return cudaGetLastError() == cudaSuccess ? 3 : -1;
 }

@@ -381,3 +381,32 @@ def config_many_lights(n_lon=1024, n_lat=512, width=1920, height=1080, n_lights=
     rig_random (directions uniform on the sphere, intensity Exp(1)/n * 255, colours uniform)."""
     sc = uv_sphere(n_lon, n_lat, seed=seed, flat=False, vertex_albedo=True)
     return sc.with_view(width=width, height=height, lights=rig_random(n_lights, light_seed), **CAMERA)
+
+
+def batch_workload(seed=3, n_frames=256, n_soups=16):
+    """The uneven batch: icospheres L2-L7 and seeded soups of 1k-500k triangles (log-uniform sizes);
+    each frame picks a mesh uniformly, a resolution from {256x256, 640x480, 1280x720, 1920x1080},
+    random rx/ry and a 1-8 light rig. Returns (meshes, frames); a frame is (mesh index, width,
+    height, angles, lights)."""
+    rng = np.random.default_rng(seed)
+    meshes = [icosphere(l) for l in range(2, 8)]
+    for k in range(n_soups):
+        n = int(round(float(det_exp(np.log(1000.0) + (np.log(500000.0) - np.log(1000.0)) * rng.random()))))
+        meshes.append(soup(n, 1280, 720, seed=1000 + k))
+    sizes = [(256, 256), (640, 480), (1280, 720), (1920, 1080)]
+    frames = []
+    for i in range(n_frames):
+        mi = int(rng.integers(len(meshes)))
+        W, H = sizes[int(rng.integers(4))]
+        nl = int(rng.integers(1, 9))
+        angles = (float(rng.uniform(-np.pi, np.pi)), float(rng.uniform(-np.pi, np.pi)), 0.0)
+        frames.append((mi, W, H, angles, rig_random(nl, seed=10_000 + i)))
+    return meshes, frames
+
+
+def batch_frame_scene(meshes, frame):
+    """The Scene one batch frame draws (60 deg / 0.1 / 100 projection)."""
+    mi, W, H, angles, lights = frame
+    return meshes[mi].with_view(width=W, height=H, angles=angles, lights=lights, fovy_deg=60.0, z_near=0.1,
+                                z_far=100.0)
+

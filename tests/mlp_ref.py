@@ -6,7 +6,8 @@ import numpy as np
 
 HEADER = struct.Struct("<4s7IQff")  # magic, version, n_in, n_hidden, n_out, n_freq, n_lights, reserved,
                                     # lights_hash, out_scale, train_loss
-N_IN, N_HID, N_OUT, N_FREQ = 103, 64, 3, 16  # N_IN counts the constant-1 feature
+N_IN, N_HID, N_OUT, N_FREQ = 55, 64, 3, 8  # N_IN counts the constant-1 feature
+VERSION = 2
 
 
 def bf16_round(a):
@@ -21,7 +22,7 @@ def bf16_bits(a):
 
 
 def features(n, alb):
-    """(m, 103): sin / cos(f * pi * n_c) for c in xyz, f = 1..16 (pairs), then n, albedo and 1."""
+    """(m, 55): sin / cos(f * pi * n_c) for c in xyz, f = 1..8 (pairs), then n, albedo and 1."""
     n = np.asarray(n, np.float64)
     f = np.arange(1, N_FREQ + 1, dtype=np.float64)
     cols = []
@@ -44,13 +45,13 @@ def random_weights(seed, scale=12.0):
 
 
 def make_blob(w, n_lights=0, lights_hash=0, loss=0.0):
-    head = HEADER.pack(b"RMLP", 1, N_IN, N_HID, N_OUT, N_FREQ, n_lights, 0, lights_hash, float(w["scale"]), loss)
+    head = HEADER.pack(b"RMLP", VERSION, N_IN, N_HID, N_OUT, N_FREQ, n_lights, 0, lights_hash, float(w["scale"]), loss)
     return head + b"".join([bf16_bits(w["w1"]).tobytes(), bf16_bits(w["w2"]).tobytes(), bf16_bits(w["w3"]).tobytes()])
 
 
 def parse_blob(blob):
     h = HEADER.unpack_from(blob, 0)
-    assert h[0] == b"RMLP" and h[1] == 1 and h[2] == N_IN
+    assert h[0] == b"RMLP" and h[1] == VERSION and h[2] == N_IN
     off = HEADER.size
 
     def take(count):

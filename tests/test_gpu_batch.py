@@ -91,6 +91,7 @@ def test_autotune_keeps_results_exact(port):
             frames, keep = make_batch(torch, r, n=8, seed=11)
             best = r.autotune(frames, lanes=4, repeats=1)
             assert best["tile"] in (8, 16, 32) and best["row_chunk"] in (4, 8, 32)
+            assert best["tile_threads"] in (64, 128, 256, 512)
             assert r.get_option(abi.OPT_TILE_SIZE) == best["tile"]
             reset_outputs(torch, keep)
             r.draw_batch(frames, lanes=4, graph=True)

@@ -132,3 +132,28 @@ def test_cli_rejects_bad_arguments(tmp_path):
     exe = _build.cli_path()
     r = subprocess.run([exe, "-x", "100"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "lights" in r.stderr
+
+
+def test_cli_flat_projection_and_light_scale(port, tmp_path):
+    """--flat shades with face normals computed in the path; --fovy/--near/--far replace the
+    reference's hard-coded 45 deg / 0.1 / 6 projection (geometry.cpp:30); --light-scale multiplies
+    every light's intensity as it is loaded."""
+    sc = S.icosphere(3).with_view(width=200, height=150, angles=(0.3, 0.4, 0.0), fovy_deg=60.0, z_near=0.5,
+                                  z_far=50.0)
+    write_obj(tmp_path / "m.obj", sc)
+    write_lights(tmp_path / "l.csv", sc.lights)
+    run_cli(["-l", "l.csv", "-o", "m.obj", "--mats-dir", str(tmp_path) + "/", "-x", "200", "-y", "150",
+             "--rx", "0.3", "--ry", "0.4", "--flat", "--fovy", "60", "--near", "0.5", "--far", "50",
+             "--light-scale", "2", "--out", str(tmp_path)], tmp_path)
+    loaded = abi.obj_load(str(tmp_path / "m.obj"), str(tmp_path) + "/")
+    lights = np.asarray(sc.lights, np.float32).copy()
+    lights[:, 3] *= np.float32(2.0)
+    sc2 = S.Scene("obj", loaded["pos"], loaded["tris"], loaded["nrm"], loaded["uv"], loaded["kd"], lights,
+                  width=200, height=150, angles=(np.float32(0.3), np.float32(0.4), 0.0), fovy_deg=60.0, z_near=0.5,
+                  z_far=50.0)
+    cam, nm, l7, _ = abi.scene_frame_inputs(sc2)
+    of, od, _, _ = port.draw(sc2, cam, nm, l7, flat=True)
+    assert np.array_equal(read_pnm(tmp_path / "frame.ppm"), of)
+    assert np.array_equal(read_pnm(tmp_path / "depth.pgm")[0], cimg_normalize_u8(od))
+    smooth, _, _, _ = port.draw(sc2, cam, nm, l7)
+    assert not np.array_equal(smooth, of)  # the flag changes the picture

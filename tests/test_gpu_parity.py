@@ -64,13 +64,17 @@ def random_scenes():
 
 
 @pytest.mark.parametrize("idx", range(len(random_scenes())))
-@pytest.mark.parametrize("tile,small_max,row_chunk", [(16, 4096, 4), (8, 1, 4), (32, 65536, 8), (16, 16, 8),
-                                                      (16, 4096, 32), (8, 65536, 32)])
-def test_against_port(renderer, port, idx, tile, small_max, row_chunk):
+@pytest.mark.parametrize("tile,small_max,row_chunk,threads", [
+    (16, 4096, 4, 0), (8, 1, 4, 0), (32, 65536, 8, 0), (16, 16, 8, 0), (16, 4096, 32, 0), (8, 65536, 32, 0),
+    (16, 1, 32, 64), (16, 16, 32, 128), (32, 1, 32, 128), (32, 16, 32, 512)])
+def test_against_port(renderer, port, idx, tile, small_max, row_chunk, threads):
+    """Every tile size, path split, row chunk and number of threads per tile (the tile raster's
+    pixels per thread) gives the port's depth, ids and fragment counts."""
     sc = random_scenes()[idx]
     renderer.set_option(abi.OPT_TILE_SIZE, tile)
     renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, small_max)
     renderer.set_option(abi.OPT_ROW_CHUNK, row_chunk)
+    renderer.set_option(abi.OPT_TILE_THREADS, threads)
     try:
         cam, nm, lights, _ = abi.scene_frame_inputs(sc)
         out = gpu_draw(renderer, sc, cam, nm, lights)
@@ -83,6 +87,7 @@ def test_against_port(renderer, port, idx, tile, small_max, row_chunk):
         renderer.set_option(abi.OPT_TILE_SIZE, 16)
         renderer.set_option(abi.OPT_SMALL_MAX_PIXELS, 4096)
         renderer.set_option(abi.OPT_ROW_CHUNK, 32)
+        renderer.set_option(abi.OPT_TILE_THREADS, 0)
 
 
 def test_read_modify_write_buffers(renderer, port):
@@ -338,3 +343,46 @@ def test_registered_host_buffers_used_in_place(renderer, port):
     fp, dp, _, _ = port.draw(sc, cam, nm, lights, frame0, depth0)
     assert np.array_equal(bits(d), bits(dp))
     assert np.abs(f.astype(int) - fp).max() <= RGB_TOL
+
+
+def face_normal_scene(sc):
+    """The scene with per-face normals cross(p1 - p0, p2 - p0) (float32, no fused operations) as
+    its vertex normals: what --flat shades with."""
+    p, t = np.asarray(sc.pos, np.float32), np.asarray(sc.tris)
+    a, b = p[t[:, 1]] - p[t[:, 0]], p[t[:, 2]] - p[t[:, 0]]
+    fn = np.stack([a[:, 1] * b[:, 2] - b[:, 1] * a[:, 2], a[:, 2] * b[:, 0] - b[:, 2] * a[:, 0],
+                   a[:, 0] * b[:, 1] - b[:, 0] * a[:, 1]], axis=1).astype(np.float32)
+    tris = t.copy()
+    tris[:, 3:6] = np.arange(t.shape[0], dtype=np.int32)[:, None]
+    return sc.with_view(nrm=fn, tris=tris)
+
+
+FLAT_SCENES = {
+    "icosphere4": lambda: S.config_icosphere_small(),
+    "smooth_sphere": lambda: S.uv_sphere(160, 80, seed=7, flat=False).with_view(
+        width=400, height=300, fovy_deg=60.0, z_near=0.1, z_far=100.0, angles=(0.3, 1.1, 0.0)),
+    "soup_cw": lambda: S.soup(8000, 320, 240, seed=77, area_range=(0.5, 3000.0)).with_view(wind_clockwise=True),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FLAT_SCENES))
+@pytest.mark.parametrize("clear", [True, False])
+def test_flat_shading_matches_port(renderer, port, name, clear):
+    """RAST_FLAT (--flat): face normals computed in the path, against the port's flat mode and
+    against the port drawing the same mesh with per-face normals given as its vertex normals."""
+    sc = FLAT_SCENES[name]()
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    rng = np.random.default_rng(12)
+    frame0 = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
+    depth0 = rng.uniform(-1.0, 1.5, (sc.height, sc.width)).astype(np.float32)
+    renderer.upload_scene_mesh(sc)
+    renderer.set_lights(lights)
+    flags = flags_of(sc, clear) | abi.FLAT
+    out = renderer.draw(cam, nm, sc.width, sc.height, flags, None if clear else frame0.copy(),
+                        None if clear else depth0.copy(), want_ids=True)
+    f0, d0 = (None, None) if clear else (frame0, depth0)
+    fp, dp, ip, _ = port.draw(sc, cam, nm, lights, f0, d0, flat=True)
+    assert_parity(out, fp, dp, ip)
+    assert np.array_equal(out[0], fp)
+    ff, df, _, _ = port.draw(face_normal_scene(sc), cam, nm, lights, f0, d0)
+    assert np.array_equal(bits(df), bits(dp)) and np.array_equal(ff, fp)

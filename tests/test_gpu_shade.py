@@ -179,11 +179,11 @@ def test_exact_eval_matches_oracle_shade(rnd, port):
 
 @pytest.fixture(scope="module")
 def trained(rnd):
-    """A learned shader for a 256-light rig, trained on 1M samples."""
+    """A learned shader for a 256-light rig, trained on 4M samples for 24 epochs."""
     sc = small_many_lights(256, 640, 480, (256, 128))
     _, _, lights, _ = abi.scene_frame_inputs(sc)
     rnd.set_lights(lights)
-    stats = rnd.mlp_train(samples=1 << 20, epochs=24, seed=3)
+    stats = rnd.mlp_train(samples=4 << 20, epochs=24, seed=3)
     return sc, lights, stats, rnd.mlp_save()
 
 
@@ -312,3 +312,28 @@ def test_learned_in_place_pinned(rnd, trained):
     assert np.array_equal(bits(d), bits(d0))
     assert np.array_equal(i, i0)
     assert np.array_equal(f, f0)
+
+
+def test_learned_shader_wait_timeout_recovers(rnd, trained):
+    """The bounded tensor-core waits: with the test-only stall option the first MMA wait of every
+    CTA gives up (it polls an mbarrier nothing arrives on). Each CTA then waits for its MMA in
+    flight with the full bound, frees its tensor memory and returns; the draw reports
+    RAST_ERR_TIMEOUT, and the context draws the same frame as before once the option is off."""
+    sc, lights, _, blob = trained
+    rnd.mlp_load(blob)
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
+    try:
+        f0, d0, i0 = rnd.draw_scene(sc, clear=True)
+        rnd.set_option(abi.OPT_TEST_SHADE_STALL, 1)
+        with pytest.raises(abi.RastError) as err:
+            rnd.draw_scene(sc, clear=True)
+        assert err.value.status == 7, str(err.value)  # RAST_ERR_TIMEOUT
+        rnd.set_option(abi.OPT_TEST_SHADE_STALL, 0)
+        for _ in range(2):
+            f, d, i = rnd.draw_scene(sc, clear=True)
+            assert np.array_equal(bits(d), bits(d0))
+            assert np.array_equal(i, i0)
+            assert np.array_equal(f, f0)
+    finally:
+        rnd.set_option(abi.OPT_TEST_SHADE_STALL, 0)
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)

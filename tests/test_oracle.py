@@ -122,3 +122,18 @@ def test_port_frame_inputs_match_librast_host_code(port):
             assert np.array_equal(bits(mp[k]), bits(ml[k])), k
         li = rng.normal(size=(4, 7)).astype(np.float32)
         assert np.array_equal(bits(port.transform_lights(mp["view"], li)), bits(abi.transform_lights(ml["view"], li)))
+
+
+def test_port_flat_matches_reference_with_face_normals(reference, port):
+    """The port's flat mode equals the reference's draw_frame on the same mesh whose vertex normals
+    are the per-face normals cross(p1 - p0, p2 - p0) (the reference parses --flat but ignores it,
+    so the face normals are given to it as data)."""
+    from test_gpu_parity import face_normal_scene
+    for sc in (S.config_icosphere_small(),
+               S.soup(5000, 300, 200, seed=61, area_range=(0.5, 2000.0)).with_view(wind_clockwise=True),
+               S.config_displaced_sphere(96, 48, 333, 222).with_view(angles=(0.7, -0.4, 1.9))):
+        fr, dr, td = reference.draw(face_normal_scene(sc))
+        m = reference.matrices(sc)
+        fp, dp, _, _ = port.draw(sc, m["camera"], m["normal"], oracle.lights_with_dirs(sc, td), flat=True)
+        assert np.array_equal(bits(dp), bits(dr))
+        assert np.array_equal(fp, fr)

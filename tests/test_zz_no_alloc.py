@@ -31,6 +31,26 @@ def _call(lib, torch, dev, cam, nm, W, H, flags, rgb, depth, ids):
                                  torch.cuda.current_stream().cuda_stream or None)
 
 
+def _screen_covering(n, seed, W=1920, H=1080):
+    """n triangles that each cover the whole 1920x1080 frame (one tile-bin entry per 16x16 tile
+    each), at seeded depths, all facing the camera."""
+    rng = np.random.default_rng(seed)
+    z = rng.uniform(-1.0, 1.0, n).astype(np.float32)
+    pos = np.zeros((3 * n, 3), np.float32)
+    pos[0::3] = np.stack([np.full(n, -20.0), np.full(n, -20.0), z], 1)
+    pos[1::3] = np.stack([np.full(n, 20.0), np.full(n, -20.0), z], 1)
+    pos[2::3] = np.stack([np.zeros(n), np.full(n, 20.0), z], 1)
+    tris = np.zeros((n, 10), np.int32)
+    tris[:, 0:3] = np.arange(3 * n, dtype=np.int32).reshape(n, 3)
+    tris[:, 3:6] = 0
+    tris[:, 6:9] = -1
+    nrm = np.array([[0.0, 0.0, 1.0]], np.float32)
+    lights = np.array([[1, -1, -1, 255, 1, 1, 1]], np.float32)
+    return S.Scene("screen_covering", pos, tris, nrm, np.zeros((0, 2), np.float32),
+                   np.array([[0.8, 0.6, 0.4]], np.float32), lights, width=W, height=H, fovy_deg=60.0,
+                   z_near=0.1, z_far=100.0)
+
+
 def _device_mesh(torch, sc, lights):
     def d(a, dt):
         return torch.from_numpy(np.ascontiguousarray(a, dt)).to("cuda")
@@ -38,12 +58,13 @@ def _device_mesh(torch, sc, lights):
             "kd": d(sc.kd, np.float32), "lights": d(lights, np.float32)}
 
 
-@pytest.mark.parametrize("which", ["icosphere", "soup"])
+@pytest.mark.parametrize("which", ["icosphere", "soup", "screen_covering"])
 def test_noalloc_equals_context_draw_on_consecutive_calls(which):
     torch = pytest.importorskip("torch")
     lib = abi.load()
-    sc = S.config_icosphere_small() if which == "icosphere" else \
-        S.soup(20000, 640, 360, seed=41, area_range=(0.5, 3000.0))
+    sc = {"icosphere": S.config_icosphere_small,
+          "soup": lambda: S.soup(20000, 640, 360, seed=41, area_range=(0.5, 3000.0)),
+          "screen_covering": lambda: _screen_covering(40, seed=5)}[which]()
     W, H = sc.width, sc.height
     cam, nm, lights, _ = abi.scene_frame_inputs(sc)
     rng = np.random.default_rng(7)
@@ -98,3 +119,31 @@ def test_noalloc_refuses_what_does_not_fit_and_bad_indices():
     dep = torch.ones(sc.width * sc.height, dtype=torch.float32, device="cuda")
     st = _call(lib, torch, dev, cam, nm, sc.width, sc.height, abi.CLEAR, rgb, dep, None)
     assert st == 2
+
+
+def test_noalloc_bin_overflow_leaves_the_buffers_unchanged():
+    """Thousands of screen-sized triangles need more tile-bin entries than the fixed array holds:
+    the call reports RAST_ERR_BIN_OVERFLOW and the caller's frame, depth and ids are untouched, in
+    both modes; the next call that fits draws normally."""
+    torch = pytest.importorskip("torch")
+    lib = abi.load()
+    sc = _screen_covering(4000, seed=6)
+    W, H = sc.width, sc.height
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    dev = _device_mesh(torch, sc, lights)
+    rng = np.random.default_rng(8)
+    init_rgb = torch.from_numpy(rng.integers(0, 256, 3 * W * H, dtype=np.uint8)).to("cuda")
+    init_depth = torch.from_numpy(rng.uniform(-1.0, 2.0, W * H).astype(np.float32)).to("cuda")
+    init_ids = torch.from_numpy(rng.integers(0, 1 << 30, W * H, dtype=np.int32)).to("cuda")
+    for flags in (abi.CLEAR, 0):
+        rgb, dep, ids = init_rgb.clone(), init_depth.clone(), init_ids.clone()
+        st = _call(lib, torch, dev, cam, nm, W, H, flags, rgb, dep, ids)
+        assert st == 6, (st, lib.rast_last_error(None).decode())
+        torch.cuda.synchronize()
+        assert torch.equal(rgb, init_rgb) and torch.equal(dep, init_depth) and torch.equal(ids, init_ids)
+    small = _screen_covering(8, seed=6)
+    dev = _device_mesh(torch, small, lights)
+    rgb, dep = init_rgb.clone(), init_depth.clone()
+    assert _call(lib, torch, dev, cam, nm, W, H, abi.CLEAR, rgb, dep, None) == 0
+    torch.cuda.synchronize()
+    assert not torch.equal(dep, init_depth)
