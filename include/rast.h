@@ -318,6 +318,16 @@ rast_status rast_mlp_load(rast_ctx* ctx, const void* buf, size_t size);
 rast_status rast_mlp_eval(rast_ctx* ctx, const float* normals3, const float* albedo3, int64_t n, int32_t exact,
                           float* out3);
 
+/* Benchmark helper (no counterpart in the reference): runs the deferred shading pass of the
+ * context's last draw (made with RAST_SHADER_EXACT_DEFERRED or RAST_SHADER_LEARNED) `repeats` more
+ * times, back to back on the context's stream, over the same fragment records and tiles, and
+ * returns the mean time of one pass in microseconds (CUDA events around all of them; each pass is
+ * launched as in a draw, while its predecessor finishes). The passes rewrite the same colours into
+ * that draw's frame buffer, which must still exist (use it after rast_draw_device); the learned
+ * shader's counters (rast_get_shade_stats) then hold the sums over the passes. Waits for the
+ * stream. RAST_ERR_INVALID_ARG when the last draw did not shade in a separate pass. */
+rast_status rast_time_shading(rast_ctx* ctx, int32_t repeats, float* us_per_pass);
+
 /* Learned-shader counters of the last draw (waits for the stream): [0] tiles, [1] tiles shaded
  * exactly after their check failed, [2] fragments checked, [3] largest checked channel error in
  * millionths of 1/255. */

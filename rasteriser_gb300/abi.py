@@ -95,6 +95,7 @@ SIGNATURES = {
     "rast_mlp_save": (C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "rast_mlp_load": (C.c_int, [_P, _P, C.c_size_t]),
     "rast_mlp_eval": (C.c_int, [_P, _F, _F, _I64, _I32, _F]),
+    "rast_time_shading": (C.c_int, [_P, _I32, _F]),
     "rast_get_shade_stats": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "rast_obj_load": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(_P)]),
     "rast_obj_free": (None, [_P]),
@@ -467,6 +468,12 @@ class Renderer:
         self._check(self.lib.rast_spin(self.h, C.byref(d), frame.ctypes.data_as(C.POINTER(C.c_uint8)), _fp(depth),
                                        C.byref(sec)), "rast_spin")
         return frame, depth, sec.value
+
+    def time_shading(self, repeats=200):
+        """Mean microseconds of one more run of the last draw's deferred shading pass (back to back)."""
+        v = C.c_float()
+        self._check(self.lib.rast_time_shading(self.h, repeats, C.byref(v)), "rast_time_shading")
+        return float(v.value)
 
     def shade_stats(self):
         out = (C.c_uint64 * 4)()

@@ -152,6 +152,13 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     const int n = rast::launch_draw(c->mesh, s, p, c->stream, c->timing ? c->ev : nullptr);
     c->ev_recorded = c->timing;
     if (n < 0) return cuda_fail(c, cudaGetLastError(), "launch draw");
+    c->replay_valid = p.shader != RAST_SHADER_EXACT;
+    if (c->replay_valid) {
+        c->replay_s = s;
+        c->replay_p = p;
+        c->replay_p.before_resolve = nullptr;
+        c->replay_blocks = (npx + rast::kShadeBlock - 1) / rast::kShadeBlock;
+    }
     c->last_launches = (uint64_t)n;
     c->keys_armed = true;  // the resolve pass re-arms every key it reads
     c->keys_clear = clear;
@@ -538,6 +545,29 @@ rast_status rast_sync(rast_ctx* c) {
     const rast_status st = collect_status(c);
     const rast_status sb = c->lanes.empty() ? RAST_OK : collect_batch_status(c);
     return st != RAST_OK ? st : sb;
+}
+
+rast_status rast_time_shading(rast_ctx* c, int32_t repeats, float* us_per_pass) {
+    if (!c || !us_per_pass || repeats < 1 || repeats > 100000) return RAST_ERR_INVALID_ARG;
+    if (!c->replay_valid) return fail(c, RAST_ERR_INVALID_ARG, "the last draw did not shade in a separate pass");
+    DeviceGuard g(c->device);
+    cudaEvent_t e0, e1;
+    RAST_CUDA(c, cudaEventCreate(&e0));
+    RAST_CUDA(c, cudaEventCreate(&e1));
+    rast_status st = RAST_OK;
+    float ms = 0.f;
+    if (cudaEventRecord(e0, c->stream) != cudaSuccess) st = cuda_fail(c, cudaGetLastError(), "event");
+    for (int32_t i = 0; st == RAST_OK && i < repeats; ++i)
+        if (rast::launch_shade(c->replay_s, c->replay_p, c->replay_blocks, c->stream) < 0)
+            st = cuda_fail(c, cudaGetLastError(), "shading pass");
+    if (st == RAST_OK && (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+        st = cuda_fail(c, cudaGetLastError(), "timing");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != RAST_OK) return st;
+    *us_per_pass = 1000.f * ms / (float)repeats;
+    return collect_status(c);
 }
 
 rast_status rast_get_stats(rast_ctx* c, uint64_t out[8]) {

@@ -104,6 +104,11 @@ struct rast_ctx {
     int32_t mlp_samples = 2;      // RAST_OPT_MLP_SAMPLES
     int32_t mlp_bound_milli = 500;  // RAST_OPT_MLP_BOUND_MILLI
     bool test_shade_stall = false;  // RAST_OPT_TEST_SHADE_STALL
+    // the last draw's deferred shading pass, for rast_time_shading
+    bool replay_valid = false;
+    rast::FrameScratch replay_s;
+    rast::DrawParams replay_p;
+    int64_t replay_blocks = 0;
     DevBuf gbuf, gbuf_count, shade_index, shade_stats;
     DevBuf view_mm;  // rast_depth_to_u8: the depth range
 

@@ -374,7 +374,7 @@ struct SlotMisc {
     unsigned long long mbar;          // MMA completion
     uint32_t fail[2];                 // by tile parity: a checked row exceeded the bound
     float rec[kMaxSamples][4];        // the checked rows' normals (xyz), written by their threads
-    float sum[kMaxSamples][4];        // their light sums sum_l (I c)_l max(0, n . -dir_l) (warp s)
+    float part[4][4 * kMaxSamples];   // per warp: partial light sums of the checked rows (3s + c)
 };
 struct MlpMisc {
     unsigned long long mbar_w;        // the weights' bulk copy
@@ -525,44 +525,67 @@ __device__ __forceinline__ void stage_lights_soa(const float* lights, int n, flo
     }
 }
 
-// The light sum of checked row s of a tile, by one warp: lanes split the lights, then a butterfly
-// over the lanes. The check only estimates the error (it never produces a colour), so it sums
-// sum_l (I c)_l * max(0, n . -dir_l) with fused multiply-adds; albedo and 1/pi are applied by the
-// checked row itself. Lights from the shared table when it holds them, else from global memory.
-__device__ __forceinline__ void check_sum(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int s, int lane) {
-    const float nx = S.rec[s][0], ny = S.rec[s][1], nz = S.rec[s][2];
-    float sr = 0.f, sg = 0.f, sb = 0.f;
-    if (L) {
-#pragma unroll 4
-        for (int l = lane; l < a.nl; l += 32) {
-            const float4 A = L->dirI[l];
-            const float2 B = L->gb[l];
-            const float m = fmaxf(fmaf(nz, A.z, fmaf(ny, A.y, nx * A.x)), 0.f);
-            sr = fmaf(A.w, m, sr);
-            sg = fmaf(B.x, m, sg);
-            sb = fmaf(B.y, m, sb);
-        }
-    } else {
-        for (int l = lane; l < a.nl; l += 32) {
-            const float* P = a.lights + 7 * (int64_t)l;
-            const float I = __ldg(P + 3);
-            const float m = fmaxf(fmaf(nz, -__ldg(P + 2), fmaf(ny, -__ldg(P + 1), nx * -__ldg(P))), 0.f);
-            sr = fmaf(I * __ldg(P + 4), m, sr);
-            sg = fmaf(I * __ldg(P + 5), m, sg);
-            sb = fmaf(I * __ldg(P + 6), m, sb);
+// Sums V values over the 32 lanes by halving: at each level a lane keeps half of its values and
+// adds its partner's copy of them. Returns, in lanes with (lane & (32/V - 1)) == 0, the total of
+// value lane / (32/V).
+template <int V>
+__device__ __forceinline__ float halving_sum(float (&v)[V], int lane) {
+#pragma unroll
+    for (int h = V / 2, o = 16; h >= 1; h >>= 1, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const float mine = up ? v[i + h] : v[i], other = up ? v[i] : v[i + h];
+            v[i] = mine + __shfl_xor_sync(kFull, other, o);
         }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        sr += __shfl_xor_sync(kFull, sr, o);
-        sg += __shfl_xor_sync(kFull, sg, o);
-        sb += __shfl_xor_sync(kFull, sb, o);
+    for (int o = 16 / V; o >= 1; o >>= 1) v[0] += __shfl_xor_sync(kFull, v[0], o);
+    return v[0];
+}
+
+// This thread's share of the light sums of a tile's checked rows: the slot's 128 threads split
+// the lights, each warp sums its lanes' shares (halving_sum) into S.part[warp]. The check only
+// estimates the error (it never produces a colour), so it sums sum_l (I c)_l * max(0, n . -dir_l)
+// with fused multiply-adds; albedo and 1/pi are applied by the checked row itself. Lights come
+// from the shared table when it holds them, else from global memory.
+template <int NS>
+__device__ __forceinline__ void check_part(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int row) {
+    constexpr int V = NS <= 2 ? 8 : 16;
+    float v[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) v[i] = 0.f;
+    float nx[NS], ny[NS], nz[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        nx[s] = S.rec[s][0];
+        ny[s] = S.rec[s][1];
+        nz[s] = S.rec[s][2];
     }
-    if (lane == 0) {
-        S.sum[s][0] = sr;
-        S.sum[s][1] = sg;
-        S.sum[s][2] = sb;
+    for (int l = row; l < a.nl; l += kSlotThreads) {
+        float4 A;
+        float2 B;
+        if (L) {
+            A = L->dirI[l];
+            B = L->gb[l];
+        } else {
+            const float* P = a.lights + 7 * (int64_t)l;
+            const float I = __ldg(P + 3);
+            A = make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4));
+            B = make_float2(I * __ldg(P + 5), I * __ldg(P + 6));
+        }
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const float m = fmaxf(fmaf(nz[s], A.z, fmaf(ny[s], A.y, nx[s] * A.x)), 0.f);
+            v[3 * s] = fmaf(A.w, m, v[3 * s]);
+            v[3 * s + 1] = fmaf(B.x, m, v[3 * s + 1]);
+            v[3 * s + 2] = fmaf(B.y, m, v[3 * s + 2]);
+        }
     }
+    const int lane = row & 31;
+    const float total = halving_sum<V>(v, lane);
+    const int j = lane / (32 / V);
+    if ((lane & (32 / V - 1)) == 0 && j < 3 * NS) S.part[row >> 5][j] = total;
 }
 
 __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
@@ -630,6 +653,18 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     uint32_t n_tile = 0, n_fallback = 0;
     float max_err = 0.f;
     uint32_t k = 0;  // tiles this slot shaded
+    // The previous tile's record of this row, for its exact reshading when its check failed. The
+    // verdict is read after the next slot barrier, which orders it after the checked rows' writes.
+    const bool checking = n_samples > 0;
+    float3 p_nv = make_float3(0.f, 0.f, 0.f), p_alb = p_nv;
+    uint32_t p_pix = 0;
+    bool p_valid = false;
+    auto reshade_previous = [&]() {
+        if (S.fail[(k - 1u) & 1u]) {  // the same in every thread of the slot
+            if (row == 0) ++n_fallback;
+            if (p_valid) write_rgb(a.rgb, a.npx, p_pix, shade_lights(a.lights, a.nl, p_nv, p_alb));
+        }
+    };
 
     while (!weights_pending && t < n_tiles) {
         const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
@@ -650,18 +685,24 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         if (!__any_sync(kFull, failed)) store_features(nv, alb, a_mine, (uint32_t)row);
         a_written();
         if (slot_sync_or(slot, failed)) break;
-        if (row == 0) S.fail[(k + 1u) & 1u] = 0u;  // every thread read it before this barrier
 
         // layer 1: D = X (128 x K) * W1^T
         if (row == 0) issue_layer(d_cols, a_mma, sW1, kMlpHid, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-        // the checked rows' light sums (warp w takes row w), while the MMAs run
-        if (wq < n_samples) check_sum(a, L, S, wq, lane);
+        // while the MMAs run: the previous tile's fallback, and the checked rows' light sums
+        if (checking) {
+            if (k > 0u) reshade_previous();
+            if (n_samples <= 2) check_part<2>(a, L, S, row);
+            else check_part<4>(a, L, S, row);
+        }
         failed |= !mbar_wait(mbar_first, phase, tries_first);
         phase ^= 1u;
         tc_fence_after();
         if (!__any_sync(kFull, failed)) hidden_epilogue(d_lane, a_mine, (uint32_t)row);  // h1 over the features
         a_written();
         if (slot_sync_or(slot, failed)) break;
+        // every thread read the previous tile's verdict before this barrier; the next tile's
+        // checked rows write it after two more
+        if (row == 0) S.fail[(k + 1u) & 1u] = 0u;
 
         // layer 2: D = H1 (128 x 64) * W2^T (layer 1's accumulators were read)
         if (row == 0) issue_layer(d_cols, a_mma, sW2, kMlpHid, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
@@ -710,22 +751,27 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
             if (valid)
                 write_rgb(a.rgb, a.npx, pix,
                           __float2uint_rz(radc.x) | (__float2uint_rz(radc.y) << 8) | (__float2uint_rz(radc.z) << 16));
-            if (n_samples > 0) {
-                // the checked rows against their light sums (written before two slot barriers); a
-                // failing tile is shaded again, exactly, by all its rows
+            if (checking) {
+                // the checked rows against their light sums (the warps' parts, written before two
+                // slot barriers); a failing tile is shaded again, exactly, by all its rows after
+                // the next slot barrier
                 if (my_sample >= 0 && valid) {
-                    const float er = fabsf(radc.x - fminf(S.sum[my_sample][0] * alb.x * kOneOverPi, 255.f));
-                    const float eg = fabsf(radc.y - fminf(S.sum[my_sample][1] * alb.y * kOneOverPi, 255.f));
-                    const float eb = fabsf(radc.z - fminf(S.sum[my_sample][2] * alb.z * kOneOverPi, 255.f));
+                    float sum[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        sum[c] = (S.part[0][3 * my_sample + c] + S.part[1][3 * my_sample + c]) +
+                                 (S.part[2][3 * my_sample + c] + S.part[3][3 * my_sample + c]);
+                    const float er = fabsf(radc.x - fminf(sum[0] * alb.x * kOneOverPi, 255.f));
+                    const float eg = fabsf(radc.y - fminf(sum[1] * alb.y * kOneOverPi, 255.f));
+                    const float eb = fabsf(radc.z - fminf(sum[2] * alb.z * kOneOverPi, 255.f));
                     const float err = fmaxf(er, fmaxf(eg, eb));
                     max_err = fmaxf(max_err, err);
                     if (err > a.bound) S.fail[k & 1u] = 1u;
                 }
-                slot_sync(slot);
-                if (S.fail[k & 1u]) {  // the same in every thread of the slot
-                    if (row == 0) ++n_fallback;
-                    if ((uint32_t)row < count) write_rgb(a.rgb, a.npx, pix, shade_lights(a.lights, a.nl, nv, alb));
-                }
+                p_nv = nv;
+                p_alb = alb;
+                p_pix = pix;
+                p_valid = valid;
             }
             ++n_tile;
         }
@@ -735,6 +781,10 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         g0 = g0n;
         g1 = g1n;
     }
+
+    // the last tile's verdict (every thread of the slot reaches this barrier: the loop ends at the
+    // same point in all of them)
+    if (checking && !weights_pending && !slot_sync_or(slot, failed) && k > 0u) reshade_previous();
 
     if (failed) {
         // the weights' copy or an MMA did not complete in time: record it, give the pending one

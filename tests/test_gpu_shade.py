@@ -337,3 +337,32 @@ def test_learned_shader_wait_timeout_recovers(rnd, trained):
     finally:
         rnd.set_option(abi.OPT_TEST_SHADE_STALL, 0)
         rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+
+
+def test_time_shading_replays_the_same_pass(rnd, port):
+    """rast_time_shading re-runs the last draw's deferred shading pass: positive times, and the
+    frame it rewrites is the same; after an exact (fused) draw there is no pass to time."""
+    torch = pytest.importorskip("torch")
+    sc = small_many_lights(32)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    rnd.upload_scene_mesh(sc)
+    rnd.set_lights(lights)
+    W, H = sc.width, sc.height
+    rgb = torch.empty(3 * W * H, dtype=torch.uint8, device="cuda")
+    dep = torch.empty(W * H, dtype=torch.float32, device="cuda")
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT_DEFERRED)
+    try:
+        rnd.draw_device(cam, nm, W, H, abi.CLEAR, rgb.data_ptr(), dep.data_ptr())
+        rnd.sync()
+        first = rgb.cpu().numpy().copy()
+        us = rnd.time_shading(5)
+        assert us > 0.0
+        assert np.array_equal(rgb.cpu().numpy(), first)
+        of, _, _, _ = port.draw(sc, cam, nm, lights)
+        assert np.array_equal(first.reshape(3, H, W), of)
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+    rnd.draw_device(cam, nm, W, H, abi.CLEAR, rgb.data_ptr(), dep.data_ptr())
+    rnd.sync()
+    with pytest.raises(abi.RastError):
+        rnd.time_shading(1)
