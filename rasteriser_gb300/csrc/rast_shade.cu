@@ -329,62 +329,73 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 // ---------------------------------------------------------------------------------------------
 // One CTA per SM with kSlots independent tile slots. A slot is four warps, one thread per row of a
 // 128-record tile; it walks its tiles through the three layers on its own (named barriers), so
-// while one slot waits for its MMAs the others compute features and epilogues. The slots share
-// the weights (B operands, one copy in shared memory) and the light table of the checks. A slot's
-// FP32 accumulators are 64 columns of tensor memory; its A operand (features, then h1, then h2) is
-// either 32 further columns of tensor memory (kATmem) or a [128][K] BF16 matrix in shared memory.
+// while one slot waits for its MMAs the others compute. The slots share the weights (B operands,
+// one copy in shared memory) and the light table of the checks.
 //
-// The layout can be changed at build time (RAST_MLP_SLOTS, RAST_MLP_LD, RAST_MLP_A_TMEM) to
-// measure the alternatives; the defaults are the fastest measured.
+// A slot's tensor memory is 64 columns of FP32 accumulators and two A operands of 32 columns (64
+// BF16 values per row). A tile's features, h1 and h2 alternate between the two operands, so the
+// next tile's features are computed and stored while the current tile's last MMA runs:
+//   features(k) -> A[x]; h1 -> A[1-x]; h2 -> A[x]; features(k+1) -> A[1-x] during layer 3.
+//
+// Tile k is checked during tile k + 1. Its sampled rows put their normal, albedo and output into
+// the slot's check rows (by tile parity). While tile k + 1's first MMA runs, the slot's 128 threads
+// split the lights and each warp sums its part; while the second runs, one warp adds the four
+// parts, compares and records the verdict (the failed tile, or none). The whole slot reads the
+// verdict after the barrier that opens tile k + 2 and shades a failed tile again, exactly, right
+// there; the last two verdicts are read after the loop. The kernel is compiled for each number of
+// checked samples.
+//
+// RAST_MLP_SLOTS (at most 4: 4 x 128 columns fill the tensor memory) can be changed at build time
+// to measure fewer slots; the default is the fastest measured.
 #ifndef RAST_MLP_SLOTS
-#define RAST_MLP_SLOTS 5
-#endif
-#ifndef RAST_MLP_LD
-#define RAST_MLP_LD 4
-#endif
-#ifndef RAST_MLP_A_TMEM
-#define RAST_MLP_A_TMEM 1
+#define RAST_MLP_SLOTS 4
 #endif
 constexpr int kSlots = RAST_MLP_SLOTS;
-constexpr int kLdBatch = RAST_MLP_LD;  // 16-column accumulator loads in flight per wait (1, 2 or 4)
-constexpr bool kATmem = RAST_MLP_A_TMEM != 0;
+constexpr int kLdBatch = 4;        // 16-column accumulator loads in flight per wait
 constexpr int kSlotThreads = 128;  // warp w of a slot reads TMEM lanes 32w..32w+31 (w = warp id mod 4)
 constexpr int kMlpThreads = kSlots * kSlotThreads;
-constexpr uint32_t kSlotCols = 64;                       // a slot's accumulators
-constexpr uint32_t kACols = kMlpIn / 2;                  // a slot's A operand in tensor memory
+constexpr uint32_t kSlotCols = 64;                   // a slot's accumulators
+constexpr uint32_t kACols = kMlpIn / 2;              // one A operand
+constexpr uint32_t kSlotTmem = kSlotCols + 2u * kACols;
 constexpr uint32_t kTmemCols = 512;
-static_assert(kMlpIn == kMlpHid, "one A operand per slot serves every layer");
-static_assert(kSlots * kSlotCols + (kATmem ? kSlots * kACols : 0u) <= kTmemCols, "tensor memory of one SM");
-static_assert(kLdBatch == 1 || kLdBatch == 2 || kLdBatch == 4, "accumulator loads per wait");
-constexpr uint32_t kABytes = kATmem ? 0u : kMlpRows * kMlpIn * 2;  // a slot's A operand in shared memory
-constexpr uint32_t kALbo = kMlpRows * 16;                            // its K-direction core-matrix step
+static_assert(kMlpIn == kMlpHid, "one A operand shape serves every layer");
+static_assert(kSlots >= 1 && kSlots * kSlotTmem <= kTmemCols, "tensor memory of one SM");
 constexpr uint32_t kMaxSamples = 4;
-constexpr int kMlpSmemLights = 512;  // lights staged in shared memory (24 bytes each) for the checks
+constexpr int kMlpSmemLights = 512;  // lights the checks read from shared memory
+constexpr uint32_t kNoTile = 0xFFFFFFFFu;
 
-// Shared memory (bytes): the weights and output scale, the slots' A operands, the light table,
-// then the small block.
+// Shared memory (bytes): the weights and output scale, the lights as given (7 floats each, by bulk
+// copy), the checks' light table made from them, then the small block.
 constexpr uint32_t kSmW1 = 0;
 constexpr uint32_t kSmW2 = kSmW1 + kMlpHid * kMlpIn * 2;
 constexpr uint32_t kSmW3 = kSmW2 + kMlpHid * kMlpHid * 2;
-constexpr uint32_t kSmA = (sizeof(MlpImage) + 1023) / 1024 * 1024;
-constexpr uint32_t kSmLights = kSmA + kSlots * kABytes;
+constexpr uint32_t kSmRaw = (sizeof(MlpImage) + 15) / 16 * 16;
+constexpr uint32_t kSmLights = kSmRaw + 28u * kMlpSmemLights;
 constexpr uint32_t kSmMisc = kSmLights + 24u * kMlpSmemLights;
 
+struct CheckRow {
+    float n[3], alb[3], rad[3];  // the row's normal and albedo, and the learned radiance (clamped)
+    uint32_t valid;
+};
 struct SlotMisc {
-    unsigned long long mbar;          // MMA completion
-    uint32_t fail[2];                 // by tile parity: a checked row exceeded the bound
-    float rec[kMaxSamples][4];        // the checked rows' normals (xyz), written by their threads
-    float part[4][4 * kMaxSamples];   // per warp: partial light sums of the checked rows (3s + c)
+    unsigned long long mbar;                // MMA completion
+    uint32_t verdict[2];                    // by the checked tile's parity: that tile when it failed, else kNoTile
+    CheckRow q[2][kMaxSamples];             // by tile parity: the sampled rows
+    int32_t part[4][3 * kMaxSamples];       // by warp: the warps' light sums (3 s + c), fixed point
 };
 struct MlpMisc {
-    unsigned long long mbar_w;        // the weights' bulk copy
-    unsigned long long mbar_idle;     // nothing arrives on it (the stall test's first wait)
+    unsigned long long mbar_w;     // the weights' bulk copy
+    unsigned long long mbar_idle;  // nothing arrives on it (the stall test's first wait)
+    unsigned long long sums[3];    // the CTA's tiles, fallback tiles and checked rows
+    uint32_t max_err_bits;         // the CTA's largest checked error (a non-negative float's bits)
     uint32_t tmem;
-    uint32_t pad[3];
+    float light_sum;               // sum over the lights of |dir| max_c |I c|: bounds the check sums
+    uint32_t pad;
     SlotMisc slot[kSlots];
 };
 constexpr uint32_t kMlpSmem = kSmMisc + sizeof(MlpMisc);
-static_assert(kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmA % 1024 == 0 && kSmLights % 16 == 0 && kSmMisc % 16 == 0,
+static_assert(kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmRaw % 16 == 0 && kSmLights % 16 == 0 &&
+                  kSmMisc % 16 == 0,
               "operand alignment");
 static_assert(kMlpSmem <= 227 * 1024, "shared memory of one CTA");
 static_assert(sizeof(MlpImage) % 16 == 0, "bulk copy alignment");
@@ -416,82 +427,44 @@ __device__ __forceinline__ void slot_sync(int s) {
     asm volatile("bar.sync %0, %1;" ::"r"(s + 1), "r"(kSlotThreads) : "memory");
 }
 
-// Makes this thread's shared-memory stores visible to the tensor cores' reads (async proxy).
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t x, uint32_t y, uint32_t z, uint32_t w) {
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(x), "r"(y), "r"(z), "r"(w) : "memory");
-}
-
-// Row r's 16-byte chunk j (K elements 8j..8j+7) of a slot's A operand at `base`: the K-major,
-// unswizzled core layout of core_offset().
-__device__ __forceinline__ uint32_t a_chunk(uint32_t base, uint32_t r, uint32_t j) {
-    return base + j * kALbo + (r >> 3) * 128u + (r & 7u) * 16u;
-}
-
-// tcgen05.mma kind::f16, A and B from shared memory (descriptors), D in tensor memory.
-__device__ __forceinline__ void mma_bf16_ss(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                            uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-// One layer's MMAs into the slot's accumulators, A (128 x K) from its operand (tensor memory
-// columns or shared memory) and B (b_rows x K) from the weights; committed to mbar.
+// One layer's MMAs into the slot's accumulators, A (128 x K) from tensor memory and B (b_rows x
+// K) from the weights in shared memory; committed to mbar.
 __device__ __forceinline__ void issue_layer(uint32_t d, uint32_t a, uint32_t b_smem, uint32_t b_rows, int k_steps,
                                             uint32_t idesc, uint32_t mbar) {
     tc_fence_after();
     const uint32_t lbo_b = b_rows * 16u;
-    for (int s = 0; s < k_steps; ++s) {
-        const uint64_t b = mma_desc(b_smem + 2u * s * lbo_b, lbo_b, 128);
-        if constexpr (kATmem) mma_bf16_ta(d, a + 8u * s, b, idesc, s > 0);
-        else mma_bf16_ss(d, mma_desc(a + 2u * s * kALbo, kALbo, 128), b, idesc, s > 0);
-    }
+    for (int s = 0; s < k_steps; ++s)
+        mma_bf16_ta(d, a + 8u * s, mma_desc(b_smem + 2u * s * lbo_b, lbo_b, 128), idesc, s > 0);
     mma_commit(mbar);
 }
 
-// Eight packed pairs (16 K elements) of row r into the slot's A operand at chunk pair j2 (K
-// elements 16 j2 .. 16 j2 + 15): 8 tensor-memory columns of this thread's lane, or two 16-byte
-// shared-memory chunks.
-__device__ __forceinline__ void put_a8(uint32_t a, uint32_t r, uint32_t j2, const uint32_t (&q)[8]) {
-    if constexpr (kATmem) {
-        tmem_st8(a + 8u * j2, q);
-    } else {
-        st_shared_v4(a_chunk(a, r, 2u * j2), q[0], q[1], q[2], q[3]);
-        st_shared_v4(a_chunk(a, r, 2u * j2 + 1u), q[4], q[5], q[6], q[7]);
-    }
-}
-
-// Makes the A operand written by this thread visible to the MMA the slot issues next (before the
-// slot barrier).
+// Makes the A operand this thread wrote (tcgen05.st) visible to the MMA the slot issues after its
+// next barrier, and orders this thread's accumulator reads before that MMA.
 __device__ __forceinline__ void a_written() {
-    if constexpr (kATmem) tmem_wait_st();
-    else fence_async_smem();
+    tmem_wait_st();
     tc_fence_before();
 }
 
-// The features of one row (mlp_feature_pairs' order) into its A operand, 8 pairs at a time.
-__device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t a, uint32_t r) {
+// The features of one row (mlp_feature_pairs' order) into an A operand (this thread's lane of it),
+// 8 pairs (16 K elements) per store.
+__device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t a) {
     static_assert(kMlpFreq == 8, "one 8-pair store per normal component");
     const float comp[3] = {n.x, n.y, n.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         uint32_t q[8];
         fourier_pairs(comp[c], [&](int f, uint32_t p) { q[f] = p; });
-        put_a8(a, r, (uint32_t)c, q);
+        tmem_st8(a + 8u * c, q);
     }
     uint32_t t[8];
     tail_pairs(n, alb, t);
-    put_a8(a, r, 3u, t);
+    tmem_st8(a + 24u, t);
 }
 
-// Epilogue of a hidden layer: row r's 64 accumulators (TMEM columns from d) through ReLU, rounded
-// to BF16, into its A operand (over the consumed features or h1): the next layer's A.
-// kLdBatch 16-column loads are in flight per wait.
-__device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a, uint32_t r) {
+// Epilogue of a hidden layer: this thread's row of 64 accumulators (TMEM columns from d) through
+// ReLU, rounded to BF16, into an A operand: the next layer's A. kLdBatch 16-column loads are in
+// flight per wait.
+__device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a) {
 #pragma unroll
     for (int g = 0; g < kMlpHid / 16; g += kLdBatch) {
         uint32_t v[kLdBatch][16];
@@ -505,9 +478,30 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a, uint32_t
             uint32_t p[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) p[j] = relu_bf16x2(__uint_as_float(v[i][2 * j]), __uint_as_float(v[i][2 * j + 1]));
-            put_a8(a, r, (uint32_t)(g + i), p);
+            tmem_st8(a + 8u * (g + i), p);
         }
     }
+}
+
+// This thread's record of row `row` of tile t, whose descriptor is d (zeros past the tile's count).
+__device__ __forceinline__ void load_record_desc(const ShadeArgs& a, uint32_t t, uint32_t count, uint4 d, int row,
+                                                 float4& g0, float4& g1) {
+    g0 = g1 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((uint32_t)row < count) {
+        const size_t rs = shade_record_slot(a.index, a.n_blocks, d, t, row);
+        g0 = a.gbuf[2 * rs];
+        g1 = a.gbuf[2 * rs + 1];
+    }
+}
+__device__ __forceinline__ void load_record(const ShadeArgs& a, uint32_t t, uint32_t count, int row, float4& g0,
+                                            float4& g1) {
+    const uint4 d = (uint32_t)row < count ? shade_tile_desc(a.index, a.n_blocks, t) : make_uint4(0u, 0u, 0u, 0u);
+    load_record_desc(a, t, count, d, row, g0, g1);
+}
+
+// Records in tile t of n_tiles, from the fragment total.
+__device__ __forceinline__ uint32_t tile_count(uint32_t n_frag, uint32_t n_tiles, uint32_t t) {
+    return t < n_tiles ? min((uint32_t)kShadeTile, n_frag - t * (uint32_t)kShadeTile) : 0u;
 }
 
 // The light table of the checks: dirI[l] = (-dir xyz, I*r), gb[l] = (I*g, I*b).
@@ -516,53 +510,22 @@ struct SmemLights {
     const float2* gb;
 };
 
-__device__ __forceinline__ void stage_lights_soa(const float* lights, int n, float4* dirI, float2* gb) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float* p = lights + 7 * (int64_t)i;
-        const float I = __ldg(p + 3);
-        dirI[i] = make_float4(-__ldg(p), -__ldg(p + 1), -__ldg(p + 2), I * __ldg(p + 4));
-        gb[i] = make_float2(I * __ldg(p + 5), I * __ldg(p + 6));
-    }
-}
-
-// Sums V values over the 32 lanes by halving: at each level a lane keeps half of its values and
-// adds its partner's copy of them. Returns, in lanes with (lane & (32/V - 1)) == 0, the total of
-// value lane / (32/V).
-template <int V>
-__device__ __forceinline__ float halving_sum(float (&v)[V], int lane) {
-#pragma unroll
-    for (int h = V / 2, o = 16; h >= 1; h >>= 1, o >>= 1) {
-        const bool up = (lane & o) != 0;
-#pragma unroll
-        for (int i = 0; i < h; ++i) {
-            const float mine = up ? v[i + h] : v[i], other = up ? v[i] : v[i + h];
-            v[i] = mine + __shfl_xor_sync(kFull, other, o);
-        }
-    }
-#pragma unroll
-    for (int o = 16 / V; o >= 1; o >>= 1) v[0] += __shfl_xor_sync(kFull, v[0], o);
-    return v[0];
-}
-
-// This thread's share of the light sums of a tile's checked rows: the slot's 128 threads split
-// the lights, each warp sums its lanes' shares (halving_sum) into S.part[warp]. The check only
-// estimates the error (it never produces a colour), so it sums sum_l (I c)_l * max(0, n . -dir_l)
-// with fused multiply-adds; albedo and 1/pi are applied by the checked row itself. Lights come
-// from the shared table when it holds them, else from global memory.
+// A thread's part of a tile's check: the slot's 128 threads split the lights (thread `row` takes
+// lights row, row + 128, ...; the two halves take every other one) and sum, for each sampled row
+// q[s] and channel c, (I c)_l * max(0, n . -dir_l) with fused multiply-adds into v[3 s + c]. The sum
+// only estimates the exact shade: it judges the learned colour and is never itself a colour. Lights
+// come from the shared table when it holds them, else from global memory.
 template <int NS>
-__device__ __forceinline__ void check_part(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int row) {
-    constexpr int V = NS <= 2 ? 8 : 16;
-    float v[V];
-#pragma unroll
-    for (int i = 0; i < V; ++i) v[i] = 0.f;
+__device__ __forceinline__ void check_half(const ShadeArgs& a, const SmemLights* L, const CheckRow* q,
+                                           float (&v)[3 * NS], int row, int half) {
     float nx[NS], ny[NS], nz[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
-        nx[s] = S.rec[s][0];
-        ny[s] = S.rec[s][1];
-        nz[s] = S.rec[s][2];
+        nx[s] = q[s].n[0];
+        ny[s] = q[s].n[1];
+        nz[s] = q[s].n[2];
     }
-    for (int l = row; l < a.nl; l += kSlotThreads) {
+    for (int l = row + half * kSlotThreads; l < a.nl; l += 2 * kSlotThreads) {
         float4 A;
         float2 B;
         if (L) {
@@ -582,23 +545,80 @@ __device__ __forceinline__ void check_part(const ShadeArgs& a, const SmemLights*
             v[3 * s + 2] = fmaf(B.y, m, v[3 * s + 2]);
         }
     }
-    const int lane = row & 31;
-    const float total = halving_sum<V>(v, lane);
-    const int j = lane / (32 / V);
-    if ((lane & (32 / V - 1)) == 0 && j < 3 * NS) S.part[row >> 5][j] = total;
 }
 
+// Each warp adds its lanes' sums in fixed point (scale fx: any sum over the lights for a normal of
+// length <= 4 stays below 2^29 in magnitude) and stores them in part[warp][3 s + c].
+template <int NS>
+__device__ __forceinline__ void check_store(const float (&v)[3 * NS], int32_t (*part)[3 * kMaxSamples], float fx,
+                                            int row) {
+    int32_t r[3 * NS];
+#pragma unroll
+    for (int i = 0; i < 3 * NS; ++i) r[i] = __reduce_add_sync(kFull, __float2int_rn(v[i] * fx));
+    if ((row & 31) == 0)
+#pragma unroll
+        for (int i = 0; i < 3 * NS; ++i) part[row >> 5][i] = r[i];
+}
+
+// The verdict of a tile's check, by one warp: lane 3 s + c adds the four warps' parts of sampled row
+// s, channel c, and compares |learned - min(sum * albedo / pi, 255)| with the bound; a sampled
+// normal longer than 4 (outside the fixed-point range) fails the tile. Returns, in every lane,
+// whether a sampled row fails.
+template <int NS>
+__device__ __forceinline__ bool check_verdict(const ShadeArgs& a, const CheckRow* q,
+                                              const int32_t (*part)[3 * kMaxSamples], float fx, int lane,
+                                              float& max_err) {
+    bool bad = false;
+    if (lane < 3 * NS) {
+        const int s = lane / 3, c = lane - 3 * s;
+        if (q[s].valid) {
+            const float nn = fmaf(q[s].n[2], q[s].n[2], fmaf(q[s].n[1], q[s].n[1], q[s].n[0] * q[s].n[0]));
+            if (!(nn <= 16.f)) {
+                bad = true;
+            } else {
+                const int64_t p = ((int64_t)part[0][lane] + part[1][lane]) + ((int64_t)part[2][lane] + part[3][lane]);
+                const float sum = (float)p / fx;
+                const float err = fabsf(q[s].rad[c] - fminf(sum * q[s].alb[c] * kOneOverPi, 255.f));
+                max_err = fmaxf(max_err, err);
+                bad = err > a.bound;
+            }
+        }
+    }
+    return __any_sync(kFull, bad);
+}
+
+// Shades tile t again, exactly, in the reference's order: each row by the thread that shaded it
+// before, so the exact colour is the last write.
+__device__ void reshade_tile(const ShadeArgs& a, uint32_t t, int row) {
+    const uint32_t count = shade_tile_count(a.index, t);
+    float4 g0, g1;
+    load_record(a, t, count, row, g0, g1);
+    if ((uint32_t)row < count)
+        write_rgb(a.rgb, a.npx, __float_as_uint(g1.z),
+                  shade_lights(a.lights, a.nl, make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y)));
+}
+
+// NS: checked records per tile (0: none, as in the evaluation mode)
+template <int NS>
 __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
     MlpMisc& M = *reinterpret_cast<MlpMisc*>(sm + kSmMisc);
     const int slot = threadIdx.x / kSlotThreads, row = threadIdx.x % kSlotThreads;
-    const int wq = row >> 5, lane = threadIdx.x & 31;  // warp within the slot = its TMEM lane quarter
+    const int wq = row >> 5, lane = row & 31;  // warp within the slot = its TMEM lane quarter
     SlotMisc& S = M.slot[slot];
-    const int n_samples = a.eval_out ? 0 : min(a.samples, (int)kMaxSamples);
+    static_assert(NS >= 0 && NS <= (int)kMaxSamples, "checked samples");
+    constexpr int n_samples = NS;
+    constexpr bool checking = NS > 0;
+    float* lights_raw = reinterpret_cast<float*>(sm + kSmRaw);
     float4* lights_dirI = reinterpret_cast<float4*>(sm + kSmLights);
     float2* lights_gb = reinterpret_cast<float2*>(sm + kSmLights + 16u * kMlpSmemLights);
     SmemLights table{lights_dirI, lights_gb};
-    const SmemLights* L = (n_samples > 0 && a.nl <= kMlpSmemLights) ? &table : nullptr;
+    const bool staged = checking && a.nl <= kMlpSmemLights;
+    const SmemLights* L = staged ? &table : nullptr;
+    // the lights' bytes that come by bulk copy (16-byte aligned start, whole 16-byte units)
+    const uint32_t raw_bulk = staged && (reinterpret_cast<uintptr_t>(a.lights) & 15u) == 0u
+                                  ? (28u * (uint32_t)a.nl) & ~15u
+                                  : 0u;
 
     const uint32_t mbar_w = smem_addr(&M.mbar_w), mbar = smem_addr(&S.mbar);
     // The stall test's first MMA wait polls an mbarrier that nothing arrives on, briefly, and so
@@ -606,125 +626,153 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     const uint32_t mbar_first = a.stall_test ? smem_addr(&M.mbar_idle) : mbar;
     const uint32_t tries_first = a.stall_test ? kStallTestTries : kWaitTries;
     if (threadIdx.x == 0) {
+        M.sums[0] = M.sums[1] = M.sums[2] = 0ull;
+        M.max_err_bits = 0u;
+        M.light_sum = 0.f;
         mbar_init(mbar_w, 1);
         mbar_init(smem_addr(&M.mbar_idle), 1);
         for (int s = 0; s < kSlots; ++s) mbar_init(smem_addr(&M.slot[s].mbar), 1);
-        // the weights and output scale arrive by one bulk copy (independent of the grid this
-        // kernel may overlap with)
-        mbar_expect_tx(mbar_w, sizeof(MlpImage));
+        // the weights and output scale, and the lights, arrive by bulk copy (independent of the
+        // grid this kernel may overlap with)
+        mbar_expect_tx(mbar_w, (uint32_t)sizeof(MlpImage) + raw_bulk);
         bulk_copy_g2s(smem_addr(sm), a.mlp, sizeof(MlpImage), mbar_w);
+        if (raw_bulk) bulk_copy_g2s(smem_addr(lights_raw), a.lights, raw_bulk, mbar_w);
     }
-    if (row == 0) S.fail[0] = S.fail[1] = 0u;
-    if (L) stage_lights_soa(a.lights, a.nl, lights_dirI, lights_gb);
+    // the lights' floats the bulk copy leaves out
+    if (staged)
+        for (int i = (int)(raw_bulk / 4u) + threadIdx.x; i < 7 * a.nl; i += kMlpThreads) lights_raw[i] = __ldg(a.lights + i);
+    if (row == 0) S.verdict[0] = S.verdict[1] = kNoTile;
     if (threadIdx.x < 32) tmem_alloc(smem_addr(&M.tmem), kTmemCols);
     // the records and the tile list are the previous kernel's output
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
-    const uint32_t n_tiles = a.index[1];
-    // Slot g = blockIdx.x * kSlots + slot takes tiles g, g + stride, ...
+    const uint32_t n_frag = a.index[0], n_tiles = a.index[1];
+    // Slot g = blockIdx.x * kSlots + slot takes tiles g, g + stride, ...; this thread holds the
+    // records of its row in the slot's current tile and the next one.
     const uint32_t stride = gridDim.x * kSlots;
     uint32_t t = blockIdx.x * kSlots + slot;
-    uint32_t count = t < n_tiles ? shade_tile_count(a.index, t) : 0u;
-    float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f), g1 = g0;
-    if ((uint32_t)row < count) {
-        const size_t rs = shade_record_slot(a.index, a.n_blocks, shade_tile_desc(a.index, a.n_blocks, t), t, row);
-        g0 = a.gbuf[2 * rs];
-        g1 = a.gbuf[2 * rs + 1];
-    }
+    uint32_t count = tile_count(n_frag, n_tiles, t);
+    uint32_t t_next = t + stride;
+    uint32_t count_next = tile_count(n_frag, n_tiles, t_next);
+    float4 g0, g1, g0n, g1n;
+    load_record(a, t, count, row, g0, g1);
+    load_record(a, t_next, count_next, row, g0n, g1n);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    const uint32_t tmem = M.tmem;
+    const uint32_t d_cols = tmem + (uint32_t)slot * kSlotTmem;  // lane 0, this slot's accumulators
+    const uint32_t lane_off = (uint32_t)(wq * 32) << 16;         // this warp's lanes
+    const uint32_t d_lane = d_cols + lane_off;
+    const uint32_t a_op0 = d_cols + kSlotCols;  // lane 0 of the first A operand; the second follows it
+    // the first tile's features, while the weights arrive
+    if (t < n_tiles) store_features(make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y), a_op0 + lane_off);
+    a_written();
     bool failed = !__syncthreads_and(mbar_wait(mbar_w, 0));
     const bool weights_pending = failed;
-    const uint32_t tmem = M.tmem;
-    const uint32_t d_cols = tmem + (uint32_t)slot * kSlotCols;                // lane 0, this slot's accumulators
-    const uint32_t lane_off = (uint32_t)(wq * 32) << 16;                      // this warp's lanes
-    const uint32_t d_lane = d_cols + lane_off;
+    // the checks' light table, dirI[l] = (-dir xyz, I*r) and gb[l] = (I*g, I*b), and the sum over
+    // the lights of |dir| max_c |I c|
+    if (checking && !weights_pending) {
+        float lsum = 0.f;
+        for (int l = threadIdx.x; l < a.nl; l += kMlpThreads) {
+            float P[7];
+#pragma unroll
+            for (int c = 0; c < 7; ++c) P[c] = staged ? lights_raw[7 * l + c] : __ldg(a.lights + 7 * (int64_t)l + c);
+            const float I = P[3];
+            const float4 A = make_float4(-P[0], -P[1], -P[2], I * P[4]);
+            const float2 B = make_float2(I * P[5], I * P[6]);
+            if (staged) {
+                lights_dirI[l] = A;
+                lights_gb[l] = B;
+            }
+            lsum += sqrtf(fmaf(A.z, A.z, fmaf(A.y, A.y, A.x * A.x))) * fmaxf(fabsf(A.w), fmaxf(fabsf(B.x), fabsf(B.y)));
+        }
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) lsum += __shfl_xor_sync(kFull, lsum, o);
+        if (lane == 0 && lsum > 0.f) atomicAdd(&M.light_sum, lsum);
+    }
+    __syncthreads();
+    // the checks' fixed-point scale: every sum over the lights for a unit normal stays below 2^27
+    const float fx = 0x1p27f / fmaxf(M.light_sum * 1.001f, 0x1p-60f);
     const float out_scale = reinterpret_cast<const MlpImage*>(sm)->out_scale;
     const uint32_t sW1 = smem_addr(sm + kSmW1), sW2 = smem_addr(sm + kSmW2), sW3 = smem_addr(sm + kSmW3);
-    // the slot's A operand: for the MMA (lane 0) and for this thread's writes
-    const uint32_t a_mma = kATmem ? tmem + kSlots * kSlotCols + (uint32_t)slot * kACols
-                                  : smem_addr(sm + kSmA + (size_t)slot * kABytes);
-    const uint32_t a_mine = kATmem ? a_mma + lane_off : a_mma;
 
     // Every slot barrier of the loop also ORs the threads' timeout flags, so a slot's threads leave
     // the loop at the same barrier (the loop condition itself is the same in all of them).
-    uint32_t phase = 0;
+    uint32_t phase = 0, x = 0;  // x: the A operand holding the current tile's features
     uint32_t n_tile = 0, n_fallback = 0;
     float max_err = 0.f;
     uint32_t k = 0;  // tiles this slot shaded
-    // The previous tile's record of this row, for its exact reshading when its check failed. The
-    // verdict is read after the next slot barrier, which orders it after the checked rows' writes.
-    const bool checking = n_samples > 0;
-    float3 p_nv = make_float3(0.f, 0.f, 0.f), p_alb = p_nv;
-    uint32_t p_pix = 0;
-    bool p_valid = false;
-    auto reshade_previous = [&]() {
-        if (S.fail[(k - 1u) & 1u]) {  // the same in every thread of the slot
-            if (row == 0) ++n_fallback;
-            if (p_valid) write_rgb(a.rgb, a.npx, p_pix, shade_lights(a.lights, a.nl, p_nv, p_alb));
-        }
-    };
+    // Layer L of the slot's tile k is issued by lane 0 of warp (k + L) mod 4: the issue holds its
+    // warp for a few hundred cycles, and so falls on every warp (and scheduler) in turn.
 
     while (!weights_pending && t < n_tiles) {
-        const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
-        // which checked sample this row is, if any
-        int my_sample = -1;
-        for (int s = 0; s < n_samples; ++s)
-            if (sample_rank(t, s, count) == (uint32_t)row) my_sample = s;
-        if (my_sample >= 0) {
-            S.rec[my_sample][0] = nv.x;
-            S.rec[my_sample][1] = nv.y;
-            S.rec[my_sample][2] = nv.z;
-        }
-        // Rows past the tile's records hold zeros: finite features whose results are not stored.
-        // The previous tile's MMAs completed (its last wait), so the operand is free, unless that
-        // wait gave up. After a wait gave up (`failed`), a warp touches tensor memory and the A
-        // operand no more: an MMA may still be using them. The test is warp-uniform, as the
-        // .sync.aligned tcgen05 instructions need.
-        if (!__any_sync(kFull, failed)) store_features(nv, alb, a_mine, (uint32_t)row);
-        a_written();
+        // the features are stored, the previous tile's accumulators read and its sampled rows
+        // written, and tile k - 2's verdict is in
         if (slot_sync_or(slot, failed)) break;
+        if (checking) {
+            const uint32_t v = S.verdict[k & 1u];  // the same in every thread of the slot
+            if (v != kNoTile) {
+                if (row == 0) ++n_fallback;
+                reshade_tile(a, v, row);
+            }
+        }
+        const uint32_t a_cur = a_op0 + x * kACols, a_oth = a_op0 + (x ^ 1u) * kACols;
 
         // layer 1: D = X (128 x K) * W1^T
-        if (row == 0) issue_layer(d_cols, a_mma, sW1, kMlpHid, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-        // while the MMAs run: the previous tile's fallback, and the checked rows' light sums
-        if (checking) {
-            if (k > 0u) reshade_previous();
-            if (n_samples <= 2) check_part<2>(a, L, S, row);
-            else check_part<4>(a, L, S, row);
-        }
+        if (row == 32 * (int)((k + 1u) & 3u)) issue_layer(d_cols, a_cur, sW1, kMlpHid, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
+        // the slot's tile after next: its descriptor now, its records during layer 3
+        const uint32_t t_nn = t_next + stride;
+        const uint32_t count_nn = tile_count(n_frag, n_tiles, t_nn);
+        const uint4 d_nn =
+            (uint32_t)row < count_nn ? shade_tile_desc(a.index, a.n_blocks, t_nn) : make_uint4(0u, 0u, 0u, 0u);
+        // the checked samples this row is (two samples may fall on one row)
+        uint32_t my_samples = 0u;
+#pragma unroll
+        for (int s = 0; s < n_samples; ++s)
+            if (sample_rank(t, s, count) == (uint32_t)row) my_samples |= 1u << s;
+        // the previous tile's check: this thread's part
+        if constexpr (checking)
+            if (k > 0u) {
+                float cv[3 * NS];
+#pragma unroll
+                for (int i = 0; i < 3 * NS; ++i) cv[i] = 0.f;
+                check_half<NS>(a, L, S.q[(k - 1u) & 1u], cv, row, 0);
+                check_half<NS>(a, L, S.q[(k - 1u) & 1u], cv, row, 1);
+                check_store<NS>(cv, S.part, fx, row);
+            }
+        // After a wait gave up (`failed`), a warp touches tensor memory no more: an MMA may still
+        // be using it. The test is warp-uniform, as the .sync.aligned tcgen05 instructions need.
         failed |= !mbar_wait(mbar_first, phase, tries_first);
         phase ^= 1u;
         tc_fence_after();
-        if (!__any_sync(kFull, failed)) hidden_epilogue(d_lane, a_mine, (uint32_t)row);  // h1 over the features
+        if (!__any_sync(kFull, failed)) hidden_epilogue(d_lane, a_oth + lane_off);  // h1
         a_written();
         if (slot_sync_or(slot, failed)) break;
-        // every thread read the previous tile's verdict before this barrier; the next tile's
-        // checked rows write it after two more
-        if (row == 0) S.fail[(k + 1u) & 1u] = 0u;
 
-        // layer 2: D = H1 (128 x 64) * W2^T (layer 1's accumulators were read)
-        if (row == 0) issue_layer(d_cols, a_mma, sW2, kMlpHid, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-        // this thread's record of the slot's next tile, fetched during the last two MMAs
-        const uint32_t t_next = t + stride;
-        const uint32_t count_next = t_next < n_tiles ? shade_tile_count(a.index, t_next) : 0u;
-        float4 g0n = make_float4(0.f, 0.f, 0.f, 0.f), g1n = g0n;
-        if ((uint32_t)row < count_next) {
-            const size_t rs =
-                shade_record_slot(a.index, a.n_blocks, shade_tile_desc(a.index, a.n_blocks, t_next), t_next, row);
-            g0n = a.gbuf[2 * rs];
-            g1n = a.gbuf[2 * rs + 1];
-        }
+        // layer 2: D = H1 (128 x 64) * W2^T
+        if (row == 32 * (int)((k + 2u) & 3u)) issue_layer(d_cols, a_oth, sW2, kMlpHid, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
+        // the previous tile's verdict, by the warp that issues none of this tile's layers (the
+        // parts were written before the last barrier)
+        if constexpr (checking)
+            if (k > 0u && (int)(k & 3u) == wq) {
+                const uint32_t p = (k - 1u) & 1u;
+                const bool bad = check_verdict<NS>(a, S.q[p], S.part, fx, lane, max_err);
+                if (lane == 0) S.verdict[p] = bad ? t - stride : kNoTile;
+            }
         failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
         tc_fence_after();
-        if (!__any_sync(kFull, failed)) hidden_epilogue(d_lane, a_mine, (uint32_t)row);  // h2 over h1
+        if (!__any_sync(kFull, failed)) hidden_epilogue(d_lane, a_cur + lane_off);  // h2 over the features
         a_written();
         if (slot_sync_or(slot, failed)) break;
 
-        // layer 3: D[0, 16) = H2 (128 x 64) * W3^T
-        if (row == 0) issue_layer(d_cols, a_mma, sW3, kMlpOutPad, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpOutPad), mbar);
+        // layer 3: D[0, 16) = H2 (128 x 64) * W3^T; meanwhile the next tile's features go over h1
+        if (row == 32 * (int)((k + 3u) & 3u)) issue_layer(d_cols, a_cur, sW3, kMlpOutPad, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpOutPad), mbar);
+        if (t_next < n_tiles && !__any_sync(kFull, failed))
+            store_features(make_float3(g0n.x, g0n.y, g0n.z), make_float3(g0n.w, g1n.x, g1n.y), a_oth + lane_off);
+        float4 g0nn, g1nn;
+        load_record_desc(a, t_nn, count_nn, d_nn, row, g0nn, g1nn);
         failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
         tc_fence_after();
@@ -733,7 +781,9 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
             tmem_ld4(d_lane, o);
             tmem_wait4(o);
         }
-        tc_fence_before();
+        a_written();
+
+        const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
         const bool valid = (uint32_t)row < count && !failed;
         const uint32_t pix = __float_as_uint(g1.z);
         const float3 rad = make_float3(alb.x * (__uint_as_float(o[0]) * out_scale),
@@ -751,40 +801,54 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
             if (valid)
                 write_rgb(a.rgb, a.npx, pix,
                           __float2uint_rz(radc.x) | (__float2uint_rz(radc.y) << 8) | (__float2uint_rz(radc.z) << 16));
-            if (checking) {
-                // the checked rows against their light sums (the warps' parts, written before two
-                // slot barriers); a failing tile is shaded again, exactly, by all its rows after
-                // the next slot barrier
-                if (my_sample >= 0 && valid) {
-                    float sum[3];
-#pragma unroll
-                    for (int c = 0; c < 3; ++c)
-                        sum[c] = (S.part[0][3 * my_sample + c] + S.part[1][3 * my_sample + c]) +
-                                 (S.part[2][3 * my_sample + c] + S.part[3][3 * my_sample + c]);
-                    const float er = fabsf(radc.x - fminf(sum[0] * alb.x * kOneOverPi, 255.f));
-                    const float eg = fabsf(radc.y - fminf(sum[1] * alb.y * kOneOverPi, 255.f));
-                    const float eb = fabsf(radc.z - fminf(sum[2] * alb.z * kOneOverPi, 255.f));
-                    const float err = fmaxf(er, fmaxf(eg, eb));
-                    max_err = fmaxf(max_err, err);
-                    if (err > a.bound) S.fail[k & 1u] = 1u;
-                }
-                p_nv = nv;
-                p_alb = alb;
-                p_pix = pix;
-                p_valid = valid;
+            for (uint32_t m = my_samples; m; m &= m - 1u) {  // every sampled row of the tile is written once
+                CheckRow& q = S.q[k & 1u][__ffs(m) - 1];
+                q.n[0] = nv.x; q.n[1] = nv.y; q.n[2] = nv.z;
+                q.alb[0] = alb.x; q.alb[1] = alb.y; q.alb[2] = alb.z;
+                q.rad[0] = radc.x; q.rad[1] = radc.y; q.rad[2] = radc.z;
+                q.valid = valid ? 1u : 0u;
             }
             ++n_tile;
         }
         ++k;
+        x ^= 1u;
         t = t_next;
         count = count_next;
         g0 = g0n;
         g1 = g1n;
+        t_next = t_nn;
+        count_next = count_nn;
+        g0n = g0nn;
+        g1n = g1nn;
     }
 
-    // the last tile's verdict (every thread of the slot reaches this barrier: the loop ends at the
-    // same point in all of them)
-    if (checking && !weights_pending && !slot_sync_or(slot, failed) && k > 0u) reshade_previous();
+    // The last tile's check, then the last two verdicts (every thread of the slot reaches these
+    // barriers: the loop ends at the same point in all of them, and the first one orders the last
+    // tile's sampled rows before its check).
+    if (!slot_sync_or(slot, failed) && checking && !weights_pending && k > 0u) {
+        if constexpr (checking) {
+            const uint32_t p = (k - 1u) & 1u;
+            float cv[3 * NS];
+#pragma unroll
+            for (int i = 0; i < 3 * NS; ++i) cv[i] = 0.f;
+            check_half<NS>(a, L, S.q[p], cv, row, 0);
+            check_half<NS>(a, L, S.q[p], cv, row, 1);
+            check_store<NS>(cv, S.part, fx, row);
+            slot_sync(slot);
+            if ((int)(k & 3u) == wq) {
+                const bool bad = check_verdict<NS>(a, S.q[p], S.part, fx, lane, max_err);
+                if (lane == 0) S.verdict[p] = bad ? t - stride : kNoTile;
+            }
+        }
+        slot_sync(slot);
+        for (uint32_t j = (k >= 2u ? k - 2u : 0u); j < k; ++j) {
+            const uint32_t v = S.verdict[j & 1u];  // the same in every thread of the slot
+            if (v != kNoTile) {
+                if (row == 0) ++n_fallback;
+                reshade_tile(a, v, row);
+            }
+        }
+    }
 
     if (failed) {
         // the weights' copy or an MMA did not complete in time: record it, give the pending one
@@ -793,19 +857,29 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         if (weights_pending) mbar_wait(mbar_w, 0);
         else mbar_wait(mbar, phase ^ 1u);
     }
+    // the statistics, summed in the CTA first: one global atomic per counter and CTA (thousands on
+    // one address would hold the grid's completion, which the next pass waits for)
+    const bool stats = a.stats && !a.eval_out;
+    if (stats) {
+        if (row == 0 && n_tile) {
+            atomicAdd(&M.sums[0], (unsigned long long)n_tile);
+            if (n_fallback) atomicAdd(&M.sums[1], (unsigned long long)n_fallback);
+            atomicAdd(&M.sums[2], (unsigned long long)n_tile * (unsigned long long)n_samples);
+        }
+        const uint32_t e = __reduce_max_sync(kFull, __float_as_uint(max_err));  // max_err >= 0
+        if (lane == 0 && e) atomicMax(&M.max_err_bits, e);
+    }
     tc_fence_before();
     __syncthreads();
     if (threadIdx.x < 32) {
         tc_fence_after();
         tmem_dealloc(tmem, kTmemCols);
     }
-    if (a.stats && !a.eval_out) {
-        if (row == 0 && n_tile) {
-            atomicAdd(a.stats + 0, (unsigned long long)n_tile);
-            if (n_fallback) atomicAdd(a.stats + 1, (unsigned long long)n_fallback);
-            atomicAdd(a.stats + 2, (unsigned long long)n_tile * (unsigned long long)n_samples);
-        }
-        if (max_err > 0.f) atomicMax(a.stats + 3, (unsigned long long)__float_as_uint(max_err));
+    if (stats && threadIdx.x == 0) {
+        if (M.sums[0]) atomicAdd(a.stats + 0, M.sums[0]);
+        if (M.sums[1]) atomicAdd(a.stats + 1, M.sums[1]);
+        if (M.sums[2]) atomicAdd(a.stats + 2, M.sums[2]);
+        if (M.max_err_bits) atomicMax(a.stats + 3, (unsigned long long)M.max_err_bits);
     }
 }
 
@@ -1096,14 +1170,23 @@ static ShadeArgs shade_args(const FrameScratch& s, const DrawParams& p) {
     return a;
 }
 
+// The learned-shader kernel for a number of checked samples per tile (0 .. kMaxSamples).
+using MlpKernel = void (*)(ShadeArgs);
+static MlpKernel mlp_kernel(int samples) {
+    static const MlpKernel k[kMaxSamples + 1] = {k_shade_mlp<0>, k_shade_mlp<1>, k_shade_mlp<2>, k_shade_mlp<3>,
+                                                 k_shade_mlp<4>};
+    return k[std::min(std::max(samples, 0), (int)kMaxSamples)];
+}
+
 static int mlp_grid(int n_sm, int64_t blocks) {
     static bool attr_set = false;  // per process: the attribute is per function, all devices alike
     if (!attr_set) {
-        if (cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpSmem) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(k_shade_mlp, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
-            return -1;
+        for (int ns = 0; ns <= (int)kMaxSamples; ++ns)
+            if (cudaFuncSetAttribute(mlp_kernel(ns), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpSmem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(mlp_kernel(ns), cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+                return -1;
         attr_set = true;
     }
     // one CTA per SM at most, and no more CTAs than the tiles need (a block of 1024 records makes
@@ -1144,7 +1227,7 @@ int launch_shade(const FrameScratch& s, const DrawParams& p, int64_t blocks, cud
     } else {
         const int grid = mlp_grid(p.n_sm, blocks);
         if (grid < 0) return -1;
-        err = launch_dependent(k_shade_mlp, grid, kMlpThreads, mlp_smem_bytes(), stream, a);
+        err = launch_dependent(mlp_kernel(a.samples), grid, kMlpThreads, mlp_smem_bytes(), stream, a);
     }
     return err == cudaSuccess ? 1 : -1;
 }
@@ -1176,7 +1259,7 @@ int launch_mlp_eval(const float* src, int stride, int64_t n, bool exact, float4*
     } else {
         const int grid = mlp_grid(n_sm, blocks);
         if (grid < 0) return -1;
-        k_shade_mlp<<<grid, kMlpThreads, mlp_smem_bytes(), stream>>>(a);
+        k_shade_mlp<0><<<grid, kMlpThreads, mlp_smem_bytes(), stream>>>(a);
     }
     return cudaGetLastError() == cudaSuccess ? 3 : -1;
 }
