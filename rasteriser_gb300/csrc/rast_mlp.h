@@ -64,9 +64,20 @@ struct MlpImage {
     uint16_t w2[kMlpHid * kMlpHid];     // layer 2 B operand, 64 x 64
     uint16_t w3[kMlpOutPad * kMlpHid];  // layer 3 B operand, 16 x 64 (rows 3.. zero)
     float out_scale;
-    float reserved[3];
+    float light_sum;                    // sum over the rig's lights of |dir| * max_c |I c|
+    float reserved[2];
 };
 static_assert(sizeof(MlpImage) % 16 == 0, "MlpImage is copied in 16-byte units");
+
+// The light table of the learned shader's checks, built with the image for the rig the weights
+// belong to and stored right after it on the device: dirI[l] = (-dir xyz, I r), gb[l] = (I g, I b)
+// for the first kMlpCheckLights lights (a rig with more lights is read from the light records).
+constexpr int kMlpCheckLights = 512;
+struct MlpCheckTable {
+    float dirI[kMlpCheckLights][4];
+    float gb[kMlpCheckLights][2];
+};
+static_assert(sizeof(MlpImage) % 16 == 0 && sizeof(MlpCheckTable) % 16 == 0, "16-byte units");
 constexpr uint32_t kMlpWeightBytes = sizeof(uint16_t) * (kMlpHid * kMlpIn + kMlpHid * kMlpHid + kMlpOutPad * kMlpHid);
 
 // Saved weights ("RMLP" blob, little endian): header, then W1 64x55, W2 64x64, W3 3x64 as BF16

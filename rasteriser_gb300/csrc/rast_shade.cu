@@ -337,13 +337,14 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 // next tile's features are computed and stored while the current tile's last MMA runs:
 //   features(k) -> A[x]; h1 -> A[1-x]; h2 -> A[x]; features(k+1) -> A[1-x] during layer 3.
 //
-// Tile k is checked during tile k + 1. Its sampled rows put their normal, albedo and output into
-// the slot's check rows (by tile parity). While tile k + 1's first MMA runs, the slot's 128 threads
-// split the lights and each warp sums its part; while the second runs, one warp adds the four
-// parts, compares and records the verdict (the failed tile, or none). The whole slot reads the
-// verdict after the barrier that opens tile k + 2 and shades a failed tile again, exactly, right
-// there; the last two verdicts are read after the loop. The kernel is compiled for each number of
-// checked samples.
+// Tile k's sampled rows put their normal and albedo into the slot's check rows (by tile parity) while
+// its first MMA runs, and two warps that do not issue its second MMA split the lights and sum their
+// parts while that one runs; the sampled rows add their output at the end of the tile. While tile
+// k + 1's first MMA runs, the warp that issues none of tile k + 1's layers adds the two parts,
+// compares and records the verdict (the failed tile, or none). The whole slot reads the verdict
+// after the barrier that opens tile k + 2 and shades a failed tile again, exactly, right there; the
+// last two verdicts are read after the loop. The kernel is compiled for each number of checked
+// samples, and the light table comes with the weights (built with them for their rig).
 //
 // RAST_MLP_SLOTS (at most 4: 4 x 128 columns fill the tensor memory) can be changed at build time
 // to measure fewer slots; the default is the fastest measured.
@@ -364,14 +365,14 @@ constexpr uint32_t kMaxSamples = 4;
 constexpr int kMlpSmemLights = 512;  // lights the checks read from shared memory
 constexpr uint32_t kNoTile = 0xFFFFFFFFu;
 
-// Shared memory (bytes): the weights and output scale, the lights as given (7 floats each, by bulk
-// copy), the checks' light table made from them, then the small block.
+// Shared memory (bytes): the weights and output scale, the checks' light table (dirI then gb, as in
+// MlpCheckTable), then the small block.
 constexpr uint32_t kSmW1 = 0;
 constexpr uint32_t kSmW2 = kSmW1 + kMlpHid * kMlpIn * 2;
 constexpr uint32_t kSmW3 = kSmW2 + kMlpHid * kMlpHid * 2;
-constexpr uint32_t kSmRaw = (sizeof(MlpImage) + 15) / 16 * 16;
-constexpr uint32_t kSmLights = kSmRaw + 28u * kMlpSmemLights;
+constexpr uint32_t kSmLights = (sizeof(MlpImage) + 15) / 16 * 16;
 constexpr uint32_t kSmMisc = kSmLights + 24u * kMlpSmemLights;
+static_assert(kMlpSmemLights == kMlpCheckLights, "the shared table is the image's check table");
 
 struct CheckRow {
     float n[3], alb[3], rad[3];  // the row's normal and albedo, and the learned radiance (clamped)
@@ -381,7 +382,7 @@ struct SlotMisc {
     unsigned long long mbar;                // MMA completion
     uint32_t verdict[2];                    // by the checked tile's parity: that tile when it failed, else kNoTile
     CheckRow q[2][kMaxSamples];             // by tile parity: the sampled rows
-    int32_t part[4][3 * kMaxSamples];       // by warp: the warps' light sums (3 s + c), fixed point
+    int32_t part[2][3 * kMaxSamples];       // by checking warp: its light sums (3 s + c), fixed point
 };
 struct MlpMisc {
     unsigned long long mbar_w;     // the weights' bulk copy
@@ -389,13 +390,10 @@ struct MlpMisc {
     unsigned long long sums[3];    // the CTA's tiles, fallback tiles and checked rows
     uint32_t max_err_bits;         // the CTA's largest checked error (a non-negative float's bits)
     uint32_t tmem;
-    float light_sum;               // sum over the lights of |dir| max_c |I c|: bounds the check sums
-    uint32_t pad;
     SlotMisc slot[kSlots];
 };
 constexpr uint32_t kMlpSmem = kSmMisc + sizeof(MlpMisc);
-static_assert(kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmRaw % 16 == 0 && kSmLights % 16 == 0 &&
-                  kSmMisc % 16 == 0,
+static_assert(kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmLights % 16 == 0 && kSmMisc % 16 == 0,
               "operand alignment");
 static_assert(kMlpSmem <= 227 * 1024, "shared memory of one CTA");
 static_assert(sizeof(MlpImage) % 16 == 0, "bulk copy alignment");
@@ -407,9 +405,11 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     return x;
 }
 
-// The checked records of tile t: ranks floor(hash(t, s) * count / 2^32), the same in every thread.
-__device__ __forceinline__ uint32_t sample_rank(uint32_t t, int s, uint32_t count) {
-    return __umulhi(hash32(t * 8u + (uint32_t)s + 0x9E3779B9u), count);
+// The checked records of tile t: ranks floor(h_s * count / 2^32) for h_s = (hash(t) + s * c1) * c2
+// (c2 odd: a bijection of the hash for each s), the same in every thread.
+__device__ __forceinline__ uint32_t sample_hash(uint32_t t) { return hash32(t * 8u + 0x9E3779B9u); }
+__device__ __forceinline__ uint32_t sample_rank(uint32_t h, int s, uint32_t count) {
+    return __umulhi((h + (uint32_t)s * 0x9E3779B9u) * 0x85EBCA77u, count);
 }
 
 // Named barrier of slot s (ids 1..kSlots; 0 is __syncthreads), with an OR of `v` over its threads.
@@ -510,14 +510,16 @@ struct SmemLights {
     const float2* gb;
 };
 
-// A thread's part of a tile's check: the slot's 128 threads split the lights (thread `row` takes
-// lights row, row + 128, ...; the two halves take every other one) and sum, for each sampled row
-// q[s] and channel c, (I c)_l * max(0, n . -dir_l) with fused multiply-adds into v[3 s + c]. The sum
-// only estimates the exact shade: it judges the learned colour and is never itself a colour. Lights
-// come from the shared table when it holds them, else from global memory.
+// A lane's part of a tile's check, for checking warp c of two: the warps split the lights (lane
+// `lane` of warp c takes lights 32 c + lane, 32 c + lane + 64, ...) and sum, for each sampled row q[s]
+// and channel ch, (I ch)_l * max(0, n . -dir_l) with fused multiply-adds; the warp then adds its
+// lanes' sums in fixed point (scale fx: any sum over the lights for a normal of length <= 4 stays
+// below 2^29 in magnitude) and stores them in part[c][3 s + ch]. The sum only estimates the exact
+// shade: it judges the learned colour and is never itself a colour. Lights come from the shared
+// table when it holds them, else from global memory.
 template <int NS>
-__device__ __forceinline__ void check_half(const ShadeArgs& a, const SmemLights* L, const CheckRow* q,
-                                           float (&v)[3 * NS], int row, int half) {
+__device__ __forceinline__ void check_part(const ShadeArgs& a, const SmemLights* L, const CheckRow* q,
+                                           int32_t (*part)[3 * kMaxSamples], float fx, int c, int lane) {
     float nx[NS], ny[NS], nz[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
@@ -525,7 +527,11 @@ __device__ __forceinline__ void check_half(const ShadeArgs& a, const SmemLights*
         ny[s] = q[s].n[1];
         nz[s] = q[s].n[2];
     }
-    for (int l = row + half * kSlotThreads; l < a.nl; l += 2 * kSlotThreads) {
+    float v[3 * NS];
+#pragma unroll
+    for (int i = 0; i < 3 * NS; ++i) v[i] = 0.f;
+#pragma unroll 4
+    for (int l = 32 * c + lane; l < a.nl; l += 64) {
         float4 A;
         float2 B;
         if (L) {
@@ -545,28 +551,21 @@ __device__ __forceinline__ void check_half(const ShadeArgs& a, const SmemLights*
             v[3 * s + 2] = fmaf(B.y, m, v[3 * s + 2]);
         }
     }
-}
-
-// Each warp adds its lanes' sums in fixed point (scale fx: any sum over the lights for a normal of
-// length <= 4 stays below 2^29 in magnitude) and stores them in part[warp][3 s + c].
-template <int NS>
-__device__ __forceinline__ void check_store(const float (&v)[3 * NS], int32_t (*part)[3 * kMaxSamples], float fx,
-                                            int row) {
     int32_t r[3 * NS];
 #pragma unroll
     for (int i = 0; i < 3 * NS; ++i) r[i] = __reduce_add_sync(kFull, __float2int_rn(v[i] * fx));
-    if ((row & 31) == 0)
+    if (lane == 0)
 #pragma unroll
-        for (int i = 0; i < 3 * NS; ++i) part[row >> 5][i] = r[i];
+        for (int i = 0; i < 3 * NS; ++i) part[c][i] = r[i];
 }
 
-// The verdict of a tile's check, by one warp: lane 3 s + c adds the four warps' parts of sampled row
-// s, channel c, and compares |learned - min(sum * albedo / pi, 255)| with the bound; a sampled
+// The verdict of a tile's check, by one warp: lane 3 s + c adds the two checking warps' parts of
+// sampled row s, channel c (scaled back by inv_fx = 1 / fx), and compares |learned - min(sum * albedo / pi, 255)| with the bound; a sampled
 // normal longer than 4 (outside the fixed-point range) fails the tile. Returns, in every lane,
 // whether a sampled row fails.
 template <int NS>
 __device__ __forceinline__ bool check_verdict(const ShadeArgs& a, const CheckRow* q,
-                                              const int32_t (*part)[3 * kMaxSamples], float fx, int lane,
+                                              const int32_t (*part)[3 * kMaxSamples], float inv_fx, int lane,
                                               float& max_err) {
     bool bad = false;
     if (lane < 3 * NS) {
@@ -576,8 +575,7 @@ __device__ __forceinline__ bool check_verdict(const ShadeArgs& a, const CheckRow
             if (!(nn <= 16.f)) {
                 bad = true;
             } else {
-                const int64_t p = ((int64_t)part[0][lane] + part[1][lane]) + ((int64_t)part[2][lane] + part[3][lane]);
-                const float sum = (float)p / fx;
+                const float sum = (float)((int64_t)part[0][lane] + part[1][lane]) * inv_fx;
                 const float err = fabsf(q[s].rad[c] - fminf(sum * q[s].alb[c] * kOneOverPi, 255.f));
                 max_err = fmaxf(max_err, err);
                 bad = err > a.bound;
@@ -609,16 +607,14 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     static_assert(NS >= 0 && NS <= (int)kMaxSamples, "checked samples");
     constexpr int n_samples = NS;
     constexpr bool checking = NS > 0;
-    float* lights_raw = reinterpret_cast<float*>(sm + kSmRaw);
     float4* lights_dirI = reinterpret_cast<float4*>(sm + kSmLights);
     float2* lights_gb = reinterpret_cast<float2*>(sm + kSmLights + 16u * kMlpSmemLights);
     SmemLights table{lights_dirI, lights_gb};
     const bool staged = checking && a.nl <= kMlpSmemLights;
     const SmemLights* L = staged ? &table : nullptr;
-    // the lights' bytes that come by bulk copy (16-byte aligned start, whole 16-byte units)
-    const uint32_t raw_bulk = staged && (reinterpret_cast<uintptr_t>(a.lights) & 15u) == 0u
-                                  ? (28u * (uint32_t)a.nl) & ~15u
-                                  : 0u;
+    // the check table's bytes (dirI and gb of the rig's lights, each in whole 16-byte units)
+    const uint32_t tab_dirI = staged ? 16u * (uint32_t)a.nl : 0u;
+    const uint32_t tab_gb = staged ? 16u * (((uint32_t)a.nl + 1u) / 2u) : 0u;
 
     const uint32_t mbar_w = smem_addr(&M.mbar_w), mbar = smem_addr(&S.mbar);
     // The stall test's first MMA wait polls an mbarrier that nothing arrives on, briefly, and so
@@ -628,19 +624,19 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     if (threadIdx.x == 0) {
         M.sums[0] = M.sums[1] = M.sums[2] = 0ull;
         M.max_err_bits = 0u;
-        M.light_sum = 0.f;
         mbar_init(mbar_w, 1);
         mbar_init(smem_addr(&M.mbar_idle), 1);
         for (int s = 0; s < kSlots; ++s) mbar_init(smem_addr(&M.slot[s].mbar), 1);
         // the weights and output scale, and the lights, arrive by bulk copy (independent of the
         // grid this kernel may overlap with)
-        mbar_expect_tx(mbar_w, (uint32_t)sizeof(MlpImage) + raw_bulk);
+        mbar_expect_tx(mbar_w, (uint32_t)sizeof(MlpImage) + tab_dirI + tab_gb);
         bulk_copy_g2s(smem_addr(sm), a.mlp, sizeof(MlpImage), mbar_w);
-        if (raw_bulk) bulk_copy_g2s(smem_addr(lights_raw), a.lights, raw_bulk, mbar_w);
+        if (staged) {
+            const MlpCheckTable* tab = reinterpret_cast<const MlpCheckTable*>(a.mlp + 1);
+            bulk_copy_g2s(smem_addr(lights_dirI), tab->dirI, tab_dirI, mbar_w);
+            bulk_copy_g2s(smem_addr(lights_gb), tab->gb, tab_gb, mbar_w);
+        }
     }
-    // the lights' floats the bulk copy leaves out
-    if (staged)
-        for (int i = (int)(raw_bulk / 4u) + threadIdx.x; i < 7 * a.nl; i += kMlpThreads) lights_raw[i] = __ldg(a.lights + i);
     if (row == 0) S.verdict[0] = S.verdict[1] = kNoTile;
     if (threadIdx.x < 32) tmem_alloc(smem_addr(&M.tmem), kTmemCols);
     // the records and the tile list are the previous kernel's output
@@ -670,30 +666,9 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     a_written();
     bool failed = !__syncthreads_and(mbar_wait(mbar_w, 0));
     const bool weights_pending = failed;
-    // the checks' light table, dirI[l] = (-dir xyz, I*r) and gb[l] = (I*g, I*b), and the sum over
-    // the lights of |dir| max_c |I c|
-    if (checking && !weights_pending) {
-        float lsum = 0.f;
-        for (int l = threadIdx.x; l < a.nl; l += kMlpThreads) {
-            float P[7];
-#pragma unroll
-            for (int c = 0; c < 7; ++c) P[c] = staged ? lights_raw[7 * l + c] : __ldg(a.lights + 7 * (int64_t)l + c);
-            const float I = P[3];
-            const float4 A = make_float4(-P[0], -P[1], -P[2], I * P[4]);
-            const float2 B = make_float2(I * P[5], I * P[6]);
-            if (staged) {
-                lights_dirI[l] = A;
-                lights_gb[l] = B;
-            }
-            lsum += sqrtf(fmaf(A.z, A.z, fmaf(A.y, A.y, A.x * A.x))) * fmaxf(fabsf(A.w), fmaxf(fabsf(B.x), fabsf(B.y)));
-        }
-#pragma unroll
-        for (int o = 16; o >= 1; o >>= 1) lsum += __shfl_xor_sync(kFull, lsum, o);
-        if (lane == 0 && lsum > 0.f) atomicAdd(&M.light_sum, lsum);
-    }
-    __syncthreads();
     // the checks' fixed-point scale: every sum over the lights for a unit normal stays below 2^27
-    const float fx = 0x1p27f / fmaxf(M.light_sum * 1.001f, 0x1p-60f);
+    const float fx = 0x1p27f / fmaxf(reinterpret_cast<const MlpImage*>(sm)->light_sum * 1.001f, 0x1p-60f),
+                inv_fx = 1.f / fx;
     const float out_scale = reinterpret_cast<const MlpImage*>(sm)->out_scale;
     const uint32_t sW1 = smem_addr(sm + kSmW1), sW2 = smem_addr(sm + kSmW2), sW3 = smem_addr(sm + kSmW3);
 
@@ -710,17 +685,17 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         // the features are stored, the previous tile's accumulators read and its sampled rows
         // written, and tile k - 2's verdict is in
         if (slot_sync_or(slot, failed)) break;
-        if (checking) {
-            const uint32_t v = S.verdict[k & 1u];  // the same in every thread of the slot
+        const uint32_t a_cur = a_op0 + x * kACols, a_oth = a_op0 + (x ^ 1u) * kACols;
+
+        // layer 1: D = X (128 x K) * W1^T
+        if (row == 32 * (int)((k + 1u) & 3u)) issue_layer(d_cols, a_cur, sW1, kMlpHid, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
+        if constexpr (checking) {
+            const uint32_t v = S.verdict[k & 1u];  // tile k - 2's, the same in every thread of the slot
             if (v != kNoTile) {
                 if (row == 0) ++n_fallback;
                 reshade_tile(a, v, row);
             }
         }
-        const uint32_t a_cur = a_op0 + x * kACols, a_oth = a_op0 + (x ^ 1u) * kACols;
-
-        // layer 1: D = X (128 x K) * W1^T
-        if (row == 32 * (int)((k + 1u) & 3u)) issue_layer(d_cols, a_cur, sW1, kMlpHid, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
         // the slot's tile after next: its descriptor now, its records during layer 3
         const uint32_t t_nn = t_next + stride;
         const uint32_t count_nn = tile_count(n_frag, n_tiles, t_nn);
@@ -728,19 +703,27 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
             (uint32_t)row < count_nn ? shade_tile_desc(a.index, a.n_blocks, t_nn) : make_uint4(0u, 0u, 0u, 0u);
         // the checked samples this row is (two samples may fall on one row)
         uint32_t my_samples = 0u;
+        if constexpr (checking) {
+            const uint32_t h_t = sample_hash(t);
 #pragma unroll
-        for (int s = 0; s < n_samples; ++s)
-            if (sample_rank(t, s, count) == (uint32_t)row) my_samples |= 1u << s;
-        // the previous tile's check: this thread's part
-        if constexpr (checking)
-            if (k > 0u) {
-                float cv[3 * NS];
-#pragma unroll
-                for (int i = 0; i < 3 * NS; ++i) cv[i] = 0.f;
-                check_half<NS>(a, L, S.q[(k - 1u) & 1u], cv, row, 0);
-                check_half<NS>(a, L, S.q[(k - 1u) & 1u], cv, row, 1);
-                check_store<NS>(cv, S.part, fx, row);
+            for (int s = 0; s < n_samples; ++s)
+                if (sample_rank(h_t, s, count) == (uint32_t)row) my_samples |= 1u << s;
+        }
+        if constexpr (checking) {
+            // this tile's sampled rows: normal and albedo (the output follows at the end)
+            for (uint32_t m = my_samples; m; m &= m - 1u) {
+                CheckRow& q = S.q[k & 1u][__ffs(m) - 1];
+                q.n[0] = g0.x; q.n[1] = g0.y; q.n[2] = g0.z;
+                q.alb[0] = g0.w; q.alb[1] = g1.x; q.alb[2] = g1.y;
             }
+            // the previous tile's verdict, by the warp that issues none of this tile's layers (its
+            // parts and output were written before the last barrier)
+            if (k > 0u && (int)(k & 3u) == wq) {
+                const uint32_t p = (k - 1u) & 1u;
+                const bool bad = check_verdict<NS>(a, S.q[p], S.part, inv_fx, lane, max_err);
+                if (lane == 0) S.verdict[p] = bad ? t - stride : kNoTile;
+            }
+        }
         // After a wait gave up (`failed`), a warp touches tensor memory no more: an MMA may still
         // be using it. The test is warp-uniform, as the .sync.aligned tcgen05 instructions need.
         failed |= !mbar_wait(mbar_first, phase, tries_first);
@@ -752,14 +735,11 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
 
         // layer 2: D = H1 (128 x 64) * W2^T
         if (row == 32 * (int)((k + 2u) & 3u)) issue_layer(d_cols, a_oth, sW2, kMlpHid, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-        // the previous tile's verdict, by the warp that issues none of this tile's layers (the
-        // parts were written before the last barrier)
+        // this tile's check: the parts of two warps that do not issue this layer (its sampled rows
+        // were written before the last barrier)
         if constexpr (checking)
-            if (k > 0u && (int)(k & 3u) == wq) {
-                const uint32_t p = (k - 1u) & 1u;
-                const bool bad = check_verdict<NS>(a, S.q[p], S.part, fx, lane, max_err);
-                if (lane == 0) S.verdict[p] = bad ? t - stride : kNoTile;
-            }
+            if ((int)(k & 3u) == wq || (int)((k + 1u) & 3u) == wq)
+                check_part<NS>(a, L, S.q[k & 1u], S.part, fx, (int)(k & 3u) == wq ? 0 : 1, lane);
         failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
         tc_fence_after();
@@ -783,7 +763,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         }
         a_written();
 
-        const float3 nv = make_float3(g0.x, g0.y, g0.z), alb = make_float3(g0.w, g1.x, g1.y);
+        const float3 alb = make_float3(g0.w, g1.x, g1.y);
         const bool valid = (uint32_t)row < count && !failed;
         const uint32_t pix = __float_as_uint(g1.z);
         const float3 rad = make_float3(alb.x * (__uint_as_float(o[0]) * out_scale),
@@ -803,8 +783,6 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
                           __float2uint_rz(radc.x) | (__float2uint_rz(radc.y) << 8) | (__float2uint_rz(radc.z) << 16));
             for (uint32_t m = my_samples; m; m &= m - 1u) {  // every sampled row of the tile is written once
                 CheckRow& q = S.q[k & 1u][__ffs(m) - 1];
-                q.n[0] = nv.x; q.n[1] = nv.y; q.n[2] = nv.z;
-                q.alb[0] = alb.x; q.alb[1] = alb.y; q.alb[2] = alb.z;
                 q.rad[0] = radc.x; q.rad[1] = radc.y; q.rad[2] = radc.z;
                 q.valid = valid ? 1u : 0u;
             }
@@ -822,21 +800,14 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         g1n = g1nn;
     }
 
-    // The last tile's check, then the last two verdicts (every thread of the slot reaches these
-    // barriers: the loop ends at the same point in all of them, and the first one orders the last
-    // tile's sampled rows before its check).
+    // The last tile's verdict, then the last two verdicts read (every thread of the slot reaches
+    // these barriers: the loop ends at the same point in all of them, and the first one orders the
+    // last tile's parts and output before its verdict).
     if (!slot_sync_or(slot, failed) && checking && !weights_pending && k > 0u) {
         if constexpr (checking) {
             const uint32_t p = (k - 1u) & 1u;
-            float cv[3 * NS];
-#pragma unroll
-            for (int i = 0; i < 3 * NS; ++i) cv[i] = 0.f;
-            check_half<NS>(a, L, S.q[p], cv, row, 0);
-            check_half<NS>(a, L, S.q[p], cv, row, 1);
-            check_store<NS>(cv, S.part, fx, row);
-            slot_sync(slot);
             if ((int)(k & 3u) == wq) {
-                const bool bad = check_verdict<NS>(a, S.q[p], S.part, fx, lane, max_err);
+                const bool bad = check_verdict<NS>(a, S.q[p], S.part, inv_fx, lane, max_err);
                 if (lane == 0) S.verdict[p] = bad ? t - stride : kNoTile;
             }
         }
