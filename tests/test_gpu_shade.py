@@ -238,6 +238,87 @@ def test_learned_fallback_gives_exact_colour(rnd, port, trained):
     assert diff.max() <= RGB_TOL
 
 
+@pytest.mark.parametrize("samples", [1, 3, 4])
+def test_learned_each_sample_count(rnd, port, trained, samples):
+    """Each number of checked records per tile is its own kernel: every tile checks that many
+    records, depth and ids stay exact, the colour within tolerance, and tiles fall back exactly
+    when a checked error exceeds the bound (max checked error <= 0.5/255 <=> no fallback)."""
+    sc, lights, _, blob = trained
+    rnd.mlp_load(blob)
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
+    rnd.set_option(abi.OPT_MLP_SAMPLES, samples)
+    try:
+        f, d, ids = rnd.draw_scene(sc, clear=True)
+        st = rnd.shade_stats()
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+        rnd.set_option(abi.OPT_MLP_SAMPLES, 2)
+    of, od, oids = oracle_frame(port, sc)
+    print("samples", samples, "stats", st)
+    assert np.array_equal(bits(d), bits(od)) and np.array_equal(ids, oids)
+    cov = oids != 0xFFFFFFFF
+    diff = np.abs(f.astype(np.int16) - of.astype(np.int16))
+    assert diff.max() <= RGB_TOL and diff[:, cov].mean() <= MEAN_TOL
+    assert st["checked"] == st["tiles"] * samples
+    assert 0.0 < st["max_checked_err"]
+    assert (st["max_checked_err"] <= 0.5) == (st["fallback_tiles"] == 0), st
+
+
+def test_learned_checks_catch_a_wrong_network(rnd, port, trained):
+    """The trained network with its output layer scaled by 1.5 is wrong by more than the bound
+    wherever a pixel is lit: at the default bound the sampled checks send the tiles to the exact
+    shader, and only tiles whose checked records are all (nearly) dark keep the network's colour."""
+    sc, lights, _, blob = trained
+    w = mlp_ref.parse_blob(blob)
+    w["w3"] = mlp_ref.bf16_round(w["w3"] * 1.5)
+    rnd.mlp_load(mlp_ref.make_blob(w, n_lights=w["n_lights"], lights_hash=w["lights_hash"], loss=w["loss"]))
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
+    try:
+        f, d, ids = rnd.draw_scene(sc, clear=True)
+        st = rnd.shade_stats()
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+        rnd.mlp_load(blob)
+    of, od, oids = oracle_frame(port, sc)
+    print("wrong network:", st)
+    assert np.array_equal(bits(d), bits(od)) and np.array_equal(ids, oids)
+    assert st["max_checked_err"] > 1.0, st
+    assert st["fallback_tiles"] >= 0.8 * st["tiles"], st
+    cov = oids != 0xFFFFFFFF
+    exact = np.all(f == of, axis=0)
+    assert exact[cov].mean() >= 0.8
+
+
+def test_learned_checks_with_lights_beyond_the_shared_table(rnd, port):
+    """600 lights: more than the shared check table holds, so the checks read the light records
+    from global memory (their fixed-point bound still covers every light). At a bound of 0 every
+    tile whose checked records differ at all falls back: the exact colour; at the default bound the
+    verdicts agree with the largest checked error."""
+    sc = small_many_lights(600, 320, 240)
+    _, _, lights, _ = abi.scene_frame_inputs(sc)
+    rnd.upload_scene_mesh(sc)
+    rnd.set_lights(lights)
+    rnd.mlp_train(samples=1 << 20, epochs=4, seed=5)
+    of, od, oids = oracle_frame(port, sc)
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
+    try:
+        rnd.set_option(abi.OPT_MLP_BOUND_MILLI, 0)
+        f0, _, _ = rnd.draw_scene(sc, clear=True)
+        st0 = rnd.shade_stats()
+        rnd.set_option(abi.OPT_MLP_BOUND_MILLI, 500)
+        f1, d1, ids1 = rnd.draw_scene(sc, clear=True)
+        st1 = rnd.shade_stats()
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+        rnd.set_option(abi.OPT_MLP_BOUND_MILLI, 500)
+    print("600 lights, bound 0:", st0, "bound 0.5:", st1)
+    assert st0["fallback_tiles"] >= st0["tiles"] - 2, st0
+    assert np.abs(f0.astype(np.int16) - of.astype(np.int16)).max() <= RGB_TOL
+    assert np.array_equal(bits(d1), bits(od)) and np.array_equal(ids1, oids)
+    assert st1["checked"] == 2 * st1["tiles"] and st1["max_checked_err"] > 0.0
+    assert (st1["max_checked_err"] <= 0.5) == (st1["fallback_tiles"] == 0), st1
+
+
 def test_learned_needs_matching_rig(rnd, trained):
     sc, lights, _, blob = trained
     rnd.mlp_load(blob)
