@@ -189,8 +189,9 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
                                          or 32 (default): whole rows, the ends of the passing
                                          interval found from the edges' crossings */
 #define RAST_OPT_SHADER 6             /* RAST_SHADER_* (default RAST_SHADER_EXACT) */
-#define RAST_OPT_MLP_SAMPLES 7        /* learned shader: fragments of each 128-fragment tile that
-                                         are also shaded exactly to check it, 0..4 (default 2) */
+#define RAST_OPT_MLP_SAMPLES 7        /* learned shader: fragments of each 128-fragment tile whose
+                                         learned colour is checked against the per-light sum, 0..4
+                                         (default 2) */
 #define RAST_OPT_MLP_BOUND_MILLI 8    /* learned shader: a tile whose checked fragments differ from
                                          the exact shader by more than this many thousandths of
                                          1/255 in a channel is shaded exactly (default 500) */
@@ -208,9 +209,10 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
  *   EXACT_DEFERRED: the resolve pass stores the winning fragments (normal, albedo, pixel); a
  *     separate pass shades them with the same per-light sum (same colour as EXACT)
  *   LEARNED: the stored fragments are shaded by the context's MLP (rast_mlp_train / rast_mlp_load)
- *     on the tensor cores; RAST_OPT_MLP_SAMPLES fragments per 128-fragment tile are also shaded
- *     exactly and a tile whose sampled error exceeds RAST_OPT_MLP_BOUND_MILLI is shaded exactly
- *     in full. Needs weights trained or loaded for the current lights (RAST_ERR_INVALID_ARG
+ *     on the tensor cores; for RAST_OPT_MLP_SAMPLES fragments per 128-fragment tile the learned
+ *     colour is compared with the per-light sum (summed in a different order, as an estimate), and
+ *     a tile whose sampled error exceeds RAST_OPT_MLP_BOUND_MILLI is shaded exactly, in the
+ *     reference's order, in full. Needs weights trained or loaded for the current lights (RAST_ERR_INVALID_ARG
  *     otherwise). Single draws only: batches always use EXACT. */
 #define RAST_SHADER_EXACT 0
 #define RAST_SHADER_EXACT_DEFERRED 1
