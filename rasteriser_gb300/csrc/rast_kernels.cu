@@ -1254,10 +1254,25 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
         // (drawing.cpp:119), the depth buffer's value, read only where a fragment landed (the keys
         // of pixels outside the frame hold no fragment). For a NaN incoming depth nothing passes.
         // Clear mode: every fragment that landed beat 1.0 already.
-        float din[4];
+        // A lane's four pixels are read as one 16-byte load when any fragment landed among them
+        // (over the host link, where the buffers may live, four scalar loads of one line cost four
+        // transactions).
+        float din[4] = {0.f, 0.f, 0.f, 0.f};
+        if (!kClear) {
+            bool any = false;
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            din[k] = (!kClear && (uint32_t)key[k] != 0xFFFFFFFFu) ? a.depth[p0 + k] : 0.f;
+            for (int k = 0; k < 4; ++k) any |= (uint32_t)key[k] != 0xFFFFFFFFu;
+            if (vec) {
+                if (any) {
+                    const float4 d4 = *reinterpret_cast<const float4*>(a.depth + p0);
+                    din[0] = d4.x; din[1] = d4.y; din[2] = d4.z; din[3] = d4.w;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if ((uint32_t)key[k] != 0xFFFFFFFFu) din[k] = a.depth[p0 + k];
+            }
+        }
         // compact the winners of the span
         bool win[4];
         uint32_t n_win = 0;
@@ -1343,7 +1358,9 @@ __global__ void __launch_bounds__(kResolveThreads) k_resolve(ResolveArgs a) {
             col[k] = win[k] ? S.rgb[4 * lane + k] : 0u;
         }
         const int64_t plane = npx;
-        if (kClear && vec) {
+        // four winners in a row (read-modify-write) are written like a cleared frame's pixels
+        const bool all4 = vec && win[0] && win[1] && win[2] && win[3];
+        if ((kClear && vec) || all4) {
             // every pixel is written: background 0 / 1.0 where nothing won
             *reinterpret_cast<float4*>(a.depth + p0) = make_float4(dep[0], dep[1], dep[2], dep[3]);
             uint32_t pr = 0, pg = 0, pb = 0;
