@@ -337,14 +337,12 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 // next tile's features are computed and stored while the current tile's last MMA runs:
 //   features(k) -> A[x]; h1 -> A[1-x]; h2 -> A[x]; features(k+1) -> A[1-x] during layer 3.
 //
-// Tile k's sampled rows put their normal and albedo into the slot's check rows (by tile parity) while
-// its first MMA runs, and two warps that do not issue its second MMA split the lights and sum their
-// parts while that one runs; the sampled rows add their output at the end of the tile. While tile
-// k + 1's first MMA runs, the warp that issues none of tile k + 1's layers adds the two parts,
-// compares and records the verdict (the failed tile, or none). The whole slot reads the verdict
-// after the barrier that opens tile k + 2 and shades a failed tile again, exactly, right there; the
-// last two verdicts are read after the loop. The kernel is compiled for each number of checked
-// samples, and the light table comes with the weights (built with them for their rig).
+// Checks: the sampled rows of each tile put their normal, albedo and learned colour into the slot's
+// check buffer at the end of the tile; after every kCheckTiles tiles, and after the slot's last
+// tile, the slot checks the buffered rows in one pass (each warp a few rows at a time, its lanes
+// splitting the lights) and shades the tiles that failed again, exactly. The kernel is compiled for
+// each number of checked samples, and the light table comes with the weights (built with them for
+// their rig).
 //
 // RAST_MLP_SLOTS (at most 4: 4 x 128 columns fill the tensor memory) can be changed at build time
 // to measure fewer slots; the default is the fastest measured.
@@ -363,7 +361,6 @@ static_assert(kMlpIn == kMlpHid, "one A operand shape serves every layer");
 static_assert(kSlots >= 1 && kSlots * kSlotTmem <= kTmemCols, "tensor memory of one SM");
 constexpr uint32_t kMaxSamples = 4;
 constexpr int kMlpSmemLights = 512;  // lights the checks read from shared memory
-constexpr uint32_t kNoTile = 0xFFFFFFFFu;
 
 // Shared memory (bytes): the weights and output scale, the checks' light table (dirI then gb, as in
 // MlpCheckTable), then the small block.
@@ -378,11 +375,12 @@ struct CheckRow {
     float n[3], alb[3], rad[3];  // the row's normal and albedo, and the learned radiance (clamped)
     uint32_t valid;
 };
+constexpr uint32_t kCheckTiles = 16;       // tiles a slot buffers before it checks them
 struct SlotMisc {
     unsigned long long mbar;                // MMA completion
-    uint32_t verdict[2];                    // by the checked tile's parity: that tile when it failed, else kNoTile
-    CheckRow q[2][kMaxSamples];             // by tile parity: the sampled rows
-    int32_t part[2][3 * kMaxSamples];       // by checking warp: its light sums (3 s + c), fixed point
+    uint32_t fail_mask;                     // after a check: bit j set when buffered tile j failed
+    uint32_t pad;
+    CheckRow q[kCheckTiles][kMaxSamples];   // the buffered tiles' sampled rows
 };
 struct MlpMisc {
     unsigned long long mbar_w;     // the weights' bulk copy
@@ -510,79 +508,78 @@ struct SmemLights {
     const float2* gb;
 };
 
-// A lane's part of a tile's check, for checking warp c of two: the warps split the lights (lane
-// `lane` of warp c takes lights 32 c + lane, 32 c + lane + 64, ...) and sum, for each sampled row q[s]
-// and channel ch, (I ch)_l * max(0, n . -dir_l) with fused multiply-adds; the warp then adds its
-// lanes' sums in fixed point (scale fx: any sum over the lights for a normal of length <= 4 stays
-// below 2^29 in magnitude) and stores them in part[c][3 s + ch]. The sum only estimates the exact
-// shade: it judges the learned colour and is never itself a colour. Lights come from the shared
-// table when it holds them, else from global memory.
+// The check of the slot's buffered tiles (n_rows = tiles * NS sampled rows, tile j's sample s at
+// q[j][s]): warp w takes rows w, w + 4, ..., up to G at a time, its lanes split the lights (lane
+// `lane` takes lights lane, lane + 32, ...) and sum, per row and channel c, (I c)_l * max(0,
+// n . -dir_l) with fused multiply-adds; the warp adds the lanes' sums in fixed point (scale fx: any
+// sum over the lights for a normal of length <= 4 stays below 2^29 in magnitude), and lane 3 i + c
+// compares |learned - min(sum * albedo / pi, 255)| with the bound, marking the row's tile in
+// fail_mask. A normal longer than 4 fails its tile. The sum only estimates the exact shade: it
+// judges the learned colour and is never itself a colour. Lights come from the shared table when it
+// holds them, else from global memory.
 template <int NS>
-__device__ __forceinline__ void check_part(const ShadeArgs& a, const SmemLights* L, const CheckRow* q,
-                                           int32_t (*part)[3 * kMaxSamples], float fx, int c, int lane) {
-    float nx[NS], ny[NS], nz[NS];
+__device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int n_rows, float fx, float inv_fx,
+                           int wq, int lane, float& max_err) {
+    constexpr int G = 3;
+    for (int r0 = wq; r0 < n_rows; r0 += 4 * G) {
+        int rr[G];
+        float nx[G], ny[G], nz[G];
 #pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        nx[s] = q[s].n[0];
-        ny[s] = q[s].n[1];
-        nz[s] = q[s].n[2];
-    }
-    float v[3 * NS];
+        for (int i = 0; i < G; ++i) {
+            rr[i] = r0 + 4 * i;
+            const bool in = rr[i] < n_rows;
+            const CheckRow& q = S.q[in ? rr[i] / NS : 0][in ? rr[i] % NS : 0];
+            nx[i] = in ? q.n[0] : 0.f;
+            ny[i] = in ? q.n[1] : 0.f;
+            nz[i] = in ? q.n[2] : 0.f;
+        }
+        float v[3 * G];
 #pragma unroll
-    for (int i = 0; i < 3 * NS; ++i) v[i] = 0.f;
+        for (int i = 0; i < 3 * G; ++i) v[i] = 0.f;
 #pragma unroll 4
-    for (int l = 32 * c + lane; l < a.nl; l += 64) {
-        float4 A;
-        float2 B;
-        if (L) {
-            A = L->dirI[l];
-            B = L->gb[l];
-        } else {
-            const float* P = a.lights + 7 * (int64_t)l;
-            const float I = __ldg(P + 3);
-            A = make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4));
-            B = make_float2(I * __ldg(P + 5), I * __ldg(P + 6));
-        }
-#pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            const float m = fmaxf(fmaf(nz[s], A.z, fmaf(ny[s], A.y, nx[s] * A.x)), 0.f);
-            v[3 * s] = fmaf(A.w, m, v[3 * s]);
-            v[3 * s + 1] = fmaf(B.x, m, v[3 * s + 1]);
-            v[3 * s + 2] = fmaf(B.y, m, v[3 * s + 2]);
-        }
-    }
-    int32_t r[3 * NS];
-#pragma unroll
-    for (int i = 0; i < 3 * NS; ++i) r[i] = __reduce_add_sync(kFull, __float2int_rn(v[i] * fx));
-    if (lane == 0)
-#pragma unroll
-        for (int i = 0; i < 3 * NS; ++i) part[c][i] = r[i];
-}
-
-// The verdict of a tile's check, by one warp: lane 3 s + c adds the two checking warps' parts of
-// sampled row s, channel c (scaled back by inv_fx = 1 / fx), and compares |learned - min(sum * albedo / pi, 255)| with the bound; a sampled
-// normal longer than 4 (outside the fixed-point range) fails the tile. Returns, in every lane,
-// whether a sampled row fails.
-template <int NS>
-__device__ __forceinline__ bool check_verdict(const ShadeArgs& a, const CheckRow* q,
-                                              const int32_t (*part)[3 * kMaxSamples], float inv_fx, int lane,
-                                              float& max_err) {
-    bool bad = false;
-    if (lane < 3 * NS) {
-        const int s = lane / 3, c = lane - 3 * s;
-        if (q[s].valid) {
-            const float nn = fmaf(q[s].n[2], q[s].n[2], fmaf(q[s].n[1], q[s].n[1], q[s].n[0] * q[s].n[0]));
-            if (!(nn <= 16.f)) {
-                bad = true;
+        for (int l = lane; l < a.nl; l += 32) {
+            float4 A;
+            float2 B;
+            if (L) {
+                A = L->dirI[l];
+                B = L->gb[l];
             } else {
-                const float sum = (float)((int64_t)part[0][lane] + part[1][lane]) * inv_fx;
-                const float err = fabsf(q[s].rad[c] - fminf(sum * q[s].alb[c] * kOneOverPi, 255.f));
-                max_err = fmaxf(max_err, err);
-                bad = err > a.bound;
+                const float* P = a.lights + 7 * (int64_t)l;
+                const float I = __ldg(P + 3);
+                A = make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4));
+                B = make_float2(I * __ldg(P + 5), I * __ldg(P + 6));
+            }
+#pragma unroll
+            for (int i = 0; i < G; ++i) {
+                const float m = fmaxf(fmaf(nz[i], A.z, fmaf(ny[i], A.y, nx[i] * A.x)), 0.f);
+                v[3 * i] = fmaf(A.w, m, v[3 * i]);
+                v[3 * i + 1] = fmaf(B.x, m, v[3 * i + 1]);
+                v[3 * i + 2] = fmaf(B.y, m, v[3 * i + 2]);
+            }
+        }
+        float sum = 0.f;
+#pragma unroll
+        for (int j = 0; j < 3 * G; ++j) {
+            const float t = (float)__reduce_add_sync(kFull, __float2int_rn(v[j] * fx)) * inv_fx;
+            if (lane == j) sum = t;
+        }
+        if (lane < 3 * G) {
+            const int i = lane / 3, c = lane - 3 * i, r = r0 + 4 * i;
+            if (r < n_rows) {
+                const CheckRow& q = S.q[r / NS][r % NS];
+                if (q.valid) {
+                    const float nn = fmaf(q.n[2], q.n[2], fmaf(q.n[1], q.n[1], q.n[0] * q.n[0]));
+                    bool bad = !(nn <= 16.f);
+                    if (!bad) {
+                        const float err = fabsf(q.rad[c] - fminf(sum * q.alb[c] * kOneOverPi, 255.f));
+                        max_err = fmaxf(max_err, err);
+                        bad = err > a.bound;
+                    }
+                    if (bad) atomicOr(&S.fail_mask, 1u << (r / NS));
+                }
             }
         }
     }
-    return __any_sync(kFull, bad);
 }
 
 // Shades tile t again, exactly, in the reference's order: each row by the thread that shaded it
@@ -637,7 +634,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
             bulk_copy_g2s(smem_addr(lights_gb), tab->gb, tab_gb, mbar_w);
         }
     }
-    if (row == 0) S.verdict[0] = S.verdict[1] = kNoTile;
+    if (row == 0) S.fail_mask = 0u;
     if (threadIdx.x < 32) tmem_alloc(smem_addr(&M.tmem), kTmemCols);
     // the records and the tile list are the previous kernel's output
     asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -678,6 +675,22 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     uint32_t n_tile = 0, n_fallback = 0;
     float max_err = 0.f;
     uint32_t k = 0;  // tiles this slot shaded
+    uint32_t kb = 0, t_batch = t;  // tiles in the check buffer, the first of them
+    // Checks the buffered tiles and shades those that failed again, exactly (buffered tile j is
+    // t0 + j * stride); every thread of the slot calls it after a slot barrier.
+    auto check_buffer = [&](uint32_t n_buf, uint32_t t0) {
+        if constexpr (checking) {
+            check_rows<checking ? NS : 1>(a, L, S, (int)(n_buf * n_samples), fx, inv_fx, wq, lane, max_err);
+            slot_sync(slot);
+            const uint32_t f = S.fail_mask;
+            slot_sync(slot);  // every thread read the verdicts before they are cleared
+            if (row == 0) S.fail_mask = 0u;
+            for (uint32_t m = f; m; m &= m - 1u) {
+                if (row == 0) ++n_fallback;
+                reshade_tile(a, t0 + (uint32_t)(__ffs(m) - 1) * stride, row);
+            }
+        }
+    };
     // Layer L of the slot's tile k is issued by lane 0 of warp (k + L) mod 4: the issue holds its
     // warp for a few hundred cycles, and so falls on every warp (and scheduler) in turn.
 
@@ -689,13 +702,6 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
 
         // layer 1: D = X (128 x K) * W1^T
         if (row == 32 * (int)((k + 1u) & 3u)) issue_layer(d_cols, a_cur, sW1, kMlpHid, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-        if constexpr (checking) {
-            const uint32_t v = S.verdict[k & 1u];  // tile k - 2's, the same in every thread of the slot
-            if (v != kNoTile) {
-                if (row == 0) ++n_fallback;
-                reshade_tile(a, v, row);
-            }
-        }
         // the slot's tile after next: its descriptor now, its records during layer 3
         const uint32_t t_nn = t_next + stride;
         const uint32_t count_nn = tile_count(n_frag, n_tiles, t_nn);
@@ -709,21 +715,6 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
             for (int s = 0; s < n_samples; ++s)
                 if (sample_rank(h_t, s, count) == (uint32_t)row) my_samples |= 1u << s;
         }
-        if constexpr (checking) {
-            // this tile's sampled rows: normal and albedo (the output follows at the end)
-            for (uint32_t m = my_samples; m; m &= m - 1u) {
-                CheckRow& q = S.q[k & 1u][__ffs(m) - 1];
-                q.n[0] = g0.x; q.n[1] = g0.y; q.n[2] = g0.z;
-                q.alb[0] = g0.w; q.alb[1] = g1.x; q.alb[2] = g1.y;
-            }
-            // the previous tile's verdict, by the warp that issues none of this tile's layers (its
-            // parts and output were written before the last barrier)
-            if (k > 0u && (int)(k & 3u) == wq) {
-                const uint32_t p = (k - 1u) & 1u;
-                const bool bad = check_verdict<NS>(a, S.q[p], S.part, inv_fx, lane, max_err);
-                if (lane == 0) S.verdict[p] = bad ? t - stride : kNoTile;
-            }
-        }
         // After a wait gave up (`failed`), a warp touches tensor memory no more: an MMA may still
         // be using it. The test is warp-uniform, as the .sync.aligned tcgen05 instructions need.
         failed |= !mbar_wait(mbar_first, phase, tries_first);
@@ -735,11 +726,6 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
 
         // layer 2: D = H1 (128 x 64) * W2^T
         if (row == 32 * (int)((k + 2u) & 3u)) issue_layer(d_cols, a_oth, sW2, kMlpHid, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
-        // this tile's check: the parts of two warps that do not issue this layer (its sampled rows
-        // were written before the last barrier)
-        if constexpr (checking)
-            if ((int)(k & 3u) == wq || (int)((k + 1u) & 3u) == wq)
-                check_part<NS>(a, L, S.q[k & 1u], S.part, fx, (int)(k & 3u) == wq ? 0 : 1, lane);
         failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
         tc_fence_after();
@@ -782,11 +768,20 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
                 write_rgb(a.rgb, a.npx, pix,
                           __float2uint_rz(radc.x) | (__float2uint_rz(radc.y) << 8) | (__float2uint_rz(radc.z) << 16));
             for (uint32_t m = my_samples; m; m &= m - 1u) {  // every sampled row of the tile is written once
-                CheckRow& q = S.q[k & 1u][__ffs(m) - 1];
+                CheckRow& q = S.q[kb][__ffs(m) - 1];
+                q.n[0] = g0.x; q.n[1] = g0.y; q.n[2] = g0.z;
+                q.alb[0] = alb.x; q.alb[1] = alb.y; q.alb[2] = alb.z;
                 q.rad[0] = radc.x; q.rad[1] = radc.y; q.rad[2] = radc.z;
                 q.valid = valid ? 1u : 0u;
             }
             ++n_tile;
+            if constexpr (checking)
+                if (++kb == kCheckTiles) {  // the same in every thread of the slot
+                    if (slot_sync_or(slot, failed)) break;
+                    check_buffer(kb, t_batch);
+                    kb = 0u;
+                    t_batch = t_next;
+                }
         }
         ++k;
         x ^= 1u;
@@ -800,26 +795,9 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         g1n = g1nn;
     }
 
-    // The last tile's verdict, then the last two verdicts read (every thread of the slot reaches
-    // these barriers: the loop ends at the same point in all of them, and the first one orders the
-    // last tile's parts and output before its verdict).
-    if (!slot_sync_or(slot, failed) && checking && !weights_pending && k > 0u) {
-        if constexpr (checking) {
-            const uint32_t p = (k - 1u) & 1u;
-            if ((int)(k & 3u) == wq) {
-                const bool bad = check_verdict<NS>(a, S.q[p], S.part, inv_fx, lane, max_err);
-                if (lane == 0) S.verdict[p] = bad ? t - stride : kNoTile;
-            }
-        }
-        slot_sync(slot);
-        for (uint32_t j = (k >= 2u ? k - 2u : 0u); j < k; ++j) {
-            const uint32_t v = S.verdict[j & 1u];  // the same in every thread of the slot
-            if (v != kNoTile) {
-                if (row == 0) ++n_fallback;
-                reshade_tile(a, v, row);
-            }
-        }
-    }
+    // the rest of the check buffer (every thread of the slot reaches this barrier: the loop ends
+    // at the same point in all of them, and it orders the buffer's rows before the check)
+    if (!slot_sync_or(slot, failed) && checking && !weights_pending && kb > 0u) check_buffer(kb, t_batch);
 
     if (failed) {
         // the weights' copy or an MMA did not complete in time: record it, give the pending one
