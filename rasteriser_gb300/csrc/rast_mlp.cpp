@@ -94,34 +94,26 @@ std::vector<float> rounded(const std::vector<float>& w) {
     return q;
 }
 
-// The checks' light table for the rig, in the float arithmetic the shading kernel's checks use,
-// and the bound of their sums (sum over the lights of |dir| * max_c |I c|).
-void pack_check_table(const std::vector<float>& lights, int nl, MlpCheckTable& t, float& light_sum) {
+// The checks' light table for the rig (the first kMlpCheckLights lights).
+void pack_check_table(const std::vector<float>& lights, int nl, MlpCheckTable& t) {
     std::memset(&t, 0, sizeof t);
-    double sum = 0.0;
-    for (int l = 0; l < nl; ++l) {
+    for (int l = 0; l < nl && l < kMlpCheckLights; ++l) {
         const float* P = lights.data() + 7 * (size_t)l;
         const float I = P[3];
-        const float w[3] = {I * P[4], I * P[5], I * P[6]};
-        if (l < kMlpCheckLights) {
-            t.dirI[l][0] = -P[0];
-            t.dirI[l][1] = -P[1];
-            t.dirI[l][2] = -P[2];
-            t.dirI[l][3] = w[0];
-            t.gb[l][0] = w[1];
-            t.gb[l][1] = w[2];
-        }
-        const double len = std::sqrt((double)P[0] * P[0] + (double)P[1] * P[1] + (double)P[2] * P[2]);
-        sum += len * std::max(std::fabs((double)w[0]), std::max(std::fabs((double)w[1]), std::fabs((double)w[2])));
+        t.dirI[l][0] = -P[0];
+        t.dirI[l][1] = -P[1];
+        t.dirI[l][2] = -P[2];
+        t.dirI[l][3] = I * P[4];
+        t.gb[l][0] = I * P[5];
+        t.gb[l][1] = I * P[6];
     }
-    light_sum = (float)sum;
 }
 
 rast_status install(rast_ctx* c, const std::vector<float>& q, float scale, float loss) {
     MlpImage im;
     pack_image(q, scale, im);
     MlpCheckTable tab;
-    pack_check_table(c->lights_host, c->nl, tab, im.light_sum);
+    pack_check_table(c->lights_host, c->nl, tab);
     RAST_CUDA(c, c->mlp_image.reserve(sizeof(MlpImage) + sizeof(MlpCheckTable)));
     RAST_CUDA(c, cudaMemcpy(c->mlp_image.ptr, &im, sizeof im, cudaMemcpyHostToDevice));
     RAST_CUDA(c, cudaMemcpy(static_cast<char*>(c->mlp_image.ptr) + sizeof im, &tab, sizeof tab, cudaMemcpyHostToDevice));

@@ -64,8 +64,7 @@ struct MlpImage {
     uint16_t w2[kMlpHid * kMlpHid];     // layer 2 B operand, 64 x 64
     uint16_t w3[kMlpOutPad * kMlpHid];  // layer 3 B operand, 16 x 64 (rows 3.. zero)
     float out_scale;
-    float light_sum;                    // sum over the rig's lights of |dir| * max_c |I c|
-    float reserved[2];
+    float reserved[3];
 };
 static_assert(sizeof(MlpImage) % 16 == 0, "MlpImage is copied in 16-byte units");
 

@@ -509,17 +509,16 @@ struct SmemLights {
 };
 
 // The check of the slot's buffered tiles (n_rows = tiles * NS sampled rows, tile j's sample s at
-// q[j][s]): warp w takes rows w, w + 4, ..., up to G at a time, its lanes split the lights (lane
-// `lane` takes lights lane, lane + 32, ...) and sum, per row and channel c, (I c)_l * max(0,
-// n . -dir_l) with fused multiply-adds; the warp adds the lanes' sums in fixed point (scale fx: any
-// sum over the lights for a normal of length <= 4 stays below 2^29 in magnitude), and lane 3 i + c
-// compares |learned - min(sum * albedo / pi, 255)| with the bound, marking the row's tile in
-// fail_mask. A normal longer than 4 fails its tile. The sum only estimates the exact shade: it
-// judges the learned colour and is never itself a colour. Lights come from the shared table when it
-// holds them, else from global memory.
+// q[j][s]): warp w takes rows w, w + 4, ..., G at a time, its lanes split the lights (lane `lane`
+// takes lights lane, lane + 32, ...) and sum, per row and channel c, (I c)_l * max(0, n . -dir_l)
+// with fused multiply-adds; the warp adds the lanes' sums by halving (each level a lane keeps half
+// of its values and adds its partner's copy of them), and lane 3 i + c compares
+// |learned - min(sum * albedo / pi, 255)| with the bound, marking the row's tile in fail_mask. The
+// sum only estimates the exact shade: it judges the learned colour and is never itself a colour.
+// Lights come from the shared table when it holds them, else from global memory.
 template <int NS>
-__device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int n_rows, float fx, float inv_fx,
-                           int wq, int lane, float& max_err) {
+__device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int n_rows, int wq, int lane,
+                           float& max_err) {
     constexpr int G = 3;
     for (int r0 = wq; r0 < n_rows; r0 += 4 * G) {
         int rr[G];
@@ -536,19 +535,7 @@ __device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S,
         float v[3 * G];
 #pragma unroll
         for (int i = 0; i < 3 * G; ++i) v[i] = 0.f;
-#pragma unroll 4
-        for (int l = lane; l < a.nl; l += 32) {
-            float4 A;
-            float2 B;
-            if (L) {
-                A = L->dirI[l];
-                B = L->gb[l];
-            } else {
-                const float* P = a.lights + 7 * (int64_t)l;
-                const float I = __ldg(P + 3);
-                A = make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4));
-                B = make_float2(I * __ldg(P + 5), I * __ldg(P + 6));
-            }
+        auto acc = [&](float4 A, float2 B) {
 #pragma unroll
             for (int i = 0; i < G; ++i) {
                 const float m = fmaxf(fmaf(nz[i], A.z, fmaf(ny[i], A.y, nx[i] * A.x)), 0.f);
@@ -556,26 +543,42 @@ __device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S,
                 v[3 * i + 1] = fmaf(B.x, m, v[3 * i + 1]);
                 v[3 * i + 2] = fmaf(B.y, m, v[3 * i + 2]);
             }
+        };
+        if (L) {
+#pragma unroll 4
+            for (int l = lane; l < a.nl; l += 32) acc(L->dirI[l], L->gb[l]);
+        } else {
+            for (int l = lane; l < a.nl; l += 32) {
+                const float* P = a.lights + 7 * (int64_t)l;
+                const float I = __ldg(P + 3);
+                acc(make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4)),
+                    make_float2(I * __ldg(P + 5), I * __ldg(P + 6)));
+            }
         }
-        float sum = 0.f;
+        static_assert(3 * G <= 16, "values per lane");
+        float w[16];
 #pragma unroll
-        for (int j = 0; j < 3 * G; ++j) {
-            const float t = (float)__reduce_add_sync(kFull, __float2int_rn(v[j] * fx)) * inv_fx;
-            if (lane == j) sum = t;
+        for (int j = 0; j < 16; ++j) w[j] = j < 3 * G ? v[j < 3 * G ? j : 0] : 0.f;
+#pragma unroll
+        for (int h = 8, o = 16; h >= 1; h >>= 1, o >>= 1) {
+            const bool up = (lane & o) != 0;
+#pragma unroll
+            for (int i = 0; i < h; ++i) {
+                const float mine = up ? w[i + h] : w[i], other = up ? w[i] : w[i + h];
+                w[i] = mine + __shfl_xor_sync(kFull, other, o);
+            }
         }
+        w[0] += __shfl_xor_sync(kFull, w[0], 1);
+        // lane 2j (and 2j + 1) holds value j
+        float sum = __shfl_sync(kFull, w[0], (2 * lane) & 31);
         if (lane < 3 * G) {
             const int i = lane / 3, c = lane - 3 * i, r = r0 + 4 * i;
             if (r < n_rows) {
                 const CheckRow& q = S.q[r / NS][r % NS];
                 if (q.valid) {
-                    const float nn = fmaf(q.n[2], q.n[2], fmaf(q.n[1], q.n[1], q.n[0] * q.n[0]));
-                    bool bad = !(nn <= 16.f);
-                    if (!bad) {
-                        const float err = fabsf(q.rad[c] - fminf(sum * q.alb[c] * kOneOverPi, 255.f));
-                        max_err = fmaxf(max_err, err);
-                        bad = err > a.bound;
-                    }
-                    if (bad) atomicOr(&S.fail_mask, 1u << (r / NS));
+                    const float err = fabsf(q.rad[c] - fminf(sum * q.alb[c] * kOneOverPi, 255.f));
+                    max_err = fmaxf(max_err, err);
+                    if (!(err <= a.bound)) atomicOr(&S.fail_mask, 1u << (r / NS));
                 }
             }
         }
@@ -663,9 +666,6 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     a_written();
     bool failed = !__syncthreads_and(mbar_wait(mbar_w, 0));
     const bool weights_pending = failed;
-    // the checks' fixed-point scale: every sum over the lights for a unit normal stays below 2^27
-    const float fx = 0x1p27f / fmaxf(reinterpret_cast<const MlpImage*>(sm)->light_sum * 1.001f, 0x1p-60f),
-                inv_fx = 1.f / fx;
     const float out_scale = reinterpret_cast<const MlpImage*>(sm)->out_scale;
     const uint32_t sW1 = smem_addr(sm + kSmW1), sW2 = smem_addr(sm + kSmW2), sW3 = smem_addr(sm + kSmW3);
 
@@ -680,7 +680,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     // t0 + j * stride); every thread of the slot calls it after a slot barrier.
     auto check_buffer = [&](uint32_t n_buf, uint32_t t0) {
         if constexpr (checking) {
-            check_rows<checking ? NS : 1>(a, L, S, (int)(n_buf * n_samples), fx, inv_fx, wq, lane, max_err);
+            check_rows<checking ? NS : 1>(a, L, S, (int)(n_buf * n_samples), wq, lane, max_err);
             slot_sync(slot);
             const uint32_t f = S.fail_mask;
             slot_sync(slot);  // every thread read the verdicts before they are cleared

@@ -291,7 +291,7 @@ def test_learned_checks_catch_a_wrong_network(rnd, port, trained):
 
 def test_learned_checks_with_lights_beyond_the_shared_table(rnd, port):
     """600 lights: more than the shared check table holds, so the checks read the light records
-    from global memory (their fixed-point bound still covers every light). At a bound of 0 every
+    from global memory. At a bound of 0 every
     tile whose checked records differ at all falls back: the exact colour; at the default bound the
     verdicts agree with the largest checked error."""
     sc = small_many_lights(600, 320, 240)
