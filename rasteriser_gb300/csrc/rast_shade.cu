@@ -339,8 +339,8 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 //
 // Checks: the sampled rows of each tile put their normal, albedo and learned colour into the slot's
 // check buffer at the end of the tile; after every kCheckTiles tiles, and after the slot's last
-// tile, the slot checks the buffered rows in one pass (each warp a few rows at a time, its lanes
-// splitting the lights) and shades the tiles that failed again, exactly. The kernel is compiled for
+// tile, the slot checks the buffered rows (ten at a time, its four warps splitting the lights) and
+// shades the tiles that failed again, exactly. The kernel is compiled for
 // each number of checked samples, and the light table comes with the weights (built with them for
 // their rig).
 //
@@ -381,6 +381,7 @@ struct SlotMisc {
     uint32_t fail_mask;                     // after a check: bit j set when buffered tile j failed
     uint32_t pad;
     CheckRow q[kCheckTiles][kMaxSamples];   // the buffered tiles' sampled rows
+    float part[4][32];                      // a check pass: each warp's sums (3 i + c)
 };
 struct MlpMisc {
     unsigned long long mbar_w;     // the weights' bulk copy
@@ -509,35 +510,38 @@ struct SmemLights {
 };
 
 // The check of the slot's buffered tiles (n_rows = tiles * NS sampled rows, tile j's sample s at
-// q[j][s]): warp w takes rows w, w + 4, ..., G at a time, its lanes split the lights (lane `lane`
-// takes lights lane, lane + 32, ...) and sum, per row and channel c, (I c)_l * max(0, n . -dir_l)
-// with fused multiply-adds; the warp adds the lanes' sums by halving (each level a lane keeps half
-// of its values and adds its partner's copy of them), and lane 3 i + c compares
-// |learned - min(sum * albedo / pi, 255)| with the bound, marking the row's tile in fail_mask. The
-// sum only estimates the exact shade: it judges the learned colour and is never itself a colour.
-// Lights come from the shared table when it holds them, else from global memory.
+// q[j][s]), up to kCheckPass rows per pass: the slot's four warps split the lights (lane `lane` of
+// warp w takes lights 32 w + lane, 32 w + lane + 128, ...), so the light table is read once per
+// pass, and sum, per row i and channel c, (I c)_l * max(0, n . -dir_l) with fused multiply-adds;
+// each warp adds its lanes' sums by halving (each level a lane keeps half of its values and adds its
+// partner's copy of them, leaving value j in lane j) into part[w][3 i + c], and after a slot barrier
+// lane 3 i + c of warp 0 adds the four parts and compares |learned - min(sum * albedo / pi, 255)|
+// with the bound, marking the row's tile in fail_mask. The sum only estimates the exact shade: it
+// judges the learned colour and is never itself a colour. Lights come from the shared table when it
+// holds them, else from global memory. Every thread of the slot calls it.
+constexpr int kCheckPass = 10;
+static_assert(3 * kCheckPass <= 32, "one value per lane");
 template <int NS>
-__device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int n_rows, int wq, int lane,
-                           float& max_err) {
-    constexpr int G = 3;
-    for (int r0 = wq; r0 < n_rows; r0 += 4 * G) {
-        int rr[G];
-        float nx[G], ny[G], nz[G];
+__device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int n_rows, int slot, int wq,
+                           int lane, float& max_err) {
+    for (int r0 = 0; r0 < n_rows; r0 += kCheckPass) {
+        const int nr = min(kCheckPass, n_rows - r0);
+        float nx[kCheckPass], ny[kCheckPass], nz[kCheckPass];
 #pragma unroll
-        for (int i = 0; i < G; ++i) {
-            rr[i] = r0 + 4 * i;
-            const bool in = rr[i] < n_rows;
-            const CheckRow& q = S.q[in ? rr[i] / NS : 0][in ? rr[i] % NS : 0];
+        for (int i = 0; i < kCheckPass; ++i) {
+            const int r = r0 + i;
+            const bool in = i < nr;
+            const CheckRow& q = S.q[in ? r / NS : 0][in ? r % NS : 0];
             nx[i] = in ? q.n[0] : 0.f;
             ny[i] = in ? q.n[1] : 0.f;
             nz[i] = in ? q.n[2] : 0.f;
         }
-        float v[3 * G];
+        float v[32];
 #pragma unroll
-        for (int i = 0; i < 3 * G; ++i) v[i] = 0.f;
+        for (int j = 0; j < 32; ++j) v[j] = 0.f;
         auto acc = [&](float4 A, float2 B) {
 #pragma unroll
-            for (int i = 0; i < G; ++i) {
+            for (int i = 0; i < kCheckPass; ++i) {
                 const float m = fmaxf(fmaf(nz[i], A.z, fmaf(ny[i], A.y, nx[i] * A.x)), 0.f);
                 v[3 * i] = fmaf(A.w, m, v[3 * i]);
                 v[3 * i + 1] = fmaf(B.x, m, v[3 * i + 1]);
@@ -545,43 +549,37 @@ __device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S,
             }
         };
         if (L) {
-#pragma unroll 4
-            for (int l = lane; l < a.nl; l += 32) acc(L->dirI[l], L->gb[l]);
+            for (int l = 32 * wq + lane; l < a.nl; l += 128) acc(L->dirI[l], L->gb[l]);
         } else {
-            for (int l = lane; l < a.nl; l += 32) {
+            for (int l = 32 * wq + lane; l < a.nl; l += 128) {
                 const float* P = a.lights + 7 * (int64_t)l;
                 const float I = __ldg(P + 3);
                 acc(make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4)),
                     make_float2(I * __ldg(P + 5), I * __ldg(P + 6)));
             }
         }
-        static_assert(3 * G <= 16, "values per lane");
-        float w[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) w[j] = j < 3 * G ? v[j < 3 * G ? j : 0] : 0.f;
-#pragma unroll
-        for (int h = 8, o = 16; h >= 1; h >>= 1, o >>= 1) {
+        for (int h = 16, o = 16; h >= 1; h >>= 1, o >>= 1) {
             const bool up = (lane & o) != 0;
 #pragma unroll
             for (int i = 0; i < h; ++i) {
-                const float mine = up ? w[i + h] : w[i], other = up ? w[i] : w[i + h];
-                w[i] = mine + __shfl_xor_sync(kFull, other, o);
+                const float mine = up ? v[i + h] : v[i], other = up ? v[i] : v[i + h];
+                v[i] = mine + __shfl_xor_sync(kFull, other, o);
             }
         }
-        w[0] += __shfl_xor_sync(kFull, w[0], 1);
-        // lane 2j (and 2j + 1) holds value j
-        float sum = __shfl_sync(kFull, w[0], (2 * lane) & 31);
-        if (lane < 3 * G) {
-            const int i = lane / 3, c = lane - 3 * i, r = r0 + 4 * i;
-            if (r < n_rows) {
-                const CheckRow& q = S.q[r / NS][r % NS];
-                if (q.valid) {
-                    const float err = fabsf(q.rad[c] - fminf(sum * q.alb[c] * kOneOverPi, 255.f));
-                    max_err = fmaxf(max_err, err);
-                    if (!(err <= a.bound)) atomicOr(&S.fail_mask, 1u << (r / NS));
-                }
+        if (lane < 3 * nr) S.part[wq][lane] = v[0];
+        slot_sync(slot);
+        if (wq == 0 && lane < 3 * nr) {
+            const int i = lane / 3, c = lane - 3 * i, r = r0 + i;
+            const CheckRow& q = S.q[r / NS][r % NS];
+            if (q.valid) {
+                const float sum = (S.part[0][lane] + S.part[1][lane]) + (S.part[2][lane] + S.part[3][lane]);
+                const float err = fabsf(q.rad[c] - fminf(sum * q.alb[c] * kOneOverPi, 255.f));
+                max_err = fmaxf(max_err, err);
+                if (!(err <= a.bound)) atomicOr(&S.fail_mask, 1u << (r / NS));
             }
         }
+        slot_sync(slot);  // the parts are read before the next pass writes them
     }
 }
 
@@ -680,7 +678,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     // t0 + j * stride); every thread of the slot calls it after a slot barrier.
     auto check_buffer = [&](uint32_t n_buf, uint32_t t0) {
         if constexpr (checking) {
-            check_rows<checking ? NS : 1>(a, L, S, (int)(n_buf * n_samples), wq, lane, max_err);
+            check_rows<checking ? NS : 1>(a, L, S, (int)(n_buf * n_samples), slot, wq, lane, max_err);
             slot_sync(slot);
             const uint32_t f = S.fail_mask;
             slot_sync(slot);  // every thread read the verdicts before they are cleared
