@@ -4,9 +4,9 @@
 //   k_shade_exact  shading.cpp:20-34 per fragment, lights staged in shared memory: the plain
 //                  shader, bit for bit the reference's colour
 //   k_shade_mlp    per tile of 128 records: Fourier features -> three tcgen05 BF16 MMAs with FP32
-//                  accumulators in tensor memory -> radiance; a few records of every tile are also
-//                  shaded exactly, and a tile whose checked error exceeds the bound is shaded
-//                  exactly in full
+//                  accumulators in tensor memory -> radiance; a few records of every tile are
+//                  checked against the per-light sum, and a tile whose checked error exceeds the
+//                  bound is shaded exactly in full (compiled per number of checked records)
 //   k_shade_scan   the tile list for records staged by k_mlp_stage (draws list their tiles in the
 //                  resolve pass)
 //   k_mlp_samples / k_mlp_train / k_mlp_adam   training on (normal, albedo) samples labelled by
