@@ -198,6 +198,11 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 #define RAST_OPT_TILE_THREADS 10      /* threads per tile of the tile raster (binned triangles):
                                          64, 128, 256 or, with tile 32, 512; 0 (default):
                                          min(tile * tile, 256) */
+#define RAST_OPT_HOST_IN_PLACE 11     /* rast_draw's host buffers. 1 (default): used in place by the
+                                         kernels when the device reaches them (page-locked memory
+                                         it maps; ordinary pageable memory when it translates host
+                                         addresses through the host's page tables, as on Grace);
+                                         0: always copied through device memory */
 #define RAST_OPT_TEST_SHADE_STALL 9   /* test only (default 0). 1: the learned shader's first wait
                                          for a tensor-core MMA polls an mbarrier nothing arrives
                                          on, 1024 times, so it gives up as a lost MMA would: the

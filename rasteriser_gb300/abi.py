@@ -22,6 +22,7 @@ STATUS_NAMES = {0: "RAST_OK", 1: "RAST_ERR_INVALID_ARG", 2: "RAST_ERR_BAD_INDEX"
 WIND_CLOCKWISE, CLEAR, FLAT = 1, 2, 4
 OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY, OPT_STAGE_TIMING, OPT_ROW_CHUNK = 1, 2, 3, 4, 5
 OPT_SHADER, OPT_MLP_SAMPLES, OPT_MLP_BOUND_MILLI, OPT_TEST_SHADE_STALL, OPT_TILE_THREADS = 6, 7, 8, 9, 10
+OPT_HOST_IN_PLACE = 11
 SHADER_EXACT, SHADER_EXACT_DEFERRED, SHADER_LEARNED = 0, 1, 2
 STAGES = ["arm", "vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve", "shade", "total"]
 NO_TRIANGLE = 0xFFFFFFFF

@@ -2,6 +2,8 @@
 // orchestration of one draw. The kernels are in rast_kernels.cu.
 #include <cuda.h>  // pointer attribute names; the driver function is reached through cudart
 #include <cuda_runtime.h>
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <chrono>
@@ -24,10 +26,42 @@ namespace {
 
 uint32_t tile_shift(uint32_t tile) { return tile == 8 ? 3u : (tile == 16 ? 4u : 5u); }
 
-// The device address of [p, p + bytes) when the whole range lies in one page-locked host
-// allocation that the device maps (cudaHostAlloc, cudaHostRegister, torch's pinned memory), else
-// nullptr. Both ends must be host memory of the same CUDA allocation (one buffer id), mapped
-// contiguously for the device.
+// Whether the current device reaches ordinary pageable host memory through the host's page tables
+// (address translation services, as on Grace): kernels may then use such buffers in place.
+bool pageable_reachable() {
+    static int known[64];  // per device: 0 unknown, 1 no, 2 yes
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (known[dev] == 0) {
+        int ats = 0;
+        known[dev] = cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) ==
+                                 cudaSuccess &&
+                             ats
+                         ? 2
+                         : 1;
+    }
+    return known[dev] == 2;
+}
+
+// Makes every page of [p, p + bytes) present and writable in the host's page tables
+// (MADV_POPULATE_WRITE), so the device, translating host addresses, never has to fault a page in.
+// False when the host cannot (an older kernel, a read-only or unmapped range): the caller then
+// copies the buffer instead.
+#ifndef MADV_POPULATE_WRITE
+#define MADV_POPULATE_WRITE 23  // Linux UAPI value
+#endif
+bool populate_writable(const void* p, size_t bytes) {
+    static const uintptr_t page = (uintptr_t)sysconf(_SC_PAGESIZE);
+    if (page == 0 || (page & (page - 1)) != 0) return false;
+    const uintptr_t b = (uintptr_t)p & ~(page - 1), e = ((uintptr_t)p + bytes + page - 1) & ~(page - 1);
+    return madvise(reinterpret_cast<void*>(b), e - b, MADV_POPULATE_WRITE) == 0;
+}
+
+// The device address of [p, p + bytes) when the kernels can use the range in place, else nullptr:
+// the whole range lies in one page-locked host allocation that the device maps (cudaHostAlloc,
+// cudaHostRegister, torch's pinned memory; both ends in the same CUDA allocation, one buffer id,
+// mapped contiguously), or it is ordinary pageable memory, the device translates host addresses
+// (pageable_reachable) and its pages could be made present and writable (populate_writable).
 void* mapped_host_range(const void* p, size_t bytes) {
     using GetAttrs = CUresult (*)(unsigned int, CUpointer_attribute*, void**, CUdeviceptr);
     static const GetAttrs get = [] {
@@ -39,6 +73,14 @@ void* mapped_host_range(const void* p, size_t bytes) {
         return reinterpret_cast<GetAttrs>(fn);
     }();
     if (!get || !p || bytes == 0) return nullptr;
+    {
+        unsigned int type = 0;
+        CUpointer_attribute a0 = CU_POINTER_ATTRIBUTE_MEMORY_TYPE;
+        void* d0 = &type;
+        // a pointer of no CUDA allocation (pageable memory) reads back type 0
+        if (get(1, &a0, &d0, (CUdeviceptr)(uintptr_t)p) == CUDA_SUCCESS && type == 0)
+            return pageable_reachable() && populate_writable(p, bytes) ? const_cast<void*>(p) : nullptr;
+    }
     struct Ends {
         unsigned int type = 0;
         unsigned long long id = 0;
@@ -460,12 +502,13 @@ rast_status rast_draw(rast_ctx* c, const float camera[16], const float normal[16
     const size_t npx = (size_t)w * h;
     const bool rmw = !(flags & RAST_CLEAR);
     if (!c->h_status) RAST_CUDA(c, cudaMallocHost(&c->h_status, sizeof(uint32_t)));
-    // Page-locked host buffers that the device maps are used in place: the resolve pass reads the
-    // incoming depth where a fragment landed and writes the frame's pixels (read-modify-write:
-    // only the winners; deferred shading then writes their colour) straight into the host
-    // buffers, so no frame-sized copy crosses the link. After a bin-pool overflow nothing is
-    // written, and the redraw starts from the same buffers.
-    {
+    // Host buffers the device reaches (page-locked memory it maps; pageable memory where it
+    // translates host addresses) are used in place: the resolve pass reads the incoming depth
+    // where a fragment landed and writes the frame's pixels (read-modify-write: only the winners;
+    // deferred shading then writes their colour) straight into the host buffers, so no
+    // frame-sized copy crosses the link. After a bin-pool overflow nothing is written, and the
+    // redraw starts from the same buffers.
+    if (c->host_in_place) {
         uint8_t* hr = static_cast<uint8_t*>(mapped_host_range(rgb, 3 * npx));
         float* hd = static_cast<float*>(mapped_host_range(depth, sizeof(float) * npx));
         uint32_t* hi = ids ? static_cast<uint32_t*>(mapped_host_range(ids, sizeof(uint32_t) * npx)) : nullptr;
@@ -631,6 +674,10 @@ rast_status rast_set_option(rast_ctx* c, int option, int64_t value) {
             if (value != 0 && value != 1) return fail(c, RAST_ERR_INVALID_ARG, "shade stall test is 0 or 1");
             c->test_shade_stall = value == 1;
             return RAST_OK;
+        case RAST_OPT_HOST_IN_PLACE:
+            if (value != 0 && value != 1) return fail(c, RAST_ERR_INVALID_ARG, "host in place is 0 or 1");
+            c->host_in_place = value == 1;
+            return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
 }
@@ -648,6 +695,7 @@ rast_status rast_get_option(rast_ctx* c, int option, int64_t* value) {
         case RAST_OPT_MLP_BOUND_MILLI: *value = c->mlp_bound_milli; return RAST_OK;
         case RAST_OPT_TEST_SHADE_STALL: *value = c->test_shade_stall ? 1 : 0; return RAST_OK;
         case RAST_OPT_TILE_THREADS: *value = c->tile_threads; return RAST_OK;
+        case RAST_OPT_HOST_IN_PLACE: *value = c->host_in_place ? 1 : 0; return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
 }

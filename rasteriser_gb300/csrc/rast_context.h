@@ -104,6 +104,7 @@ struct rast_ctx {
     int32_t mlp_samples = 2;      // RAST_OPT_MLP_SAMPLES
     int32_t mlp_bound_milli = 500;  // RAST_OPT_MLP_BOUND_MILLI
     bool test_shade_stall = false;  // RAST_OPT_TEST_SHADE_STALL
+    bool host_in_place = true;      // RAST_OPT_HOST_IN_PLACE
     // the last draw's deferred shading pass, for rast_time_shading
     bool replay_valid = false;
     rast::FrameScratch replay_s;

@@ -298,6 +298,47 @@ def test_pinned_host_buffers_overflow_recovers(renderer, port):
     assert np.abs(f.astype(int) - fp).max() <= RGB_TOL
 
 
+@pytest.mark.parametrize("clear", [False, True])
+def test_pageable_host_buffers_in_place_and_copied(renderer, port, clear):
+    """Ordinary (pageable) host buffers: used in place where the device translates host addresses
+    (RAST_OPT_HOST_IN_PLACE 1, the default), copied through device memory with 0. Both equal the
+    port: read-modify-write keeps the pixels nothing wins, clear mode writes them all."""
+    sc = S.soup(8000, 300, 200, seed=29, area_range=(0.5, 4000.0))
+    rng = np.random.default_rng(11)
+    depth0 = rng.uniform(-1.5, 1.5, (sc.height, sc.width)).astype(np.float32)
+    depth0[::7, ::5] = -0.0
+    depth0[3::11, ::3] = np.nan
+    frame0 = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    fp, dp, ip, _ = port.draw(sc, cam, nm, lights, None if clear else frame0, None if clear else depth0)
+    try:
+        for in_place in (1, 0):
+            renderer.set_option(abi.OPT_HOST_IN_PLACE, in_place)
+            assert renderer.get_option(abi.OPT_HOST_IN_PLACE) == in_place
+            assert_parity(gpu_draw(renderer, sc, cam, nm, lights, frame0, depth0, clear=clear), fp, dp, ip)
+    finally:
+        renderer.set_option(abi.OPT_HOST_IN_PLACE, 1)
+
+
+def test_pageable_host_buffers_overflow_recovers(renderer, port):
+    """Pageable buffers used in place: after a bin-pool overflow the draw has written nothing, and
+    the redraw is exact."""
+    sc = S.soup(5000, 400, 300, seed=43, area_range=(200.0, 5000.0))
+    rng = np.random.default_rng(5)
+    depth0 = rng.uniform(-1.0, 1.5, (sc.height, sc.width)).astype(np.float32)
+    frame0 = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
+    cam, nm, lights, _ = abi.scene_frame_inputs(sc)
+    renderer.set_option(abi.OPT_BIN_CAPACITY, 16)
+    try:
+        f, d, _ = gpu_draw(renderer, sc, cam, nm, lights, frame0, depth0)
+        assert renderer.get_option(abi.OPT_BIN_CAPACITY) > 16
+    finally:
+        renderer.set_option(abi.OPT_BIN_CAPACITY, 0)
+    fp, dp, _, _ = port.draw(sc, cam, nm, lights, frame0, depth0)
+    assert np.array_equal(bits(d), bits(dp))
+    assert np.abs(f.astype(int) - fp).max() <= RGB_TOL
+
+
 def test_pinned_slice_of_larger_allocation(renderer, port):
     """A frame that is a slice of a bigger page-locked buffer is used in place too."""
     torch = pytest.importorskip("torch")
