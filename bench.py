@@ -10,7 +10,8 @@ the timed region.
 One JSON line on rank 0: value = frames/s over all ranks; e2e = the same through the C ABI with
 host buffers (rast_draw, read-modify-write as draw_frame, mesh resident) on page-locked buffers,
 which the exact shader's kernels read and write in place over the link; e2e_pageable = the same on
-ordinary pageable arrays, copied host->device and back; roofline of the dominant kernel from
+ordinary pageable numpy arrays, used in place too where the device translates host addresses (Grace),
+else copied host->device and back; roofline of the dominant kernel from
 per-stage CUDA events; the CPU baseline (the oracle port, one core) on a bounded sample of the same
 frames.
 
@@ -515,15 +516,21 @@ def extra_batch(torch, abi, stream, steps=10):
             "l2": "not flushed (the batch's working set exceeds L2)"}
 
 
-def e2e_line(value, shader, W, H, stats):
-    """The e2e entry for page-locked host buffers, which the kernels use in place: the resolve pass
-    reads the incoming depth of each pixel a fragment landed on and writes the winners' colour (3 B)
-    and depth (4 B), plus the 4-byte status word; deferred shading writes the colour once more."""
+def e2e_line(value, shader, W, H, stats, memory="page-locked", in_place=True):
+    """The e2e entry for host buffers. Used in place, the resolve pass reads the incoming depth of
+    each pixel a fragment landed on and writes the winners' colour (3 B) and depth (4 B), plus the
+    4-byte status word; deferred shading writes the colour once more. Copied, the whole frame and
+    depth cross the link both ways."""
+    if not in_place:
+        return {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 7 * W * H,
+                "d2h_bytes_per_step": 7 * W * H + 4,
+                "path": f"rast_draw with {memory} host frame (planar RGB8) and depth buffers, copied both ways "
+                        "(read-modify-write); mesh resident"}
     covered = int(stats["written"])
     colour = 3 * covered if shader != "exact" else 0
     return {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 4 * covered,
             "d2h_bytes_per_step": 7 * covered + colour + 4,
-            "path": "rast_draw with page-locked host frame (planar RGB8) and depth buffers used in place "
+            "path": f"rast_draw with {memory} host frame (planar RGB8) and depth buffers used in place "
                     "(read-modify-write; the kernels read the incoming depth of covered pixels and write "
                     "their colour and depth over the link); mesh resident"}
 
@@ -635,8 +642,9 @@ def run_ours(args):
     stage_ms = {k: v / n_st for k, v in acc.items()}
 
     # End to end through the C ABI with host buffers (read-modify-write, as draw_frame), mesh
-    # resident. Page-locked buffers are used in place by the exact shader (the kernels read and
-    # write them over the link); ordinary pageable arrays are copied both ways. Both are timed.
+    # resident. Page-locked buffers are used in place (the kernels read and write them over the
+    # link); ordinary pageable arrays too where the device translates host addresses, else they
+    # are copied both ways. Both are timed; the draw's statistics say which path ran.
     def e2e_run(pinned):
         if pinned:
             h_rgb = torch.zeros(3 * W * H, dtype=torch.uint8).pin_memory().numpy().reshape(3, H, W)
@@ -656,10 +664,10 @@ def run_ours(args):
             r.draw(cam, nm, W, H, 0, h_rgb, h_depth)
             if k >= 3:
                 e2e_s += time.perf_counter() - t0
-        return world * n_e2e / max_over_ranks(dist, e2e_s, "cuda")
+        return world * n_e2e / max_over_ranks(dist, e2e_s, "cuda"), r.stats()["host_in_place"] == 1
 
-    e2e_value = e2e_run(True)
-    e2e_pageable = e2e_run(False)
+    e2e_value, e2e_in_place = e2e_run(True)
+    e2e_pageable, pageable_in_place = e2e_run(False)
 
     if rank != 0:
         if dist is not None:
@@ -692,11 +700,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(scene, workload, n_frames, frames[0][3].shape[0], world, args.shader),
-        "e2e": e2e_line(e2e_value, args.shader, W, H, stats),
-        "e2e_pageable": {"value": e2e_pageable, "unit": "frames/s", "h2d_bytes_per_step": 7 * W * H,
-                         "d2h_bytes_per_step": 7 * W * H,
-                         "path": "rast_draw with pageable numpy frame (planar RGB8) and depth buffers, copied both "
-                                 "ways (read-modify-write); mesh resident"},
+        "e2e": e2e_line(e2e_value, args.shader, W, H, stats, in_place=e2e_in_place),
+        "e2e_pageable": e2e_line(e2e_pageable, args.shader, W, H, stats, "pageable numpy", pageable_in_place),
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"kernel": kernel_names[dom], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,

@@ -143,10 +143,13 @@ rast_status rast_set_lights(rast_ctx* ctx, const float* lights7, int32_t n);
 /* ------------------------------------------------------------------------------------------ */
 
 /* One frame of draw_frame with HOST buffers (the reference's calling convention); returns when
- * done. Buffers in page-locked memory that the device maps (cudaHostAlloc, cudaHostRegister),
- * each within one allocation, are used in place: the kernels read the incoming depth where a
- * fragment landed and write the pixels they draw over the link. Other
- * buffers are copied in (unless RAST_CLEAR), rendered on the device and copied back.
+ * done. Buffers the device reaches are used in place (RAST_OPT_HOST_IN_PLACE, default on):
+ * page-locked memory that the device maps (cudaHostAlloc, cudaHostRegister), each buffer within
+ * one allocation, and ordinary pageable memory on devices that translate host addresses through
+ * the host's page tables (Grace), whose pages are first made present and writable on the host.
+ * The kernels then read the incoming depth where a fragment landed and write the pixels they
+ * draw over the link. Other buffers are copied in (unless RAST_CLEAR), rendered on the device
+ * and copied back. rast_get_stats word 7 says which path the last draw took.
  *   camera, normal: the frame's camera and normal matrices (rast_frame_matrices)
  *   rgb_planar: width*height*3 bytes, planar (x + y*width + c*width*height) as CImg stores
  *               CImg<unsigned char>(W,H,1,3) (renderer.cpp:85); read and written
@@ -174,7 +177,8 @@ rast_status rast_sync(rast_ctx* ctx);
  *   [0] front-facing triangles      [1] bounding-box pixels tested
  *   [2] inside fragments            [3] pixels written
  *   [4] triangles on the binned path [5] tile-bin entries
- *   [6] kernel launches of the draw  [7] reserved (0) */
+ *   [6] kernel launches of the draw  [7] 1 when it was a rast_draw that used its host buffers in
+ *                                        place (RAST_OPT_HOST_IN_PLACE), else 0 */
 rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
 
 /* Tuning knobs (see rast_set_option keys). Values outside the supported set are refused. */

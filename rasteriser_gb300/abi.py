@@ -392,7 +392,7 @@ class Renderer:
     def stats(self):
         out = (C.c_uint64 * 8)()
         self._check(self.lib.rast_get_stats(self.h, out), "rast_get_stats")
-        keys = ["front", "tested", "inside", "written", "binned_tris", "bin_entries", "launches", "reserved"]
+        keys = ["front", "tested", "inside", "written", "binned_tris", "bin_entries", "launches", "host_in_place"]
         return dict(zip(keys, list(out)))
 
     def device_status(self):

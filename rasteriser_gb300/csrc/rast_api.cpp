@@ -202,6 +202,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
         c->replay_blocks = (npx + rast::kShadeBlock - 1) / rast::kShadeBlock;
     }
     c->last_launches = (uint64_t)n;
+    c->last_in_place = false;
     c->keys_armed = true;  // the resolve pass re-arms every key it reads
     c->keys_clear = clear;
     c->keys_px = npx;
@@ -518,6 +519,7 @@ rast_status rast_draw(rast_ctx* c, const float camera[16], const float normal[16
                 rast_status st = enqueue_draw(c, camera, normal, w, h, flags, hr, hd, hi);
                 c->keep_outputs = false;
                 if (st != RAST_OK) return st;
+                c->last_in_place = true;
                 RAST_CUDA(c, cudaMemcpyAsync(c->h_status, c->counters.as<uint32_t>() + 1, sizeof(uint32_t),
                                              cudaMemcpyDeviceToHost, c->stream));
                 RAST_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -624,6 +626,7 @@ rast_status rast_get_stats(rast_ctx* c, uint64_t out[8]) {
     for (int i = 0; i < 8; ++i)
         for (int k = 0; k < rast::kStatSlots; ++k) out[i] += s[((size_t)i * rast::kStatSlots + k) * rast::kSlotWords];
     out[rast::STAT_LAUNCHES] = c->last_launches;
+    out[rast::STAT_HOST_IN_PLACE] = c->last_in_place ? 1 : 0;
     return RAST_OK;
 }
 

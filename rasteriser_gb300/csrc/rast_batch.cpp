@@ -202,6 +202,7 @@ extern "C" rast_status rast_draw_batch(rast_ctx* c, const rast_frame_desc* frame
     if (st != RAST_OK) return st;
     c->batch_frames = n;
     c->last_launches = 0;
+    c->last_in_place = false;
     if (!(batch_flags & RAST_BATCH_GRAPH)) return enqueue_batch(c, frames, n, lanes);
 
     std::vector<unsigned char> key = batch_key(c, frames, n, lanes);

@@ -130,6 +130,7 @@ struct rast_ctx {
     int64_t bin_capacity = 0;  // 0: sized from the mesh
 
     uint64_t last_launches = 0;
+    bool last_in_place = false;     // the last draw wrote rast_draw's host buffers in place
     int n_sm = 1;
 
     // batched drawing

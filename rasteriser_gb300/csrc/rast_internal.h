@@ -32,7 +32,7 @@ constexpr int kStatWords = kStatCounters * kStatSlots * kSlotWords;
 
 enum StatIndex : int {
     STAT_FRONT = 0, STAT_TESTED = 1, STAT_INSIDE = 2, STAT_WRITTEN = 3,
-    STAT_BINNED_TRIS = 4, STAT_BIN_ENTRIES = 5, STAT_LAUNCHES = 6, STAT_RESERVED = 7
+    STAT_BINNED_TRIS = 4, STAT_BIN_ENTRIES = 5, STAT_LAUNCHES = 6, STAT_HOST_IN_PLACE = 7
 };
 
 // Device status word bits (counters[1]); counters[2] and [3] hold the code and detail of the

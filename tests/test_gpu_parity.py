@@ -239,6 +239,24 @@ def test_full_size_against_reference_digest(renderer, port, key, row_chunk):
     assert (s["front"], s["tested"], s["inside"]) == (int(st[0]), int(st[1]), int(st[2]))
 
 
+def _translates_host_addresses(device=0):
+    """cudaDevAttrPageableMemoryAccessUsesHostPageTables (100) of the device through the CUDA
+    runtime, or None when no runtime library can be loaded."""
+    import ctypes
+    import ctypes.util
+    for name in (ctypes.util.find_library("cudart"), "libcudart.so", "/usr/local/cuda/lib64/libcudart.so"):
+        if not name:
+            continue
+        try:
+            rt = ctypes.CDLL(name)
+        except OSError:
+            continue
+        v = ctypes.c_int(0)
+        if rt.cudaDeviceGetAttribute(ctypes.byref(v), 100, device) == 0:
+            return bool(v.value)
+    return None
+
+
 def _pinned(torch, shape, dtype):
     """A numpy view of page-locked host memory (the device maps it)."""
     tdt = {np.uint8: torch.uint8, np.float32: torch.float32, np.uint32: torch.int32}[dtype]
@@ -266,6 +284,7 @@ def test_pinned_host_buffers_used_in_place(renderer, port, clear):
     f[...] = frame0
     d[...] = depth0
     renderer.draw(cam, nm, sc.width, sc.height, flags_of(sc, clear), f, d, ids=i)
+    assert renderer.stats()["host_in_place"] == 1
     fp, dp, ip, _ = port.draw(sc, cam, nm, lights, None if clear else frame0, None if clear else depth0)
     assert_parity((f, d, i), fp, dp, ip)
     pageable = gpu_draw(renderer, sc, cam, nm, lights, frame0, depth0, clear=clear)
@@ -302,7 +321,8 @@ def test_pinned_host_buffers_overflow_recovers(renderer, port):
 def test_pageable_host_buffers_in_place_and_copied(renderer, port, clear):
     """Ordinary (pageable) host buffers: used in place where the device translates host addresses
     (RAST_OPT_HOST_IN_PLACE 1, the default), copied through device memory with 0. Both equal the
-    port: read-modify-write keeps the pixels nothing wins, clear mode writes them all."""
+    port: read-modify-write keeps the pixels nothing wins, clear mode writes them all. The draw's
+    statistics say which path ran."""
     sc = S.soup(8000, 300, 200, seed=29, area_range=(0.5, 4000.0))
     rng = np.random.default_rng(11)
     depth0 = rng.uniform(-1.5, 1.5, (sc.height, sc.width)).astype(np.float32)
@@ -311,11 +331,15 @@ def test_pageable_host_buffers_in_place_and_copied(renderer, port, clear):
     frame0 = rng.integers(0, 256, (3, sc.height, sc.width), dtype=np.uint8)
     cam, nm, lights, _ = abi.scene_frame_inputs(sc)
     fp, dp, ip, _ = port.draw(sc, cam, nm, lights, None if clear else frame0, None if clear else depth0)
+    reach = _translates_host_addresses()
     try:
         for in_place in (1, 0):
             renderer.set_option(abi.OPT_HOST_IN_PLACE, in_place)
             assert renderer.get_option(abi.OPT_HOST_IN_PLACE) == in_place
             assert_parity(gpu_draw(renderer, sc, cam, nm, lights, frame0, depth0, clear=clear), fp, dp, ip)
+            used = renderer.stats()["host_in_place"]
+            if in_place == 0 or reach is not None:
+                assert used == (1 if in_place and reach else 0)
     finally:
         renderer.set_option(abi.OPT_HOST_IN_PLACE, 1)
 
