@@ -419,10 +419,10 @@ def extra_many_lights(torch, abi, stream, flush, steps=30):
             if name.startswith("learned"):
                 ck = m["checks"]
                 m["fallback_tile_fraction"] = ck["fallback_tiles"] / max(ck["tiles"], 1)
-                # algorithmic tensor work: 2 * (55*64 + 64*64 + 64*3) FLOP per shaded pixel (55
-                # features in use, two hidden layers of 64, 3 outputs); executed: padded K 64, N 16
-                alg = covered * 2.0 * (55 * 64 + 64 * 64 + 64 * 3)
-                executed = ck["tiles"] * 128 * 2.0 * (64 * 64 + 64 * 64 + 64 * 16)
+                # algorithmic tensor work: 2 * (25*32 + 32*32 + 32*3) FLOP per shaded pixel (25
+                # features in use, two hidden layers of 32, 3 outputs); executed: padded K 32, N 16
+                alg = covered * 2.0 * (25 * 32 + 32 * 32 + 32 * 3)
+                executed = ck["tiles"] * 128 * 2.0 * (32 * 32 + 32 * 32 + 32 * 16)
                 tflops = alg / (m["shade_ms"] * 1e-3) / 1e12
                 m["tensor"] = {"algorithmic_flop": alg, "executed_flop": executed, "achieved_tflops": tflops,
                                "peak_tflops": peak, "frac": tflops / peak, "peak_source": peak_kind}

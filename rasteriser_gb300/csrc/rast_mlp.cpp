@@ -70,8 +70,8 @@ uint64_t splitmix(uint64_t& x) {
     return z ^ (z >> 31);
 }
 
-// He-uniform weights; zero biases (W1 column 102, W2 and W3 column 63); the constant units
-// (W1 row 63 = e_102, W2 row 63 = e_63) and zero padding columns.
+// He-uniform weights; zero biases (W1 column kMlpConst, W2 and W3 column kMlpUnit1); the constant
+// units (W1 row kMlpUnit1 = e_kMlpConst, W2 row kMlpUnit1 = e_kMlpUnit1) and zero padding columns.
 std::vector<float> init_params(uint64_t seed) {
     std::vector<float> w(kMlpParams, 0.f);
     uint64_t st = seed * 0x2545F4914F6CDD1Dull + 7;
@@ -255,7 +255,7 @@ rast_status rast_mlp_save(rast_ctx* c, void* buf, size_t cap, size_t* size) {
     MlpBlobHeader h;
     std::memset(&h, 0, sizeof h);
     std::memcpy(h.magic, "RMLP", 4);
-    h.version = 2;
+    h.version = kMlpBlobVersion;
     h.n_in = kMlpFeat;
     h.n_hidden = kMlpHid;
     h.n_out = kMlpOut;
@@ -285,8 +285,8 @@ rast_status rast_mlp_load(rast_ctx* c, const void* buf, size_t size) {
     if (size != kMlpBlobBytes) return fail(c, RAST_ERR_INVALID_ARG, "weight blob has the wrong size");
     MlpBlobHeader h;
     std::memcpy(&h, buf, sizeof h);
-    if (std::memcmp(h.magic, "RMLP", 4) != 0 || h.version != 2)
-        return fail(c, RAST_ERR_INVALID_ARG, "not an RMLP version 2 blob");
+    if (std::memcmp(h.magic, "RMLP", 4) != 0 || h.version != kMlpBlobVersion)
+        return fail(c, RAST_ERR_INVALID_ARG, "not an RMLP version " + std::to_string(kMlpBlobVersion) + " blob");
     if (h.n_in != (uint32_t)kMlpFeat || h.n_hidden != (uint32_t)kMlpHid || h.n_out != (uint32_t)kMlpOut ||
         h.n_freq != (uint32_t)kMlpFreq || !(h.out_scale > 0.f))
         return fail(c, RAST_ERR_INVALID_ARG, "weight blob has other dimensions");

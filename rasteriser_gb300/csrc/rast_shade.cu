@@ -183,24 +183,21 @@ __device__ __forceinline__ void fourier_pairs(float v, Emit&& emit) {
 
 // The last 8 pairs of the features: n, albedo, the constant 1 that carries layer 1's bias
 // (feature kMlpConst), zeros.
-__device__ __forceinline__ void tail_pairs(float3 n, float3 alb, uint32_t (&t)[8]) {
-    t[0] = pack_bf16x2(n.x, n.y);
-    t[1] = pack_bf16x2(n.z, alb.x);
-    t[2] = pack_bf16x2(alb.y, alb.z);
-    t[3] = pack_bf16x2(1.f, 0.f);
-    t[4] = t[5] = t[6] = t[7] = 0u;
-}
-
-// The kMlpIn input features, each rounded to BF16, as packed pairs (feature 2i in the low half).
-static_assert(kMlpIn / 2 == 3 * kMlpFreq + 8 && kMlpConst == 6 * kMlpFreq + 6, "feature layout");
+// The kMlpIn input features, each rounded to BF16, as packed pairs (feature 2i in the low half):
+// the Fourier pairs of n.x, n.y and n.z, then (n.x, n.y), (n.z, alb.x), (alb.y, alb.z), (1, 0) and
+// zero pairs.
+constexpr int kTailPairs = 4;
+static_assert(kMlpConst == 6 * kMlpFreq + 6 && 3 * kMlpFreq + kTailPairs <= kMlpIn / 2, "feature layout");
 __device__ __forceinline__ void mlp_feature_pairs(float3 n, float3 alb, uint32_t (&pairs)[kMlpIn / 2]) {
     const float comp[3] = {n.x, n.y, n.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c) fourier_pairs(comp[c], [&](int f, uint32_t p) { pairs[c * kMlpFreq + f] = p; });
-    uint32_t t[8];
-    tail_pairs(n, alb, t);
+    pairs[3 * kMlpFreq] = pack_bf16x2(n.x, n.y);
+    pairs[3 * kMlpFreq + 1] = pack_bf16x2(n.z, alb.x);
+    pairs[3 * kMlpFreq + 2] = pack_bf16x2(alb.y, alb.z);
+    pairs[3 * kMlpFreq + 3] = pack_bf16x2(1.f, 0.f);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) pairs[3 * kMlpFreq + i] = t[i];
+    for (int i = 3 * kMlpFreq + kTailPairs; i < kMlpIn / 2; ++i) pairs[i] = 0u;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -332,9 +329,10 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 // while one slot waits for its MMAs the others compute. The slots share the weights (B operands,
 // one copy in shared memory) and the light table of the checks.
 //
-// A slot's tensor memory is 64 columns of FP32 accumulators and two A operands of 32 columns (64
-// BF16 values per row). A tile's features, h1 and h2 alternate between the two operands, so the
-// next tile's features are computed and stored while the current tile's last MMA runs:
+// A slot's tensor memory is 64 columns for its FP32 accumulators (32 in use) and two A operands 32
+// columns apart (16 columns in use: 32 BF16 values per row). A tile's features, h1 and h2
+// alternate between the two operands, so the next tile's features are computed and stored while
+// the current tile's last MMA runs:
 //   features(k) -> A[x]; h1 -> A[1-x]; h2 -> A[x]; features(k+1) -> A[1-x] during layer 3.
 //
 // Checks: the sampled rows of each tile put their normal, albedo and learned colour into the slot's
@@ -354,8 +352,10 @@ constexpr int kLdBatch = 4;        // 16-column accumulator loads in flight per 
 constexpr int kSlotThreads = 128;  // warp w of a slot reads TMEM lanes 32w..32w+31 (w = warp id mod 4)
 constexpr int kMlpThreads = kSlots * kSlotThreads;
 constexpr uint32_t kSlotCols = 64;                   // a slot's accumulators
-constexpr uint32_t kACols = kMlpIn / 2;              // one A operand
+constexpr uint32_t kACols = 32;                      // from one A operand to the other
 constexpr uint32_t kSlotTmem = kSlotCols + 2u * kACols;
+static_assert(kMlpHid <= (int)kSlotCols && kMlpOutPad <= (int)kSlotCols && kMlpIn / 2 <= (int)kACols,
+              "the accumulators and the A operands fit their columns");
 constexpr uint32_t kTmemCols = 512;
 static_assert(kMlpIn == kMlpHid, "one A operand shape serves every layer");
 static_assert(kSlots >= 1 && kSlots * kSlotTmem <= kTmemCols, "tensor memory of one SM");
@@ -447,33 +447,34 @@ __device__ __forceinline__ void a_written() {
 // The features of one row (mlp_feature_pairs' order) into an A operand (this thread's lane of it),
 // 8 pairs (16 K elements) per store.
 __device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t a) {
-    static_assert(kMlpFreq == 8, "one 8-pair store per normal component");
-    const float comp[3] = {n.x, n.y, n.z};
+    static_assert(kMlpIn % 16 == 0, "whole 8-pair stores");
+    uint32_t q[kMlpIn / 2];
+    mlp_feature_pairs(n, alb, q);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        uint32_t q[8];
-        fourier_pairs(comp[c], [&](int f, uint32_t p) { q[f] = p; });
-        tmem_st8(a + 8u * c, q);
+    for (int i = 0; i < kMlpIn / 16; ++i) {
+        uint32_t p[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) p[j] = q[8 * i + j];
+        tmem_st8(a + 8u * i, p);
     }
-    uint32_t t[8];
-    tail_pairs(n, alb, t);
-    tmem_st8(a + 24u, t);
 }
 
-// Epilogue of a hidden layer: this thread's row of 64 accumulators (TMEM columns from d) through
-// ReLU, rounded to BF16, into an A operand: the next layer's A. kLdBatch 16-column loads are in
-// flight per wait.
+// Epilogue of a hidden layer: this thread's row of kMlpHid accumulators (TMEM columns from d)
+// through ReLU, rounded to BF16, into an A operand: the next layer's A. Up to kLdBatch 16-column
+// loads are in flight per wait.
+constexpr int kEpiBatch = kMlpHid / 16 < kLdBatch ? kMlpHid / 16 : kLdBatch;
+static_assert(kMlpHid % 16 == 0 && (kMlpHid / 16) % kEpiBatch == 0, "whole batches of 16-column loads");
 __device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a) {
 #pragma unroll
-    for (int g = 0; g < kMlpHid / 16; g += kLdBatch) {
-        uint32_t v[kLdBatch][16];
+    for (int g = 0; g < kMlpHid / 16; g += kEpiBatch) {
+        uint32_t v[kEpiBatch][16];
 #pragma unroll
-        for (int i = 0; i < kLdBatch; ++i) tmem_ld16(d + 16u * (g + i), v[i]);
+        for (int i = 0; i < kEpiBatch; ++i) tmem_ld16(d + 16u * (g + i), v[i]);
         tmem_wait16(v[0]);
 #pragma unroll
-        for (int i = 1; i < kLdBatch; ++i) reg_fence16(v[i]);
+        for (int i = 1; i < kEpiBatch; ++i) reg_fence16(v[i]);
 #pragma unroll
-        for (int i = 0; i < kLdBatch; ++i) {
+        for (int i = 0; i < kEpiBatch; ++i) {
             uint32_t p[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) p[j] = relu_bf16x2(__uint_as_float(v[i][2 * j]), __uint_as_float(v[i][2 * j + 1]));
@@ -722,7 +723,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         a_written();
         if (slot_sync_or(slot, failed)) break;
 
-        // layer 2: D = H1 (128 x 64) * W2^T
+        // layer 2: D = H1 (128 x kMlpHid) * W2^T
         if (row == 32 * (int)((k + 2u) & 3u)) issue_layer(d_cols, a_oth, sW2, kMlpHid, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
         failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
@@ -731,7 +732,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         a_written();
         if (slot_sync_or(slot, failed)) break;
 
-        // layer 3: D[0, 16) = H2 (128 x 64) * W3^T; meanwhile the next tile's features go over h1
+        // layer 3: D[0, 16) = H2 (128 x kMlpHid) * W3^T; meanwhile the next tile's features go over h1
         if (row == 32 * (int)((k + 3u) & 3u)) issue_layer(d_cols, a_cur, sW3, kMlpOutPad, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpOutPad), mbar);
         if (t_next < n_tiles && !__any_sync(kFull, failed))
             store_features(make_float3(g0n.x, g0n.y, g0n.z), make_float3(g0n.w, g1n.x, g1n.y), a_oth + lane_off);
@@ -878,7 +879,16 @@ __global__ void k_mlp_stage(const float* __restrict__ src, int stride, int64_t n
 constexpr int kTrainB = 64;          // samples per CTA and step
 constexpr int kTrainThreads = 256;
 constexpr int kSX = kMlpIn + 4;      // shared row stride (floats) of X and W1: rows stay 16-byte
-constexpr int kSH = 68;              // aligned and eight rows cover all banks; of H, D and W2
+constexpr int kSH = kMlpHid + 4;     // aligned and eight rows cover all banks; of H, D and W2
+// Thread tid works on unit j = tid % kMlpHid for group tid / kMlpHid of the samples (forward, dH)
+// or of the inputs (weight gradients).
+constexpr int kTrainGroups = kTrainThreads / kMlpHid;
+constexpr int kSPG = kTrainB / kTrainGroups;   // samples per group
+constexpr int kHPG = kMlpHid / kTrainGroups;   // hidden inputs per group (layer 2 gradients)
+constexpr int kXPG = kMlpIn / kTrainGroups;    // features per group (layer 1 gradients)
+static_assert(kTrainThreads % kMlpHid == 0 && kTrainB % kTrainGroups == 0 && kHPG % 4 == 0 && kXPG % 4 == 0 &&
+                  kMlpIn % 4 == 0 && kTrainB * kMlpOut <= kTrainThreads && kMlpOut * kMlpHid <= kTrainThreads,
+              "training thread layout");
 
 struct TrainSmem {
     float w1[kMlpHid * kSX];
@@ -906,7 +916,7 @@ struct TrainArgs {
     float* loss;             // per CTA partial sum of squared errors
 };
 
-// One step's forward and backward pass for 64 samples per CTA, in FP32 with the rounding of the
+// One step's forward and backward pass for kTrainB samples per CTA, in FP32 with the rounding of the
 // tensor-core kernel (BF16 features, weights and hidden activations); per-CTA partial gradients.
 __global__ void __launch_bounds__(kTrainThreads) k_mlp_train(TrainArgs a) {
     extern __shared__ __align__(16) uint8_t smraw[];
@@ -932,39 +942,39 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train(TrainArgs a) {
     }
     __syncthreads();
 
-    const int j = tid & 63, q4 = tid >> 6;  // unit j, quarter q4 of the samples / inputs
-    // forward, layer 1: 16 samples of unit j
+    const int j = tid % kMlpHid, q4 = tid / kMlpHid;  // unit j, group q4 of the samples / inputs
+    // forward, layer 1: kSPG samples of unit j
     {
-        float acc[16];
+        float acc[kSPG];
 #pragma unroll
-        for (int bb = 0; bb < 16; ++bb) acc[bb] = 0.f;
+        for (int bb = 0; bb < kSPG; ++bb) acc[bb] = 0.f;
         for (int k = 0; k < kMlpIn; k += 4) {
             const float4 w = *reinterpret_cast<const float4*>(S.w1 + j * kSX + k);
 #pragma unroll
-            for (int bb = 0; bb < 16; ++bb) {
-                const float4 x = *reinterpret_cast<const float4*>(S.x + (16 * q4 + bb) * kSX + k);
+            for (int bb = 0; bb < kSPG; ++bb) {
+                const float4 x = *reinterpret_cast<const float4*>(S.x + (kSPG * q4 + bb) * kSX + k);
                 acc[bb] = fmaf(w.x, x.x, fmaf(w.y, x.y, fmaf(w.z, x.z, fmaf(w.w, x.w, acc[bb]))));
             }
         }
 #pragma unroll
-        for (int bb = 0; bb < 16; ++bb) S.h1[(16 * q4 + bb) * kSH + j] = bf16_round(fmaxf(acc[bb], 0.f));
+        for (int bb = 0; bb < kSPG; ++bb) S.h1[(kSPG * q4 + bb) * kSH + j] = bf16_round(fmaxf(acc[bb], 0.f));
     }
     __syncthreads();
     // layer 2
     {
-        float acc[16];
+        float acc[kSPG];
 #pragma unroll
-        for (int bb = 0; bb < 16; ++bb) acc[bb] = 0.f;
+        for (int bb = 0; bb < kSPG; ++bb) acc[bb] = 0.f;
         for (int k = 0; k < kMlpHid; k += 4) {
             const float4 w = *reinterpret_cast<const float4*>(S.w2 + j * kSH + k);
 #pragma unroll
-            for (int bb = 0; bb < 16; ++bb) {
-                const float4 x = *reinterpret_cast<const float4*>(S.h1 + (16 * q4 + bb) * kSH + k);
+            for (int bb = 0; bb < kSPG; ++bb) {
+                const float4 x = *reinterpret_cast<const float4*>(S.h1 + (kSPG * q4 + bb) * kSH + k);
                 acc[bb] = fmaf(w.x, x.x, fmaf(w.y, x.y, fmaf(w.z, x.z, fmaf(w.w, x.w, acc[bb]))));
             }
         }
 #pragma unroll
-        for (int bb = 0; bb < 16; ++bb) S.h2[(16 * q4 + bb) * kSH + j] = bf16_round(fmaxf(acc[bb], 0.f));
+        for (int bb = 0; bb < kSPG; ++bb) S.h2[(kSPG * q4 + bb) * kSH + j] = bf16_round(fmaxf(acc[bb], 0.f));
     }
     __syncthreads();
     // layer 3, loss and output gradient
@@ -988,24 +998,24 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train(TrainArgs a) {
         g[kPW3 + c * kMlpHid + k] = s;
     }
 #pragma unroll 4
-    for (int bb = 0; bb < 16; ++bb) {
-        const int b = 16 * q4 + bb;
+    for (int bb = 0; bb < kSPG; ++bb) {
+        const int b = kSPG * q4 + bb;
         float v = 0.f;
 #pragma unroll
         for (int c = 0; c < kMlpOut; ++c) v = fmaf(S.w3[c * kMlpHid + j], S.y[4 * b + c], v);
         S.d2[b * kSH + j] = S.h2[b * kSH + j] > 0.f ? v : 0.f;
     }
     __syncthreads();
-    // layer 2 gradients (unit j, inputs 16*q4..) and dH1 (input unit j, samples 16*q4..)
+    // layer 2 gradients (unit j, inputs kHPG*q4..) and dH1 (input unit j, samples kSPG*q4..)
     {
-        float acc[16];
+        float acc[kHPG];
 #pragma unroll
-        for (int ii = 0; ii < 16; ++ii) acc[ii] = 0.f;
+        for (int ii = 0; ii < kHPG; ++ii) acc[ii] = 0.f;
         for (int b = 0; b < kTrainB; ++b) {
             const float d = S.d2[b * kSH + j];
 #pragma unroll
-            for (int ii = 0; ii < 16; ii += 4) {
-                const float4 h = *reinterpret_cast<const float4*>(S.h1 + b * kSH + 16 * q4 + ii);
+            for (int ii = 0; ii < kHPG; ii += 4) {
+                const float4 h = *reinterpret_cast<const float4*>(S.h1 + b * kSH + kHPG * q4 + ii);
                 acc[ii] = fmaf(d, h.x, acc[ii]);
                 acc[ii + 1] = fmaf(d, h.y, acc[ii + 1]);
                 acc[ii + 2] = fmaf(d, h.z, acc[ii + 2]);
@@ -1013,26 +1023,25 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train(TrainArgs a) {
             }
         }
 #pragma unroll
-        for (int ii = 0; ii < 16; ++ii) g[kPW2 + j * kMlpHid + 16 * q4 + ii] = acc[ii];
-        float dh[16];
+        for (int ii = 0; ii < kHPG; ++ii) g[kPW2 + j * kMlpHid + kHPG * q4 + ii] = acc[ii];
+        float dh[kSPG];
 #pragma unroll
-        for (int bb = 0; bb < 16; ++bb) dh[bb] = 0.f;
+        for (int bb = 0; bb < kSPG; ++bb) dh[bb] = 0.f;
         for (int u = 0; u < kMlpHid; ++u) {
             const float w = S.w2[u * kSH + j];
 #pragma unroll
-            for (int bb = 0; bb < 16; ++bb) dh[bb] = fmaf(w, S.d2[(16 * q4 + bb) * kSH + u], dh[bb]);
+            for (int bb = 0; bb < kSPG; ++bb) dh[bb] = fmaf(w, S.d2[(kSPG * q4 + bb) * kSH + u], dh[bb]);
         }
 #pragma unroll
-        for (int bb = 0; bb < 16; ++bb) {
-            const int b = 16 * q4 + bb;
+        for (int bb = 0; bb < kSPG; ++bb) {
+            const int b = kSPG * q4 + bb;
             S.d1[b * kSH + j] = S.h1[b * kSH + j] > 0.f ? dh[bb] : 0.f;
         }
     }
     __syncthreads();
     // layer 1 gradients: unit j, inputs kQ*q4 .. kQ*q4 + kQ - 1
     {
-        constexpr int kQ = kMlpIn / 4;
-        static_assert(kQ % 4 == 0, "a quarter of the inputs is whole float4s");
+        constexpr int kQ = kXPG;
         float acc[kQ];
 #pragma unroll
         for (int kk = 0; kk < kQ; ++kk) acc[kk] = 0.f;

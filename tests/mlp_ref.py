@@ -6,8 +6,8 @@ import numpy as np
 
 HEADER = struct.Struct("<4s7IQff")  # magic, version, n_in, n_hidden, n_out, n_freq, n_lights, reserved,
                                     # lights_hash, out_scale, train_loss
-N_IN, N_HID, N_OUT, N_FREQ = 55, 64, 3, 8  # N_IN counts the constant-1 feature
-VERSION = 2
+N_IN, N_HID, N_OUT, N_FREQ = 25, 32, 3, 3  # N_IN counts the constant-1 feature
+VERSION = 3
 
 
 def bf16_round(a):
@@ -22,7 +22,7 @@ def bf16_bits(a):
 
 
 def features(n, alb):
-    """(m, 55): sin / cos(f * pi * n_c) for c in xyz, f = 1..8 (pairs), then n, albedo and 1."""
+    """(m, N_IN): sin / cos(f * pi * n_c) for c in xyz, f = 1..N_FREQ (pairs), then n, albedo and 1."""
     n = np.asarray(n, np.float64)
     f = np.arange(1, N_FREQ + 1, dtype=np.float64)
     cols = []
