@@ -329,29 +329,32 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 // while one slot waits for its MMAs the others compute. The slots share the weights (B operands,
 // one copy in shared memory) and the light table of the checks.
 //
-// A slot's tensor memory is 64 columns for its FP32 accumulators (32 in use) and two A operands 32
-// columns apart (16 columns in use: 32 BF16 values per row). A tile's features, h1 and h2
-// alternate between the two operands, so the next tile's features are computed and stored while
-// the current tile's last MMA runs:
+// A slot's tensor memory is 32 columns of FP32 accumulators and two A operands 32 columns apart
+// (16 columns in use: 32 BF16 values per row), every region starting on a multiple of 32 columns.
+// A tile's features, h1 and h2 alternate between the two operands, so the next tile's features
+// are computed and stored while the current tile's last MMA runs:
 //   features(k) -> A[x]; h1 -> A[1-x]; h2 -> A[x]; features(k+1) -> A[1-x] during layer 3.
 //
 // Checks: the sampled rows of each tile put their normal, albedo and learned colour into the slot's
 // check buffer at the end of the tile; after every kCheckTiles tiles, and after the slot's last
-// tile, the slot checks the buffered rows (ten at a time, its four warps splitting the lights) and
-// shades the tiles that failed again, exactly. The kernel is compiled for
-// each number of checked samples, and the light table comes with the weights (built with them for
-// their rig).
+// tile, the slot checks the buffered rows (each warp its own rows, its lanes splitting the lights)
+// and shades the tiles that failed again, exactly. The kernel is compiled for each number of
+// checked samples, and the light table comes with the weights (built with them for their rig).
 //
-// RAST_MLP_SLOTS (at most 4: 4 x 128 columns fill the tensor memory) can be changed at build time
-// to measure fewer slots; the default is the fastest measured.
+// RAST_MLP_SLOTS, RAST_MLP_SLOT_COLS and RAST_MLP_CHECK_ROWS can be changed at build time to measure
+// other shapes (slots x (accumulator columns + 2 x 32) must fit the 512 columns of tensor memory);
+// the defaults are the fastest measured: five slots, whose 640 threads leave 96 registers each.
 #ifndef RAST_MLP_SLOTS
-#define RAST_MLP_SLOTS 4
+#define RAST_MLP_SLOTS 5
 #endif
 constexpr int kSlots = RAST_MLP_SLOTS;
 constexpr int kLdBatch = 4;        // 16-column accumulator loads in flight per wait
 constexpr int kSlotThreads = 128;  // warp w of a slot reads TMEM lanes 32w..32w+31 (w = warp id mod 4)
 constexpr int kMlpThreads = kSlots * kSlotThreads;
-constexpr uint32_t kSlotCols = 64;                   // a slot's accumulators
+#ifndef RAST_MLP_SLOT_COLS
+#define RAST_MLP_SLOT_COLS 32
+#endif
+constexpr uint32_t kSlotCols = RAST_MLP_SLOT_COLS;   // a slot's accumulators
 constexpr uint32_t kACols = 32;                      // from one A operand to the other
 constexpr uint32_t kSlotTmem = kSlotCols + 2u * kACols;
 static_assert(kMlpHid <= (int)kSlotCols && kMlpOutPad <= (int)kSlotCols && kMlpIn / 2 <= (int)kACols,
@@ -381,7 +384,6 @@ struct SlotMisc {
     uint32_t fail_mask;                     // after a check: bit j set when buffered tile j failed
     uint32_t pad;
     CheckRow q[kCheckTiles][kMaxSamples];   // the buffered tiles' sampled rows
-    float part[4][32];                      // a check pass: each warp's sums (3 i + c)
 };
 struct MlpMisc {
     unsigned long long mbar_w;     // the weights' bulk copy
@@ -498,6 +500,12 @@ __device__ __forceinline__ void load_record(const ShadeArgs& a, uint32_t t, uint
     const uint4 d = (uint32_t)row < count ? shade_tile_desc(a.index, a.n_blocks, t) : make_uint4(0u, 0u, 0u, 0u);
     load_record_desc(a, t, count, d, row, g0, g1);
 }
+// Tile t's descriptor, read before the tile count is known: the list has room for 8 tiles per
+// block, so every t below that reads inside it (what it reads past the last tile goes unused).
+__device__ __forceinline__ uint4 tile_desc_early(const ShadeArgs& a, uint32_t t) {
+    return t < a.n_blocks * (uint32_t)(kShadeBlock / kShadeTile) ? shade_tile_desc(a.index, a.n_blocks, t)
+                                                                 : make_uint4(0u, 0u, 0u, 0u);
+}
 
 // Records in tile t of n_tiles, from the fragment total.
 __device__ __forceinline__ uint32_t tile_count(uint32_t n_frag, uint32_t n_tiles, uint32_t t) {
@@ -511,38 +519,41 @@ struct SmemLights {
 };
 
 // The check of the slot's buffered tiles (n_rows = tiles * NS sampled rows, tile j's sample s at
-// q[j][s]), up to kCheckPass rows per pass: the slot's four warps split the lights (lane `lane` of
-// warp w takes lights 32 w + lane, 32 w + lane + 128, ...), so the light table is read once per
-// pass, and sum, per row i and channel c, (I c)_l * max(0, n . -dir_l) with fused multiply-adds;
-// each warp adds its lanes' sums by halving (each level a lane keeps half of its values and adds its
-// partner's copy of them, leaving value j in lane j) into part[w][3 i + c], and after a slot barrier
-// lane 3 i + c of warp 0 adds the four parts and compares |learned - min(sum * albedo / pi, 255)|
-// with the bound, marking the row's tile in fail_mask. The sum only estimates the exact shade: it
-// judges the learned colour and is never itself a colour. Lights come from the shared table when it
-// holds them, else from global memory. Every thread of the slot calls it.
-constexpr int kCheckPass = 10;
-static_assert(3 * kCheckPass <= 32, "one value per lane");
+// q[j][s]): warp w of the slot takes rows w, w + 4, ... (kCheckRows of them per pass), its lanes
+// split the lights (lane `lane` takes lights lane, lane + 32, ...), and each lane sums, per row i
+// and channel c, (I c)_l * max(0, n . -dir_l) with fused multiply-adds. The warp adds its lanes'
+// sums by halving (each level a lane keeps half of its values and adds its partner's copy of them,
+// leaving value j in the lanes j mod kCheckVals), then the lane groups, and lane 3 i + c compares
+// |learned - min(sum * albedo / pi, 255)| with the bound, marking the row's tile in fail_mask. The
+// sum only estimates the exact shade: it judges the learned colour and is never itself a colour.
+// Lights come from the shared table when it holds them, else from global memory. The caller's next
+// slot barrier orders the marks before they are read.
+#ifndef RAST_MLP_CHECK_ROWS
+#define RAST_MLP_CHECK_ROWS 2
+#endif
+constexpr int kCheckRows = RAST_MLP_CHECK_ROWS;  // rows of one warp per pass
+constexpr int kCheckVals = 3 * kCheckRows <= 8 ? 8 : 16;  // sums per lane, a power of two
+static_assert(3 * kCheckRows <= kCheckVals, "one sum per lane");
 template <int NS>
-__device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int n_rows, int slot, int wq,
-                           int lane, float& max_err) {
-    for (int r0 = 0; r0 < n_rows; r0 += kCheckPass) {
-        const int nr = min(kCheckPass, n_rows - r0);
-        float nx[kCheckPass], ny[kCheckPass], nz[kCheckPass];
+__device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S, int n_rows, int wq, int lane,
+                           float& max_err) {
+    for (int r0 = wq; r0 < n_rows; r0 += 4 * kCheckRows) {
+        float nx[kCheckRows], ny[kCheckRows], nz[kCheckRows];
 #pragma unroll
-        for (int i = 0; i < kCheckPass; ++i) {
-            const int r = r0 + i;
-            const bool in = i < nr;
+        for (int i = 0; i < kCheckRows; ++i) {
+            const int r = r0 + 4 * i;
+            const bool in = r < n_rows;
             const CheckRow& q = S.q[in ? r / NS : 0][in ? r % NS : 0];
             nx[i] = in ? q.n[0] : 0.f;
             ny[i] = in ? q.n[1] : 0.f;
             nz[i] = in ? q.n[2] : 0.f;
         }
-        float v[32];
+        float v[kCheckVals];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] = 0.f;
+        for (int j = 0; j < kCheckVals; ++j) v[j] = 0.f;
         auto acc = [&](float4 A, float2 B) {
 #pragma unroll
-            for (int i = 0; i < kCheckPass; ++i) {
+            for (int i = 0; i < kCheckRows; ++i) {
                 const float m = fmaxf(fmaf(nz[i], A.z, fmaf(ny[i], A.y, nx[i] * A.x)), 0.f);
                 v[3 * i] = fmaf(A.w, m, v[3 * i]);
                 v[3 * i + 1] = fmaf(B.x, m, v[3 * i + 1]);
@@ -550,9 +561,9 @@ __device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S,
             }
         };
         if (L) {
-            for (int l = 32 * wq + lane; l < a.nl; l += 128) acc(L->dirI[l], L->gb[l]);
+            for (int l = lane; l < a.nl; l += 32) acc(L->dirI[l], L->gb[l]);
         } else {
-            for (int l = 32 * wq + lane; l < a.nl; l += 128) {
+            for (int l = lane; l < a.nl; l += 32) {
                 const float* P = a.lights + 7 * (int64_t)l;
                 const float I = __ldg(P + 3);
                 acc(make_float4(-__ldg(P), -__ldg(P + 1), -__ldg(P + 2), I * __ldg(P + 4)),
@@ -560,27 +571,25 @@ __device__ void check_rows(const ShadeArgs& a, const SmemLights* L, SlotMisc& S,
             }
         }
 #pragma unroll
-        for (int h = 16, o = 16; h >= 1; h >>= 1, o >>= 1) {
-            const bool up = (lane & o) != 0;
+        for (int h = kCheckVals / 2; h >= 1; h >>= 1) {
+            const bool up = (lane & h) != 0;
 #pragma unroll
             for (int i = 0; i < h; ++i) {
                 const float mine = up ? v[i + h] : v[i], other = up ? v[i] : v[i + h];
-                v[i] = mine + __shfl_xor_sync(kFull, other, o);
+                v[i] = mine + __shfl_xor_sync(kFull, other, h);
             }
         }
-        if (lane < 3 * nr) S.part[wq][lane] = v[0];
-        slot_sync(slot);
-        if (wq == 0 && lane < 3 * nr) {
-            const int i = lane / 3, c = lane - 3 * i, r = r0 + i;
+#pragma unroll
+        for (int o = kCheckVals; o < 32; o <<= 1) v[0] += __shfl_xor_sync(kFull, v[0], o);
+        const int i = lane / 3, c = lane - 3 * i, r = r0 + 4 * i;
+        if (lane < 3 * kCheckRows && r < n_rows) {
             const CheckRow& q = S.q[r / NS][r % NS];
             if (q.valid) {
-                const float sum = (S.part[0][lane] + S.part[1][lane]) + (S.part[2][lane] + S.part[3][lane]);
-                const float err = fabsf(q.rad[c] - fminf(sum * q.alb[c] * kOneOverPi, 255.f));
+                const float err = fabsf(q.rad[c] - fminf(v[0] * q.alb[c] * kOneOverPi, 255.f));
                 max_err = fmaxf(max_err, err);
                 if (!(err <= a.bound)) atomicOr(&S.fail_mask, 1u << (r / NS));
             }
         }
-        slot_sync(slot);  // the parts are read before the next pass writes them
     }
 }
 
@@ -641,17 +650,19 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     // the records and the tile list are the previous kernel's output
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
-    const uint32_t n_frag = a.index[0], n_tiles = a.index[1];
     // Slot g = blockIdx.x * kSlots + slot takes tiles g, g + stride, ...; this thread holds the
-    // records of its row in the slot's current tile and the next one.
+    // records of its row in the slot's current tile and the next one. The first two descriptors
+    // are read with the list's header, not after it.
     const uint32_t stride = gridDim.x * kSlots;
     uint32_t t = blockIdx.x * kSlots + slot;
-    uint32_t count = tile_count(n_frag, n_tiles, t);
     uint32_t t_next = t + stride;
+    const uint4 d_first = tile_desc_early(a, t), d_second = tile_desc_early(a, t_next);
+    const uint32_t n_frag = a.index[0], n_tiles = a.index[1];
+    uint32_t count = tile_count(n_frag, n_tiles, t);
     uint32_t count_next = tile_count(n_frag, n_tiles, t_next);
     float4 g0, g1, g0n, g1n;
-    load_record(a, t, count, row, g0, g1);
-    load_record(a, t_next, count_next, row, g0n, g1n);
+    load_record_desc(a, t, count, d_first, row, g0, g1);
+    load_record_desc(a, t_next, count_next, d_second, row, g0n, g1n);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -679,8 +690,8 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     // t0 + j * stride); every thread of the slot calls it after a slot barrier.
     auto check_buffer = [&](uint32_t n_buf, uint32_t t0) {
         if constexpr (checking) {
-            check_rows<checking ? NS : 1>(a, L, S, (int)(n_buf * n_samples), slot, wq, lane, max_err);
-            slot_sync(slot);
+            check_rows<checking ? NS : 1>(a, L, S, (int)(n_buf * n_samples), wq, lane, max_err);
+            slot_sync(slot);  // the marks are in
             const uint32_t f = S.fail_mask;
             slot_sync(slot);  // every thread read the verdicts before they are cleared
             if (row == 0) S.fail_mask = 0u;
