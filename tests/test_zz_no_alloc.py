@@ -1,8 +1,8 @@
 """rast_draw_noalloc: the draw for callers that must not allocate device memory (a host
 application whose own pool owns all device memory, or a frame loop that cannot take the
 device-wide synchronisation of cudaMalloc / cudaFree). It uses only the caller's device buffers and
-a fixed array inside the library. Its output must equal the context entry point's
-(rast_draw_device) on the same inputs, call after call.
+a fixed array inside the library. Its output must equal the oracle port's and the context entry
+point's (rast_draw_device) on the same inputs, call after call.
 
 This file is collected last, so that a run stopping at the first failure has run every other test;
 it builds and loads the library itself and also passes on its own in a fresh process.
@@ -59,7 +59,7 @@ def _device_mesh(torch, sc, lights):
 
 
 @pytest.mark.parametrize("which", ["icosphere", "soup", "screen_covering"])
-def test_noalloc_equals_context_draw_on_consecutive_calls(which):
+def test_noalloc_equals_port_and_context_draw_on_consecutive_calls(which, port):
     torch = pytest.importorskip("torch")
     lib = abi.load()
     sc = {"icosphere": S.config_icosphere_small,
@@ -98,6 +98,13 @@ def test_noalloc_equals_context_draw_on_consecutive_calls(which):
             assert np.array_equal(dep.cpu().numpy().view(np.uint32), w_dep.view(np.uint32))
             assert np.array_equal(ids.cpu().numpy(), w_ids)
             assert np.abs(rgb.cpu().numpy().astype(int) - w_rgb.astype(int)).max() <= RGB_TOL
+            # and directly against the oracle port, fed the same incoming frame and depth
+            frame0 = None if flags == abi.CLEAR else init_rgb.cpu().numpy().reshape(3, H, W)
+            depth0 = None if flags == abi.CLEAR else init_depth.cpu().numpy().reshape(H, W)
+            fp, dp, ip, _ = port.draw(sc, cam, nm, lights, frame0, depth0)
+            assert np.array_equal(dep.cpu().numpy().reshape(H, W).view(np.uint32), dp.view(np.uint32))
+            assert np.array_equal(ids.cpu().numpy().reshape(H, W).view(np.uint32), np.asarray(ip).view(np.uint32))
+            assert np.abs(rgb.cpu().numpy().reshape(3, H, W).astype(int) - fp.astype(int)).max() <= RGB_TOL
 
 
 def test_noalloc_refuses_what_does_not_fit_and_bad_indices():
