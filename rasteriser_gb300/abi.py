@@ -150,6 +150,15 @@ def _fp(a):
     return a.ctypes.data_as(_F) if a is not None else None
 
 
+def _addr(a):
+    """Address of an array's data: a ctypes view of a writable buffer costs a fraction of
+    `a.ctypes.data`, which the per-frame calls would otherwise pay for every buffer."""
+    try:
+        return C.addressof(C.c_char.from_buffer(a))
+    except (TypeError, ValueError, BufferError):  # read-only or empty
+        return a.ctypes.data
+
+
 def frame_matrices(width, height, scale=1.0, disp=(0, 0, 0), angles=(0, 0, 0), fovy_deg=45.0, z_near=0.1,
                    z_far=6.0):
     """The draw_frame matrices (model, view, modelview, camera, normal) as (16,) float32 arrays."""
@@ -335,16 +344,16 @@ class Renderer:
         if ids is not None:
             assert ids.dtype == np.uint32 and ids.flags.c_contiguous and ids.size == width * height
         cam, nrm = _f32(camera), _f32(normal)  # kept alive across the call
-        st = self.lib.rast_draw(self.h, cam.ctypes.data, nrm.ctypes.data, width, height, flags, frame.ctypes.data,
-                                depth.ctypes.data, ids.ctypes.data if ids is not None else None)
+        st = self.lib.rast_draw(self.h, _addr(cam), _addr(nrm), width, height, flags, _addr(frame), _addr(depth),
+                                _addr(ids) if ids is not None else None)
         self._check(st, "rast_draw")
         return frame, depth, ids
 
     def draw_device(self, camera, normal, width, height, flags, d_rgb, d_depth, d_ids=0):
         """Device-buffer draw on the context's stream; pointers are integers (e.g. tensor.data_ptr())."""
         cam, nrm = _f32(camera), _f32(normal)  # kept alive across the call
-        st = self.lib.rast_draw_device(self.h, cam.ctypes.data, nrm.ctypes.data, width, height, flags, d_rgb,
-                                       d_depth, d_ids or None)
+        st = self.lib.rast_draw_device(self.h, _addr(cam), _addr(nrm), width, height, flags, d_rgb, d_depth,
+                                       d_ids or None)
         self._check(st, "rast_draw_device")
 
     def sync(self):
