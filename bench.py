@@ -379,6 +379,11 @@ def extra_many_lights(torch, abi, stream, flush, steps=30):
         out["training"] = r.mlp_train(samples=4 << 20, epochs=24, seed=3)
         out["training"]["wall_s"] = time.perf_counter() - t0
         out["training"]["samples"] = 4 << 20
+        # the network measured here, and the one the workload's description names: the smaller one
+        # was chosen for equal held-out error (3 against 16 frequencies, hidden layers of 32 against 64)
+        out["network"] = {"features": "3 Fourier frequencies per normal component, normal, albedo, 1 (25)",
+                          "layers": "25 -> 32 -> 32 -> 3", "dtype": "bf16 weights, fp32 accumulation",
+                          "named_in_workload": "16 Fourier frequencies, 64 -> 64 -> 3"}
         frames, modes = {}, {}
         for name, shader, samples in (("exact_fused", abi.SHADER_EXACT, 2),
                                       ("exact_deferred", abi.SHADER_EXACT_DEFERRED, 2),
