@@ -363,7 +363,8 @@ def bf16_peak():
 def extra_many_lights(torch, abi, stream, flush, steps=30):
     """The 1M-triangle displaced sphere with smooth normals and per-vertex albedo at
     1920x1080 under 256 lights. The plain per-light shader (deferred exact; fused exact beside it)
-    against the learned shader, which is trained here on 4M samples the exact shader labels."""
+    against the learned shader, which is trained here on 4M samples the exact shader labels: the
+    compact network (the default) and the wide one the workload's description names."""
     from rasteriser_gb300 import scenes as S
     sc = S.config_many_lights()
     fr = frame_inputs(sc, 1)
@@ -379,16 +380,29 @@ def extra_many_lights(torch, abi, stream, flush, steps=30):
         out["training"] = r.mlp_train(samples=4 << 20, epochs=24, seed=3)
         out["training"]["wall_s"] = time.perf_counter() - t0
         out["training"]["samples"] = 4 << 20
-        # the network measured here, and the one the workload's description names: the smaller one
-        # was chosen for equal held-out error (3 against 16 frequencies, hidden layers of 32 against 64)
-        out["network"] = {"features": "3 Fourier frequencies per normal component, normal, albedo, 1 (25)",
-                          "layers": "25 -> 32 -> 32 -> 3", "dtype": "bf16 weights, fp32 accumulation",
-                          "named_in_workload": "16 Fourier frequencies, 64 -> 64 -> 3"}
+        # the networks measured here: the compact default, and the wide one the workload's
+        # description names (the compact one was chosen for about equal held-out error)
+        out["network"] = {
+            "learned": {"features": "3 Fourier frequencies per normal component, normal, albedo, 1 (25)",
+                        "layers": "25 -> 32 -> 32 -> 3", "dtype": "bf16 weights, fp32 accumulation"},
+            "learned_wide": {"features": "16 Fourier frequencies per normal component, normal, albedo, 1 (103)",
+                             "layers": "103 -> 64 -> 64 -> 3", "dtype": "bf16 weights, fp32 accumulation"},
+            "named_in_workload": "16 Fourier frequencies, 64 -> 64 -> 3"}
+        dims = {abi.MLP_COMPACT: (25, 32, 32), abi.MLP_WIDE: (103, 112, 64)}  # features, K, hidden
         frames, modes = {}, {}
-        for name, shader, samples in (("exact_fused", abi.SHADER_EXACT, 2),
-                                      ("exact_deferred", abi.SHADER_EXACT_DEFERRED, 2),
-                                      ("learned", abi.SHADER_LEARNED, 2),
-                                      ("learned_unchecked", abi.SHADER_LEARNED, 0)):
+        net_now = abi.MLP_COMPACT
+        for name, shader, samples, net in (("exact_fused", abi.SHADER_EXACT, 2, abi.MLP_COMPACT),
+                                           ("exact_deferred", abi.SHADER_EXACT_DEFERRED, 2, abi.MLP_COMPACT),
+                                           ("learned", abi.SHADER_LEARNED, 2, abi.MLP_COMPACT),
+                                           ("learned_unchecked", abi.SHADER_LEARNED, 0, abi.MLP_COMPACT),
+                                           ("learned_wide", abi.SHADER_LEARNED, 2, abi.MLP_WIDE),
+                                           ("learned_wide_unchecked", abi.SHADER_LEARNED, 0, abi.MLP_WIDE)):
+            if net != net_now:
+                r.set_option(abi.OPT_MLP_NETWORK, net)
+                t0 = time.perf_counter()
+                out["training_wide"] = r.mlp_train(samples=4 << 20, epochs=24, seed=3)
+                out["training_wide"]["wall_s"] = time.perf_counter() - t0
+                net_now = net
             r.set_option(abi.OPT_SHADER, shader)
             r.set_option(abi.OPT_MLP_SAMPLES, samples)
             fps, st, stage = time_scene_device(torch, abi, r, stream, fr, steps, 3, flush)
@@ -408,9 +422,11 @@ def extra_many_lights(torch, abi, stream, flush, steps=30):
             if shader == abi.SHADER_LEARNED:
                 m["checks"] = r.shade_stats()  # of this one draw
                 m["check_samples_per_tile"] = samples
+                m["network"] = net
             frames[name] = (f, ids)
             modes[name] = m
         r.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+        r.set_option(abi.OPT_MLP_NETWORK, abi.MLP_COMPACT)
         ref, ids = frames["exact_fused"]
         cov = ids != abi.NO_TRIANGLE
         covered = int(cov.sum())
@@ -424,10 +440,12 @@ def extra_many_lights(torch, abi, stream, flush, steps=30):
             if name.startswith("learned"):
                 ck = m["checks"]
                 m["fallback_tile_fraction"] = ck["fallback_tiles"] / max(ck["tiles"], 1)
-                # algorithmic tensor work: 2 * (25*32 + 32*32 + 32*3) FLOP per shaded pixel (25
-                # features in use, two hidden layers of 32, 3 outputs); executed: padded K 32, N 16
-                alg = covered * 2.0 * (25 * 32 + 32 * 32 + 32 * 3)
-                executed = ck["tiles"] * 128 * 2.0 * (32 * 32 + 32 * 32 + 32 * 16)
+                # algorithmic tensor work: 2 * (F*H + H*H + H*3) FLOP per shaded pixel (F features
+                # in use, two hidden layers of H, 3 outputs); executed: K padded to a multiple of
+                # 16, N of the last layer 16
+                nf, nk, nh = dims[m["network"]]
+                alg = covered * 2.0 * (nf * nh + nh * nh + nh * 3)
+                executed = ck["tiles"] * 128 * 2.0 * (nk * nh + nh * nh + nh * 16)
                 tflops = alg / (m["shade_ms"] * 1e-3) / 1e12
                 m["tensor"] = {"algorithmic_flop": alg, "executed_flop": executed, "achieved_tflops": tflops,
                                "peak_tflops": peak, "frac": tflops / peak, "peak_source": peak_kind}
@@ -439,6 +457,8 @@ def extra_many_lights(torch, abi, stream, flush, steps=30):
         out["speedup_learned_unchecked_vs_plain"] = plain / modes["learned_unchecked"]["shade_ms"]
         out["speedup_stage_events"] = (modes["exact_deferred"]["shade_ms_stage_events"] /
                                        modes["learned"]["shade_ms_stage_events"])
+        out["speedup_learned_wide_vs_plain"] = plain / modes["learned_wide"]["shade_ms"]
+        out["speedup_learned_wide_unchecked_vs_plain"] = plain / modes["learned_wide_unchecked"]["shade_ms"]
     finally:
         r.close()
     return out

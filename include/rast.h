@@ -207,6 +207,11 @@ rast_status rast_get_stats(rast_ctx* ctx, uint64_t out[8]);
                                          it maps; ordinary pageable memory when it translates host
                                          addresses through the host's page tables, as on Grace);
                                          0: always copied through device memory */
+#define RAST_OPT_MLP_NETWORK 12      /* learned shader: the network rast_mlp_train builds. 0 (default):
+                                         3 Fourier frequencies per normal component, hidden layers of
+                                         32; 1: 16 frequencies, hidden layers of 64 (the 16-frequency
+                                         64 -> 64 -> 3 network). Weights already trained or loaded
+                                         keep their own network; rast_mlp_load takes it from the blob */
 #define RAST_OPT_TEST_SHADE_STALL 9   /* test only (default 0). 1: the learned shader's first wait
                                          for a tensor-core MMA polls an mbarrier nothing arrives
                                          on, 1024 times, so it gives up as a lost MMA would: the

@@ -23,6 +23,8 @@ WIND_CLOCKWISE, CLEAR, FLAT = 1, 2, 4
 OPT_SMALL_MAX_PIXELS, OPT_TILE_SIZE, OPT_BIN_CAPACITY, OPT_STAGE_TIMING, OPT_ROW_CHUNK = 1, 2, 3, 4, 5
 OPT_SHADER, OPT_MLP_SAMPLES, OPT_MLP_BOUND_MILLI, OPT_TEST_SHADE_STALL, OPT_TILE_THREADS = 6, 7, 8, 9, 10
 OPT_HOST_IN_PLACE = 11
+OPT_MLP_NETWORK = 12
+MLP_COMPACT, MLP_WIDE = 0, 1
 SHADER_EXACT, SHADER_EXACT_DEFERRED, SHADER_LEARNED = 0, 1, 2
 STAGES = ["arm", "vertex", "setup_raster", "bin_scan", "bin_scatter", "tile_raster", "resolve", "shade", "total"]
 NO_TRIANGLE = 0xFFFFFFFF

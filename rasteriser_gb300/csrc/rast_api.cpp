@@ -184,6 +184,7 @@ rast_status enqueue_draw(rast_ctx* c, const float* camera, const float* normal, 
     p.tri_id = d_ids;
     p.shader = c->shader;
     p.mlp = c->mlp_image.ptr;
+    p.mlp_net = c->mlp_net;
     p.mlp_samples = c->mlp_samples;
     p.mlp_bound = (float)c->mlp_bound_milli * 1e-3f;
     p.mlp_stall_test = c->test_shade_stall;
@@ -681,6 +682,11 @@ rast_status rast_set_option(rast_ctx* c, int option, int64_t value) {
             if (value != 0 && value != 1) return fail(c, RAST_ERR_INVALID_ARG, "host in place is 0 or 1");
             c->host_in_place = value == 1;
             return RAST_OK;
+        case RAST_OPT_MLP_NETWORK:
+            if (value != rast::kMlpNetCompact && value != rast::kMlpNetWide)
+                return fail(c, RAST_ERR_INVALID_ARG, "MLP network is 0 (compact) or 1 (wide)");
+            c->mlp_train_net = (int32_t)value;
+            return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
 }
@@ -699,6 +705,7 @@ rast_status rast_get_option(rast_ctx* c, int option, int64_t* value) {
         case RAST_OPT_TEST_SHADE_STALL: *value = c->test_shade_stall ? 1 : 0; return RAST_OK;
         case RAST_OPT_TILE_THREADS: *value = c->tile_threads; return RAST_OK;
         case RAST_OPT_HOST_IN_PLACE: *value = c->host_in_place ? 1 : 0; return RAST_OK;
+        case RAST_OPT_MLP_NETWORK: *value = c->mlp_train_net; return RAST_OK;
     }
     return fail(c, RAST_ERR_INVALID_ARG, "unknown option");
 }

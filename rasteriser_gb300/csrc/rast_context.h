@@ -114,13 +114,15 @@ struct rast_ctx {
     DevBuf view_mm;  // rast_depth_to_u8: the depth range
 
     // learned shader state (rast_mlp.cpp)
-    DevBuf mlp_image;             // rast::MlpImage
+    DevBuf mlp_image;             // the weights' device image (rast::MlpNet), then the check table
+    int32_t mlp_net = 0;          // the network of the installed weights (kMlpNetCompact or kMlpNetWide)
+    int32_t mlp_train_net = 0;    // RAST_OPT_MLP_NETWORK: the network rast_mlp_train builds
     bool mlp_ready = false;
     uint64_t mlp_lights_hash = 0;
     int32_t mlp_nl = 0;
     float mlp_scale = 1.f;
     float mlp_loss = 0.f;
-    std::vector<float> mlp_q;     // rounded parameters of the current weights (rast::kMlpParams)
+    std::vector<float> mlp_q;     // rounded parameters of the current weights (MlpNet::kParams)
 
     // options
     uint32_t small_max = 4096;

@@ -132,7 +132,8 @@ struct DrawParams {
     float* depth;           // device
     uint32_t* tri_id;       // device, nullable
     int32_t shader = 0;     // 0 exact in the resolve pass, 1 exact deferred, 2 learned deferred
-    const void* mlp = nullptr;  // shader 2: the device MlpImage
+    const void* mlp = nullptr;  // shader 2: the device image of the weights (MlpNet)
+    int32_t mlp_net = 0;        // shader 2: its network (kMlpNetCompact or kMlpNetWide)
     int32_t mlp_samples = 2;    // shader 2: fragments per tile checked against the exact shader
     float mlp_bound = 0.5f;     // shader 2: largest checked channel error (1/255 units) a tile may have
     bool mlp_stall_test = false;  // shader 2, test only: the first MMA wait gives up (RAST_OPT_TEST_SHADE_STALL)

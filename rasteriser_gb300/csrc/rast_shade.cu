@@ -39,7 +39,7 @@ struct ShadeArgs {
     uint8_t* rgb;
     uint32_t* counters;
     // learned shader
-    const MlpImage* mlp;
+    const uint8_t* mlp;      // the weights' device image (MlpNet), then the check table
     int32_t samples;
     float bound;
     unsigned long long* stats;
@@ -161,11 +161,11 @@ __device__ __forceinline__ float bf16_round(float v) { return __bfloat162float(_
 
 constexpr float kPi = 3.14159265358979323846f;
 
-// sin and cos of f*pi*v for f = 1..kMlpFreq come from the base pair (the hardware sine and cosine of
-// pi*v, |pi*v| <= pi) by the three-term recurrence x_{f+1} = 2 cos(pi v) x_f - x_{f-1}, which both
+// sin and cos of f*pi*v for f = 1..F come from the base pair (the hardware sine and cosine of pi*v,
+// |pi*v| <= pi) by the three-term recurrence x_{f+1} = 2 cos(pi v) x_f - x_{f-1}, which both
 // sequences satisfy; one packed FMA advances the pair. Its error stays far below BF16's step.
 // emit(f, pair) receives the BF16 pair (sin, cos) of frequency f + 1 (sin in the low half).
-template <class Emit>
+template <int F, class Emit>
 __device__ __forceinline__ void fourier_pairs(float v, Emit&& emit) {
     float s1, c1;
     __sincosf(kPi * v, &s1, &c1);
@@ -173,7 +173,7 @@ __device__ __forceinline__ void fourier_pairs(float v, Emit&& emit) {
     float2 prev = make_float2(0.f, 1.f);
     float2 cur = make_float2(s1, c1);
 #pragma unroll
-    for (int f = 0; f < kMlpFreq; ++f) {
+    for (int f = 0; f < F; ++f) {
         emit(f, pack_bf16x2(cur.x, cur.y));
         const float2 next = __ffma2_rn(k2, cur, make_float2(-prev.x, -prev.y));
         prev = cur;
@@ -181,23 +181,23 @@ __device__ __forceinline__ void fourier_pairs(float v, Emit&& emit) {
     }
 }
 
-// The last 8 pairs of the features: n, albedo, the constant 1 that carries layer 1's bias
-// (feature kMlpConst), zeros.
-// The kMlpIn input features, each rounded to BF16, as packed pairs (feature 2i in the low half):
-// the Fourier pairs of n.x, n.y and n.z, then (n.x, n.y), (n.z, alb.x), (alb.y, alb.z), (1, 0) and
-// zero pairs.
+// Network N's N::kIn input features, each rounded to BF16, as packed pairs (feature 2i in the low
+// half): the Fourier pairs of n.x, n.y and n.z, then (n.x, n.y), (n.z, alb.x), (alb.y, alb.z),
+// (1, 0) -- the constant that carries layer 1's bias -- and zero pairs.
 constexpr int kTailPairs = 4;
-static_assert(kMlpConst == 6 * kMlpFreq + 6 && 3 * kMlpFreq + kTailPairs <= kMlpIn / 2, "feature layout");
-__device__ __forceinline__ void mlp_feature_pairs(float3 n, float3 alb, uint32_t (&pairs)[kMlpIn / 2]) {
+template <class N>
+__device__ __forceinline__ void mlp_feature_pairs(float3 n, float3 alb, uint32_t (&pairs)[N::kIn / 2]) {
+    constexpr int F = N::kFreq;
+    static_assert(N::kConst == 6 * F + 6 && 3 * F + kTailPairs <= N::kIn / 2, "feature layout");
     const float comp[3] = {n.x, n.y, n.z};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) fourier_pairs(comp[c], [&](int f, uint32_t p) { pairs[c * kMlpFreq + f] = p; });
-    pairs[3 * kMlpFreq] = pack_bf16x2(n.x, n.y);
-    pairs[3 * kMlpFreq + 1] = pack_bf16x2(n.z, alb.x);
-    pairs[3 * kMlpFreq + 2] = pack_bf16x2(alb.y, alb.z);
-    pairs[3 * kMlpFreq + 3] = pack_bf16x2(1.f, 0.f);
+    for (int c = 0; c < 3; ++c) fourier_pairs<F>(comp[c], [&](int f, uint32_t p) { pairs[c * F + f] = p; });
+    pairs[3 * F] = pack_bf16x2(n.x, n.y);
+    pairs[3 * F + 1] = pack_bf16x2(n.z, alb.x);
+    pairs[3 * F + 2] = pack_bf16x2(alb.y, alb.z);
+    pairs[3 * F + 3] = pack_bf16x2(1.f, 0.f);
 #pragma unroll
-    for (int i = 3 * kMlpFreq + kTailPairs; i < kMlpIn / 2; ++i) pairs[i] = 0u;
+    for (int i = 3 * F + kTailPairs; i < N::kIn / 2; ++i) pairs[i] = 0u;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -329,49 +329,31 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 // while one slot waits for its MMAs the others compute. The slots share the weights (B operands,
 // one copy in shared memory) and the light table of the checks.
 //
-// A slot's tensor memory is 32 columns of FP32 accumulators and two A operands 32 columns apart
-// (16 columns in use: 32 BF16 values per row), every region starting on a multiple of 32 columns.
-// A tile's features, h1 and h2 alternate between the two operands, so the next tile's features
-// are computed and stored while the current tile's last MMA runs:
+// A slot's tensor memory is its FP32 accumulators and two A operands, every region starting on a
+// multiple of 32 columns: for the compact network 32 accumulator columns and A operands 32 columns
+// apart (16 in use: 32 BF16 values per row); for the wide one 64 and 64 (56 in use). A tile's
+// features, h1 and h2 alternate between the two operands, so the next tile's features are computed
+// and stored while the current tile's last MMA runs:
 //   features(k) -> A[x]; h1 -> A[1-x]; h2 -> A[x]; features(k+1) -> A[1-x] during layer 3.
 //
 // Checks: the sampled rows of each tile put their normal, albedo and learned colour into the slot's
 // check buffer at the end of the tile; after every kCheckTiles tiles, and after the slot's last
 // tile, the slot checks the buffered rows (each warp its own rows, its lanes splitting the lights)
-// and shades the tiles that failed again, exactly. The kernel is compiled for each number of
-// checked samples, and the light table comes with the weights (built with them for their rig).
+// and shades the tiles that failed again, exactly. The kernel is compiled for each network and
+// number of checked samples, and the light table comes with the weights (built with them for
+// their rig).
 //
-// RAST_MLP_SLOTS, RAST_MLP_SLOT_COLS and RAST_MLP_CHECK_ROWS can be changed at build time to measure
-// other shapes (slots x (accumulator columns + 2 x 32) must fit the 512 columns of tensor memory);
-// the defaults are the fastest measured: five slots, whose 640 threads leave 96 registers each.
+// RAST_MLP_SLOTS (at most that many slots fit the 512 columns of tensor memory) and
+// RAST_MLP_CHECK_ROWS can be changed at build time to measure other shapes; the defaults are the
+// fastest measured for the compact network: five slots, whose 640 threads leave 96 registers each.
 #ifndef RAST_MLP_SLOTS
 #define RAST_MLP_SLOTS 5
 #endif
-constexpr int kSlots = RAST_MLP_SLOTS;
 constexpr int kLdBatch = 4;        // 16-column accumulator loads in flight per wait
 constexpr int kSlotThreads = 128;  // warp w of a slot reads TMEM lanes 32w..32w+31 (w = warp id mod 4)
-constexpr int kMlpThreads = kSlots * kSlotThreads;
-#ifndef RAST_MLP_SLOT_COLS
-#define RAST_MLP_SLOT_COLS 32
-#endif
-constexpr uint32_t kSlotCols = RAST_MLP_SLOT_COLS;   // a slot's accumulators
-constexpr uint32_t kACols = 32;                      // from one A operand to the other
-constexpr uint32_t kSlotTmem = kSlotCols + 2u * kACols;
-static_assert(kMlpHid <= (int)kSlotCols && kMlpOutPad <= (int)kSlotCols && kMlpIn / 2 <= (int)kACols,
-              "the accumulators and the A operands fit their columns");
 constexpr uint32_t kTmemCols = 512;
-static_assert(kMlpIn == kMlpHid, "one A operand shape serves every layer");
-static_assert(kSlots >= 1 && kSlots * kSlotTmem <= kTmemCols, "tensor memory of one SM");
 constexpr uint32_t kMaxSamples = 4;
 constexpr int kMlpSmemLights = 512;  // lights the checks read from shared memory
-
-// Shared memory (bytes): the weights and output scale, the checks' light table (dirI then gb, as in
-// MlpCheckTable), then the small block.
-constexpr uint32_t kSmW1 = 0;
-constexpr uint32_t kSmW2 = kSmW1 + kMlpHid * kMlpIn * 2;
-constexpr uint32_t kSmW3 = kSmW2 + kMlpHid * kMlpHid * 2;
-constexpr uint32_t kSmLights = (sizeof(MlpImage) + 15) / 16 * 16;
-constexpr uint32_t kSmMisc = kSmLights + 24u * kMlpSmemLights;
 static_assert(kMlpSmemLights == kMlpCheckLights, "the shared table is the image's check table");
 
 struct CheckRow {
@@ -385,6 +367,7 @@ struct SlotMisc {
     uint32_t pad;
     CheckRow q[kCheckTiles][kMaxSamples];   // the buffered tiles' sampled rows
 };
+template <int kSlots>
 struct MlpMisc {
     unsigned long long mbar_w;     // the weights' bulk copy
     unsigned long long mbar_idle;  // nothing arrives on it (the stall test's first wait)
@@ -393,13 +376,30 @@ struct MlpMisc {
     uint32_t tmem;
     SlotMisc slot[kSlots];
 };
-constexpr uint32_t kMlpSmem = kSmMisc + sizeof(MlpMisc);
-static_assert(kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmLights % 16 == 0 && kSmMisc % 16 == 0,
-              "operand alignment");
-static_assert(kMlpSmem <= 227 * 1024, "shared memory of one CTA");
-static_assert(sizeof(MlpImage) % 16 == 0, "bulk copy alignment");
 
-inline uint32_t mlp_smem_bytes() { return kMlpSmem; }
+constexpr uint32_t round32(uint32_t v) { return (v + 31u) / 32u * 32u; }
+
+// The kernel's layout for network N: tensor-memory columns and slots, threads, and shared memory
+// (bytes): the weights and output scale as in the device image, the checks' light table (dirI then
+// gb, as in MlpCheckTable), then the small block.
+template <class N>
+struct MlpLayout {
+    static constexpr uint32_t kSlotCols = round32((uint32_t)(N::kHid > kMlpOutPad ? N::kHid : kMlpOutPad));
+    static constexpr uint32_t kACols = round32((uint32_t)(N::kIn > N::kHid ? N::kIn : N::kHid) / 2u);
+    static constexpr uint32_t kSlotTmem = kSlotCols + 2u * kACols;
+    static constexpr int kSlots = (int)(kTmemCols / kSlotTmem) < RAST_MLP_SLOTS ? (int)(kTmemCols / kSlotTmem)
+                                                                                : RAST_MLP_SLOTS;
+    static constexpr int kThreads = kSlots * kSlotThreads;
+    static constexpr uint32_t kSmW1 = N::kW1Off, kSmW2 = N::kW2Off, kSmW3 = N::kW3Off, kSmScale = N::kScaleOff;
+    static constexpr uint32_t kSmLights = N::kImageBytes;
+    static constexpr uint32_t kSmMisc = kSmLights + 24u * kMlpSmemLights;
+    static constexpr uint32_t kSmem = kSmMisc + (uint32_t)sizeof(MlpMisc<kSlots>);
+    static_assert(kSlots >= 1 && kSlots * kSlotTmem <= kTmemCols, "tensor memory of one SM");
+    static_assert(kSmW2 % 16 == 0 && kSmW3 % 16 == 0 && kSmLights % 16 == 0 && kSmMisc % 16 == 0,
+                  "operand alignment");
+    static_assert(kSmem <= 227 * 1024, "shared memory of one CTA");
+};
+static_assert(MlpLayout<MlpCompact>::kSlots == 5 || RAST_MLP_SLOTS != 5, "the compact network runs five slots");
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
@@ -448,12 +448,13 @@ __device__ __forceinline__ void a_written() {
 
 // The features of one row (mlp_feature_pairs' order) into an A operand (this thread's lane of it),
 // 8 pairs (16 K elements) per store.
+template <class N>
 __device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t a) {
-    static_assert(kMlpIn % 16 == 0, "whole 8-pair stores");
-    uint32_t q[kMlpIn / 2];
-    mlp_feature_pairs(n, alb, q);
+    static_assert(N::kIn % 16 == 0, "whole 8-pair stores");
+    uint32_t q[N::kIn / 2];
+    mlp_feature_pairs<N>(n, alb, q);
 #pragma unroll
-    for (int i = 0; i < kMlpIn / 16; ++i) {
+    for (int i = 0; i < N::kIn / 16; ++i) {
         uint32_t p[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) p[j] = q[8 * i + j];
@@ -461,14 +462,15 @@ __device__ __forceinline__ void store_features(float3 n, float3 alb, uint32_t a)
     }
 }
 
-// Epilogue of a hidden layer: this thread's row of kMlpHid accumulators (TMEM columns from d)
+// Epilogue of a hidden layer: this thread's row of N::kHid accumulators (TMEM columns from d)
 // through ReLU, rounded to BF16, into an A operand: the next layer's A. Up to kLdBatch 16-column
 // loads are in flight per wait.
-constexpr int kEpiBatch = kMlpHid / 16 < kLdBatch ? kMlpHid / 16 : kLdBatch;
-static_assert(kMlpHid % 16 == 0 && (kMlpHid / 16) % kEpiBatch == 0, "whole batches of 16-column loads");
+template <class N>
 __device__ __forceinline__ void hidden_epilogue(uint32_t d, uint32_t a) {
+    constexpr int kEpiBatch = N::kHid / 16 < kLdBatch ? N::kHid / 16 : kLdBatch;
+    static_assert(N::kHid % 16 == 0 && (N::kHid / 16) % kEpiBatch == 0, "whole batches of 16-column loads");
 #pragma unroll
-    for (int g = 0; g < kMlpHid / 16; g += kEpiBatch) {
+    for (int g = 0; g < N::kHid / 16; g += kEpiBatch) {
         uint32_t v[kEpiBatch][16];
 #pragma unroll
         for (int i = 0; i < kEpiBatch; ++i) tmem_ld16(d + 16u * (g + i), v[i]);
@@ -604,11 +606,15 @@ __device__ void reshade_tile(const ShadeArgs& a, uint32_t t, int row) {
                   shade_lights(a.lights, a.nl, make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y)));
 }
 
-// NS: checked records per tile (0: none, as in the evaluation mode)
-template <int NS>
-__global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
+// N: the network; NS: checked records per tile (0: none, as in the evaluation mode)
+template <class N, int NS>
+__global__ void __launch_bounds__(MlpLayout<N>::kThreads, 1) k_shade_mlp(ShadeArgs a) {
+    using Lay = MlpLayout<N>;
+    constexpr int kSlots = Lay::kSlots;
+    constexpr uint32_t kSlotTmem = Lay::kSlotTmem, kSlotCols = Lay::kSlotCols, kACols = Lay::kACols;
+    constexpr uint32_t kSmLights = Lay::kSmLights, kSmMisc = Lay::kSmMisc;
     extern __shared__ __align__(1024) uint8_t sm[];
-    MlpMisc& M = *reinterpret_cast<MlpMisc*>(sm + kSmMisc);
+    MlpMisc<kSlots>& M = *reinterpret_cast<MlpMisc<kSlots>*>(sm + kSmMisc);
     const int slot = threadIdx.x / kSlotThreads, row = threadIdx.x % kSlotThreads;
     const int wq = row >> 5, lane = row & 31;  // warp within the slot = its TMEM lane quarter
     SlotMisc& S = M.slot[slot];
@@ -637,10 +643,10 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         for (int s = 0; s < kSlots; ++s) mbar_init(smem_addr(&M.slot[s].mbar), 1);
         // the weights and output scale, and the lights, arrive by bulk copy (independent of the
         // grid this kernel may overlap with)
-        mbar_expect_tx(mbar_w, (uint32_t)sizeof(MlpImage) + tab_dirI + tab_gb);
-        bulk_copy_g2s(smem_addr(sm), a.mlp, sizeof(MlpImage), mbar_w);
+        mbar_expect_tx(mbar_w, N::kImageBytes + tab_dirI + tab_gb);
+        bulk_copy_g2s(smem_addr(sm), a.mlp, N::kImageBytes, mbar_w);
         if (staged) {
-            const MlpCheckTable* tab = reinterpret_cast<const MlpCheckTable*>(a.mlp + 1);
+            const MlpCheckTable* tab = reinterpret_cast<const MlpCheckTable*>(a.mlp + N::kImageBytes);
             bulk_copy_g2s(smem_addr(lights_dirI), tab->dirI, tab_dirI, mbar_w);
             bulk_copy_g2s(smem_addr(lights_gb), tab->gb, tab_gb, mbar_w);
         }
@@ -672,12 +678,12 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
     const uint32_t d_lane = d_cols + lane_off;
     const uint32_t a_op0 = d_cols + kSlotCols;  // lane 0 of the first A operand; the second follows it
     // the first tile's features, while the weights arrive
-    if (t < n_tiles) store_features(make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y), a_op0 + lane_off);
+    if (t < n_tiles) store_features<N>(make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y), a_op0 + lane_off);
     a_written();
     bool failed = !__syncthreads_and(mbar_wait(mbar_w, 0));
     const bool weights_pending = failed;
-    const float out_scale = reinterpret_cast<const MlpImage*>(sm)->out_scale;
-    const uint32_t sW1 = smem_addr(sm + kSmW1), sW2 = smem_addr(sm + kSmW2), sW3 = smem_addr(sm + kSmW3);
+    const float out_scale = *reinterpret_cast<const float*>(sm + Lay::kSmScale);
+    const uint32_t sW1 = smem_addr(sm + Lay::kSmW1), sW2 = smem_addr(sm + Lay::kSmW2), sW3 = smem_addr(sm + Lay::kSmW3);
 
     // Every slot barrier of the loop also ORs the threads' timeout flags, so a slot's threads leave
     // the loop at the same barrier (the loop condition itself is the same in all of them).
@@ -711,7 +717,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         const uint32_t a_cur = a_op0 + x * kACols, a_oth = a_op0 + (x ^ 1u) * kACols;
 
         // layer 1: D = X (128 x K) * W1^T
-        if (row == 32 * (int)((k + 1u) & 3u)) issue_layer(d_cols, a_cur, sW1, kMlpHid, kMlpIn / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
+        if (row == 32 * (int)((k + 1u) & 3u)) issue_layer(d_cols, a_cur, sW1, N::kHid, N::kIn / 16, idesc_bf16(kMlpRows, N::kHid), mbar);
         // the slot's tile after next: its descriptor now, its records during layer 3
         const uint32_t t_nn = t_next + stride;
         const uint32_t count_nn = tile_count(n_frag, n_tiles, t_nn);
@@ -730,23 +736,23 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_shade_mlp(ShadeArgs a) {
         failed |= !mbar_wait(mbar_first, phase, tries_first);
         phase ^= 1u;
         tc_fence_after();
-        if (!__any_sync(kFull, failed)) hidden_epilogue(d_lane, a_oth + lane_off);  // h1
+        if (!__any_sync(kFull, failed)) hidden_epilogue<N>(d_lane, a_oth + lane_off);  // h1
         a_written();
         if (slot_sync_or(slot, failed)) break;
 
-        // layer 2: D = H1 (128 x kMlpHid) * W2^T
-        if (row == 32 * (int)((k + 2u) & 3u)) issue_layer(d_cols, a_oth, sW2, kMlpHid, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpHid), mbar);
+        // layer 2: D = H1 (128 x H) * W2^T
+        if (row == 32 * (int)((k + 2u) & 3u)) issue_layer(d_cols, a_oth, sW2, N::kHid, N::kHid / 16, idesc_bf16(kMlpRows, N::kHid), mbar);
         failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
         tc_fence_after();
-        if (!__any_sync(kFull, failed)) hidden_epilogue(d_lane, a_cur + lane_off);  // h2 over the features
+        if (!__any_sync(kFull, failed)) hidden_epilogue<N>(d_lane, a_cur + lane_off);  // h2 over the features
         a_written();
         if (slot_sync_or(slot, failed)) break;
 
-        // layer 3: D[0, 16) = H2 (128 x kMlpHid) * W3^T; meanwhile the next tile's features go over h1
-        if (row == 32 * (int)((k + 3u) & 3u)) issue_layer(d_cols, a_cur, sW3, kMlpOutPad, kMlpHid / 16, idesc_bf16(kMlpRows, kMlpOutPad), mbar);
+        // layer 3: D[0, 16) = H2 (128 x H) * W3^T; meanwhile the next tile's features go over h1
+        if (row == 32 * (int)((k + 3u) & 3u)) issue_layer(d_cols, a_cur, sW3, kMlpOutPad, N::kHid / 16, idesc_bf16(kMlpRows, kMlpOutPad), mbar);
         if (t_next < n_tiles && !__any_sync(kFull, failed))
-            store_features(make_float3(g0n.x, g0n.y, g0n.z), make_float3(g0n.w, g1n.x, g1n.y), a_oth + lane_off);
+            store_features<N>(make_float3(g0n.x, g0n.y, g0n.z), make_float3(g0n.w, g1n.x, g1n.y), a_oth + lane_off);
         float4 g0nn, g1nn;
         load_record_desc(a, t_nn, count_nn, d_nn, row, g0nn, g1nn);
         failed |= !mbar_wait(mbar, phase);
@@ -889,22 +895,27 @@ __global__ void k_mlp_stage(const float* __restrict__ src, int stride, int64_t n
 
 constexpr int kTrainB = 64;          // samples per CTA and step
 constexpr int kTrainThreads = 256;
-constexpr int kSX = kMlpIn + 4;      // shared row stride (floats) of X and W1: rows stay 16-byte
-constexpr int kSH = kMlpHid + 4;     // aligned and eight rows cover all banks; of H, D and W2
-// Thread tid works on unit j = tid % kMlpHid for group tid / kMlpHid of the samples (forward, dH)
-// or of the inputs (weight gradients).
-constexpr int kTrainGroups = kTrainThreads / kMlpHid;
-constexpr int kSPG = kTrainB / kTrainGroups;   // samples per group
-constexpr int kHPG = kMlpHid / kTrainGroups;   // hidden inputs per group (layer 2 gradients)
-constexpr int kXPG = kMlpIn / kTrainGroups;    // features per group (layer 1 gradients)
-static_assert(kTrainThreads % kMlpHid == 0 && kTrainB % kTrainGroups == 0 && kHPG % 4 == 0 && kXPG % 4 == 0 &&
-                  kMlpIn % 4 == 0 && kTrainB * kMlpOut <= kTrainThreads && kMlpOut * kMlpHid <= kTrainThreads,
-              "training thread layout");
+// The training step's layout for network N. Thread tid works on unit j = tid % H for group
+// tid / H of the samples (forward, dH) or of the inputs (weight gradients).
+template <class N>
+struct TrainLayout {
+    static constexpr int kSX = N::kIn + 4;   // shared row stride (floats) of X and W1: rows stay 16-byte
+    static constexpr int kSH = N::kHid + 4;  // aligned and eight rows cover all banks; of H, D and W2
+    static constexpr int kGroups = kTrainThreads / N::kHid;
+    static constexpr int kSPG = kTrainB / kGroups;     // samples per group
+    static constexpr int kHPG = N::kHid / kGroups;     // hidden inputs per group (layer 2 gradients)
+    static constexpr int kXPG = N::kIn / kGroups;      // features per group (layer 1 gradients)
+    static_assert(kTrainThreads % N::kHid == 0 && kTrainB % kGroups == 0 && kHPG % 4 == 0 && kXPG % 4 == 0 &&
+                      N::kIn % 4 == 0 && kTrainB * kMlpOut <= kTrainThreads && kMlpOut * N::kHid <= kTrainThreads,
+                  "training thread layout");
+};
 
+template <class N>
 struct TrainSmem {
-    float w1[kMlpHid * kSX];
-    float w2[kMlpHid * kSH];
-    float w3[kMlpOut * kMlpHid];
+    static constexpr int kSX = TrainLayout<N>::kSX, kSH = TrainLayout<N>::kSH;
+    float w1[N::kHid * kSX];
+    float w2[N::kHid * kSH];
+    float w3[kMlpOut * N::kHid];
     float pad[4];
     float x[kTrainB * kSX];
     float h1[kTrainB * kSH];
@@ -929,9 +940,14 @@ struct TrainArgs {
 
 // One step's forward and backward pass for kTrainB samples per CTA, in FP32 with the rounding of the
 // tensor-core kernel (BF16 features, weights and hidden activations); per-CTA partial gradients.
+template <class N>
 __global__ void __launch_bounds__(kTrainThreads) k_mlp_train(TrainArgs a) {
+    using TL = TrainLayout<N>;
+    constexpr int kSX = TL::kSX, kSH = TL::kSH, kSPG = TL::kSPG, kHPG = TL::kHPG, kXPG = TL::kXPG;
+    constexpr int kMlpIn = N::kIn, kMlpHid = N::kHid, kPW1 = N::kPW1, kPW2 = N::kPW2, kPW3 = N::kPW3;
+    constexpr int kMlpParams = N::kParams;
     extern __shared__ __align__(16) uint8_t smraw[];
-    TrainSmem& S = *reinterpret_cast<TrainSmem*>(smraw);
+    TrainSmem<N>& S = *reinterpret_cast<TrainSmem<N>*>(smraw);
     const int tid = threadIdx.x;
     for (int i = tid; i < kMlpHid * kMlpIn; i += kTrainThreads) S.w1[(i / kMlpIn) * kSX + i % kMlpIn] = a.q[kPW1 + i];
     for (int i = tid; i < kMlpHid * kMlpHid; i += kTrainThreads) S.w2[(i / kMlpHid) * kSH + i % kMlpHid] = a.q[kPW2 + i];
@@ -941,7 +957,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train(TrainArgs a) {
         const float* s = a.samples + 9 * i;
         const float3 nv = make_float3(s[0], s[1], s[2]), alb = make_float3(s[3], s[4], s[5]);
         uint32_t pairs[kMlpIn / 2];
-        mlp_feature_pairs(nv, alb, pairs);
+        mlp_feature_pairs<N>(nv, alb, pairs);
         float* x = S.x + tid * kSX;
 #pragma unroll
         for (int k = 0; k < kMlpIn / 2; ++k) {
@@ -1092,6 +1108,7 @@ struct AdamArgs {
     float* loss_out;       // this step's summed squared error
 };
 
+template <class N>
 __global__ void k_mlp_adam(AdamArgs a) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p == 0 && a.loss_out) {
@@ -1099,9 +1116,9 @@ __global__ void k_mlp_adam(AdamArgs a) {
         for (int i = 0; i < a.n_part; ++i) s += a.loss_part[i];
         *a.loss_out = s;
     }
-    if (p >= kMlpParams || mlp_param_fixed(p)) return;
+    if (p >= N::kParams || N::fixed(p)) return;
     float gs = 0.f;
-    for (int i = 0; i < a.n_part; ++i) gs += a.grad[(size_t)i * kMlpParams + p];
+    for (int i = 0; i < a.n_part; ++i) gs += a.grad[(size_t)i * N::kParams + p];
     const float m = a.beta1 * a.m[p] + (1.f - a.beta1) * gs;
     const float v = a.beta2 * a.v[p] + (1.f - a.beta2) * gs * gs;
     a.m[p] = m;
@@ -1128,7 +1145,7 @@ static ShadeArgs shade_args(const FrameScratch& s, const DrawParams& p) {
     a.nl = p.nl;
     a.rgb = p.rgb;
     a.counters = s.counters;
-    a.mlp = static_cast<const MlpImage*>(p.mlp);
+    a.mlp = static_cast<const uint8_t*>(p.mlp);
     a.samples = p.mlp_samples;
     a.bound = p.mlp_bound;
     a.stats = s.shade_stats;
@@ -1137,27 +1154,30 @@ static ShadeArgs shade_args(const FrameScratch& s, const DrawParams& p) {
     return a;
 }
 
-// The learned-shader kernel for a number of checked samples per tile (0 .. kMaxSamples).
+// Network N's learned-shader kernel for a number of checked samples per tile (0 .. kMaxSamples).
 using MlpKernel = void (*)(ShadeArgs);
+template <class N>
 static MlpKernel mlp_kernel(int samples) {
-    static const MlpKernel k[kMaxSamples + 1] = {k_shade_mlp<0>, k_shade_mlp<1>, k_shade_mlp<2>, k_shade_mlp<3>,
-                                                 k_shade_mlp<4>};
+    static const MlpKernel k[kMaxSamples + 1] = {k_shade_mlp<N, 0>, k_shade_mlp<N, 1>, k_shade_mlp<N, 2>,
+                                                 k_shade_mlp<N, 3>, k_shade_mlp<N, 4>};
     return k[std::min(std::max(samples, 0), (int)kMaxSamples)];
 }
 
+template <class N>
 static int mlp_grid(int n_sm, int64_t blocks) {
     static bool attr_set = false;  // per process: the attribute is per function, all devices alike
     if (!attr_set) {
         for (int ns = 0; ns <= (int)kMaxSamples; ++ns)
-            if (cudaFuncSetAttribute(mlp_kernel(ns), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpSmem) !=
-                    cudaSuccess ||
-                cudaFuncSetAttribute(mlp_kernel(ns), cudaFuncAttributePreferredSharedMemoryCarveout,
+            if (cudaFuncSetAttribute(mlp_kernel<N>(ns), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)MlpLayout<N>::kSmem) != cudaSuccess ||
+                cudaFuncSetAttribute(mlp_kernel<N>(ns), cudaFuncAttributePreferredSharedMemoryCarveout,
                                      (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
                 return -1;
         attr_set = true;
     }
     // one CTA per SM at most, and no more CTAs than the tiles need (a block of 1024 records makes
     // at most 8 tiles)
+    constexpr int kSlots = MlpLayout<N>::kSlots;
     const int64_t max_tiles = (int64_t)(kShadeBlock / kShadeTile) * blocks;
     return (int)std::min<int64_t>((int64_t)n_sm, std::max<int64_t>((max_tiles + kSlots - 1) / kSlots, 1));
 }
@@ -1192,14 +1212,18 @@ int launch_shade(const FrameScratch& s, const DrawParams& p, int64_t blocks, cud
     if (p.shader == 1) {
         err = launch_dependent(k_shade_exact, exact_grid(p.n_sm, blocks), kExactThreads, 0, stream, a);
     } else {
-        const int grid = mlp_grid(p.n_sm, blocks);
-        if (grid < 0) return -1;
-        err = launch_dependent(mlp_kernel(a.samples), grid, kMlpThreads, mlp_smem_bytes(), stream, a);
+        err = with_mlp_net(p.mlp_net, [&](auto n) {
+            using N = decltype(n);
+            const int grid = mlp_grid<N>(p.n_sm, blocks);
+            if (grid < 0) return cudaErrorInvalidConfiguration;
+            return launch_dependent(mlp_kernel<N>(a.samples), grid, MlpLayout<N>::kThreads, MlpLayout<N>::kSmem,
+                                    stream, a);
+        });
     }
     return err == cudaSuccess ? 1 : -1;
 }
 
-int launch_mlp_eval(const float* src, int stride, int64_t n, bool exact, float4* gbuf, uint32_t* count,
+int launch_mlp_eval(int net, const float* src, int stride, int64_t n, bool exact, float4* gbuf, uint32_t* count,
                     uint32_t* index, const float* lights, int nl, const void* mlp, uint32_t* counters, int n_sm,
                     float* out, cudaStream_t stream) {
     if (n <= 0) return 0;
@@ -1215,7 +1239,7 @@ int launch_mlp_eval(const float* src, int stride, int64_t n, bool exact, float4*
     a.nl = nl;
     a.rgb = nullptr;
     a.counters = counters;
-    a.mlp = static_cast<const MlpImage*>(mlp);
+    a.mlp = static_cast<const uint8_t*>(mlp);
     a.samples = 0;
     a.bound = 0.f;
     a.stats = nullptr;
@@ -1224,9 +1248,13 @@ int launch_mlp_eval(const float* src, int stride, int64_t n, bool exact, float4*
     if (exact) {
         k_shade_exact<<<exact_grid(n_sm, blocks), kExactThreads, 0, stream>>>(a);
     } else {
-        const int grid = mlp_grid(n_sm, blocks);
+        const int grid = with_mlp_net(net, [&](auto m) {
+            using N = decltype(m);
+            const int g = mlp_grid<N>(n_sm, blocks);
+            if (g > 0) k_shade_mlp<N, 0><<<g, MlpLayout<N>::kThreads, MlpLayout<N>::kSmem, stream>>>(a);
+            return g;
+        });
         if (grid < 0) return -1;
-        k_shade_mlp<0><<<grid, kMlpThreads, mlp_smem_bytes(), stream>>>(a);
     }
     return cudaGetLastError() == cudaSuccess ? 3 : -1;
 }
@@ -1237,15 +1265,17 @@ int launch_mlp_samples(float* out, int64_t n, uint64_t seed, const float* lights
     return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 
-int launch_mlp_train_step(const float* q, const float* samples, int64_t n, int64_t first, int n_cta, float out_scale,
-                          float grad_scale, float* grad, float* loss, cudaStream_t stream) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TrainSmem)) !=
-            cudaSuccess)
-            return -1;
-        attr_set = true;
-    }
+template <class N>
+static bool train_attr() {
+    static bool attr_set = false;  // per process: the attribute is per function
+    if (!attr_set)
+        attr_set = cudaFuncSetAttribute(k_mlp_train<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sizeof(TrainSmem<N>)) == cudaSuccess;
+    return attr_set;
+}
+
+int launch_mlp_train_step(int net, const float* q, const float* samples, int64_t n, int64_t first, int n_cta,
+                          float out_scale, float grad_scale, float* grad, float* loss, cudaStream_t stream) {
     TrainArgs a;
     a.q = q;
     a.samples = samples;
@@ -1255,19 +1285,28 @@ int launch_mlp_train_step(const float* q, const float* samples, int64_t n, int64
     a.grad_scale = grad_scale;
     a.grad = grad;
     a.loss = loss;
-    k_mlp_train<<<n_cta, kTrainThreads, sizeof(TrainSmem), stream>>>(a);
-    return cudaGetLastError() == cudaSuccess ? 1 : -1;
+    const bool ok = with_mlp_net(net, [&](auto m) {
+        using N = decltype(m);
+        if (!train_attr<N>()) return false;
+        k_mlp_train<N><<<n_cta, kTrainThreads, sizeof(TrainSmem<N>), stream>>>(a);
+        return true;
+    });
+    return ok && cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 
-int launch_mlp_adam(float* w, float* q, float* m, float* v, const float* grad, int n_part, float lr, float beta1,
-                    float beta2, float eps, float c1, float c2, const float* loss_part, float* loss_out,
+int launch_mlp_adam(int net, float* w, float* q, float* m, float* v, const float* grad, int n_part, float lr,
+                    float beta1, float beta2, float eps, float c1, float c2, const float* loss_part, float* loss_out,
                     cudaStream_t stream) {
     AdamArgs a;
     a.w = w; a.q = q; a.m = m; a.v = v; a.grad = grad; a.n_part = n_part;
     a.lr = lr; a.beta1 = beta1; a.beta2 = beta2; a.eps = eps; a.c1 = c1; a.c2 = c2;
     a.loss_part = loss_part;
     a.loss_out = loss_out;
-    k_mlp_adam<<<grid_for(kMlpParams, 256), 256, 0, stream>>>(a);
+    with_mlp_net(net, [&](auto n) {
+        using N = decltype(n);
+        k_mlp_adam<N><<<grid_for(N::kParams, 256), 256, 0, stream>>>(a);
+        return 0;
+    });
     return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 

@@ -6,8 +6,19 @@ import numpy as np
 
 HEADER = struct.Struct("<4s7IQff")  # magic, version, n_in, n_hidden, n_out, n_freq, n_lights, reserved,
                                     # lights_hash, out_scale, train_loss
-N_IN, N_HID, N_OUT, N_FREQ = 25, 32, 3, 3  # N_IN counts the constant-1 feature
+N_OUT = 3
 VERSION = 3
+# the networks of RAST_OPT_MLP_NETWORK: (Fourier frequencies, hidden width); inputs are 6F + 7,
+# the constant-1 feature included
+NETWORKS = {0: (3, 32), 1: (16, 64)}
+N_FREQ, N_HID = NETWORKS[0]
+N_IN = 6 * N_FREQ + 7
+
+
+def dims(net):
+    """(n_in, n_hidden, n_freq) of network `net`."""
+    f, h = NETWORKS[net]
+    return 6 * f + 7, h, f
 
 
 def bf16_round(a):
@@ -21,37 +32,42 @@ def bf16_bits(a):
     return (bf16_round(a).view(np.uint32) >> 16).astype(np.uint16)
 
 
-def features(n, alb):
-    """(m, N_IN): sin / cos(f * pi * n_c) for c in xyz, f = 1..N_FREQ (pairs), then n, albedo and 1."""
+def features(n, alb, n_freq=N_FREQ):
+    """(m, 6F + 7): sin / cos(f * pi * n_c) for c in xyz, f = 1..F (pairs), then n, albedo and 1."""
     n = np.asarray(n, np.float64)
-    f = np.arange(1, N_FREQ + 1, dtype=np.float64)
+    f = np.arange(1, n_freq + 1, dtype=np.float64)
     cols = []
     for c in range(3):
         ang = np.pi * f[None, :] * n[:, c:c + 1]
-        cols.append(np.stack([np.sin(ang), np.cos(ang)], axis=2).reshape(-1, 2 * N_FREQ))
+        cols.append(np.stack([np.sin(ang), np.cos(ang)], axis=2).reshape(-1, 2 * n_freq))
     ones = np.ones((n.shape[0], 1))
     return np.concatenate(cols + [n, np.asarray(alb, np.float64), ones], axis=1)
 
 
-def random_weights(seed, scale=12.0):
-    """Arbitrary BF16 weights of the network's shapes (biases folded in: W1's last column)."""
+def random_weights(seed, scale=12.0, net=0):
+    """Arbitrary BF16 weights of network `net`'s shapes (biases folded in: W1's last column)."""
+    n_in, n_hid, n_freq = dims(net)
     rng = np.random.default_rng(seed)
     return {
-        "w1": bf16_round(rng.uniform(-1, 1, (N_HID, N_IN)) * np.sqrt(6.0 / N_IN)),
-        "w2": bf16_round(rng.uniform(-1, 1, (N_HID, N_HID)) * np.sqrt(6.0 / N_HID)),
-        "w3": bf16_round(rng.uniform(-1, 1, (N_OUT, N_HID)) * np.sqrt(6.0 / N_HID) * 0.5),
+        "w1": bf16_round(rng.uniform(-1, 1, (n_hid, n_in)) * np.sqrt(6.0 / n_in)),
+        "w2": bf16_round(rng.uniform(-1, 1, (n_hid, n_hid)) * np.sqrt(6.0 / n_hid)),
+        "w3": bf16_round(rng.uniform(-1, 1, (N_OUT, n_hid)) * np.sqrt(6.0 / n_hid) * 0.5),
         "scale": np.float32(scale),
+        "n_freq": n_freq,
     }
 
 
 def make_blob(w, n_lights=0, lights_hash=0, loss=0.0):
-    head = HEADER.pack(b"RMLP", VERSION, N_IN, N_HID, N_OUT, N_FREQ, n_lights, 0, lights_hash, float(w["scale"]), loss)
+    n_hid, n_in = w["w1"].shape
+    head = HEADER.pack(b"RMLP", VERSION, n_in, n_hid, N_OUT, w["n_freq"], n_lights, 0, lights_hash,
+                       float(w["scale"]), loss)
     return head + b"".join([bf16_bits(w["w1"]).tobytes(), bf16_bits(w["w2"]).tobytes(), bf16_bits(w["w3"]).tobytes()])
 
 
 def parse_blob(blob):
     h = HEADER.unpack_from(blob, 0)
-    assert h[0] == b"RMLP" and h[1] == VERSION and h[2] == N_IN
+    assert h[0] == b"RMLP" and h[1] == VERSION and (h[2], h[3], h[5]) in [dims(k) for k in NETWORKS]
+    n_in, n_hid = h[2], h[3]
     off = HEADER.size
 
     def take(count):
@@ -60,8 +76,8 @@ def parse_blob(blob):
         off += a.nbytes
         return (a.astype(np.uint32) << 16).view(np.float32)
 
-    w = {"w1": take(N_HID * N_IN).reshape(N_HID, N_IN), "w2": take(N_HID * N_HID).reshape(N_HID, N_HID),
-         "w3": take(N_OUT * N_HID).reshape(N_OUT, N_HID),
+    w = {"w1": take(n_hid * n_in).reshape(n_hid, n_in), "w2": take(n_hid * n_hid).reshape(n_hid, n_hid),
+         "w3": take(N_OUT * n_hid).reshape(N_OUT, n_hid), "n_freq": h[5],
          "scale": np.float32(h[9]), "n_lights": h[6], "lights_hash": h[8], "loss": h[10]}
     assert off == len(blob)
     return w
@@ -69,7 +85,7 @@ def parse_blob(blob):
 
 def forward(w, n, alb):
     """Radiance (m, 3) before clamping: BF16 inputs and hidden activations, float64 sums."""
-    x = bf16_round(features(n, alb).astype(np.float32)).astype(np.float64)
+    x = bf16_round(features(n, alb, w["n_freq"]).astype(np.float32)).astype(np.float64)
     h1 = bf16_round(np.maximum(x @ w["w1"].T.astype(np.float64), 0).astype(np.float32)).astype(np.float64)
     h2 = bf16_round(np.maximum(h1 @ w["w2"].T.astype(np.float64), 0).astype(np.float32)).astype(np.float64)
     o = h2 @ w["w3"].T.astype(np.float64)

@@ -107,7 +107,7 @@ def test_vertex_albedo_size_checked(rnd):
 
 def test_options_validated(rnd):
     for opt, bad in [(abi.OPT_SHADER, 3), (abi.OPT_MLP_SAMPLES, 5), (abi.OPT_MLP_SAMPLES, -1),
-                     (abi.OPT_MLP_BOUND_MILLI, -1)]:
+                     (abi.OPT_MLP_BOUND_MILLI, -1), (abi.OPT_MLP_NETWORK, 2), (abi.OPT_MLP_NETWORK, -1)]:
         with pytest.raises(abi.RastError):
             rnd.set_option(opt, bad)
     assert rnd.get_option(abi.OPT_SHADER) == abi.SHADER_EXACT
@@ -115,9 +115,10 @@ def test_options_validated(rnd):
     assert rnd.get_option(abi.OPT_MLP_BOUND_MILLI) == 500
 
 
-def test_mlp_kernel_matches_numpy(rnd):
-    """The tcgen05 path against a float64 forward pass of the same BF16 weights."""
-    w = mlp_ref.random_weights(7)
+@pytest.mark.parametrize("net", sorted(mlp_ref.NETWORKS))
+def test_mlp_kernel_matches_numpy(rnd, net):
+    """The tcgen05 path against a float64 forward pass of the same BF16 weights, for each network."""
+    w = mlp_ref.random_weights(7, net=net)
     rnd.mlp_load(mlp_ref.make_blob(w))
     rng = np.random.default_rng(11)
     n = 5000  # 40 tiles, the last one partial
@@ -138,8 +139,9 @@ def test_mlp_kernel_matches_numpy(rnd):
     assert np.all(err <= tol), f"max err {err.max()} at {np.unravel_index(err.argmax(), err.shape)}"
 
 
-def test_mlp_blob_round_trip(rnd):
-    w = mlp_ref.random_weights(8)
+@pytest.mark.parametrize("net", sorted(mlp_ref.NETWORKS))
+def test_mlp_blob_round_trip(rnd, net):
+    w = mlp_ref.random_weights(8, net=net)
     blob = mlp_ref.make_blob(w, n_lights=3, lights_hash=12345, loss=0.25)
     rnd.mlp_load(blob)
     assert rnd.mlp_save() == blob
@@ -157,9 +159,13 @@ def test_mlp_blob_refused(rnd):
     with pytest.raises(abi.RastError):
         rnd.mlp_load(bytes(bad))
     other = bytearray(blob)
-    other[8:12] = (102).to_bytes(4, "little")  # n_in of another network
+    other[8:12] = (102).to_bytes(4, "little")  # n_in of no network
     with pytest.raises(abi.RastError):
         rnd.mlp_load(bytes(other))
+    mixed = bytearray(blob)
+    mixed[12:16] = (64).to_bytes(4, "little")  # the compact inputs with the wide hidden width
+    with pytest.raises(abi.RastError):
+        rnd.mlp_load(bytes(mixed))
 
 
 def test_exact_eval_matches_oracle_shade(rnd, port):
@@ -214,6 +220,41 @@ def test_learned_frame(rnd, port, trained):
     assert diff[:, cov].mean() <= MEAN_TOL
     # tiles: 128 consecutive covered pixels (in block order, which is raster order) each
     assert st["tiles"] == (int(cov.sum()) + 127) // 128
+
+
+def test_wide_network_trains_and_shades(rnd, port, trained):
+    """RAST_OPT_MLP_NETWORK 1 trains the 16-frequency network with hidden layers of 64; its frame
+    keeps coverage and depth exact and its colour within the same bounds. Weights keep their own
+    network: the compact blob loaded afterwards shades as the compact network again."""
+    sc, lights, _, blob = trained
+    rnd.set_lights(lights)
+    assert rnd.get_option(abi.OPT_MLP_NETWORK) == abi.MLP_COMPACT
+    rnd.set_option(abi.OPT_MLP_NETWORK, abi.MLP_WIDE)
+    try:
+        st = rnd.mlp_train(samples=4 << 20, epochs=24, seed=3)
+        wide_blob = rnd.mlp_save()
+    finally:
+        rnd.set_option(abi.OPT_MLP_NETWORK, abi.MLP_COMPACT)
+    print("wide training:", st)
+    assert st["mean_err"] < 0.25 and st["max_err"] < 2.0, st
+    hdr = mlp_ref.parse_blob(wide_blob)
+    assert hdr["w1"].shape == (64, 103) and hdr["n_freq"] == 16
+    assert len(wide_blob) != len(blob)
+    rnd.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
+    try:
+        f, d, ids = rnd.draw_scene(sc, clear=True)
+        st = rnd.shade_stats()
+    finally:
+        rnd.set_option(abi.OPT_SHADER, abi.SHADER_EXACT)
+    of, od, oids = oracle_frame(port, sc)
+    assert np.array_equal(bits(d), bits(od)) and np.array_equal(ids, oids)
+    cov = oids != 0xFFFFFFFF
+    diff = np.abs(f.astype(np.int16) - of.astype(np.int16))
+    print("wide frame: max", diff.max(), "mean", diff[:, cov].mean(), "stats", st)
+    assert diff.max() <= RGB_TOL and diff[:, cov].mean() <= MEAN_TOL
+    assert st["tiles"] == (int(cov.sum()) + 127) // 128
+    rnd.mlp_load(blob)
+    assert rnd.mlp_save() == blob
 
 
 def test_learned_fallback_gives_exact_colour(rnd, port, trained):
