@@ -329,12 +329,12 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 // while one slot waits for its MMAs the others compute. The slots share the weights (B operands,
 // one copy in shared memory) and the light table of the checks.
 //
-// A slot's tensor memory is its FP32 accumulators and two A operands, every region starting on a
-// multiple of 32 columns: for the compact network 32 accumulator columns and A operands 32 columns
-// apart (16 in use: 32 BF16 values per row); for the wide one 64 and 64 (56 in use). A tile's
-// features, h1 and h2 alternate between the two operands, so the next tile's features are computed
-// and stored while the current tile's last MMA runs:
-//   features(k) -> A[x]; h1 -> A[1-x]; h2 -> A[x]; features(k+1) -> A[1-x] during layer 3.
+// A slot's tensor memory is its FP32 accumulators and two A operands, F for the features and H for
+// the hidden layers, every region starting on a multiple of 32 columns: for the compact network
+// 32 accumulator columns, F and H 32 each (16 in use: 32 BF16 values per row), 96 in all; for the
+// wide one 64, 64 (56 in use) and 32, 160 in all. h2 overwrites h1 once layer 2 has read it, and
+// the next tile's features overwrite this tile's while its last MMA runs:
+//   features(k) -> F; h1 -> H; h2 -> H; features(k+1) -> F during layer 3.
 //
 // Checks: the sampled rows of each tile put their normal, albedo and learned colour into the slot's
 // check buffer at the end of the tile; after every kCheckTiles tiles, and after the slot's last
@@ -343,7 +343,7 @@ __device__ __forceinline__ void reg_fence16(uint32_t (&v)[16]) {
 // number of checked samples, and the light table comes with the weights (built with them for
 // their rig).
 //
-// RAST_MLP_SLOTS (at most that many slots fit the 512 columns of tensor memory) and
+// RAST_MLP_SLOTS (at most as many slots as fit the 512 columns of tensor memory: 5 compact, 3 wide) and
 // RAST_MLP_CHECK_ROWS can be changed at build time to measure other shapes; the defaults are the
 // fastest measured for the compact network: five slots, whose 640 threads leave 96 registers each.
 #ifndef RAST_MLP_SLOTS
@@ -385,8 +385,9 @@ constexpr uint32_t round32(uint32_t v) { return (v + 31u) / 32u * 32u; }
 template <class N>
 struct MlpLayout {
     static constexpr uint32_t kSlotCols = round32((uint32_t)(N::kHid > kMlpOutPad ? N::kHid : kMlpOutPad));
-    static constexpr uint32_t kACols = round32((uint32_t)(N::kIn > N::kHid ? N::kIn : N::kHid) / 2u);
-    static constexpr uint32_t kSlotTmem = kSlotCols + 2u * kACols;
+    static constexpr uint32_t kFCols = round32((uint32_t)N::kIn / 2u);   // the features' A operand
+    static constexpr uint32_t kHCols = round32((uint32_t)N::kHid / 2u);  // the hidden layers' A operand
+    static constexpr uint32_t kSlotTmem = kSlotCols + kFCols + kHCols;
     static constexpr int kSlots = (int)(kTmemCols / kSlotTmem) < RAST_MLP_SLOTS ? (int)(kTmemCols / kSlotTmem)
                                                                                 : RAST_MLP_SLOTS;
     static constexpr int kThreads = kSlots * kSlotThreads;
@@ -611,7 +612,7 @@ template <class N, int NS>
 __global__ void __launch_bounds__(MlpLayout<N>::kThreads, 1) k_shade_mlp(ShadeArgs a) {
     using Lay = MlpLayout<N>;
     constexpr int kSlots = Lay::kSlots;
-    constexpr uint32_t kSlotTmem = Lay::kSlotTmem, kSlotCols = Lay::kSlotCols, kACols = Lay::kACols;
+    constexpr uint32_t kSlotTmem = Lay::kSlotTmem, kSlotCols = Lay::kSlotCols, kFCols = Lay::kFCols;
     constexpr uint32_t kSmLights = Lay::kSmLights, kSmMisc = Lay::kSmMisc;
     extern __shared__ __align__(1024) uint8_t sm[];
     MlpMisc<kSlots>& M = *reinterpret_cast<MlpMisc<kSlots>*>(sm + kSmMisc);
@@ -676,9 +677,10 @@ __global__ void __launch_bounds__(MlpLayout<N>::kThreads, 1) k_shade_mlp(ShadeAr
     const uint32_t d_cols = tmem + (uint32_t)slot * kSlotTmem;  // lane 0, this slot's accumulators
     const uint32_t lane_off = (uint32_t)(wq * 32) << 16;         // this warp's lanes
     const uint32_t d_lane = d_cols + lane_off;
-    const uint32_t a_op0 = d_cols + kSlotCols;  // lane 0 of the first A operand; the second follows it
+    const uint32_t a_f = d_cols + kSlotCols;  // lane 0 of the features' A operand
+    const uint32_t a_h = a_f + kFCols;        // lane 0 of the hidden layers' A operand
     // the first tile's features, while the weights arrive
-    if (t < n_tiles) store_features<N>(make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y), a_op0 + lane_off);
+    if (t < n_tiles) store_features<N>(make_float3(g0.x, g0.y, g0.z), make_float3(g0.w, g1.x, g1.y), a_f + lane_off);
     a_written();
     bool failed = !__syncthreads_and(mbar_wait(mbar_w, 0));
     const bool weights_pending = failed;
@@ -687,7 +689,7 @@ __global__ void __launch_bounds__(MlpLayout<N>::kThreads, 1) k_shade_mlp(ShadeAr
 
     // Every slot barrier of the loop also ORs the threads' timeout flags, so a slot's threads leave
     // the loop at the same barrier (the loop condition itself is the same in all of them).
-    uint32_t phase = 0, x = 0;  // x: the A operand holding the current tile's features
+    uint32_t phase = 0;
     uint32_t n_tile = 0, n_fallback = 0;
     float max_err = 0.f;
     uint32_t k = 0;  // tiles this slot shaded
@@ -714,10 +716,9 @@ __global__ void __launch_bounds__(MlpLayout<N>::kThreads, 1) k_shade_mlp(ShadeAr
         // the features are stored, the previous tile's accumulators read and its sampled rows
         // written, and tile k - 2's verdict is in
         if (slot_sync_or(slot, failed)) break;
-        const uint32_t a_cur = a_op0 + x * kACols, a_oth = a_op0 + (x ^ 1u) * kACols;
 
         // layer 1: D = X (128 x K) * W1^T
-        if (row == 32 * (int)((k + 1u) & 3u)) issue_layer(d_cols, a_cur, sW1, N::kHid, N::kIn / 16, idesc_bf16(kMlpRows, N::kHid), mbar);
+        if (row == 32 * (int)((k + 1u) & 3u)) issue_layer(d_cols, a_f, sW1, N::kHid, N::kIn / 16, idesc_bf16(kMlpRows, N::kHid), mbar);
         // the slot's tile after next: its descriptor now, its records during layer 3
         const uint32_t t_nn = t_next + stride;
         const uint32_t count_nn = tile_count(n_frag, n_tiles, t_nn);
@@ -736,23 +737,24 @@ __global__ void __launch_bounds__(MlpLayout<N>::kThreads, 1) k_shade_mlp(ShadeAr
         failed |= !mbar_wait(mbar_first, phase, tries_first);
         phase ^= 1u;
         tc_fence_after();
-        if (!__any_sync(kFull, failed)) hidden_epilogue<N>(d_lane, a_oth + lane_off);  // h1
+        if (!__any_sync(kFull, failed)) hidden_epilogue<N>(d_lane, a_h + lane_off);  // h1
         a_written();
         if (slot_sync_or(slot, failed)) break;
 
         // layer 2: D = H1 (128 x H) * W2^T
-        if (row == 32 * (int)((k + 2u) & 3u)) issue_layer(d_cols, a_oth, sW2, N::kHid, N::kHid / 16, idesc_bf16(kMlpRows, N::kHid), mbar);
+        if (row == 32 * (int)((k + 2u) & 3u)) issue_layer(d_cols, a_h, sW2, N::kHid, N::kHid / 16, idesc_bf16(kMlpRows, N::kHid), mbar);
         failed |= !mbar_wait(mbar, phase);
         phase ^= 1u;
         tc_fence_after();
-        if (!__any_sync(kFull, failed)) hidden_epilogue<N>(d_lane, a_cur + lane_off);  // h2 over the features
+        if (!__any_sync(kFull, failed)) hidden_epilogue<N>(d_lane, a_h + lane_off);  // h2 over h1 (layer 2 has read it)
         a_written();
         if (slot_sync_or(slot, failed)) break;
 
-        // layer 3: D[0, 16) = H2 (128 x H) * W3^T; meanwhile the next tile's features go over h1
-        if (row == 32 * (int)((k + 3u) & 3u)) issue_layer(d_cols, a_cur, sW3, kMlpOutPad, N::kHid / 16, idesc_bf16(kMlpRows, kMlpOutPad), mbar);
+        // layer 3: D[0, 16) = H2 (128 x H) * W3^T; meanwhile the next tile's features go over this
+        // tile's (layer 1 has read them)
+        if (row == 32 * (int)((k + 3u) & 3u)) issue_layer(d_cols, a_h, sW3, kMlpOutPad, N::kHid / 16, idesc_bf16(kMlpRows, kMlpOutPad), mbar);
         if (t_next < n_tiles && !__any_sync(kFull, failed))
-            store_features<N>(make_float3(g0n.x, g0n.y, g0n.z), make_float3(g0n.w, g1n.x, g1n.y), a_oth + lane_off);
+            store_features<N>(make_float3(g0n.x, g0n.y, g0n.z), make_float3(g0n.w, g1n.x, g1n.y), a_f + lane_off);
         float4 g0nn, g1nn;
         load_record_desc(a, t_nn, count_nn, d_nn, row, g0nn, g1nn);
         failed |= !mbar_wait(mbar, phase);
@@ -800,7 +802,6 @@ __global__ void __launch_bounds__(MlpLayout<N>::kThreads, 1) k_shade_mlp(ShadeAr
                 }
         }
         ++k;
-        x ^= 1u;
         t = t_next;
         count = count_next;
         g0 = g0n;
