@@ -382,8 +382,10 @@ struct SetupArgs {
 // of the window's first item, carried over from the previous window. Each edge function
 //   e = (b.x - a.x)*(py - a.y) - (b.y - a.y)*(px - a.x)     (drawing.cpp:36-39)
 // is evaluated in the reference's operation order, its first product taken once per item.
-// At most 48 registers, so 5 CTAs (40 warps) fit an SM: the kernel is issue-bound on dependent
-// chains, and the extra warps hide them (6 CTAs, at 40 registers, spill and measured slower).
+// At most 48 registers, so 10 CTAs of 4 warps (40 warps) fit an SM: the kernel is issue-bound on
+// dependent chains, and the extra warps hide them (48 warps, at 40 registers, spill and measured
+// slower). CTAs of 4 warps measured faster than of 2, 3, 8 or 16: the warps share no work across
+// their CTA, and smaller CTAs leave fewer SMs idle at the end of the pass.
 template <uint32_t kRowChunk>  // pixels of one bounding-box row per work item; 32: whole rows or columns
 __global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) {
     __shared__ SetupStage stage[kSetupWarps];
