@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(256) k_split_triangles(const int32_t* __restri
     }
 }
 
-constexpr int kSetupThreads = 256;
+constexpr int kSetupThreads = 128;
 constexpr int kSetupWarps = kSetupThreads / 32;
 // Bounding boxes at most this many pixels wide take the per-triangle path; wider ones are binned.
 // Whole-row items cost the same whatever their length and run along the box's longer side, so for
@@ -387,7 +387,7 @@ struct SetupArgs {
 // slower). CTAs of 4 warps measured faster than of 2, 3, 8 or 16: the warps share no work across
 // their CTA, and smaller CTAs leave fewer SMs idle at the end of the pass.
 template <uint32_t kRowChunk>  // pixels of one bounding-box row per work item; 32: whole rows or columns
-__global__ void __launch_bounds__(kSetupThreads, 5) k_setup_raster(SetupArgs a) {
+__global__ void __launch_bounds__(kSetupThreads, 10) k_setup_raster(SetupArgs a) {
     __shared__ SetupStage stage[kSetupWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     SetupStage& S = stage[warp];
