@@ -935,7 +935,7 @@ struct TrainArgs {
     int64_t first;           // first sample of the step; CTA c takes [first + 64c, +64) mod n
     float out_scale;
     float grad_scale;        // d loss / d prediction = grad_scale * (prediction - label)
-    float* grad;             // per CTA kMlpParams partial gradients
+    float* grad;             // per CTA, one partial gradient per parameter of the network
     float* loss;             // per CTA partial sum of squared errors
 };
 
@@ -945,6 +945,7 @@ template <class N>
 __global__ void __launch_bounds__(kTrainThreads) k_mlp_train(TrainArgs a) {
     using TL = TrainLayout<N>;
     constexpr int kSX = TL::kSX, kSH = TL::kSH, kSPG = TL::kSPG, kHPG = TL::kHPG, kXPG = TL::kXPG;
+    // the network's sizes under the names the step's loops use
     constexpr int kMlpIn = N::kIn, kMlpHid = N::kHid, kPW1 = N::kPW1, kPW2 = N::kPW2, kPW3 = N::kPW3;
     constexpr int kMlpParams = N::kParams;
     extern __shared__ __align__(16) uint8_t smraw[];
