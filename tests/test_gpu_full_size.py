@@ -3,8 +3,8 @@
 - The many-light frame: the 1,046,528-triangle displaced sphere with smooth normals and per-vertex
   albedo at 1920x1080 under 256 lights. The exact shaders (fused into the resolve pass, and the
   deferred plain per-light shader) give the port's depth, triangle ids and colour bit for bit
-  (shading.cpp:20-34 in its order). The learned shader keeps depth and ids bit-exact, and its colour
-  stays within mean 0.5/255 and max 1/255 of the port's.
+  (shading.cpp:20-34 in its order). The learned shader, with either network, keeps depth and ids
+  bit-exact, and its colour stays within mean 0.5/255 and max 1/255 of the port's.
 - The uneven batch: all 256 frames (icospheres L2-L7, soups of 1k-500k triangles, four
   resolutions, 1-8 lights) drawn by rast_draw_batch as one CUDA graph over 8 lanes with the
   autotuner's options; eight frames, among them the L7 icosphere and the largest soup at 1920x1080,
@@ -53,9 +53,15 @@ def test_many_lights_exact_shaders_full_size(many_lights, shader):
     assert np.array_equal(f, of), f"RGB differs at {np.argwhere(f != of)[:5]}"
 
 
-def test_many_lights_learned_shader_full_size(many_lights):
+@pytest.mark.parametrize("network", [abi.MLP_COMPACT, abi.MLP_WIDE])
+def test_many_lights_learned_shader_full_size(many_lights, network):
+    """Both networks: the compact default and the 16-frequency 64-64 one the workload names."""
     sc, cam, nm, (of, od, oids), r = many_lights
-    st = r.mlp_train(samples=4 << 20, epochs=24, seed=3)
+    r.set_option(abi.OPT_MLP_NETWORK, network)
+    try:
+        st = r.mlp_train(samples=4 << 20, epochs=24, seed=3)
+    finally:
+        r.set_option(abi.OPT_MLP_NETWORK, abi.MLP_COMPACT)
     r.set_option(abi.OPT_SHADER, abi.SHADER_LEARNED)
     try:
         f, d, ids = r.draw(cam, nm, sc.width, sc.height, abi.CLEAR, want_ids=True)
